@@ -1,0 +1,329 @@
+/*
+ * sphmp.h — C ABI of the GB300-native multiphase SPH step.
+ *
+ * This is the drop-in boundary for the per-step particle pipeline of
+ * ZP-Z/sph-multiphase: uniform-grid hashing, stable counting sort, reorder,
+ * density + equation-of-state pressure, pressure/viscosity/boundary (and
+ * optional surface-tension) forces, drift-flux drift velocity, volume-fraction
+ * advance and correction, and symplectic-Euler advection.
+ *
+ * Two layers are exported:
+ *   1. a handle-based API (sphmp_*) that owns device buffers per context and
+ *      returns a status code from every call;
+ *   2. the reference's own entry-point names (GetParticleIndexCUDA, ...) as
+ *      thin `void` wrappers over one default context, declared in
+ *      sphmp_legacy.h.
+ *
+ * All pointers in this header are host pointers unless stated otherwise.
+ * No CUDA or torch types appear in the signatures; a CUDA stream is passed as
+ * an opaque `void*` (a cudaStream_t).
+ */
+#ifndef SPHMP_H
+#define SPHMP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHMP_MAX_PHASES 3        /* reference MAX_FLUIDNUM, SPH_Solver/common_header.h:17 */
+#define SPHMP_GRID_UNDEF 0xFFFFFFFFu /* reference GRID_UNDEF, SPH_Solver/fluids/fluid_system_kern.cuh:18 */
+
+#define SPHMP_TYPE_FLUID 0        /* SPH_Solver/common_header.h:20 */
+#define SPHMP_TYPE_BOUNDARY 1     /* SPH_Solver/common_header.h:21 */
+
+typedef enum sphmp_status {
+    SPHMP_OK = 0,
+    SPHMP_ERR_INVALID_ARG = 1,     /* null pointer, bad size, bad enum */
+    SPHMP_ERR_CAPACITY = 2,        /* n > capacity fixed at create */
+    SPHMP_ERR_CUDA = 3,            /* a CUDA runtime call failed */
+    SPHMP_ERR_UNSUPPORTED_TYPE = 4,/* particle type other than fluid(0)/boundary(1) */
+    SPHMP_ERR_NOT_FINITE = 5,      /* NaN/Inf in uploaded positions or params */
+    SPHMP_ERR_CELL_OVERFLOW = 6,   /* one grid cell holds more particles than the sort supports */
+    SPHMP_ERR_STATE = 7,           /* call order violated (e.g. force before sort) */
+    SPHMP_ERR_NO_DEVICE = 8,       /* no CUDA device / extension not loadable */
+    SPHMP_ERR_BAD_MASS = 9,        /* fluid particle with mass <= 0 */
+    SPHMP_ERR_GRID = 10            /* grid parameters inconsistent (res < 3, total overflow) */
+} sphmp_status;
+
+/* Equation of state used by the density pass. */
+typedef enum sphmp_eos {
+    SPHMP_EOS_TAIT = 0,   /* p = 2.5*rho0*((rho/rho0)^7 - 1), clamped >= 0
+                             (SPH_Solver/fluids/fluid_system_kern.cu:310-313) */
+    SPHMP_EOS_LINEAR = 1  /* p = k*(rho - rho0), clamped >= 0 (the commented
+                             linear form at fluid_system_kern.cu:308, k = eos_stiffness) */
+} sphmp_eos;
+
+/* Order in which one step composes the per-pass functions. */
+typedef enum sphmp_schedule {
+    /* sort, density, [drift, alpha, correction], force, advance: the reference's
+       call order (legacy multiphase step SPH_Solver/fluids/fluid_system.cpp:375-420,
+       plain step :514-539), one kernel per function. */
+    SPHMP_SCHEDULE_REFERENCE = 0,
+    /* sort, density+pressure, force+drift, alpha+correction+advance: three
+       neighbour passes. The force reads the mixture rest density and viscosity
+       from before this step's correction (the correction lands one step later
+       in the force); everything else is identical to the reference order. */
+    SPHMP_SCHEDULE_FUSED = 1
+} sphmp_schedule;
+
+/*
+ * Parameters. The first 464 bytes are byte-compatible with the reference's
+ * `ParamCarrier` (SPH_Solver/common_header.h:28-109), so a caller holding a
+ * ParamCarrier can copy it over the prefix. The fields after `fBlending` are
+ * extensions for the multiphase kernels (whose constants lived in the removed
+ * legacy `FluidParams simData`) and for this implementation.
+ */
+typedef struct sphmp_params {
+    /* environment */
+    float acclimit;
+    float vlimit;
+    float gravity[3];
+    float volmin[3];
+    float volmax[3];
+    float softminx[3];
+    float softmaxx[3];
+    /* case */
+    int32_t num;        /* active particle slots */
+    int32_t maxNum;     /* capacity */
+    float dt;
+    float simscale;
+    /* fluid */
+    float viscosity;
+    float restdensity;
+    float mass;
+    float radius;
+    float smoothradius;
+    float scalep;
+    float massArr[SPHMP_MAX_PHASES];
+    float densArr[SPHMP_MAX_PHASES];  /* per-phase rest density (mf_dens) */
+    float viscArr[SPHMP_MAX_PHASES];  /* per-phase viscosity (mf_visc) */
+    float boundstiff;
+    /* sph kernel constants (derived by sphmp_setup_constants) */
+    float kpoly6;
+    float kspiky;
+    float kspikydiff;
+    float klaplacian;
+    float kspline;
+    /* boundary particles */
+    float bmass;
+    float bRestdensity;
+    float bvisc;
+    /* index-sort grid (derived by sphmp_setup_grid) */
+    float cellsize;
+    int32_t searchnum;
+    int32_t neighbornum;
+    int32_t neighborid[27];
+    float gridmin[3];
+    float gridmax[3];
+    float gridsize[3];
+    float gridIdfac[3];
+    int32_t gridres[3];
+    int32_t gridtotal;
+    /* MPM grid, solid, Drucker-Prager, FLIP: carried for layout only, unused */
+    float mpmcellsize;
+    float mpmXmin[3];
+    float mpmXmax[3];
+    int32_t mpmRes[3];
+    int32_t mpmNodeNum;
+    float solidK;
+    float solidG;
+    float a_phi;
+    float a_psi;
+    float k_c;
+    float w_deltax;
+    float fijn;
+    float SFlipControl;
+    float LFlipControl;
+    int32_t mpmSplitNum;
+    float collisionStiff;
+    float surfaceTensionK;       /* tension radius factor K (radius = K*h) */
+    float surfaceTensionFluidC;  /* cohesion coefficient C */
+    float fBlending;
+    /* ---- extensions (offset 464) ---- */
+    int32_t nphase;              /* mf_catnum: number of phases, 1..3 */
+    int32_t multiphase;          /* 1: run drift / alpha / correction in sphmp_step */
+    int32_t surface_tension;     /* 1: add the reference SurfaceTension term in the force pass */
+    int32_t eos;                 /* sphmp_eos */
+    float eos_stiffness;         /* k for SPHMP_EOS_LINEAR */
+    float mf_relax;              /* drift relaxation time coefficient (simData.relax) */
+    float mf_diffusion;          /* alpha-gradient diffusion sigma (simData.mf_diffusion) */
+    float mf_cont;               /* simData.cont */
+    float mf_cont1;              /* simData.cont1 (diffusion term switch) */
+    float mf_cont2;              /* simData.cont2 (pressure term switch) */
+    float mf_pintstiff;          /* simData.pintstiff (pressure-correction stiffness) */
+    int32_t reserved[5];
+} sphmp_params;
+
+/* Byte-compatible copies of the reference records (SPH_Solver/common_header.h:112-137). */
+typedef struct sphmp_display_pack {
+    float pos[3];
+    float color[4];
+    int32_t type;
+} sphmp_display_pack; /* 32 bytes */
+
+typedef struct sphmp_calc_pack {
+    float vel[3];
+    float veleval[3];
+    float pressure;
+    float dens;       /* fluid: 1/rho; boundary: particle volume V_b */
+    float restdens;
+    float mass;
+    float visc;
+    int32_t bornid;
+    float accel[3];
+    float deformGrad[9]; /* solid/MPM fields: carried for layout only */
+    float stress[9];
+    float B[9];
+    float solidG;
+    float solidK;
+    float X[3];
+    float invA[9];
+} sphmp_calc_pack; /* 224 bytes */
+
+/* Per-particle / per-cell arrays addressable by sphmp_upload_field / sphmp_download_field.
+   Element layouts follow the reference: vectors are 3 consecutive floats per
+   particle, phase arrays use the MAX_FLUIDNUM stride (3 floats per particle),
+   drift velocities are 3 phases x 3 floats per particle (mf_vel_phrel[i*3+k]). */
+typedef enum sphmp_field {
+    SPHMP_F_POS = 0,       /* float[3n] */
+    SPHMP_F_VEL = 1,       /* float[3n] */
+    SPHMP_F_VELEVAL = 2,   /* float[3n] */
+    SPHMP_F_PRESSURE = 3,  /* float[n]  */
+    SPHMP_F_DENS = 4,      /* float[n]  1/rho (fluid) or V_b (boundary); download only */
+    SPHMP_F_RESTDENS = 5,  /* float[n]  */
+    SPHMP_F_VISC = 6,      /* float[n]  */
+    SPHMP_F_ACCEL = 7,     /* float[3n] */
+    SPHMP_F_ALPHA = 8,     /* float[3n] mf_alpha (after the alpha advance) */
+    SPHMP_F_ALPHA_PRE = 9, /* float[3n] mf_alpha_pre (start-of-step fractions) */
+    SPHMP_F_DRIFT = 10,    /* float[9n] mf_vel_phrel */
+    SPHMP_F_APREV = 11,    /* float[3n] mforce: gravity - total accel of the last advance */
+    SPHMP_F_PMOD = 12,     /* float[n]  mf_pressure_modify */
+    SPHMP_F_TYPE = 13,     /* int32[n]  download only */
+    SPHMP_F_MASS = 14,     /* float[n]  download only */
+    SPHMP_F_BORNID = 15,   /* int32[n]  download only */
+    SPHMP_F_MGCELL = 16,   /* uint32[n] cell id per slot */
+    SPHMP_F_MIDSORT = 17,  /* uint32[n] pre-sort slot of each sorted slot */
+    SPHMP_F_MGNDX = 18,    /* uint32[n] rank inside its cell (GRID_UNDEF for out-of-grid slots) */
+    SPHMP_F_MGRIDOFF = 19, /* int32[gridtotal] first slot of each occupied cell, 0 if empty */
+    SPHMP_F_MGRIDCNT = 20, /* int32[gridtotal] particle count per cell */
+    SPHMP_F_COUNT = 21
+} sphmp_field;
+
+typedef struct sphmp_ctx sphmp_ctx;
+
+/* ---- host-side setup (reference FluidSystem setup, SPH_Solver/fluids/fluid_system.cpp) ---- */
+
+/* Fill every field with the defaults of a water-like single-phase scene. */
+sphmp_status sphmp_params_default(sphmp_params* p);
+/* SPH kernel constants from smoothradius, and cellsize = 2h
+   (reference SetupSimpleSphCase, fluid_system.cpp:308-313). */
+sphmp_status sphmp_setup_constants(sphmp_params* p);
+/* Grid resolution, cell index factors and the 27-neighbour offsets from
+   volmin/volmax/cellsize/simscale (reference SetupGrid, fluid_system.cpp:119-145). */
+sphmp_status sphmp_setup_grid(sphmp_params* p);
+
+/* Append a fluid block on a lattice (reference AddFluidVolume,
+   fluid_system.cpp:719-762, with the jitter drawn from a seeded generator
+   instead of rand()). Writes at most `cap - *count` particles into the host
+   arrays starting at index *count and advances *count. */
+sphmp_status sphmp_add_fluid_volume(const sphmp_params* p, const float vmin[3], const float vmax[3],
+                                    float spacing, const float offs[3], int32_t phase, float jitter,
+                                    uint64_t seed, sphmp_display_pack* disp, sphmp_calc_pack* calc,
+                                    int32_t cap, int32_t* count);
+/* Append a boundary wall lattice (reference SetupAddWall, SPH_Solver/fluids/AddShape.cpp:306-353). */
+sphmp_status sphmp_add_wall(const sphmp_params* p, const float vmin[3], const float vmax[3],
+                            sphmp_display_pack* disp, sphmp_calc_pack* calc, int32_t cap, int32_t* count);
+/* Append an open box of five walls (reference SetupAddOpenBox, AddShape.cpp:355-366). */
+sphmp_status sphmp_add_open_box(const sphmp_params* p, const float vmin[3], const float vmax[3],
+                                float thickness, sphmp_display_pack* disp, sphmp_calc_pack* calc,
+                                int32_t cap, int32_t* count);
+/* Boundary lattice spacing (bmass/bRestdensity)^(1/3)/simscale (AddShape.cpp:265-271). */
+float sphmp_boundary_spacing(const sphmp_params* p);
+
+/* ---- context lifetime (reference FluidSetupCUDA / FluidClearCUDA, fluid_system_host.cu:79-144) ---- */
+
+/* Allocate device buffers for p->maxNum particles and p->gridtotal cells on the
+   current CUDA device. The params are copied (reference CarryParam). */
+sphmp_status sphmp_create(const sphmp_params* p, sphmp_ctx** out);
+sphmp_status sphmp_destroy(sphmp_ctx* ctx);
+/* Replace the parameters (reference CarryParam, fluid_system_kern.cu:22-25).
+   maxNum and the grid size may not grow beyond what create allocated. */
+sphmp_status sphmp_set_params(sphmp_ctx* ctx, const sphmp_params* p);
+sphmp_status sphmp_get_params(const sphmp_ctx* ctx, sphmp_params* p);
+/* Run all later work of this context on `stream` (a cudaStream_t; NULL = the
+   context's own stream). */
+sphmp_status sphmp_set_stream(sphmp_ctx* ctx, void* stream);
+sphmp_status sphmp_sync(sphmp_ctx* ctx);
+int32_t sphmp_num_particles(const sphmp_ctx* ctx);
+
+/* ---- host transfers (reference TransferToCUDA / TransferFromCUDA / EmitUpdateCUDA,
+        SPH_Solver/fluids/fluid_system.cpp:979-999) ---- */
+
+/* Upload n reference records into slots [0, n) and set num = n. Multiphase
+   arrays are initialised one-hot from `phase` = 0 unless uploaded later. */
+sphmp_status sphmp_upload_aos(sphmp_ctx* ctx, const sphmp_display_pack* disp,
+                              const sphmp_calc_pack* calc, int32_t n);
+/* Download slots [0, n) in the current (sorted) slot order. `calc` may be NULL
+   (the reference's per-frame TransferFromCUDA copies display records only). */
+sphmp_status sphmp_download_aos(sphmp_ctx* ctx, sphmp_display_pack* disp,
+                                sphmp_calc_pack* calc, int32_t n);
+/* Append records into slots [start, end) and set num = end (EmitUpdateCUDA). */
+sphmp_status sphmp_emit_aos(sphmp_ctx* ctx, const sphmp_display_pack* disp,
+                            const sphmp_calc_pack* calc, int32_t start, int32_t end);
+/* Upload / download one array (sphmp_field) for n slots (gridtotal cells for the
+   MGRIDOFF/MGRIDCNT fields). Fields marked "download only" reject uploads. */
+sphmp_status sphmp_upload_field(sphmp_ctx* ctx, int32_t field, const void* host, int32_t n);
+sphmp_status sphmp_download_field(sphmp_ctx* ctx, int32_t field, void* host, int32_t n);
+
+/* ---- per-pass entry points (one per reference launch wrapper) ---- */
+
+/* GetParticleIndexCUDA (fluid_system_host.cu:147-159): cell id of every slot. */
+sphmp_status sphmp_get_particle_index(sphmp_ctx* ctx);
+/* GetGridListCUDA (fluid_system_host.cu:161-185): stable key sort, cell
+   offsets/counts and rank-in-cell. */
+sphmp_status sphmp_get_grid_list(sphmp_ctx* ctx);
+/* RearrageDataCUDA (fluid_system_host.cu:187-210): move every particle to its
+   sorted slot; out-of-grid slots are parked at (-1000,-1000,-1000). */
+sphmp_status sphmp_rearrange_data(sphmp_ctx* ctx);
+/* ComputeBoundaryDensity (fluid_system_host.cu:510-513): boundary particle volumes. */
+sphmp_status sphmp_compute_boundary_density(sphmp_ctx* ctx);
+/* MfComputePressureCUDA (fluid_system_host.cu:337-348): density + EOS pressure. */
+sphmp_status sphmp_compute_pressure(sphmp_ctx* ctx);
+/* MfComputeDriftVelCUDA (decl fluid_system_host.cuh:62; kernel multiphase.cu:78-166). */
+sphmp_status sphmp_compute_drift_vel(sphmp_ctx* ctx);
+/* MfComputeAlphaAdvanceCUDA (decl fluid_system_host.cuh:63; kernel multiphase.cu:218-272). */
+sphmp_status sphmp_compute_alpha_advance(sphmp_ctx* ctx);
+/* MfComputeCorrectionCUDA (decl fluid_system_host.cuh:64; kernel multiphase.cu:275-349). */
+sphmp_status sphmp_compute_correction(sphmp_ctx* ctx);
+/* MfComputeForceCUDA (fluid_system_host.cu:421-438), plus the reference
+   SurfaceTension term (fluid_system_kern.cu:605-625) when enabled. */
+sphmp_status sphmp_compute_force(sphmp_ctx* ctx);
+/* MfAdvanceCUDA (fluid_system_host.cu:385-394). */
+sphmp_status sphmp_advance(sphmp_ctx* ctx);
+
+/* nsteps full steps (sort ... advance) in the given sphmp_schedule. Steps run
+   from a captured CUDA graph when `use_graph` is 1. */
+sphmp_status sphmp_step(sphmp_ctx* ctx, int32_t nsteps, int32_t schedule, int32_t use_graph);
+
+/* FP64 conservation sums over in-grid, non-boundary slots, computed on the GPU:
+   out[0] = total mass, out[1] = total volume sum(m/rho), out[2+k] = phase-k volume
+   sum(alpha_k m/rho) for k < nphase, out[2+nphase] = max |sum_k alpha_k - 1|. */
+sphmp_status sphmp_conservation(sphmp_ctx* ctx, double* out, int32_t nout);
+
+/* Device-side error word accumulated by the kernels since the last call (bit set of
+   (1 << sphmp_status)); reading it clears it. */
+sphmp_status sphmp_device_errors(sphmp_ctx* ctx, uint32_t* bits);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* sphmp_last_error(void);
+/* Library build identification, e.g. "sphmp 0.1 sm_103a". */
+const char* sphmp_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHMP_H */

@@ -1,0 +1,2 @@
+/* host_defines.h stand-in for the oracle host build */
+#include "cudashim.h"

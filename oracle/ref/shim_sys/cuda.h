@@ -1,0 +1,2 @@
+/* cuda.h stand-in for the oracle host build */
+#include "cudashim.h"

@@ -1,0 +1,2 @@
+/* device_launch_parameters.h stand-in for the oracle host build */
+#include "cudashim.h"

@@ -1,0 +1,807 @@
+// sphmp_api.cu — the C ABI (include/sphmp.h, include/sphmp_legacy.h): context
+// lifetime, host transfers, per-pass entry points, the graph-captured step and
+// the reference's own entry-point names over a default context.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+
+#include "sphmp.h"
+#include "sphmp_internal.h"
+#include "sphmp_legacy.h"
+
+using namespace sphmp;
+
+struct sphmp_ctx {
+    sphmp_params prm;
+    int cap = 0;         // particle capacity
+    int gcap = 0;        // grid cells allocated
+    int n = 0;           // active slots
+    int cur[kNumFloat4Fields] = {0, 0, 0, 0, 0};
+    bool alpha_advanced = false;  // alpha4[cur] = advanced fractions, alpha4[cur^1] = start of step
+    bool grid_valid = false;      // cell starts built for the current slot order
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuffers B{};
+    void* stage = nullptr;  // device staging: reference records / field arrays
+    size_t stage_bytes = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_n = -1;
+    int graph_schedule = -1;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+sphmp_status fail(sphmp_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+sphmp_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(SPHMP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                                    \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);         \
+    } while (0)
+
+#define CHECK_LAUNCH(what)                                          \
+    do {                                                            \
+        cudaError_t e_ = cudaGetLastError();                        \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);          \
+    } while (0)
+
+sphmp_status validate_params(const sphmp_params* p) {
+    if (!p) return fail(SPHMP_ERR_INVALID_ARG, "params is NULL");
+    if (p->maxNum <= 0) return fail(SPHMP_ERR_INVALID_ARG, "maxNum must be > 0 (got %d)", p->maxNum);
+    if (p->num < 0 || p->num > p->maxNum) return fail(SPHMP_ERR_CAPACITY, "num %d outside [0, maxNum=%d]", p->num, p->maxNum);
+    if (p->nphase < 1 || p->nphase > SPHMP_MAX_PHASES)
+        return fail(SPHMP_ERR_INVALID_ARG, "nphase must be 1..3 (got %d)", p->nphase);
+    if (!(p->smoothradius > 0.f) || !isfinite(p->smoothradius)) return fail(SPHMP_ERR_NOT_FINITE, "smoothradius must be > 0");
+    if (!(p->simscale > 0.f) || !isfinite(p->simscale)) return fail(SPHMP_ERR_NOT_FINITE, "simscale must be > 0");
+    if (!isfinite(p->dt)) return fail(SPHMP_ERR_NOT_FINITE, "dt not finite");
+    for (int a = 0; a < 3; a++) {
+        if (p->gridres[a] < 3) return fail(SPHMP_ERR_GRID, "gridres[%d] = %d < 3 (call sphmp_setup_grid)", a, p->gridres[a]);
+        if (!isfinite(p->gridmin[a]) || !(p->gridIdfac[a] > 0.f) || !isfinite(p->gridIdfac[a]))
+            return fail(SPHMP_ERR_GRID, "grid origin/factor not finite on axis %d", a);
+    }
+    const long long g = (long long)p->gridres[0] * p->gridres[1] * p->gridres[2];
+    if (g != p->gridtotal) return fail(SPHMP_ERR_GRID, "gridtotal %d != product of gridres %lld", p->gridtotal, g);
+    if (g > (1ll << 31) - 16) return fail(SPHMP_ERR_GRID, "grid too large (%lld cells)", g);
+    if (p->eos != SPHMP_EOS_TAIT && p->eos != SPHMP_EOS_LINEAR) return fail(SPHMP_ERR_INVALID_ARG, "unknown eos %d", p->eos);
+    return SPHMP_OK;
+}
+
+DevParams dev_params(const sphmp_ctx* c) {
+    const sphmp_params& p = c->prm;
+    DevParams P;
+    memset(&P, 0, sizeof(P));
+    P.n = c->n;
+    P.cap = c->cap;
+    P.G = p.gridtotal;
+    P.rx = p.gridres[0];
+    P.ry = p.gridres[1];
+    P.rz = p.gridres[2];
+    for (int a = 0; a < 3; a++) {
+        P.gmin[a] = p.gridmin[a];
+        P.fac[a] = p.gridIdfac[a];
+        P.srad[a] = (float)((double)p.smoothradius / (double)p.simscale * (double)p.gridIdfac[a] + 1.0e-3);
+        P.grav[a] = p.gravity[a];
+    }
+    P.ss = p.simscale;
+    P.h = p.smoothradius;
+    P.r2 = p.smoothradius * p.smoothradius;
+    P.dt = p.dt;
+    P.kpoly6 = p.kpoly6;
+    P.kspikydiff = p.kspikydiff;
+    P.bvisc = p.bvisc;
+    P.nphase = p.nphase;
+    P.multiphase = p.multiphase;
+    for (int k = 0; k < 3; k++) {
+        P.dens_k[k] = p.densArr[k];
+        P.visc_k[k] = p.viscArr[k];
+    }
+    P.relax = p.mf_relax;
+    P.sigma = p.mf_diffusion;
+    P.cont = p.mf_cont;
+    P.cont1 = p.mf_cont1;
+    P.cont2 = p.mf_cont2;
+    P.pintstiff = p.mf_pintstiff;
+    P.eos = p.eos;
+    P.eos_k = p.eos_stiffness;
+    P.st_on = p.surface_tension;
+    P.st_K = p.surfaceTensionK;
+    P.st_C = p.surfaceTensionFluidC;
+    for (int k = 0; k < 27; k++) P.neighborid[k] = p.neighborid[k];
+    return P;
+}
+
+void drop_graph(sphmp_ctx* c) {
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_n = -1;
+    c->graph_schedule = -1;
+}
+
+void free_buffers(sphmp_ctx* c) {
+    DevBuffers& B = c->B;
+    for (int f = 0; f < kNumFloat4Fields; f++)
+        for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
+    void* ptrs[] = {B.densp, B.accel4, B.drift4, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
+                    B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
+                    B.mass_raw, B.err, B.red, B.vtmp, c->stage};
+    for (void* q : ptrs) cudaFree(q);
+    memset(&c->B, 0, sizeof(c->B));
+    c->stage = nullptr;
+}
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+}
+
+sphmp_status alloc_buffers(sphmp_ctx* c) {
+    const size_t N = (size_t)c->cap;
+    const size_t G = (size_t)c->gcap;
+    DevBuffers& B = c->B;
+    for (int f = 0; f < kNumFloat4Fields; f++)
+        for (int b = 0; b < 2; b++) CK(dalloc(&B.f4[f][b], N));
+    CK(dalloc(&B.densp, N));
+    CK(dalloc(&B.accel4, N));
+    CK(dalloc(&B.drift4, 3 * N));
+    CK(dalloc(&B.pmod, N));
+    CK(dalloc(&B.mgcell, N));
+    CK(dalloc(&B.midsort, N));
+    CK(dalloc(&B.mgndx, N));
+    CK(dalloc(&B.mgridoff, G));
+    CK(dalloc(&B.mgridcnt, G));
+    CK(dalloc(&B.key, N));
+    CK(dalloc(&B.arank, N));
+    CK(dalloc(&B.sidx, N));
+    CK(dalloc(&B.ccount, G + 1));
+    CK(dalloc(&B.cstart, G + 2));
+    const size_t per = (size_t)kScanBlock * kScanItems;
+    CK(dalloc(&B.bsum, (G + per - 1) / per + 1));
+    CK(dalloc(&B.uchunk, N / kHashBlock + 2));
+    CK(dalloc(&B.big, N / (kWarpSortMax + 1) + 2));
+    CK(dalloc(&B.color, N));
+    CK(dalloc(&B.bornid, N));
+    CK(dalloc(&B.mass_raw, N));
+    CK(dalloc(&B.err, 1));
+    CK(dalloc(&B.red, 16));
+    CK(dalloc(&B.vtmp, N));
+    c->stage_bytes = N * (sizeof(sphmp_display_pack) + sizeof(sphmp_calc_pack));
+    if (c->stage_bytes < G * sizeof(int32_t)) c->stage_bytes = G * sizeof(int32_t);
+    CK(cudaMalloc(&c->stage, c->stage_bytes));
+    // zero everything the kernels may read before it is first written
+    for (int f = 0; f < kNumFloat4Fields; f++)
+        for (int b = 0; b < 2; b++) CK(cudaMemset(B.f4[f][b], 0, sizeof(float4) * N));
+    CK(cudaMemset(B.densp, 0, sizeof(float2) * N));
+    CK(cudaMemset(B.accel4, 0, sizeof(float4) * N));
+    CK(cudaMemset(B.drift4, 0, sizeof(float4) * 3 * N));
+    CK(cudaMemset(B.pmod, 0, sizeof(float) * N));
+    CK(cudaMemset(B.mgcell, 0xFF, sizeof(uint32_t) * N));
+    CK(cudaMemset(B.midsort, 0, sizeof(uint32_t) * N));
+    CK(cudaMemset(B.mgndx, 0xFF, sizeof(uint32_t) * N));
+    CK(cudaMemset(B.mgridoff, 0, sizeof(int32_t) * G));
+    CK(cudaMemset(B.mgridcnt, 0, sizeof(int32_t) * G));
+    CK(cudaMemset(B.cstart, 0, sizeof(uint32_t) * (G + 2)));
+    CK(cudaMemset(B.err, 0, sizeof(uint32_t)));
+    CK(cudaMemset(B.color, 0, sizeof(float4) * N));
+    CK(cudaMemset(B.bornid, 0, sizeof(int32_t) * N));
+    CK(cudaMemset(B.mass_raw, 0, sizeof(float) * N));
+    return SPHMP_OK;
+}
+
+// Read and clear the device error word; map the lowest set bit to a status.
+sphmp_status take_device_errors(sphmp_ctx* c, uint32_t* bits_out) {
+    uint32_t bits = 0;
+    CK(cudaMemcpyAsync(&bits, c->B.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->B.err, 0, sizeof(uint32_t), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (bits_out) *bits_out = bits;
+    if (bits) {
+        for (int s = 1; s < 32; s++)
+            if (bits & (1u << s)) {
+                const char* what = s == SPHMP_ERR_UNSUPPORTED_TYPE ? "particle type other than fluid (0) or boundary (1)"
+                                   : s == SPHMP_ERR_NOT_FINITE     ? "non-finite particle position"
+                                   : s == SPHMP_ERR_BAD_MASS       ? "fluid particle with mass <= 0 or not finite"
+                                   : s == SPHMP_ERR_CELL_OVERFLOW  ? "a grid cell holds more than 8192 particles"
+                                                                   : "device error";
+                return fail((sphmp_status)s, "device reported: %s", what);
+            }
+    }
+    return SPHMP_OK;
+}
+
+inline sphmp_status need_ctx(const sphmp_ctx* c) {
+    if (!c) return fail(SPHMP_ERR_INVALID_ARG, "context is NULL");
+    return SPHMP_OK;
+}
+
+inline sphmp_status need_grid(const sphmp_ctx* c) {
+    if (!c->grid_valid) return fail(SPHMP_ERR_STATE, "no cell list for the current slot order (run the sort first)");
+    return SPHMP_OK;
+}
+
+inline void swap_all(sphmp_ctx* c) {
+    for (int f = 0; f < kNumFloat4Fields; f++) c->cur[f] ^= 1;
+}
+
+// Queue one full step on the context stream (no host synchronisation).
+sphmp_status enqueue_step(sphmp_ctx* c, int schedule) {
+    const DevParams P = dev_params(c);
+    const cudaStream_t s = c->stream;
+    launch_hash(P, c->B, c->cur, s);
+    launch_grid_list(P, c->B, s);
+    launch_rearrange(P, c->B, c->cur, s);
+    swap_all(c);
+    c->alpha_advanced = false;
+    c->grid_valid = true;
+    launch_density(P, c->B, c->cur, s);
+    if (schedule == SPHMP_SCHEDULE_FUSED) {
+        launch_force_drift(P, c->B, c->cur, true, P.multiphase != 0, s);
+        if (P.st_on) launch_surface_tension(P, c->B, c->cur, s);
+        launch_pass_c(P, c->B, c->cur, s);
+        swap_all(c);
+    } else {
+        if (P.multiphase) {
+            launch_force_drift(P, c->B, c->cur, false, true, s);
+            launch_alpha_advance(P, c->B, c->cur, s);
+            c->cur[ALPHA] ^= 1;
+            c->alpha_advanced = true;
+            launch_correction(P, c->B, c->cur, c->cur[ALPHA] ^ 1, s);
+        }
+        launch_force_drift(P, c->B, c->cur, true, false, s);
+        if (P.st_on) launch_surface_tension(P, c->B, c->cur, s);
+        launch_advance(P, c->B, c->cur, s);
+    }
+    CHECK_LAUNCH("step");
+    return SPHMP_OK;
+}
+
+int field_width(int field) {
+    switch (field) {
+        case SPHMP_F_POS: case SPHMP_F_VEL: case SPHMP_F_VELEVAL: case SPHMP_F_ACCEL:
+        case SPHMP_F_ALPHA: case SPHMP_F_ALPHA_PRE: case SPHMP_F_APREV: return 3;
+        case SPHMP_F_DRIFT: return 9;
+        default: return 1;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+const char* sphmp_last_error(void) { return g_err.c_str(); }
+
+const char* sphmp_version(void) { return "sphmp 0.1 sm_103a"; }
+
+sphmp_status sphmp_create(const sphmp_params* p, sphmp_ctx** out) {
+    if (!out) return fail(SPHMP_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    sphmp_status st = validate_params(p);
+    if (st) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return fail(SPHMP_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    sphmp_ctx* c = new sphmp_ctx();
+    c->prm = *p;
+    c->cap = p->maxNum;
+    c->gcap = p->gridtotal;
+    c->n = p->num;
+    cudaGetDevice(&c->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "cudaStreamCreate");
+    }
+    c->stream = c->own_stream;
+    st = alloc_buffers(c);
+    if (st) {
+        free_buffers(c);
+        cudaStreamDestroy(c->own_stream);
+        delete c;
+        return st;
+    }
+    *out = c;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_destroy(sphmp_ctx* c) {
+    if (!c) return SPHMP_OK;
+    cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    free_buffers(c);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_set_params(sphmp_ctx* c, const sphmp_params* p) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = validate_params(p)) return st;
+    if (p->maxNum > c->cap) return fail(SPHMP_ERR_CAPACITY, "maxNum %d exceeds the allocated capacity %d", p->maxNum, c->cap);
+    if (p->gridtotal > c->gcap) return fail(SPHMP_ERR_CAPACITY, "gridtotal %d exceeds the allocated %d cells", p->gridtotal, c->gcap);
+    const bool grid_changed = memcmp(p->gridres, c->prm.gridres, sizeof(p->gridres)) != 0 ||
+                              memcmp(p->gridmin, c->prm.gridmin, sizeof(p->gridmin)) != 0 ||
+                              memcmp(p->gridIdfac, c->prm.gridIdfac, sizeof(p->gridIdfac)) != 0;
+    c->prm = *p;
+    c->prm.maxNum = c->cap;
+    c->prm.num = c->n;
+    if (grid_changed) c->grid_valid = false;
+    drop_graph(c);
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_get_params(const sphmp_ctx* c, sphmp_params* p) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!p) return fail(SPHMP_ERR_INVALID_ARG, "params is NULL");
+    *p = c->prm;
+    p->num = c->n;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_set_stream(sphmp_ctx* c, void* stream) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    drop_graph(c);
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_sync(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    return take_device_errors(c, nullptr);
+}
+
+int32_t sphmp_num_particles(const sphmp_ctx* c) { return c ? c->n : 0; }
+
+sphmp_status sphmp_device_errors(sphmp_ctx* c, uint32_t* bits) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    uint32_t b = 0;
+    sphmp_status st = take_device_errors(c, &b);
+    if (bits) *bits = b;
+    return st == SPHMP_ERR_CUDA ? st : SPHMP_OK;
+}
+
+// ---- transfers ----
+
+static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp, const sphmp_calc_pack* calc,
+                                   int start, int end) {
+    if (!disp || !calc) return fail(SPHMP_ERR_INVALID_ARG, "record pointers are NULL");
+    if (start < 0 || end < start) return fail(SPHMP_ERR_INVALID_ARG, "bad range [%d, %d)", start, end);
+    if (end > c->cap) return fail(SPHMP_ERR_CAPACITY, "%d particles exceed the capacity %d", end, c->cap);
+    const int m = end - start;
+    auto* d_disp = reinterpret_cast<sphmp_display_pack*>(c->stage);
+    auto* d_calc = reinterpret_cast<sphmp_calc_pack*>(reinterpret_cast<char*>(c->stage) +
+                                                      sizeof(sphmp_display_pack) * (size_t)c->cap);
+    if (take_device_errors(c, nullptr) == SPHMP_ERR_CUDA) return SPHMP_ERR_CUDA;  // clear stale bits
+    if (m > 0) {
+        CK(cudaMemcpyAsync(d_disp, disp, sizeof(sphmp_display_pack) * (size_t)m, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(d_calc, calc, sizeof(sphmp_calc_pack) * (size_t)m, cudaMemcpyHostToDevice, c->stream));
+    }
+    c->n = end;
+    c->prm.num = end;
+    const DevParams P = dev_params(c);
+    launch_unpack_aos(P, c->B, c->cur, d_disp, d_calc, start, end, c->stream);
+    CHECK_LAUNCH("unpack records");
+    c->alpha_advanced = false;
+    c->grid_valid = false;
+    drop_graph(c);
+    CK(cudaStreamSynchronize(c->stream));
+    return take_device_errors(c, nullptr);
+}
+
+sphmp_status sphmp_upload_aos(sphmp_ctx* c, const sphmp_display_pack* disp, const sphmp_calc_pack* calc, int32_t n) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (n < 0) return fail(SPHMP_ERR_INVALID_ARG, "n < 0");
+    return upload_records(c, disp, calc, 0, n);
+}
+
+sphmp_status sphmp_emit_aos(sphmp_ctx* c, const sphmp_display_pack* disp, const sphmp_calc_pack* calc,
+                            int32_t start, int32_t end) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (start != c->n) return fail(SPHMP_ERR_INVALID_ARG, "emission must append at slot %d (got start %d)", c->n, start);
+    return upload_records(c, disp, calc, start, end);
+}
+
+sphmp_status sphmp_download_aos(sphmp_ctx* c, sphmp_display_pack* disp, sphmp_calc_pack* calc, int32_t n) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!disp) return fail(SPHMP_ERR_INVALID_ARG, "display pointer is NULL");
+    if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
+    auto* d_disp = reinterpret_cast<sphmp_display_pack*>(c->stage);
+    auto* d_calc = calc ? reinterpret_cast<sphmp_calc_pack*>(reinterpret_cast<char*>(c->stage) +
+                                                             sizeof(sphmp_display_pack) * (size_t)c->cap)
+                        : nullptr;
+    const DevParams P = dev_params(c);
+    launch_pack_aos(P, c->B, c->cur, d_disp, d_calc, n, c->stream);
+    CHECK_LAUNCH("pack records");
+    if (n > 0) {
+        CK(cudaMemcpyAsync(disp, d_disp, sizeof(sphmp_display_pack) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        if (calc)
+            CK(cudaMemcpyAsync(calc, d_calc, sizeof(sphmp_calc_pack) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+static void* sort_array(sphmp_ctx* c, int field, size_t* count) {
+    switch (field) {
+        case SPHMP_F_MGCELL: *count = c->n; return c->B.mgcell;
+        case SPHMP_F_MIDSORT: *count = c->n; return c->B.midsort;
+        case SPHMP_F_MGNDX: *count = c->n; return c->B.mgndx;
+        case SPHMP_F_MGRIDOFF: *count = c->prm.gridtotal; return c->B.mgridoff;
+        case SPHMP_F_MGRIDCNT: *count = c->prm.gridtotal; return c->B.mgridcnt;
+        default: return nullptr;
+    }
+}
+
+sphmp_status sphmp_download_field(sphmp_ctx* c, int32_t field, void* host, int32_t n) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!host) return fail(SPHMP_ERR_INVALID_ARG, "host pointer is NULL");
+    if (field < 0 || field >= SPHMP_F_COUNT) return fail(SPHMP_ERR_INVALID_ARG, "unknown field %d", field);
+    size_t count = 0;
+    if (void* arr = sort_array(c, field, &count)) {
+        if (n < 0 || (size_t)n > count) return fail(SPHMP_ERR_CAPACITY, "n %d exceeds %zu entries", n, count);
+        CK(cudaMemcpyAsync(host, arr, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return SPHMP_OK;
+    }
+    if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
+    const int a_cur = c->cur[ALPHA];
+    const int a_pre = c->alpha_advanced ? a_cur ^ 1 : a_cur;
+    const DevParams P = dev_params(c);
+    launch_pack_field(P, c->B, c->cur, field, a_cur, a_pre, c->stage, n, c->stream);
+    CHECK_LAUNCH("pack field");
+    CK(cudaMemcpyAsync(host, c->stage, sizeof(float) * (size_t)field_width(field) * n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, int32_t n) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!host) return fail(SPHMP_ERR_INVALID_ARG, "host pointer is NULL");
+    if (field < 0 || field >= SPHMP_F_COUNT) return fail(SPHMP_ERR_INVALID_ARG, "unknown field %d", field);
+    if (field == SPHMP_F_DENS || field == SPHMP_F_TYPE || field == SPHMP_F_MASS || field == SPHMP_F_BORNID)
+        return fail(SPHMP_ERR_INVALID_ARG, "field %d is download-only (upload it with sphmp_upload_aos)", field);
+    size_t count = 0;
+    if (void* arr = sort_array(c, field, &count)) {
+        if (n < 0 || (size_t)n > count) return fail(SPHMP_ERR_CAPACITY, "n %d exceeds %zu entries", n, count);
+        CK(cudaMemcpyAsync(arr, host, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+        if (field == SPHMP_F_MGRIDCNT) {
+            // rebuild the cell starts (and mgridoff) from the uploaded counts
+            CK(cudaMemcpyAsync(c->B.ccount, c->B.mgridcnt, sizeof(uint32_t) * (size_t)c->prm.gridtotal,
+                               cudaMemcpyDeviceToDevice, c->stream));
+            DevParams P = dev_params(c);
+            const int saved = P.n;
+            P.n = 0;  // scan only: no scatter / cell sort
+            launch_grid_list(P, c->B, c->stream);
+            P.n = saved;
+            // cstart[G+1] must still be n
+            const uint32_t nn = (uint32_t)c->n;
+            CK(cudaMemcpyAsync(c->B.cstart + c->prm.gridtotal + 1, &nn, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+            CHECK_LAUNCH("rebuild cell starts");
+            c->grid_valid = true;
+        }
+        drop_graph(c);
+        CK(cudaStreamSynchronize(c->stream));
+        return SPHMP_OK;
+    }
+    if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
+    if (field == SPHMP_F_ALPHA && !c->alpha_advanced) {
+        // keep the start-of-step fractions in the other buffer, then overwrite the current ones
+        CK(cudaMemcpyAsync(c->B.f4[ALPHA][c->cur[ALPHA] ^ 1], c->B.f4[ALPHA][c->cur[ALPHA]],
+                           sizeof(float4) * (size_t)c->cap, cudaMemcpyDeviceToDevice, c->stream));
+        c->cur[ALPHA] ^= 1;
+        CK(cudaMemcpyAsync(c->B.f4[ALPHA][c->cur[ALPHA]], c->B.f4[ALPHA][c->cur[ALPHA] ^ 1],
+                           sizeof(float4) * (size_t)c->cap, cudaMemcpyDeviceToDevice, c->stream));
+        c->alpha_advanced = true;
+    }
+    const int a_cur = c->cur[ALPHA];
+    const int a_pre = c->alpha_advanced ? a_cur ^ 1 : a_cur;
+    CK(cudaMemcpyAsync(c->stage, host, sizeof(float) * (size_t)field_width(field) * n, cudaMemcpyHostToDevice, c->stream));
+    const DevParams P = dev_params(c);
+    launch_unpack_field(P, c->B, c->cur, field, a_cur, a_pre, c->stage, n, c->stream);
+    CHECK_LAUNCH("unpack field");
+    drop_graph(c);
+    CK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+// ---- per-pass entry points ----
+
+sphmp_status sphmp_get_particle_index(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    launch_hash(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("GetParticleIndex");
+    c->grid_valid = false;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_get_grid_list(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    launch_grid_list(dev_params(c), c->B, c->stream);
+    CHECK_LAUNCH("GetGridList");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_rearrange_data(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    launch_rearrange(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("RearrageData");
+    swap_all(c);
+    c->alpha_advanced = false;
+    c->grid_valid = true;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_compute_boundary_density(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    launch_boundary_volume(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("ComputeBoundaryDensity");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_compute_pressure(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    launch_density(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("MfComputePressure");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_compute_drift_vel(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    launch_force_drift(dev_params(c), c->B, c->cur, false, true, c->stream);
+    CHECK_LAUNCH("MfComputeDriftVel");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_compute_alpha_advance(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    if (c->alpha_advanced)
+        return fail(SPHMP_ERR_STATE, "volume fractions already advanced in this step (re-sort first)");
+    launch_alpha_advance(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("MfComputeAlphaAdvance");
+    c->cur[ALPHA] ^= 1;
+    c->alpha_advanced = true;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_compute_correction(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    const int pre = c->alpha_advanced ? c->cur[ALPHA] ^ 1 : c->cur[ALPHA];
+    launch_correction(dev_params(c), c->B, c->cur, pre, c->stream);
+    CHECK_LAUNCH("MfComputeCorrection");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_compute_force(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    const DevParams P = dev_params(c);
+    launch_force_drift(P, c->B, c->cur, true, false, c->stream);
+    if (P.st_on) launch_surface_tension(P, c->B, c->cur, c->stream);
+    CHECK_LAUNCH("MfComputeForce");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_advance(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    launch_advance(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("MfAdvance");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t use_graph) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (nsteps < 0) return fail(SPHMP_ERR_INVALID_ARG, "nsteps < 0");
+    if (schedule != SPHMP_SCHEDULE_REFERENCE && schedule != SPHMP_SCHEDULE_FUSED)
+        return fail(SPHMP_ERR_INVALID_ARG, "unknown schedule %d", schedule);
+    if (nsteps == 0) return SPHMP_OK;
+    // A fused step leaves every double buffer where it found it, so one captured
+    // step replays for all later steps. The reference schedule flips buffers an
+    // odd number of times per step and runs eagerly.
+    if (use_graph && schedule == SPHMP_SCHEDULE_FUSED) {
+        if (!c->graph || c->graph_n != c->n || c->graph_schedule != schedule) {
+            drop_graph(c);
+            cudaStream_t cap = c->stream;
+            CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            int saved[kNumFloat4Fields];
+            memcpy(saved, c->cur, sizeof(saved));
+            sphmp_status st = enqueue_step(c, schedule);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(cap, &g);
+            if (st) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            if (memcmp(saved, c->cur, sizeof(saved)) != 0) {
+                cudaGraphDestroy(g);
+                return fail(SPHMP_ERR_STATE, "internal: fused step did not restore buffer selectors");
+            }
+            e = cudaGraphInstantiate(&c->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                c->graph = nullptr;
+                return cuda_fail(e, "cudaGraphInstantiate");
+            }
+            c->graph_n = c->n;
+            c->graph_schedule = schedule;
+        }
+        for (int t = 0; t < nsteps; t++) CK(cudaGraphLaunch(c->graph, c->stream));
+        c->alpha_advanced = false;
+        c->grid_valid = true;
+        return SPHMP_OK;
+    }
+    for (int t = 0; t < nsteps; t++)
+        if (sphmp_status st = enqueue_step(c, schedule)) return st;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_conservation(sphmp_ctx* c, double* out, int32_t nout) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!out || nout < 3 + c->prm.nphase) return fail(SPHMP_ERR_INVALID_ARG, "need %d output slots", 3 + c->prm.nphase);
+    const DevParams P = dev_params(c);
+    launch_conservation(P, c->B, c->cur, c->stream);
+    CHECK_LAUNCH("conservation");
+    double red[16];
+    CK(cudaMemcpyAsync(red, c->B.red, sizeof(red), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    out[0] = red[0];
+    out[1] = red[1];
+    for (int k = 0; k < c->prm.nphase; k++) out[2 + k] = red[2 + k];
+    out[2 + c->prm.nphase] = red[5];
+    return SPHMP_OK;
+}
+
+// ===========================================================================
+// Reference entry-point names over a default context
+// ===========================================================================
+
+static sphmp_ctx* g_legacy = nullptr;
+static std::mutex g_legacy_mu;
+
+static void legacy_report(const char* call, sphmp_status st) {
+    if (st != SPHMP_OK) fprintf(stderr, "CUDA ERROR: %s: %s\n", call, g_err.c_str());
+}
+
+static void legacy_run(const char* call, sphmp_status (*fn)(sphmp_ctx*)) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    if (!g_legacy) {
+        fail(SPHMP_ERR_STATE, "FluidSetupCUDA has not been called");
+        legacy_report(call, SPHMP_ERR_STATE);
+        return;
+    }
+    sphmp_status st = fn(g_legacy);
+    if (st == SPHMP_OK) st = sphmp_sync(g_legacy);
+    legacy_report(call, st);
+}
+
+sphmp_ctx* sphmp_legacy_context(void) { return g_legacy; }
+
+void cudaInit(int, char**) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, 0) != cudaSuccess) {
+        fprintf(stderr, "CUDA ERROR: cudaInit: no device\n");
+        return;
+    }
+    printf("-- CUDA --\n");
+    printf("Name:       %s\n", p.name);
+    printf("Revision:   %d.%d\n", p.major, p.minor);
+    printf("Global Mem: %zu\n", p.totalGlobalMem);
+    printf("Shared/Blk: %zu\n", p.sharedMemPerBlock);
+    printf("Regs/Blk:   %d\n", p.regsPerBlock);
+    printf("Warp Size:  %d\n", p.warpSize);
+    printf("Thrds/Blk:  %d\n", p.maxThreadsPerBlock);
+    printf("SMs:        %d\n", p.multiProcessorCount);
+}
+
+void cudaExit(int, char**) {}
+
+void FluidClearCUDA(void) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    sphmp_destroy(g_legacy);
+    g_legacy = nullptr;
+}
+
+void FluidSetupCUDA(const sphmp_params* params) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    if (!params) {
+        fail(SPHMP_ERR_INVALID_ARG, "params is NULL");
+        legacy_report("FluidSetupCUDA", SPHMP_ERR_INVALID_ARG);
+        return;
+    }
+    sphmp_params p;
+    sphmp_params_default(&p);
+    memcpy(&p, params, 464);  // the ParamCarrier prefix
+    p.nphase = SPHMP_MAX_PHASES;
+    sphmp_destroy(g_legacy);
+    g_legacy = nullptr;
+    legacy_report("FluidSetupCUDA", sphmp_create(&p, &g_legacy));
+}
+
+void GetParticleIndexCUDA(void) { legacy_run("InsertParticlesCUDA", sphmp_get_particle_index); }
+void GetGridListCUDA(void) { legacy_run("Sort Grid", sphmp_get_grid_list); }
+void RearrageDataCUDA(void) { legacy_run("Sorting Failed", sphmp_rearrange_data); }
+void MfComputePressureCUDA(void) { legacy_run("MfComputePressureCUDA", sphmp_compute_pressure); }
+void MfComputeDriftVelCUDA(void) { legacy_run("MfComputeDriftVelCUDA", sphmp_compute_drift_vel); }
+void MfComputeAlphaAdvanceCUDA(void) { legacy_run("MfComputeAlphaAdvanceCUDA", sphmp_compute_alpha_advance); }
+void MfComputeCorrectionCUDA(void) { legacy_run("MfComputeCorrectionCUDA", sphmp_compute_correction); }
+void MfComputeForceCUDA(void) { legacy_run("MfComputeForceCUDA", sphmp_compute_force); }
+void MfAdvanceCUDA(void) { legacy_run("MfAdvanceCUDA", sphmp_advance); }
+void ComputeBoundaryDensity(void) { legacy_run("ComputeBoundaryDensity", sphmp_compute_boundary_density); }
+
+void computeNumBlocks(int numPnts, int maxThreads, int* numBlocks, int* numThreads) {
+    int t = numPnts < maxThreads ? numPnts : maxThreads;
+    int b;
+    if (t == 0) b = 1;
+    else b = (numPnts % t != 0) ? (numPnts / t + 1) : (numPnts / t);
+    if (t == 0) t = 1;
+    if (numBlocks) *numBlocks = b;
+    if (numThreads) *numThreads = t;
+}
+
+void TransferToCUDA(const sphmp_display_pack* disp, const sphmp_calc_pack* calc, int n) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    sphmp_status st = g_legacy ? sphmp_upload_aos(g_legacy, disp, calc, n)
+                               : fail(SPHMP_ERR_STATE, "FluidSetupCUDA has not been called");
+    legacy_report("TransferToCUDA", st);
+}
+
+void TransferFromCUDA(sphmp_display_pack* disp, int n) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    sphmp_status st = g_legacy ? sphmp_download_aos(g_legacy, disp, nullptr, n)
+                               : fail(SPHMP_ERR_STATE, "FluidSetupCUDA has not been called");
+    legacy_report("TransferFromCUDA", st);
+}
+
+void EmitUpdateCUDA(int startnum, int endnum, const sphmp_display_pack* disp, const sphmp_calc_pack* calc) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    sphmp_status st = g_legacy ? sphmp_emit_aos(g_legacy, disp ? disp + startnum : nullptr,
+                                                calc ? calc + startnum : nullptr, startnum, endnum)
+                               : fail(SPHMP_ERR_STATE, "FluidSetupCUDA has not been called");
+    legacy_report("EmitUpdateCUDA", st);
+}
+
+}  // extern "C"
+
+// CarryParam(ParamCarrier&) with the reference's C++ linkage.
+struct ParamCarrier;
+void CarryParam(ParamCarrier& hostCarrier) {
+    std::lock_guard<std::mutex> lk(g_legacy_mu);
+    if (!g_legacy) {
+        fail(SPHMP_ERR_STATE, "FluidSetupCUDA has not been called");
+        legacy_report("CarryParam", SPHMP_ERR_STATE);
+        return;
+    }
+    sphmp_params p = g_legacy->prm;
+    memcpy(&p, &hostCarrier, 464);
+    legacy_report("CarryParam", sphmp_set_params(g_legacy, &p));
+}

@@ -1,0 +1,129 @@
+// sphmp_internal.h — device-side data layout and kernel launchers of the
+// GB300 multiphase SPH step (shared by sphmp_kernels.cu and sphmp_api.cu).
+//
+// Particle state lives in HBM as structure-of-arrays in the reference's sorted
+// slot order (stable sort by the reference's linear 2h cell id). Every
+// per-particle array that survives a step is a float4 so neighbour gathers are
+// single 16-byte loads, and each is double-buffered: a pass that moves or
+// advances particles reads buffer `cur` and writes buffer `cur ^ 1`.
+//
+//   pos4   : x, y, z (sim units), w = mass (fluid) or -V_b (boundary volume)
+//   vel4   : vx, vy, vz, visc
+//   vev4   : veleval x, y, z, (unused)
+//   alpha4 : alpha_0, alpha_1, alpha_2, restdens
+//   aprev4 : gravity - total accel of the last advance (x, y, z), w = origin slot
+//            (bits of a uint32: the slot the particle was uploaded to)
+//
+// Per-step arrays (single buffer): densp (1/rho or V_b, pressure), accel4,
+// drift4 (phase-major: drift of phase k for slot i at [k * cap + i]), pmod.
+// Per-origin arrays (never moved): color, bornid, raw calc mass.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sphmp.h"
+
+namespace sphmp {
+
+constexpr uint32_t kUndef = 0xFFFFFFFFu;
+constexpr int kHashBlock = 256;       // threads per hash block (= one chunk for out-of-grid ranks)
+constexpr int kScanBlock = 1024;      // threads per scan block
+constexpr int kScanItems = 4;         // items per thread in the scan
+constexpr int kWarpSortMax = 256;     // cells up to this size are sorted by one warp
+constexpr int kCtaSortMax = 8192;     // larger cells up to this size are sorted by one CTA
+constexpr int kNumFloat4Fields = 5;   // pos4, vel4, vev4, alpha4, aprev4
+
+// Error bits accumulated in the device error word (1 << sphmp_status).
+constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
+constexpr uint32_t kErrType = 1u << SPHMP_ERR_UNSUPPORTED_TYPE;
+constexpr uint32_t kErrNotFinite = 1u << SPHMP_ERR_NOT_FINITE;
+constexpr uint32_t kErrBadMass = 1u << SPHMP_ERR_BAD_MASS;
+
+// Scalars every kernel needs, passed by value.
+struct DevParams {
+    int n;           // active slots
+    int cap;         // capacity (stride of phase-major arrays)
+    int G;           // grid cells
+    int rx, ry, rz;  // grid resolution
+    float gmin[3];
+    float fac[3];    // gridIdfac
+    float srad[3];   // search radius h/simscale in cell units per axis, plus a rounding margin
+    float ss;        // simscale
+    float h, r2;     // smoothing radius and its square
+    float dt;
+    float kpoly6, kspikydiff;
+    float bvisc;
+    float grav[3];
+    int nphase;
+    int multiphase;
+    float dens_k[3], visc_k[3];
+    float relax, sigma, cont, cont1, cont2, pintstiff;
+    int eos;
+    float eos_k;
+    int st_on;
+    float st_K, st_C;
+    int neighborid[27];
+};
+
+struct DevBuffers {
+    float4* f4[kNumFloat4Fields][2];  // pos4, vel4, vev4, alpha4, aprev4 double buffers
+    float2* densp;
+    float4* accel4;
+    float4* drift4;   // [3 * cap]
+    float* pmod;
+    uint32_t* mgcell;   // sorted cell id per slot (unsorted key after the hash)
+    uint32_t* midsort;  // pre-sort slot of each sorted slot
+    uint32_t* mgndx;    // rank in cell
+    int32_t* mgridoff;  // [G]
+    int32_t* mgridcnt;  // [G]
+    uint32_t* key;      // [cap] unsorted cell key per slot
+    uint32_t* arank;    // [cap] rank inside the bin (atomic order; exact for out-of-grid)
+    uint32_t* sidx;     // [cap] scatter target (pre-sort slots grouped by cell)
+    uint32_t* ccount;   // [G + 1] histogram, bin G = out-of-grid
+    uint32_t* cstart;   // [G + 2] exclusive scan of ccount; cstart[G] = in-grid count, cstart[G+1] = n
+    uint32_t* bsum;     // [nblocks] scan block sums
+    uint32_t* uchunk;   // [cap / kHashBlock + 1] out-of-grid count per hash chunk, scanned in place
+    uint32_t* big;      // [cap / (kWarpSortMax+1) + 2]: big[0] = count, then big cell ids
+    float4* color;      // [cap] per origin
+    int32_t* bornid;    // [cap] per origin
+    float* mass_raw;    // [cap] per origin
+    uint32_t* err;      // device error word
+    double* red;        // [16] FP64 reduction results
+    float* vtmp;        // [cap] scratch (boundary volumes)
+};
+
+enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
+
+// ---- launchers (sphmp_kernels.cu) ----
+// All take the current double-buffer selectors in `cur` (one per Field4).
+void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_force_drift(const DevParams& P, const DevBuffers& B, const int* cur, bool force, bool drift,
+                        cudaStream_t s);
+void launch_surface_tension(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// alpha advance: reads alpha4[cur], writes alpha4[cur^1] (new fractions, same restdens)
+void launch_alpha_advance(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// correction: fractions in alpha4[cur[ALPHA]], start-of-step fractions in alpha4[pre]; in place
+void launch_correction(const DevParams& P, const DevBuffers& B, const int* cur, int pre, cudaStream_t s);
+// advance in place on the cur buffers
+void launch_advance(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// fused alpha + correction + advance: reads cur, writes cur^1 for all five float4 fields
+void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+
+// transfers (staging buffers hold reference records)
+void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,
+                       const sphmp_calc_pack* c, int start, int end, cudaStream_t s);
+void launch_pack_aos(const DevParams& P, const DevBuffers& B, const int* cur, sphmp_display_pack* d,
+                     sphmp_calc_pack* c, int n, cudaStream_t s);
+// field pack/unpack through a float/uint32 staging array; `aux` = alpha_pre buffer selector
+void launch_pack_field(const DevParams& P, const DevBuffers& B, const int* cur, int field, int alpha_cur,
+                       int alpha_pre, void* stage, int n, cudaStream_t s);
+void launch_unpack_field(const DevParams& P, const DevBuffers& B, const int* cur, int field, int alpha_cur,
+                         int alpha_pre, const void* stage, int n, cudaStream_t s);
+
+}  // namespace sphmp

@@ -1,0 +1,1217 @@
+// sphmp_kernels.cu — CUDA kernels of the multiphase SPH step for sm_103a.
+//
+// Reference parity notes (ZP-Z/sph-multiphase):
+//  * the hash reproduces InitialSort (SPH_Solver/fluids/fluid_system_kern.cu:36-64)
+//    with the same float operations, so cell ids are bit-identical;
+//  * the sort reproduces thrust::sort_by_key's stable order (fluid_system_host.cu:164-166)
+//    by ranking every cell's members by their pre-sort slot;
+//  * neighbour sums follow the reference formulas (fluid_system_kern.cu:183-424,
+//    multiphase.cu:19-349) in FP32; density and volume-fraction sums are Kahan-
+//    compensated. Only the 8 (of 27) cells that can hold a particle within h are
+//    visited: with cells of 2h the search sphere spans at most two cells per
+//    axis, chosen by which half of its cell the particle sits in.
+//  * the advance reproduces AdvanceParticles (fluid_system_kern.cu:426-534) with
+//    un-contracted float operations, so it is bit-identical given the same accel.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "sphmp_internal.h"
+
+namespace sphmp {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// Kahan-compensated float accumulator.
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ Kahan() : s(0.f), c(0.f) {}
+    __device__ __forceinline__ void add(float y) {
+        float yy = __fsub_rn(y, c);
+        float t = __fadd_rn(s, yy);
+        c = __fsub_rn(__fsub_rn(t, s), yy);
+        s = t;
+    }
+};
+
+// Grid coordinate in cell units, the reference's (pos - gridmin) * gridIdfac.
+__device__ __forceinline__ float grid_t(float p, float gmin, float fac) { return __fmul_rn(__fsub_rn(p, gmin), fac); }
+// int(t) is only defined inside the int range; outside it (and for NaN) the
+// particle is out of the grid.
+__device__ __forceinline__ bool t_ok(float t) { return t > -2147483520.f && t < 2147483520.f; }
+
+__device__ __forceinline__ uint32_t cell_key(const DevParams& P, float x, float y, float z) {
+    const float tx = grid_t(x, P.gmin[0], P.fac[0]);
+    const float ty = grid_t(y, P.gmin[1], P.fac[1]);
+    const float tz = grid_t(z, P.gmin[2], P.fac[2]);
+    if (!(t_ok(tx) && t_ok(ty) && t_ok(tz))) return kUndef;
+    const int gx = __float2int_rz(tx), gy = __float2int_rz(ty), gz = __float2int_rz(tz);
+    if (gx >= 1 && gx < P.rx - 1 && gy >= 1 && gy < P.ry - 1 && gz >= 1 && gz < P.rz - 1)
+        return (uint32_t)((gy * P.rz + gz) * P.rx + gx);
+    return kUndef;
+}
+
+// Visit the candidate slots of an in-grid particle at (x, y, z): along each axis
+// the cells within [t - R, t + R] (R = h in cell units plus a margin), limited
+// to the reference's +-1 cell. Cells along x are adjacent in the sorted order,
+// so each (y, z) row of cells is one contiguous slot range.
+template <class F>
+__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart, float x,
+                                               float y, float z, F&& f) {
+    const float t[3] = {grid_t(x, P.gmin[0], P.fac[0]), grid_t(y, P.gmin[1], P.fac[1]),
+                        grid_t(z, P.gmin[2], P.fac[2])};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int g = __float2int_rz(t[a]);
+        lo[a] = max(g - 1, __float2int_rd(t[a] - P.srad[a]));
+        hi[a] = min(g + 1, __float2int_rd(t[a] + P.srad[a]));
+    }
+    for (int yy = lo[1]; yy <= hi[1]; yy++) {
+        for (int zz = lo[2]; zz <= hi[2]; zz++) {
+            const int base = (yy * P.rz + zz) * P.rx;
+            const uint32_t j0 = __ldg(&cstart[base + lo[0]]);
+            const uint32_t j1 = __ldg(&cstart[base + hi[0] + 1]);
+            for (uint32_t j = j0; j < j1; j++) f(j);
+        }
+    }
+}
+
+__device__ __forceinline__ void set_err(const DevBuffers& B, uint32_t bit) { atomicOr(B.err, bit); }
+
+// ---------------------------------------------------------------------------
+// Hash + histogram (GetParticleIndexCUDA)
+// ---------------------------------------------------------------------------
+
+// One block = one chunk of kHashBlock slots. In-grid slots take a rank inside
+// their cell from a warp-aggregated atomic (the order is fixed later by the
+// cell sort); out-of-grid slots get their exact rank inside the chunk, and the
+// chunk totals are scanned later, which places them in slot order.
+__global__ void __launch_bounds__(kHashBlock) k_hash(const __grid_constant__ DevParams P,
+                                                     const __grid_constant__ DevBuffers B,
+                                                     const float4* __restrict__ pos4) {
+    __shared__ uint32_t wcount[kHashBlock / 32];
+    const int i = blockIdx.x * kHashBlock + threadIdx.x;
+    const bool valid = i < P.n;
+    uint32_t key = kUndef;
+    if (valid) {
+        const float4 p = pos4[i];
+        key = cell_key(P, p.x, p.y, p.z);
+        B.key[i] = key;
+        B.mgcell[i] = key;
+    }
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const bool und = valid && key == kUndef;
+    const unsigned ub = __ballot_sync(0xffffffffu, und);
+    if (lane == 0) wcount[warp] = __popc(ub);
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int nw = kHashBlock / 32;
+        uint32_t v = lane < nw ? wcount[lane] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((int)lane >= o) x += y;
+        }
+        if ((int)lane < nw) wcount[lane] = x - v;
+        if ((int)lane == nw - 1) B.uchunk[blockIdx.x] = x;
+    }
+    __syncthreads();
+    if (und) B.arank[i] = wcount[warp] + __popc(ub & lanemask_lt());
+    const bool in = valid && key != kUndef;
+    const unsigned im = __ballot_sync(0xffffffffu, in);
+    if (in) {
+        const unsigned peers = __match_any_sync(im, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&B.ccount[key], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        B.arank[i] = base + __popc(peers & lanemask_lt());
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Prefix sums (GetGridListCUDA, part 1)
+// ---------------------------------------------------------------------------
+
+// Exclusive scan of one value per thread across a 1024-thread block.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t ws[32];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((int)lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if ((int)lane >= o) w += y;
+        }
+        ws[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t off = warp ? ws[warp - 1] : 0u;
+    *total = ws[31];
+    __syncthreads();
+    return off + x - v;
+}
+
+__device__ __forceinline__ void load4(const uint32_t* in, int len, int idx, uint32_t v[4]) {
+    if (idx + 3 < len && ((reinterpret_cast<uintptr_t>(in + idx) & 15u) == 0)) {
+        const uint4 q = *reinterpret_cast<const uint4*>(in + idx);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) v[k] = (idx + k < len) ? in[idx + k] : 0u;
+    }
+}
+
+// Phase A: block sums of the cell histogram.
+__global__ void __launch_bounds__(kScanBlock) k_scan_reduce(const __grid_constant__ DevParams P,
+                                                            const __grid_constant__ DevBuffers B) {
+    const int idx = (blockIdx.x * kScanBlock + threadIdx.x) * kScanItems;
+    uint32_t v[4];
+    load4(B.ccount, P.G, idx, v);
+    uint32_t total;
+    block_excl_scan(v[0] + v[1] + v[2] + v[3], &total);
+    if (threadIdx.x == 0) B.bsum[blockIdx.x] = total;
+}
+
+// Phase B: one block scans the block sums and the out-of-grid chunk counts.
+__global__ void __launch_bounds__(kScanBlock) k_scan_top(const __grid_constant__ DevParams P,
+                                                         const __grid_constant__ DevBuffers B, int nblocks,
+                                                         int nchunks) {
+    uint32_t carry = 0;
+    for (int base = 0; base < nblocks; base += kScanBlock) {
+        const int k = base + threadIdx.x;
+        const uint32_t v = k < nblocks ? B.bsum[k] : 0u;
+        uint32_t total;
+        const uint32_t e = block_excl_scan(v, &total);
+        if (k < nblocks) B.bsum[k] = carry + e;
+        carry += total;
+    }
+    const uint32_t nin = carry;
+    carry = 0;
+    for (int base = 0; base < nchunks; base += kScanBlock) {
+        const int k = base + threadIdx.x;
+        const uint32_t v = k < nchunks ? B.uchunk[k] : 0u;
+        uint32_t total;
+        const uint32_t e = block_excl_scan(v, &total);
+        if (k < nchunks) B.uchunk[k] = carry + e;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        B.cstart[P.G] = nin;
+        B.cstart[P.G + 1] = (uint32_t)P.n;
+        B.big[0] = 0u;
+    }
+}
+
+// Phase C: cell starts, the reference's mgridoff / mgridcnt, and the list of
+// cells too large for the warp sort.
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(const __grid_constant__ DevParams P,
+                                                           const __grid_constant__ DevBuffers B) {
+    const int idx = (blockIdx.x * kScanBlock + threadIdx.x) * kScanItems;
+    uint32_t v[4];
+    load4(B.ccount, P.G, idx, v);
+    uint32_t total;
+    uint32_t run = B.bsum[blockIdx.x] + block_excl_scan(v[0] + v[1] + v[2] + v[3], &total);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int c = idx + k;
+        if (c < P.G) {
+            B.cstart[c] = run;
+            B.mgridoff[c] = v[k] ? (int32_t)run : 0;
+            B.mgridcnt[c] = (int32_t)v[k];
+            if (v[k] > (uint32_t)kWarpSortMax) {
+                if (v[k] > (uint32_t)kCtaSortMax) set_err(B, kErrCellOverflow);
+                else {
+                    const uint32_t slot = atomicAdd(&B.big[0], 1u);
+                    B.big[1 + slot] = (uint32_t)c;
+                }
+            }
+        }
+        run += v[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scatter + per-cell stable order (GetGridListCUDA, part 2)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) k_scatter(const __grid_constant__ DevParams P,
+                                                      const __grid_constant__ DevBuffers B) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= P.n) return;
+    const uint32_t key = B.key[i];
+    const uint32_t r = B.arank[i];
+    if (key != kUndef) {
+        B.sidx[B.cstart[key] + r] = (uint32_t)i;
+    } else {
+        const uint32_t d = B.cstart[P.G] + B.uchunk[i / kHashBlock] + r;
+        B.midsort[d] = (uint32_t)i;
+        B.mgcell[d] = kUndef;
+        B.mgndx[d] = kUndef;
+    }
+}
+
+// Bitonic sort of 32*E keys held E per lane (element index = lane*E + r),
+// ascending, entirely in registers.
+template <int E>
+__device__ __forceinline__ void warp_bitonic(uint32_t (&v)[E]) {
+    const unsigned lane = lane_id();
+    constexpr int M = 32 * E;
+#pragma unroll
+    for (int k = 2; k <= M; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= E) {
+                const int lj = j / E;
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, v[r], lj);
+                    const unsigned idx = lane * E + r;
+                    const bool asc = (idx & k) == 0;
+                    const bool lower = (idx & j) == 0;
+                    const uint32_t mn = min(v[r], o), mx = max(v[r], o);
+                    v[r] = (lower == asc) ? mn : mx;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const int p = r ^ j;
+                    if (p > r) {
+                        const unsigned idx = lane * E + r;
+                        const bool asc = (idx & k) == 0;
+                        const uint32_t a = v[r], b = v[p];
+                        const bool sw = asc ? (a > b) : (a < b);
+                        v[r] = sw ? b : a;
+                        v[p] = sw ? a : b;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void warp_sort_cell(const DevBuffers& B, uint32_t c, uint32_t start, uint32_t cnt) {
+    uint32_t v[E];
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const uint32_t idx = lane * E + r;
+        v[r] = idx < cnt ? B.sidx[start + idx] : 0xFFFFFFFFu;
+    }
+    warp_bitonic<E>(v);
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const uint32_t idx = lane * E + r;
+        if (idx < cnt) {
+            B.midsort[start + idx] = v[r];
+            B.mgcell[start + idx] = c;
+            B.mgndx[start + idx] = idx;
+        }
+    }
+}
+
+// One warp per cell (cells of up to kWarpSortMax members).
+__global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ DevParams P,
+                                                        const __grid_constant__ DevBuffers B) {
+    const int nwarps = (gridDim.x * kThreads) >> 5;
+    for (int c = (blockIdx.x * kThreads + threadIdx.x) >> 5; c < P.G; c += nwarps) {
+        const uint32_t start = B.cstart[c];
+        const uint32_t cnt = B.cstart[c + 1] - start;
+        if (cnt == 0 || cnt > (uint32_t)kWarpSortMax) continue;
+        if (cnt <= 32) warp_sort_cell<1>(B, c, start, cnt);
+        else if (cnt <= 64) warp_sort_cell<2>(B, c, start, cnt);
+        else if (cnt <= 128) warp_sort_cell<4>(B, c, start, cnt);
+        else warp_sort_cell<8>(B, c, start, cnt);
+    }
+}
+
+// One CTA per large cell (kWarpSortMax < members <= kCtaSortMax): bitonic sort in shared memory.
+__global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ DevParams P,
+                                                        const __grid_constant__ DevBuffers B) {
+    __shared__ uint32_t sm[kCtaSortMax];
+    const uint32_t nbig = B.big[0];
+    for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+        const uint32_t c = B.big[1 + b];
+        const uint32_t start = B.cstart[c];
+        const uint32_t cnt = B.cstart[c + 1] - start;
+        uint32_t M = 1;
+        while (M < cnt) M <<= 1;
+        for (uint32_t k = threadIdx.x; k < M; k += blockDim.x) sm[k] = k < cnt ? B.sidx[start + k] : 0xFFFFFFFFu;
+        __syncthreads();
+        for (uint32_t k = 2; k <= M; k <<= 1) {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t t = threadIdx.x; t < M; t += blockDim.x) {
+                    const uint32_t p = t ^ j;
+                    if (p > t) {
+                        const bool asc = (t & k) == 0;
+                        const uint32_t a = sm[t], q = sm[p];
+                        if (asc ? (a > q) : (a < q)) { sm[t] = q; sm[p] = a; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
+            B.midsort[start + k] = sm[k];
+            B.mgcell[start + k] = c;
+            B.mgndx[start + k] = k;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reorder (RearrageDataCUDA)
+// ---------------------------------------------------------------------------
+
+struct F4Set {
+    const float4* __restrict__ in[kNumFloat4Fields];
+    float4* __restrict__ out[kNumFloat4Fields];
+};
+
+__global__ void __launch_bounds__(kThreads) k_rearrange(const __grid_constant__ DevParams P,
+                                                        const __grid_constant__ DevBuffers B,
+                                                        const __grid_constant__ F4Set S) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    const bool undef = B.mgcell[s] == kUndef;
+    const uint32_t src = undef ? (uint32_t)s : B.midsort[s];
+#pragma unroll
+    for (int f = 0; f < kNumFloat4Fields; f++) {
+        float4 v = S.in[f][src];
+        if (f == POS && undef) { v.x = -1000.f; v.y = -1000.f; v.z = -1000.f; }
+        S.out[f][s] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary volume (ComputeBoundaryDensity)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) k_boundary_volume(const __grid_constant__ DevParams P,
+                                                              const __grid_constant__ DevBuffers B,
+                                                              const float4* __restrict__ pos4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    const float4 pi = pos4[s];
+    if (!(pi.w < 0.f)) return;
+    Kahan sum;
+    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        if (!(pj.w < 0.f)) return;
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (dsq < P.r2) {
+            const float c = P.r2 - dsq;
+            sum.add(c * c * c);
+        }
+    });
+    float v = sum.s * P.kpoly6;
+    if (v == 0.f) v = 1.f;
+    B.vtmp[s] = 1.f / v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid_constant__ DevParams P,
+                                                                    const __grid_constant__ DevBuffers B,
+                                                                    float4* __restrict__ pos4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    float4 p = pos4[s];
+    if (!(p.w < 0.f)) return;
+    p.w = -B.vtmp[s];
+    pos4[s] = p;
+    B.densp[s] = make_float2(-p.w, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Density + EOS pressure (MfComputePressureCUDA)
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ DevParams P,
+                                                      const __grid_constant__ DevBuffers B,
+                                                      const float4* __restrict__ pos4,
+                                                      const float4* __restrict__ alpha4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    const float4 pi = pos4[s];
+    if (pi.w < 0.f) {  // boundary: carries its volume, no pressure
+        B.densp[s] = make_float2(-pi.w, 0.f);
+        return;
+    }
+    const float rho0 = alpha4[s].w;
+    Kahan sum;
+    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (dsq < P.r2) {
+            const float c = P.r2 - dsq;
+            const float m = pj.w > 0.f ? pj.w : rho0 * (-pj.w);
+            sum.add(c * c * c * m);
+        }
+    });
+    float rho = sum.s * P.kpoly6;
+    if (rho == 0.f) rho = 1.f;
+    float p;
+    if (P.eos == SPHMP_EOS_LINEAR) p = P.eos_k * (rho - rho0);
+    else p = 2.5f * rho0 * (powf(rho / rho0, 7.0f) - 1.0f);
+    if (p < 0.f) p = 0.f;
+    B.densp[s] = make_float2(1.f / rho, p);
+}
+
+// ---------------------------------------------------------------------------
+// Force + drift velocity (MfComputeForceCUDA, MfComputeDriftVelCUDA)
+// ---------------------------------------------------------------------------
+
+template <bool FORCE, bool DRIFT, int NP>
+__global__ void __launch_bounds__(kThreads) k_force_drift(const __grid_constant__ DevParams P,
+                                                          const __grid_constant__ DevBuffers B,
+                                                          const float4* __restrict__ pos4,
+                                                          const float4* __restrict__ vel4,
+                                                          const float4* __restrict__ alpha4,
+                                                          const float4* __restrict__ aprev4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    const float4 pi = pos4[s];
+    if (pi.w < 0.f) {
+        if (FORCE) B.accel4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float4 vi = vel4[s];
+    const float2 dpi = B.densp[s];
+    const float4 ai = alpha4[s];
+    const float idens = dpi.x, ipress = dpi.y, ivisc = vi.w, rho0 = ai.w;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    float ia[3] = {ai.x, ai.y, ai.z};
+    float mc[NP > 0 ? NP : 1];
+    float3 dv[NP > 0 ? NP : 1], ag[NP > 0 ? NP : 1];
+    float relax_coef = 0.f, invdens = 0.f;
+    if (DRIFT) {
+        relax_coef = P.relax / ivisc;
+        invdens = 1.f / rho0;
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            mc[k] = ia[k] * P.dens_k[k] * invdens;
+            dv[k] = make_float3(0.f, 0.f, 0.f);
+            ag[k] = make_float3(0.f, 0.f, 0.f);
+        }
+    }
+    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (!(dsq < P.r2 && dsq > 0.f)) return;
+        const float r = sqrtf(dsq);
+        const float c = P.h - r;
+        const float g1 = P.kspikydiff * c * c / r;
+        if (pj.w > 0.f) {  // fluid neighbour
+            const float2 dpj = __ldg(&B.densp[j]);
+            const float g = g1 * pj.w * dpj.x;
+            if (FORCE) {
+                const float4 vj = __ldg(&vel4[j]);
+                const float pm = -0.5f * g * dpj.y * idens;
+                fx += dx * pm; fy += dy * pm; fz += dz * pm;
+                const float vm = g * (ivisc + vj.w) * idens;
+                fx += (vi.x - vj.x) * vm; fy += (vi.y - vj.y) * vm; fz += (vi.z - vj.z) * vm;
+            }
+            if (DRIFT) {
+                const float4 aj = __ldg(&alpha4[j]);
+                const float ja[3] = {aj.x, aj.y, aj.z};
+                float3 pg[NP > 0 ? NP : 1];
+                float3 psum = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    const float pm = g * (-ia[k] * ipress + ja[k] * dpj.y);
+                    pg[k] = make_float3(pm * dx, pm * dy, pm * dz);
+                    psum.x += pg[k].x * mc[k]; psum.y += pg[k].y * mc[k]; psum.z += pg[k].z * mc[k];
+                    const float ga = (ja[k] - ia[k]) * g;
+                    ag[k].x += ga * dx; ag[k].y += ga * dy; ag[k].z += ga * dz;
+                }
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    dv[k].x -= relax_coef * (pg[k].x - psum.x);
+                    dv[k].y -= relax_coef * (pg[k].y - psum.y);
+                    dv[k].z -= relax_coef * (pg[k].z - psum.z);
+                }
+            }
+        } else if (FORCE) {  // boundary neighbour, volume V_j = -w
+            const float V = -pj.w;
+            const float4 vj = __ldg(&vel4[j]);
+            const float pm = -g1 * rho0 * V * ipress * idens * idens;
+            fx += dx * pm; fy += dy * pm; fz += dz * pm;
+            float pij = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            if (pij < 0.f) {
+                pij = pij / (dsq + P.r2 * 0.01f);
+                pij = pij * P.bvisc * P.h / 2.f / rho0;
+                pij = g1 * rho0 * V * pij;
+                fx += dx * pij; fy += dy * pij; fz += dz * pij;
+            }
+        }
+    });
+    if (FORCE) B.accel4[s] = make_float4(fx, fy, fz, 0.f);
+    if (DRIFT) {
+        const float4 ap = aprev4[s];
+        const float cc = P.cont * P.cont2;
+        const float cs = P.cont * P.cont1 * P.sigma;
+        float3 out[NP > 0 ? NP : 1], st[NP > 0 ? NP : 1];
+        float dsum = 0.f;
+        float3 ssum = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            out[k] = make_float3(cc * dv[k].x, cc * dv[k].y, cc * dv[k].z);
+            const float temp = ia[k];
+            dsum += temp * P.dens_k[k] * P.dens_k[k] * invdens;
+            // `temp > 0.0001` in double is exactly `temp > 1e-4f` in float
+            st[k] = temp > 1e-4f ? make_float3(ag[k].x / temp, ag[k].y / temp, ag[k].z / temp)
+                                 : make_float3(0.f, 0.f, 0.f);
+            ssum.x += st[k].x * temp * P.dens_k[k] * invdens;
+            ssum.y += st[k].y * temp * P.dens_k[k] * invdens;
+            ssum.z += st[k].z * temp * P.dens_k[k] * invdens;
+        }
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const float tdiff = (P.dens_k[k] - dsum) * relax_coef;
+            out[k].x += ap.x * tdiff; out[k].y += ap.y * tdiff; out[k].z += ap.z * tdiff;
+            out[k].x -= cs * (st[k].x - ssum.x);
+            out[k].y -= cs * (st[k].y - ssum.y);
+            out[k].z -= cs * (st[k].z - ssum.z);
+            B.drift4[(size_t)k * P.cap + s] = make_float4(out[k].x, out[k].y, out[k].z, 0.f);
+        }
+    }
+}
+
+// Surface tension (reference SurfaceTension, fluid_system_kern.cu:569-625): all
+// 27 cells, squared distance compared with the radius K*h, added to accel.
+__global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_constant__ DevParams P,
+                                                              const __grid_constant__ DevBuffers B,
+                                                              const float4* __restrict__ pos4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    const uint32_t gc = B.mgcell[s];
+    if (gc == kUndef) return;
+    const float4 pi = pos4[s];
+    const float tR = sqrtf(P.st_K * P.st_K * (P.h * P.h));
+    float rx = 0.f, ry = 0.f, rz = 0.f;
+    for (int c = 0; c < 27; c++) {
+        const uint32_t cell = gc + (uint32_t)P.neighborid[c];
+        const uint32_t j0 = B.cstart[cell], j1 = B.cstart[cell + 1];
+        for (uint32_t j = j0; j < j1; j++) {
+            const float4 pj = __ldg(&pos4[j]);
+            const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+            float dsq = dx * dx + dy * dy + dz * dz;
+            if (dsq != 0.f && dsq <= tR) {
+                dsq = sqrtf(dsq);
+                const float fm = P.st_C * cosf(1.5f * 3.14159f * dsq / tR) / dsq;
+                rx += dx * fm; ry += dy * fm; rz += dz * fm;
+            }
+        }
+    }
+    float4 a = B.accel4[s];
+    a.x += rx; a.y += ry; a.z += rz;
+    B.accel4[s] = a;
+}
+
+// ---------------------------------------------------------------------------
+// Volume-fraction advance, correction, advection
+// ---------------------------------------------------------------------------
+
+// Sum of the alpha change over the neighbours of an in-grid fluid particle
+// (contributeAlphaChange, multiphase.cu:169-216), Kahan-compensated per phase.
+template <int NP>
+__device__ __forceinline__ void alpha_change(const DevParams& P, const DevBuffers& B, const float4* __restrict__ pos4,
+                                             const float4* __restrict__ vev4, const float4* __restrict__ alpha4,
+                                             int s, const float4 pi, const float4 vei, const float (&ia)[3],
+                                             float (&change)[3]) {
+    float3 um[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        const float4 u = B.drift4[(size_t)k * P.cap + s];
+        um[k] = make_float3(u.x, u.y, u.z);
+    }
+    Kahan acc[NP];
+    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        if (pj.w < 0.f) return;  // boundary neighbours do not exchange volume fraction
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (!(dsq < P.r2 && dsq > 0.f)) return;
+        const float r = sqrtf(dsq);
+        const float c = P.h - r;
+        const float2 dpj = __ldg(&B.densp[j]);
+        const float cm = P.kspikydiff * c * c / r * pj.w * dpj.x;
+        const float4 vej = __ldg(&vev4[j]);
+        const float dot1 = (vej.x - vei.x) * dx + (vej.y - vei.y) * dy + (vej.z - vei.z) * dz;
+        const float4 aj = __ldg(&alpha4[j]);
+        const float ja[3] = {aj.x, aj.y, aj.z};
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const float4 uj = __ldg(&B.drift4[(size_t)k * P.cap + j]);
+            acc[k].add(-(0.5f * cm * (ja[k] + ia[k]) * dot1));
+            const float vx = ja[k] * uj.x + ia[k] * um[k].x;
+            const float vy = ja[k] * uj.y + ia[k] * um[k].y;
+            const float vz = ja[k] * uj.z + ia[k] * um[k].z;
+            acc[k].add(-(cm * (vx * dx + vy * dy + vz * dz)));
+        }
+    });
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        float ch = acc[k].s * P.dt;
+        // `ch < -0.99` in double is exactly `ch <= -0.99f` in float
+        if (ch <= -0.99f) ch = -0.99f;
+        change[k] = ch + ia[k];
+    }
+}
+
+// mfComputeCorrection (multiphase.cu:275-349) for one particle. `a` holds the
+// advanced fractions on entry and the corrected ones on exit; `apre` are the
+// start-of-step fractions (argmax fallback).
+template <int NP>
+__device__ __forceinline__ void correct(const DevParams& P, float (&a)[3], const float (&apre)[3], float dens,
+                                        float rho0, float& pmod, float& newrho0, float& newvisc) {
+    float before[3];
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        before[k] = a[k];
+        if (a[k] < 0.f) a[k] = 0.f;
+        sum += a[k];
+    }
+    const bool flag = sum > 0.f;
+    if (!flag) sum = 1.f;
+    int maxcat = 0;
+#pragma unroll
+    for (int k = 1; k < NP; k++)
+        if (apre[k] > apre[maxcat]) maxcat = k;
+    const float inv = 1.f / sum;
+    const float x = 1.f / (dens * rho0);
+    const float coef = -(6.f * powf(x, 7.0f) + 1.f) * P.pintstiff;
+    float pm = 0.f;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        a[k] = flag ? a[k] * inv : (k == maxcat ? 1.f : 0.f);
+        pm += coef * P.dens_k[k] * (a[k] - before[k]);
+    }
+    float nd = 0.f, nv = 0.f;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        nd += a[k] * P.dens_k[k];
+        nv += a[k] * P.visc_k[k];
+    }
+    pmod = pm;
+    newrho0 = nd;
+    newvisc = nv;
+}
+
+// AdvanceParticles (fluid_system_kern.cu:426-534) for one in-grid non-boundary
+// particle, with un-contracted float operations in the reference's order.
+__device__ __forceinline__ void advance_one(const DevParams& P, float4& p, float4& v, float4& ve, float4& ap,
+                                            const float4 acc) {
+    const float a[3] = {__fadd_rn(acc.x, P.grav[0]), __fadd_rn(acc.y, P.grav[1]), __fadd_rn(acc.z, P.grav[2])};
+    float* pp[3] = {&p.x, &p.y, &p.z};
+    float* vv[3] = {&v.x, &v.y, &v.z};
+    float* ee[3] = {&ve.x, &ve.y, &ve.z};
+    float* aa[3] = {&ap.x, &ap.y, &ap.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float v0 = *vv[k];
+        const float vn = __fadd_rn(__fmul_rn(a[k], P.dt), v0);
+        *pp[k] = __fadd_rn(*pp[k], __fdiv_rn(__fmul_rn(vn, P.dt), P.ss));
+        *ee[k] = __fmul_rn(__fadd_rn(v0, vn), 0.5f);
+        *vv[k] = vn;
+        *aa[k] = __fsub_rn(P.grav[k], a[k]);
+    }
+}
+
+// Separate alpha advance: new fractions into alpha4 out (restdens copied).
+template <int NP>
+__global__ void __launch_bounds__(kThreads) k_alpha_advance(const __grid_constant__ DevParams P,
+                                                            const __grid_constant__ DevBuffers B,
+                                                            const float4* __restrict__ pos4,
+                                                            const float4* __restrict__ vev4,
+                                                            const float4* __restrict__ alpha_in,
+                                                            float4* __restrict__ alpha_out) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    const float4 ai = alpha_in[s];
+    const float4 pi = pos4[s];
+    if (B.mgcell[s] == kUndef || pi.w < 0.f) {
+        alpha_out[s] = ai;
+        return;
+    }
+    const float ia[3] = {ai.x, ai.y, ai.z};
+    float na[3] = {ai.x, ai.y, ai.z};
+    alpha_change<NP>(P, B, pos4, vev4, alpha_in, s, pi, vev4[s], ia, na);
+    alpha_out[s] = make_float4(na[0], na[1], na[2], ai.w);
+}
+
+// Separate correction, in place: fractions in alpha_cur, start-of-step in alpha_pre.
+template <int NP>
+__global__ void __launch_bounds__(kThreads) k_correction(const __grid_constant__ DevParams P,
+                                                         const __grid_constant__ DevBuffers B,
+                                                         float4* alpha_cur, const float4* alpha_pre,
+                                                         float4* __restrict__ vel4,
+                                                         const float4* __restrict__ pos4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    if (B.mgcell[s] == kUndef || pos4[s].w < 0.f) return;
+    const float4 ac = alpha_cur[s];
+    const float4 ap = alpha_pre[s];
+    float a[3] = {ac.x, ac.y, ac.z};
+    const float apre[3] = {ap.x, ap.y, ap.z};
+    float pmod, nr, nv;
+    correct<NP>(P, a, apre, B.densp[s].x, ac.w, pmod, nr, nv);
+    alpha_cur[s] = make_float4(a[0], a[1], a[2], nr);
+    float4 v = vel4[s];
+    v.w = nv;
+    vel4[s] = v;
+    B.pmod[s] = pmod;
+}
+
+// Separate advance, in place.
+__global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ DevParams P,
+                                                      const __grid_constant__ DevBuffers B, float4* pos4,
+                                                      float4* vel4, float4* vev4, float4* aprev4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    float4 p = pos4[s];
+    if (p.w < 0.f) return;
+    float4 v = vel4[s];
+    if (B.mgcell[s] == kUndef) {
+        p.x = -1000.f; p.y = -1000.f; p.z = -1000.f;
+        v.x = 0.f; v.y = 0.f; v.z = 0.f;
+        pos4[s] = p;
+        vel4[s] = v;
+        return;
+    }
+    float4 ve = vev4[s], ap = aprev4[s];
+    advance_one(P, p, v, ve, ap, B.accel4[s]);
+    pos4[s] = p;
+    vel4[s] = v;
+    vev4[s] = ve;
+    aprev4[s] = ap;
+}
+
+// Fused alpha advance + correction + advance: reads the cur buffers, writes
+// every float4 field of every slot into the other buffer.
+template <int NP, bool MP>
+__global__ void __launch_bounds__(kThreads) k_pass_c(const __grid_constant__ DevParams P,
+                                                     const __grid_constant__ DevBuffers B,
+                                                     const __grid_constant__ F4Set S) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    float4 p = S.in[POS][s], v = S.in[VEL][s], ve = S.in[VEV][s], al = S.in[ALPHA][s], ap = S.in[APREV][s];
+    if (!(p.w < 0.f)) {
+        if (B.mgcell[s] == kUndef) {
+            p.x = -1000.f; p.y = -1000.f; p.z = -1000.f;
+            v.x = 0.f; v.y = 0.f; v.z = 0.f;
+        } else {
+            if (MP) {
+                const float ia[3] = {al.x, al.y, al.z};
+                float a[3] = {al.x, al.y, al.z};
+                alpha_change<NP>(P, B, S.in[POS], S.in[VEV], S.in[ALPHA], s, p, ve, ia, a);
+                float pmod, nr, nv;
+                correct<NP>(P, a, ia, B.densp[s].x, al.w, pmod, nr, nv);
+                al = make_float4(a[0], a[1], a[2], nr);
+                v.w = nv;
+                B.pmod[s] = pmod;
+            }
+            advance_one(P, p, v, ve, ap, B.accel4[s]);
+        }
+    }
+    S.out[POS][s] = p;
+    S.out[VEL][s] = v;
+    S.out[VEV][s] = ve;
+    S.out[ALPHA][s] = al;
+    S.out[APREV][s] = ap;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 conservation sums
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_conservation(const __grid_constant__ DevParams P,
+                                                           const __grid_constant__ DevBuffers B,
+                                                           const float4* __restrict__ pos4,
+                                                           const float4* __restrict__ alpha4) {
+    __shared__ double sh[6][kThreads / 32];
+    double acc[6] = {0, 0, 0, 0, 0, 0};  // mass, volume, vol_k (3), max |sum alpha - 1|
+    for (int s = blockIdx.x * kThreads + threadIdx.x; s < P.n; s += gridDim.x * kThreads) {
+        if (B.mgcell[s] == kUndef) continue;
+        const float4 p = pos4[s];
+        if (p.w < 0.f) continue;
+        const double m = p.w;
+        const double vol = m * (double)B.densp[s].x;
+        const float4 a = alpha4[s];
+        const float al[3] = {a.x, a.y, a.z};
+        acc[0] += m;
+        acc[1] += vol;
+        double sa = 0.0;
+        for (int k = 0; k < P.nphase; k++) {
+            acc[2 + k] += (double)al[k] * vol;
+            sa += (double)al[k];
+        }
+        acc[5] = fmax(acc[5], fabs(sa - 1.0));
+    }
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        const double v = warp_sum_d(acc[q]);
+        if (lane == 0) sh[q][warp] = v;
+    }
+    double mx = acc[5];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) sh[5][warp] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 5; q++) {
+            double t = 0.0;
+            for (int w = 0; w < kThreads / 32; w++) t += sh[q][w];
+            atomicAdd(&B.red[q], t);
+        }
+        double m = 0.0;
+        for (int w = 0; w < kThreads / 32; w++) m = fmax(m, sh[5][w]);
+        atomicMax(reinterpret_cast<unsigned long long*>(&B.red[5]), (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Transfers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool finite3(float x, float y, float z) { return isfinite(x) && isfinite(y) && isfinite(z); }
+
+__global__ void __launch_bounds__(kThreads) k_unpack_aos(const __grid_constant__ DevParams P,
+                                                         const __grid_constant__ DevBuffers B,
+                                                         const __grid_constant__ F4Set S,
+                                                         const sphmp_display_pack* __restrict__ disp,
+                                                         const sphmp_calc_pack* __restrict__ calc, int start,
+                                                         int end) {
+    const int i = start + blockIdx.x * kThreads + threadIdx.x;
+    if (i >= end) return;
+    const sphmp_display_pack d = disp[i - start];
+    const sphmp_calc_pack& c = calc[i - start];
+    int type = d.type;
+    if (type != SPHMP_TYPE_FLUID && type != SPHMP_TYPE_BOUNDARY) {
+        set_err(B, kErrType);
+        type = SPHMP_TYPE_FLUID;
+    }
+    if (!finite3(d.pos[0], d.pos[1], d.pos[2])) set_err(B, kErrNotFinite);
+    float w;
+    if (type == SPHMP_TYPE_BOUNDARY) {
+        w = -fabsf(c.dens);
+        if (!(w < 0.f)) w = -1.f;  // a boundary needs a negative tag; the volume pass sets the value
+    } else {
+        w = c.mass;
+        if (!(w > 0.f) || !isfinite(w)) {
+            set_err(B, kErrBadMass);
+            w = 1.f;
+        }
+    }
+    S.out[POS][i] = make_float4(d.pos[0], d.pos[1], d.pos[2], w);
+    S.out[VEL][i] = make_float4(c.vel[0], c.vel[1], c.vel[2], c.visc);
+    S.out[VEV][i] = make_float4(c.veleval[0], c.veleval[1], c.veleval[2], 0.f);
+    // one-hot volume fraction at the first phase whose rest density matches
+    int ph = 0;
+    for (int k = 0; k < P.nphase; k++)
+        if (P.dens_k[k] == c.restdens) { ph = k; break; }
+    S.out[ALPHA][i] = make_float4(ph == 0 ? 1.f : 0.f, ph == 1 ? 1.f : 0.f, ph == 2 ? 1.f : 0.f, c.restdens);
+    S.out[APREV][i] = make_float4(0.f, 0.f, 0.f, __uint_as_float((uint32_t)i));
+    B.densp[i] = make_float2(c.dens, c.pressure);
+    B.accel4[i] = make_float4(c.accel[0], c.accel[1], c.accel[2], 0.f);
+    B.color[i] = make_float4(d.color[0], d.color[1], d.color[2], d.color[3]);
+    B.bornid[i] = c.bornid;
+    B.mass_raw[i] = c.mass;
+}
+
+__global__ void __launch_bounds__(kThreads) k_pack_aos(const __grid_constant__ DevParams P,
+                                                       const __grid_constant__ DevBuffers B,
+                                                       const __grid_constant__ F4Set S, sphmp_display_pack* disp,
+                                                       sphmp_calc_pack* calc, int n) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = S.in[POS][i];
+    const uint32_t o = __float_as_uint(S.in[APREV][i].w);
+    const bool bnd = p.w < 0.f;
+    const float4 col = B.color[o];
+    sphmp_display_pack d;
+    d.pos[0] = p.x; d.pos[1] = p.y; d.pos[2] = p.z;
+    d.color[0] = col.x; d.color[1] = col.y; d.color[2] = col.z; d.color[3] = col.w;
+    d.type = bnd ? SPHMP_TYPE_BOUNDARY : SPHMP_TYPE_FLUID;
+    disp[i] = d;
+    if (calc == nullptr) return;
+    const float4 v = S.in[VEL][i], ve = S.in[VEV][i], al = S.in[ALPHA][i];
+    const float2 dp = B.densp[i];
+    const float4 ac = B.accel4[i];
+    sphmp_calc_pack c;
+    float* raw = reinterpret_cast<float*>(&c);
+    for (int k = 0; k < (int)(sizeof(sphmp_calc_pack) / 4); k++) raw[k] = 0.f;
+    c.vel[0] = v.x; c.vel[1] = v.y; c.vel[2] = v.z;
+    c.veleval[0] = ve.x; c.veleval[1] = ve.y; c.veleval[2] = ve.z;
+    c.pressure = bnd ? 0.f : dp.y;
+    c.dens = bnd ? -p.w : dp.x;
+    c.restdens = al.w;
+    c.mass = B.mass_raw[o];
+    c.visc = v.w;
+    c.bornid = B.bornid[o];
+    c.accel[0] = ac.x; c.accel[1] = ac.y; c.accel[2] = ac.z;
+    calc[i] = c;
+}
+
+__global__ void __launch_bounds__(kThreads) k_pack_field(const __grid_constant__ DevParams P,
+                                                         const __grid_constant__ DevBuffers B,
+                                                         const __grid_constant__ F4Set S, int field,
+                                                         const float4* __restrict__ alpha_c,
+                                                         const float4* __restrict__ alpha_p, void* stage, int n) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    float* f = reinterpret_cast<float*>(stage);
+    int32_t* q = reinterpret_cast<int32_t*>(stage);
+    const float4 p = S.in[POS][i];
+    const uint32_t o = __float_as_uint(S.in[APREV][i].w);
+    switch (field) {
+        case SPHMP_F_POS: f[3 * i] = p.x; f[3 * i + 1] = p.y; f[3 * i + 2] = p.z; break;
+        case SPHMP_F_VEL: { const float4 v = S.in[VEL][i]; f[3 * i] = v.x; f[3 * i + 1] = v.y; f[3 * i + 2] = v.z; } break;
+        case SPHMP_F_VELEVAL: { const float4 v = S.in[VEV][i]; f[3 * i] = v.x; f[3 * i + 1] = v.y; f[3 * i + 2] = v.z; } break;
+        case SPHMP_F_PRESSURE: f[i] = p.w < 0.f ? 0.f : B.densp[i].y; break;
+        case SPHMP_F_DENS: f[i] = p.w < 0.f ? -p.w : B.densp[i].x; break;
+        case SPHMP_F_RESTDENS: f[i] = alpha_c[i].w; break;
+        case SPHMP_F_VISC: f[i] = S.in[VEL][i].w; break;
+        case SPHMP_F_ACCEL: { const float4 a = B.accel4[i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
+        case SPHMP_F_ALPHA: { const float4 a = alpha_c[i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
+        case SPHMP_F_ALPHA_PRE: { const float4 a = alpha_p[i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
+        case SPHMP_F_DRIFT:
+            for (int k = 0; k < 3; k++) {
+                const float4 u = B.drift4[(size_t)k * P.cap + i];
+                f[9 * i + 3 * k] = u.x; f[9 * i + 3 * k + 1] = u.y; f[9 * i + 3 * k + 2] = u.z;
+            }
+            break;
+        case SPHMP_F_APREV: { const float4 a = S.in[APREV][i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
+        case SPHMP_F_PMOD: f[i] = B.pmod[i]; break;
+        case SPHMP_F_TYPE: q[i] = p.w < 0.f ? SPHMP_TYPE_BOUNDARY : SPHMP_TYPE_FLUID; break;
+        case SPHMP_F_MASS: f[i] = B.mass_raw[o]; break;
+        case SPHMP_F_BORNID: q[i] = B.bornid[o]; break;
+        default: break;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_unpack_field(const __grid_constant__ DevParams P,
+                                                           const __grid_constant__ DevBuffers B,
+                                                           const __grid_constant__ F4Set S, int field,
+                                                           float4* alpha_c, float4* alpha_p, const void* stage,
+                                                           int n) {
+    const int i = blockIdx.x * kThreads + threadIdx.x;
+    if (i >= n) return;
+    const float* f = reinterpret_cast<const float*>(stage);
+    float4* const __restrict__* out = S.out;
+    switch (field) {
+        case SPHMP_F_POS: { float4 p = out[POS][i]; p.x = f[3 * i]; p.y = f[3 * i + 1]; p.z = f[3 * i + 2]; out[POS][i] = p; } break;
+        case SPHMP_F_VEL: { float4 v = out[VEL][i]; v.x = f[3 * i]; v.y = f[3 * i + 1]; v.z = f[3 * i + 2]; out[VEL][i] = v; } break;
+        case SPHMP_F_VELEVAL: { float4 v = out[VEV][i]; v.x = f[3 * i]; v.y = f[3 * i + 1]; v.z = f[3 * i + 2]; out[VEV][i] = v; } break;
+        case SPHMP_F_PRESSURE: { float2 d = B.densp[i]; d.y = f[i]; B.densp[i] = d; } break;
+        case SPHMP_F_RESTDENS: { float4 a = alpha_c[i]; a.w = f[i]; alpha_c[i] = a; } break;
+        case SPHMP_F_VISC: { float4 v = out[VEL][i]; v.w = f[i]; out[VEL][i] = v; } break;
+        case SPHMP_F_ACCEL: B.accel4[i] = make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 0.f); break;
+        case SPHMP_F_ALPHA: { float4 a = alpha_c[i]; a.x = f[3 * i]; a.y = f[3 * i + 1]; a.z = f[3 * i + 2]; alpha_c[i] = a; } break;
+        case SPHMP_F_ALPHA_PRE: { float4 a = alpha_p[i]; a.x = f[3 * i]; a.y = f[3 * i + 1]; a.z = f[3 * i + 2]; alpha_p[i] = a; } break;
+        case SPHMP_F_DRIFT:
+            for (int k = 0; k < 3; k++)
+                B.drift4[(size_t)k * P.cap + i] = make_float4(f[9 * i + 3 * k], f[9 * i + 3 * k + 1], f[9 * i + 3 * k + 2], 0.f);
+            break;
+        case SPHMP_F_APREV: { float4 a = out[APREV][i]; a.x = f[3 * i]; a.y = f[3 * i + 1]; a.z = f[3 * i + 2]; out[APREV][i] = a; } break;
+        case SPHMP_F_PMOD: B.pmod[i] = f[i]; break;
+        default: break;
+    }
+}
+
+inline int blocks_for(int n, int t = kThreads) { return (n + t - 1) / t; }
+
+F4Set make_set(const DevBuffers& B, const int* cur, bool to_alt) {
+    F4Set S;
+    for (int f = 0; f < kNumFloat4Fields; f++) {
+        S.in[f] = B.f4[f][cur[f]];
+        S.out[f] = B.f4[f][to_alt ? cur[f] ^ 1 : cur[f]];
+    }
+    return S;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    cudaMemsetAsync(B.ccount, 0, sizeof(uint32_t) * (size_t)(P.G + 1), s);
+    if (P.n <= 0) return;
+    k_hash<<<blocks_for(P.n, kHashBlock), kHashBlock, 0, s>>>(P, B, B.f4[POS][cur[POS]]);
+}
+
+void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+    const int per = kScanBlock * kScanItems;
+    const int nb = (P.G + per - 1) / per;
+    const int nchunks = blocks_for(P.n, kHashBlock);
+    k_scan_reduce<<<nb, kScanBlock, 0, s>>>(P, B);
+    k_scan_top<<<1, kScanBlock, 0, s>>>(P, B, nb, nchunks);
+    k_scan_apply<<<nb, kScanBlock, 0, s>>>(P, B);
+    if (P.n <= 0) return;
+    k_scatter<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
+    const int warps = P.G;
+    const int grid = min(blocks_for(warps * 32), 152 * 16);
+    k_cell_sort<<<grid, kThreads, 0, s>>>(P, B);
+    k_big_cell_sort<<<64, 1024, 0, s>>>(P, B);
+}
+
+void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_rearrange<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, make_set(B, cur, true));
+}
+
+void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_boundary_volume<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]]);
+    k_boundary_volume_store<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]]);
+}
+
+void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_density<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[ALPHA][cur[ALPHA]]);
+}
+
+template <bool F, bool D>
+static void fd_dispatch(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    const float4* pos = B.f4[POS][cur[POS]];
+    const float4* vel = B.f4[VEL][cur[VEL]];
+    const float4* al = B.f4[ALPHA][cur[ALPHA]];
+    const float4* ap = B.f4[APREV][cur[APREV]];
+    const int g = blocks_for(P.n);
+    if (!D) {
+        k_force_drift<F, false, 0><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap);
+        return;
+    }
+    switch (P.nphase) {
+        case 1: k_force_drift<F, true, 1><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap); break;
+        case 2: k_force_drift<F, true, 2><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap); break;
+        default: k_force_drift<F, true, 3><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap); break;
+    }
+}
+
+void launch_force_drift(const DevParams& P, const DevBuffers& B, const int* cur, bool force, bool drift,
+                        cudaStream_t s) {
+    if (P.n <= 0 || (!force && !drift)) return;
+    if (force && drift) fd_dispatch<true, true>(P, B, cur, s);
+    else if (force) fd_dispatch<true, false>(P, B, cur, s);
+    else fd_dispatch<false, true>(P, B, cur, s);
+}
+
+void launch_surface_tension(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_surface_tension<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]]);
+}
+
+void launch_alpha_advance(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    const float4* pos = B.f4[POS][cur[POS]];
+    const float4* vev = B.f4[VEV][cur[VEV]];
+    const float4* ain = B.f4[ALPHA][cur[ALPHA]];
+    float4* aout = B.f4[ALPHA][cur[ALPHA] ^ 1];
+    const int g = blocks_for(P.n);
+    switch (P.nphase) {
+        case 1: k_alpha_advance<1><<<g, kThreads, 0, s>>>(P, B, pos, vev, ain, aout); break;
+        case 2: k_alpha_advance<2><<<g, kThreads, 0, s>>>(P, B, pos, vev, ain, aout); break;
+        default: k_alpha_advance<3><<<g, kThreads, 0, s>>>(P, B, pos, vev, ain, aout); break;
+    }
+}
+
+void launch_correction(const DevParams& P, const DevBuffers& B, const int* cur, int pre, cudaStream_t s) {
+    if (P.n <= 0) return;
+    float4* ac = B.f4[ALPHA][cur[ALPHA]];
+    const float4* ap = B.f4[ALPHA][pre];
+    float4* vel = B.f4[VEL][cur[VEL]];
+    const float4* pos = B.f4[POS][cur[POS]];
+    const int g = blocks_for(P.n);
+    switch (P.nphase) {
+        case 1: k_correction<1><<<g, kThreads, 0, s>>>(P, B, ac, ap, vel, pos); break;
+        case 2: k_correction<2><<<g, kThreads, 0, s>>>(P, B, ac, ap, vel, pos); break;
+        default: k_correction<3><<<g, kThreads, 0, s>>>(P, B, ac, ap, vel, pos); break;
+    }
+}
+
+void launch_advance(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_advance<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[VEL][cur[VEL]],
+                                                    B.f4[VEV][cur[VEV]], B.f4[APREV][cur[APREV]]);
+}
+
+void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    const F4Set S = make_set(B, cur, true);
+    const int g = blocks_for(P.n);
+    if (!P.multiphase) {
+        k_pass_c<1, false><<<g, kThreads, 0, s>>>(P, B, S);
+        return;
+    }
+    switch (P.nphase) {
+        case 1: k_pass_c<1, true><<<g, kThreads, 0, s>>>(P, B, S); break;
+        case 2: k_pass_c<2, true><<<g, kThreads, 0, s>>>(P, B, S); break;
+        default: k_pass_c<3, true><<<g, kThreads, 0, s>>>(P, B, S); break;
+    }
+}
+
+void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    cudaMemsetAsync(B.red, 0, sizeof(double) * 16, s);
+    if (P.n <= 0) return;
+    k_conservation<<<min(blocks_for(P.n), 152 * 8), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]],
+                                                                      B.f4[ALPHA][cur[ALPHA]]);
+}
+
+void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,
+                       const sphmp_calc_pack* c, int start, int end, cudaStream_t s) {
+    if (end <= start) return;
+    k_unpack_aos<<<blocks_for(end - start), kThreads, 0, s>>>(P, B, make_set(B, cur, false), d, c, start, end);
+}
+
+void launch_pack_aos(const DevParams& P, const DevBuffers& B, const int* cur, sphmp_display_pack* d,
+                     sphmp_calc_pack* c, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_pack_aos<<<blocks_for(n), kThreads, 0, s>>>(P, B, make_set(B, cur, false), d, c, n);
+}
+
+void launch_pack_field(const DevParams& P, const DevBuffers& B, const int* cur, int field, int alpha_cur,
+                       int alpha_pre, void* stage, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_pack_field<<<blocks_for(n), kThreads, 0, s>>>(P, B, make_set(B, cur, false), field,
+                                                     B.f4[ALPHA][alpha_cur], B.f4[ALPHA][alpha_pre], stage, n);
+}
+
+void launch_unpack_field(const DevParams& P, const DevBuffers& B, const int* cur, int field, int alpha_cur,
+                         int alpha_pre, const void* stage, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    k_unpack_field<<<blocks_for(n), kThreads, 0, s>>>(P, B, make_set(B, cur, false), field,
+                                                       B.f4[ALPHA][alpha_cur], B.f4[ALPHA][alpha_pre], stage, n);
+}
+
+}  // namespace sphmp

@@ -1,0 +1,301 @@
+"""Python binding of libsphmp.so, the GB300-native multiphase SPH step.
+
+Every call goes through the C ABI declared in include/sphmp.h. The library is
+built in-tree by ``sphmp.build.build()``; importing this package never falls
+back to anything else: if the shared library is missing or cannot be loaded,
+``load()`` raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import CalcPack, DisplayPack, Params
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libsphmp.so")
+
+_lib = None
+
+
+class SphmpError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"sphmp error {status} ({abi.STATUS_NAMES.get(status, '?')}): {msg}")
+        self.status = status
+
+
+def load():
+    """Load libsphmp.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with sphmp.build.build()")
+    L = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    vp = C.c_void_p
+    ctx = C.c_void_p
+    st = C.c_int
+    sig = {
+        "sphmp_params_default": (st, [P(Params)]),
+        "sphmp_setup_constants": (st, [P(Params)]),
+        "sphmp_setup_grid": (st, [P(Params)]),
+        "sphmp_add_fluid_volume": (st, [P(Params), P(C.c_float), P(C.c_float), C.c_float, P(C.c_float), C.c_int32,
+                                        C.c_float, C.c_uint64, vp, vp, C.c_int32, P(C.c_int32)]),
+        "sphmp_add_wall": (st, [P(Params), P(C.c_float), P(C.c_float), vp, vp, C.c_int32, P(C.c_int32)]),
+        "sphmp_add_open_box": (st, [P(Params), P(C.c_float), P(C.c_float), C.c_float, vp, vp, C.c_int32,
+                                    P(C.c_int32)]),
+        "sphmp_boundary_spacing": (C.c_float, [P(Params)]),
+        "sphmp_create": (st, [P(Params), P(ctx)]),
+        "sphmp_destroy": (st, [ctx]),
+        "sphmp_set_params": (st, [ctx, P(Params)]),
+        "sphmp_get_params": (st, [ctx, P(Params)]),
+        "sphmp_set_stream": (st, [ctx, vp]),
+        "sphmp_sync": (st, [ctx]),
+        "sphmp_num_particles": (C.c_int32, [ctx]),
+        "sphmp_upload_aos": (st, [ctx, vp, vp, C.c_int32]),
+        "sphmp_download_aos": (st, [ctx, vp, vp, C.c_int32]),
+        "sphmp_emit_aos": (st, [ctx, vp, vp, C.c_int32, C.c_int32]),
+        "sphmp_upload_field": (st, [ctx, C.c_int32, vp, C.c_int32]),
+        "sphmp_download_field": (st, [ctx, C.c_int32, vp, C.c_int32]),
+        "sphmp_get_particle_index": (st, [ctx]),
+        "sphmp_get_grid_list": (st, [ctx]),
+        "sphmp_rearrange_data": (st, [ctx]),
+        "sphmp_compute_boundary_density": (st, [ctx]),
+        "sphmp_compute_pressure": (st, [ctx]),
+        "sphmp_compute_drift_vel": (st, [ctx]),
+        "sphmp_compute_alpha_advance": (st, [ctx]),
+        "sphmp_compute_correction": (st, [ctx]),
+        "sphmp_compute_force": (st, [ctx]),
+        "sphmp_advance": (st, [ctx]),
+        "sphmp_step": (st, [ctx, C.c_int32, C.c_int32, C.c_int32]),
+        "sphmp_conservation": (st, [ctx, P(C.c_double), C.c_int32]),
+        "sphmp_device_errors": (st, [ctx, P(C.c_uint32)]),
+        "sphmp_last_error": (C.c_char_p, []),
+        "sphmp_version": (C.c_char_p, []),
+        "sphmp_legacy_context": (ctx, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error():
+    return load().sphmp_last_error().decode()
+
+
+def check(status):
+    if status != abi.OK:
+        raise SphmpError(status, last_error())
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+# ---------------------------------------------------------------------------
+# host-side setup (no GPU needed)
+# ---------------------------------------------------------------------------
+
+def params_default():
+    p = Params()
+    check(load().sphmp_params_default(C.byref(p)))
+    return p
+
+
+def setup_constants(p):
+    check(load().sphmp_setup_constants(C.byref(p)))
+    return p
+
+
+def setup_grid(p):
+    check(load().sphmp_setup_grid(C.byref(p)))
+    return p
+
+
+def boundary_spacing(p):
+    return float(load().sphmp_boundary_spacing(C.byref(p)))
+
+
+def record_arrays(cap):
+    """Zeroed numpy record arrays (display, calc) with the reference layouts."""
+    return np.zeros(cap, abi.display_dtype()), np.zeros(cap, abi.calc_dtype())
+
+
+def add_fluid_volume(p, disp, calc, count, vmin, vmax, spacing, phase=0, jitter=0.0, seed=0, offs=(0, 0, 0)):
+    n = C.c_int32(count)
+    check(load().sphmp_add_fluid_volume(C.byref(p), _f3(vmin), _f3(vmax), float(spacing), _f3(offs), int(phase),
+                                        float(jitter), int(seed), disp.ctypes.data, calc.ctypes.data, len(disp),
+                                        C.byref(n)))
+    return n.value
+
+
+def add_wall(p, disp, calc, count, vmin, vmax):
+    n = C.c_int32(count)
+    check(load().sphmp_add_wall(C.byref(p), _f3(vmin), _f3(vmax), disp.ctypes.data, calc.ctypes.data, len(disp),
+                                C.byref(n)))
+    return n.value
+
+
+def add_open_box(p, disp, calc, count, vmin, vmax, thickness):
+    n = C.c_int32(count)
+    check(load().sphmp_add_open_box(C.byref(p), _f3(vmin), _f3(vmax), float(thickness), disp.ctypes.data,
+                                    calc.ctypes.data, len(disp), C.byref(n)))
+    return n.value
+
+
+# ---------------------------------------------------------------------------
+# device context
+# ---------------------------------------------------------------------------
+
+FIELD_SHAPES = {
+    abi.F_POS: (3,), abi.F_VEL: (3,), abi.F_VELEVAL: (3,), abi.F_ACCEL: (3,), abi.F_ALPHA: (3,),
+    abi.F_ALPHA_PRE: (3,), abi.F_APREV: (3,), abi.F_DRIFT: (3, 3),
+}
+FIELD_DTYPES = {abi.F_TYPE: np.int32, abi.F_BORNID: np.int32, abi.F_MGCELL: np.uint32, abi.F_MIDSORT: np.uint32,
+                abi.F_MGNDX: np.uint32, abi.F_MGRIDOFF: np.int32, abi.F_MGRIDCNT: np.int32}
+
+
+class Context:
+    """One simulation on the current CUDA device (owns its device buffers)."""
+
+    def __init__(self, params):
+        L = load()
+        self._lib = L
+        self._ptr = C.c_void_p()
+        check(L.sphmp_create(C.byref(params), C.byref(self._ptr)))
+        self.params = params.copy()
+
+    def close(self):
+        if self._ptr:
+            self._lib.sphmp_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def n(self):
+        return int(self._lib.sphmp_num_particles(self._ptr))
+
+    def set_params(self, p):
+        check(self._lib.sphmp_set_params(self._ptr, C.byref(p)))
+        self.params = p.copy()
+
+    def get_params(self):
+        p = Params()
+        check(self._lib.sphmp_get_params(self._ptr, C.byref(p)))
+        return p
+
+    def set_stream(self, stream_ptr):
+        check(self._lib.sphmp_set_stream(self._ptr, C.c_void_p(stream_ptr or 0)))
+
+    def sync(self):
+        check(self._lib.sphmp_sync(self._ptr))
+
+    # transfers
+    def upload_aos(self, disp, calc, n=None):
+        n = len(disp) if n is None else n
+        check(self._lib.sphmp_upload_aos(self._ptr, disp.ctypes.data, calc.ctypes.data, int(n)))
+
+    def emit_aos(self, disp, calc, start, end):
+        check(self._lib.sphmp_emit_aos(self._ptr, disp.ctypes.data, calc.ctypes.data, int(start), int(end)))
+
+    def download_aos(self, n=None, calc=True, out=None):
+        n = self.n if n is None else n
+        if out is None:
+            d, c = record_arrays(n)
+        else:
+            d, c = out
+        check(self._lib.sphmp_download_aos(self._ptr, d.ctypes.data, c.ctypes.data if calc else None, int(n)))
+        return (d, c) if calc else d
+
+    def upload_field(self, field, arr):
+        dt = FIELD_DTYPES.get(field, np.float32)
+        a = np.ascontiguousarray(arr, dtype=dt)
+        n = a.shape[0]
+        check(self._lib.sphmp_upload_field(self._ptr, int(field), a.ctypes.data, int(n)))
+
+    def download_field(self, field, n=None):
+        if field in (abi.F_MGRIDOFF, abi.F_MGRIDCNT):
+            n = self.params.gridtotal if n is None else n
+        else:
+            n = self.n if n is None else n
+        dt = FIELD_DTYPES.get(field, np.float32)
+        a = np.zeros((n,) + FIELD_SHAPES.get(field, ()), dt)
+        check(self._lib.sphmp_download_field(self._ptr, int(field), a.ctypes.data, int(n)))
+        return a
+
+    # per-pass entry points (reference launch wrappers)
+    def get_particle_index(self):
+        check(self._lib.sphmp_get_particle_index(self._ptr))
+
+    def get_grid_list(self):
+        check(self._lib.sphmp_get_grid_list(self._ptr))
+
+    def rearrange_data(self):
+        check(self._lib.sphmp_rearrange_data(self._ptr))
+
+    def sort(self):
+        self.get_particle_index()
+        self.get_grid_list()
+        self.rearrange_data()
+
+    def compute_boundary_density(self):
+        check(self._lib.sphmp_compute_boundary_density(self._ptr))
+
+    def compute_pressure(self):
+        check(self._lib.sphmp_compute_pressure(self._ptr))
+
+    def compute_drift_vel(self):
+        check(self._lib.sphmp_compute_drift_vel(self._ptr))
+
+    def compute_alpha_advance(self):
+        check(self._lib.sphmp_compute_alpha_advance(self._ptr))
+
+    def compute_correction(self):
+        check(self._lib.sphmp_compute_correction(self._ptr))
+
+    def compute_force(self):
+        check(self._lib.sphmp_compute_force(self._ptr))
+
+    def advance(self):
+        check(self._lib.sphmp_advance(self._ptr))
+
+    def before_first_step(self):
+        """Sort, then boundary volumes (reference FluidSystem::BeforeFirstStep)."""
+        self.sort()
+        self.compute_boundary_density()
+
+    def step(self, nsteps=1, schedule=abi.SCHEDULE_FUSED, use_graph=True):
+        check(self._lib.sphmp_step(self._ptr, int(nsteps), int(schedule), int(bool(use_graph))))
+
+    def conservation(self):
+        k = self.params.nphase
+        out = (C.c_double * (3 + k))()
+        check(self._lib.sphmp_conservation(self._ptr, out, 3 + k))
+        return {"mass": out[0], "volume": out[1], "phase_volume": [out[2 + i] for i in range(k)],
+                "alpha_sum_err": out[2 + k]}
+
+    def device_errors(self):
+        bits = C.c_uint32(0)
+        check(self._lib.sphmp_device_errors(self._ptr, C.byref(bits)))
+        return bits.value
+
+
+__all__ = ["abi", "Params", "DisplayPack", "CalcPack", "Context", "SphmpError", "load", "check", "last_error",
+           "params_default", "setup_constants", "setup_grid", "boundary_spacing", "record_arrays",
+           "add_fluid_volume", "add_wall", "add_open_box"]

@@ -1,0 +1,173 @@
+"""Seeded synthetic scenes for the multiphase SPH step.
+
+The reference has no public benchmark or dataset; these builders stand in for
+its scene files with the particle counts, spacings, phase layouts and
+densities of the workloads this library is measured on:
+
+* ``dam_break_2phase``  — 32x32x32 liquid block (d = 0.01 m, h = 0.02 m) with a gas
+  sphere (r = 0.06 m at (0.16, 0.10, 0.16)) in a 0.64 m open box;
+* ``blobs_3phase``      — 128^3 block (d = 0.005 m, h = 0.01 m) in a 1.28 x 0.64 x 0.64 m
+  open box, phases from 64 random spherical blobs (radii 0.02-0.08 m);
+* ``small_block``       — parameterised small scenes for parity tests.
+
+Particles are generated with the library's own reference-equivalent generators
+(sphmp_add_fluid_volume / sphmp_add_open_box) and the phase of each liquid
+particle is then set from the blob layout. Boundary walls are two lattice
+layers at the fluid spacing.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from . import add_fluid_volume, add_open_box, params_default, record_arrays, setup_constants, setup_grid
+
+
+@dataclass
+class Scene:
+    params: abi.Params
+    disp: np.ndarray
+    calc: np.ndarray
+    n_fluid: int
+    n_boundary: int
+    name: str = ""
+
+    @property
+    def n(self):
+        return len(self.disp)
+
+
+def make_params(*, h, d, dt, box_min, box_max, nphase, dens, visc, simscale=1.0, gravity=(0.0, -9.81, 0.0),
+                eos=abi.EOS_LINEAR, eos_k=3.0, multiphase=1, headroom=None, bvisc=100.0, wall_layers=2):
+    """Parameters for a box [box_min, box_max] with `wall_layers` boundary layers at spacing d."""
+    p = params_default()
+    p.smoothradius = h
+    p.simscale = simscale
+    p.dt = dt
+    for a in range(3):
+        p.gravity[a] = gravity[a]
+    p.nphase = nphase
+    p.multiphase = multiphase
+    p.eos = eos
+    p.eos_stiffness = eos_k
+    for k in range(3):
+        kk = min(k, nphase - 1)
+        p.densArr[k] = dens[kk]
+        p.viscArr[k] = visc[kk]
+        p.massArr[k] = np.float32(dens[kk]) * np.float32(d) ** 3
+    p.restdensity = dens[0]
+    p.viscosity = visc[0]
+    p.mass = p.massArr[0]
+    p.bRestdensity = 1000.0
+    p.bmass = np.float32(1000.0) * np.float32(d) ** 3
+    p.bvisc = bvisc
+    setup_constants(p)
+    # grid: walls (thickness t) plus two cells of padding; extra headroom above the box
+    t = (wall_layers - 0.5) * d
+    pad = t + 2.0 * p.cellsize
+    hr = (box_max[1] - box_min[1]) * 0.5 if headroom is None else headroom
+    for a in range(3):
+        p.volmin[a] = box_min[a] - pad
+        p.volmax[a] = box_max[a] + pad + (hr if a == 1 else 0.0)
+    setup_grid(p)
+    return p
+
+
+def _block(p, disp, calc, count, corner, counts, d, jitter, seed, phase=0):
+    vmin = [corner[a] + 0.5 * d for a in range(3)]
+    vmax = [vmin[a] + (counts[a] - 0.5) * d for a in range(3)]
+    return add_fluid_volume(p, disp, calc, count, vmin, vmax, d, phase=phase, jitter=jitter * d, seed=seed)
+
+
+def _walls(p, disp, calc, count, box_min, box_max, d, layers=2):
+    return add_open_box(p, disp, calc, count, box_min, box_max, (layers - 0.5) * d)
+
+
+def _assign_phase(p, calc, sel, phase):
+    calc["restdens"][sel] = p.densArr[phase]
+    calc["mass"][sel] = p.massArr[phase]
+    calc["visc"][sel] = p.viscArr[phase]
+
+
+def _finish(p, disp, calc, count, n_fluid, name):
+    disp = disp[:count].copy()
+    calc = calc[:count].copy()
+    p.num = count
+    p.maxNum = count
+    return Scene(params=p, disp=disp, calc=calc, n_fluid=n_fluid, n_boundary=count - n_fluid, name=name)
+
+
+def dam_break_2phase(seed=1, n_side=32, d=0.01, h=0.02, box=0.64, dt=2e-4, eos=abi.EOS_LINEAR, eos_k=3.0,
+                     gas_center=(0.16, 0.10, 0.16), gas_radius=0.06, multiphase=1, walls=True):
+    """32^3 liquid block with a gas sphere in a `box`-metre open box (liquid 1000, gas 1.2 kg/m^3)."""
+    bmin, bmax = (0.0, 0.0, 0.0), (box, box, box)
+    p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=2, dens=(1000.0, 1.2), visc=(0.2, 0.2),
+                    eos=eos, eos_k=eos_k, multiphase=multiphase)
+    cap = n_side ** 3 + (int(6 * (box / d + 4) ** 2 * 2.2) if walls else 0)
+    disp, calc = record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, (n_side,) * 3, d, 0.1, seed)
+    n_fluid = count
+    pos = disp["pos"][:count]
+    gas = np.sum((pos - np.asarray(gas_center, np.float32)) ** 2, axis=1) < gas_radius ** 2
+    _assign_phase(p, calc, gas, 1)
+    if walls:
+        count = _walls(p, disp, calc, count, bmin, bmax, d)
+    return _finish(p, disp, calc, count, n_fluid, f"dam_break_2phase_{n_side}")
+
+
+def blobs_3phase(seed=2, n_side=128, d=0.005, h=0.01, box=(1.28, 0.64, 0.64), dt=1e-4, eos=abi.EOS_LINEAR,
+                 eos_k=3.0, n_blobs=64, rmin=0.02, rmax=0.08, multiphase=1, walls=True):
+    """n_side^3 block filling the low-x half of the box; phases 0/1/2 (1000/800/1.2) from random blobs."""
+    bmin, bmax = (0.0, 0.0, 0.0), tuple(box)
+    p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=3, dens=(1000.0, 800.0, 1.2),
+                    visc=(0.2, 0.2, 0.2), eos=eos, eos_k=eos_k, multiphase=multiphase)
+    wall_est = 0
+    if walls:
+        nx, ny, nz = [int(b / d) + 8 for b in box]
+        wall_est = 2 * (nx * nz + 2 * nx * ny + 2 * nz * ny) + 4096
+    cap = n_side ** 3 + wall_est
+    disp, calc = record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, (n_side,) * 3, d, 0.1, seed)
+    n_fluid = count
+    rng = np.random.default_rng(seed)
+    ext = n_side * d
+    centers = rng.uniform(0.0, ext, size=(n_blobs, 3)).astype(np.float32)
+    radii = rng.uniform(rmin, rmax, size=n_blobs).astype(np.float32)
+    phases = rng.integers(0, 3, size=n_blobs)
+    pos = disp["pos"][:count]
+    phase = np.zeros(count, np.int64)
+    for c, r, ph in zip(centers, radii, phases):  # the last blob containing a particle wins
+        inside = np.sum((pos - c) ** 2, axis=1) < r * r
+        phase[inside] = ph
+    for k in range(3):
+        _assign_phase(p, calc, np.nonzero(phase == k)[0], k)
+    if walls:
+        count = _walls(p, disp, calc, count, bmin, bmax, d)
+    return _finish(p, disp, calc, count, n_fluid, f"blobs_3phase_{n_side}")
+
+
+def small_block(seed=3, n=(12, 10, 8), d=0.01, h=0.02, box=None, dt=2e-4, nphase=2, eos=abi.EOS_TAIT,
+                dens=(1000.0, 1.2, 800.0), visc=(0.2, 0.05, 0.1), jitter=0.1, phase_frac=0.3, multiphase=1,
+                walls=True, simscale=1.0, velocity_scale=0.0):
+    """A small jittered block with random phases and (optionally) random velocities, for parity tests."""
+    if box is None:
+        box = tuple(max(n[a] * d * 1.5, 4 * h) for a in range(3))
+    bmin, bmax = (0.0, 0.0, 0.0), tuple(box)
+    p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=nphase, dens=dens[:nphase],
+                    visc=visc[:nphase], eos=eos, multiphase=multiphase, simscale=simscale)
+    cap = int(np.prod(n)) + (int(2 * 2 * sum(box[a] * box[b] for a in range(3) for b in range(a + 1, 3))
+                                 / d ** 2 * 1.6) + 2048 if walls else 0)
+    disp, calc = record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, n, d, jitter, seed)
+    n_fluid = count
+    rng = np.random.default_rng(seed)
+    if nphase > 1:
+        ph = np.where(rng.random(count) < phase_frac, rng.integers(1, nphase, size=count), 0)
+        for k in range(nphase):
+            _assign_phase(p, calc, np.nonzero(ph == k)[0], k)
+    if velocity_scale:
+        calc["vel"][:count] = rng.normal(0, velocity_scale, size=(count, 3)).astype(np.float32)
+        calc["veleval"][:count] = calc["vel"][:count]
+    if walls:
+        count = _walls(p, disp, calc, count, bmin, bmax, d)
+    return _finish(p, disp, calc, count, n_fluid, "small_block")
