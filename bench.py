@@ -1,0 +1,327 @@
+"""Benchmark: particle-steps/s of the multiphase SPH step on one GB300.
+
+Workload (BASELINE config "plain method at scale, 3 phases"): 1,048,576 fluid
+particles (128^3 lattice, d = 0.005 m, h = 0.01 m) in a 1.28 x 0.64 x 0.64 m open
+box with two layers of boundary particles, volume fractions from 64 random
+spherical blobs (phases 1000 / 800 / 1.2 kg/m^3), seeded synthetic data.
+
+A step is one fused pass of the whole pipeline (hash, stable counting sort,
+reorder, density + EOS, force + drift velocity, volume-fraction advance +
+correction + advection) replayed from a captured CUDA graph. `value` counts
+fluid particles only (boundary particles are processed but not counted) and
+the state stays resident in HBM; `e2e` is the same metric through the public
+API with one upload of the reference records from pinned host memory and a
+per-step download of the display records (the reference's per-frame
+TransferFromCUDA), timed on the host clock.
+
+--impl reference times the reference's own algorithm on the host cores: the
+CPU oracle (a statement-by-statement restatement of the reference kernels,
+bit-identical to them) on the same scene, all host threads, the same metric.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "sph-multiphase_gb300"))
+sys.path.insert(0, REPO)
+
+METRIC = "particle-steps/s at 1M (1 GB300)"
+UNIT = "particle-steps/s"
+# algorithmic bytes per particle for each stage of a fused step (HBM, FP32 SoA;
+# neighbour re-reads assumed to hit L2 / shared memory)
+ALGO_BYTES = {"hash": 24, "cell_starts": 0, "cell_order": 16, "rearrange": 128, "density": 24,
+              "force_drift": 136, "alpha_correct_advance": 168, "advance": 168}
+KERNELS_PER_FUSED_STEP = 11   # hash, 3 scan, scatter, cell sort, big-cell sort, rearrange, density, force+drift, pass C
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic(stage):
+    """DRAM bytes per launch of `stage` from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(REPO, "profiles", "ncu_traffic.json")) as f:
+            d = json.load(f)
+        v = d.get(stage)
+        return None if v is None else float(v)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"sphmp_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    parts = [x.strip() for x in line.split(",")]
+                    if len(parts) >= 9 and parts[1].isdigit():
+                        rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [int(r[1]) for r in rows]
+        mx = max(int(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def build_scene(seed):
+    from sphmp import abi, scenes
+    return scenes.blobs_3phase(seed=seed, eos=abi.EOS_LINEAR, eos_k=3.0)
+
+
+def cpu_sample(scene, steps, budget_s, threads=None):
+    """Time the CPU oracle on the bench scene; returns (particle-steps/s, steps done, seconds, threads)."""
+    from oracle import oracle as O
+    from sphmp import abi
+    O.build()
+    if threads:
+        O.set_threads(threads)
+    nthr = O.lib().orc_get_num_threads()
+    p = scene.params
+    s = O.state_from_aos(scene.disp, scene.calc, p.gridtotal)
+    import numpy as np
+    for k in range(p.nphase):
+        s.alpha[:, k] = scene.calc["restdens"] == np.float32(p.densArr[k])
+    s.alpha_pre[:] = s.alpha
+    O.before_first_step(p, s)
+    O.step(p, s, abi.SCHEDULE_FUSED, 1)  # warm-up (page-in, thread pool)
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        O.step(p, s, abi.SCHEDULE_FUSED, 1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return scene.n_fluid * done / dt, done, dt, nthr
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    scene = build_scene(args.seed)
+    # warm-up steps are part of the sample's own warm-up; the timed part is bounded
+    value, done, dt, nthr = cpu_sample(scene, max(1, args.steps), budget_s=args.cpu_budget)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": done, "warmup": 1, "ms_per_step": 1000.0 * dt / max(done, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": scene.name, "fluid_particles": scene.n_fluid,
+                   "boundary_particles": scene.n_boundary, "schedule": "fused", "eos": "linear k=3"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthr, "kind": "port",
+                         "sample": f"{done} full steps of the {scene.n_fluid}-fluid-particle scene "
+                                   f"(capped at {args.cpu_budget:.0f} s; requested {args.steps})"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import sphmp
+    from sphmp import abi
+
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev_index = torch.cuda.current_device()
+    scene = build_scene(args.seed + rank)
+    n_fluid = scene.n_fluid
+
+    ctx = sphmp.Context(scene.params)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_aos(scene.disp, scene.calc)
+    ctx.before_first_step()
+    ctx.step(args.warmup, abi.SCHEDULE_FUSED, use_graph=True)   # includes graph capture
+    ctx.sync()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident timed region ----
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev_index) as clk:
+        ev0.record(stream)
+        ctx.step(args.steps, abi.SCHEDULE_FUSED, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    ctx.sync()
+    if ws > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    n_in = int((ctx.download_field(abi.F_MGCELL) != abi.GRID_UNDEF).sum())
+    cons = ctx.conservation()
+
+    # ---- per-stage times (live CUDA events on the launch stream) for the roofline ----
+    stages = {}
+    reps = 5
+    for _ in range(reps):
+        for name, t in ctx.step_profile(abi.SCHEDULE_FUSED):
+            stages[name] = stages.get(name, 0.0) + t / reps
+    dom = max((k for k in stages if k in ALGO_BYTES and ALGO_BYTES[k] > 0), key=lambda k: stages[k])
+    units = ctx.n
+    algo = ALGO_BYTES[dom] * units
+    achieved = algo / (stages[dom] * 1e-3) / 1e9
+    peak, peak_kind = _peaks()
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": _traffic(dom),
+                "algorithmic_bytes_per_launch": algo, "launch_ms": stages[dom]}
+    step_bytes = sum(ALGO_BYTES.get(k, 0) for k in stages) * units
+    ctx.close()
+
+    # ---- end to end through the public API, host buffers ----
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    pin_disp = torch.empty(scene.n * 32, dtype=torch.uint8, pin_memory=True)
+    pin_calc = torch.empty(scene.n * 224, dtype=torch.uint8, pin_memory=True)
+    pin_out = torch.empty(scene.n * 32, dtype=torch.uint8, pin_memory=True)
+    hd = pin_disp.numpy().view(abi.display_dtype())
+    hc = pin_calc.numpy().view(abi.calc_dtype())
+    ho = pin_out.numpy().view(abi.display_dtype())
+    hd[:] = scene.disp
+    hc[:] = scene.calc
+    ctx2 = sphmp.Context(scene.params)
+    ctx2.set_stream(stream.cuda_stream)
+    ctx2.upload_aos(hd, hc)
+    ctx2.before_first_step()
+    ctx2.step(args.warmup, abi.SCHEDULE_FUSED, use_graph=True)
+    ctx2.download_aos(calc=False, out=(ho, None))
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx2.upload_aos(hd, hc)
+    ctx2.before_first_step()
+    for _ in range(e2e_steps):
+        ctx2.step(1, abi.SCHEDULE_FUSED, use_graph=True)
+        ctx2.download_aos(calc=False, out=(ho, None))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    ctx2.close()
+
+    value = ws * n_fluid * args.steps / (ms * 1e-3)
+    e2e_value = ws * n_fluid * e2e_steps / e2e_s
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": scene.name, "fluid_particles": n_fluid, "boundary_particles": scene.n_boundary,
+                   "phases": 3, "h": 0.01, "d": 0.005, "box": [1.28, 0.64, 0.64], "dt": 1e-4,
+                   "eos": "linear k=3", "schedule": "fused (3 neighbour passes)", "graph": True,
+                   "l2": "working set ~0.5 GB > 129 MB L2 (no flush needed)",
+                   "in_grid_after": n_in, "parallelism": f"replicas x{ws}",
+                   "stage_ms": {k: round(v, 4) for k, v in stages.items()},
+                   "step_algorithmic_bytes": step_bytes,
+                   "mass_fp64": cons["mass"], "alpha_sum_err": cons["alpha_sum_err"]},
+        "roofline": roofline,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": scene.n * 256 / e2e_steps,
+                "d2h_bytes_per_step": scene.n * 32,
+                "how": f"one TransferToCUDA upload + sort, then {e2e_steps} x (step + TransferFromCUDA), host clock"},
+        "gpu_launches": KERNELS_PER_FUSED_STEP * args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, done, dt, nthr = cpu_sample(scene, args.cpu_steps, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthr, "kind": "port",
+                                "sample": f"{done} fused steps of the same scene on the CPU oracle "
+                                          f"({dt:.1f} s, {nthr} threads)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="sphmp", choices=["sphmp", "reference"])
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=200)
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -308,6 +308,13 @@ sphmp_status sphmp_advance(sphmp_ctx* ctx);
    from a captured CUDA graph when `use_graph` is 1. */
 sphmp_status sphmp_step(sphmp_ctx* ctx, int32_t nsteps, int32_t schedule, int32_t use_graph);
 
+/* Run one step eagerly with a CUDA event recorded on the context stream between
+   consecutive stages (hash, cell_starts, cell_order, rearrange, density, then the
+   neighbour passes of the schedule). Writes the milliseconds of each stage into
+   ms[i] and its name into names + 32*i (NUL-terminated, may be NULL); returns the
+   number of stages, or minus a sphmp_status on error. */
+int32_t sphmp_step_profile(sphmp_ctx* ctx, int32_t schedule, float* ms, char* names, int32_t nmax);
+
 /* FP64 conservation sums over in-grid, non-boundary slots, computed on the GPU:
    out[0] = total mass, out[1] = total volume sum(m/rho), out[2+k] = phase-k volume
    sum(alpha_k m/rho) for k < nphase, out[2+nphase] = max |sum_k alpha_k - 1|. */

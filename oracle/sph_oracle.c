@@ -181,11 +181,14 @@ void FN(orc_get_grid_list)(const sphmp_params* p, ST* s) {
 
 /* RearrageDataCUDA (fluid_system_host.cu:187-210): both record buffers are copied to
    msortbuf, then RearrangeData (fluid_system_kern.cu:98-121) gathers the record of
-   pre-sort slot midsort[i] into sorted slot i. A GRID_UNDEF slot keeps its own old
-   record except for pos, which is parked at (-1000,-1000,-1000). The legacy
-   multiphase arrays travel with the record; mf_alpha_pre receives the sorted
-   fractions (the start-of-step values the multiphase kernels read).
-   MFidTable (written at :112, never read) is not restated. Returns 0 on success. */
+   pre-sort slot midsort[i] into sorted slot i. The kernel keeps the cell in an
+   `int` and tests `cell != GRID_UNDEF` against the literal 4294967295, which is a
+   64-bit `long` on LP64 hosts (every Linux / GB300 build), so the test is always
+   true and out-of-grid slots are gathered like the others; their parking at
+   (-1000,-1000,-1000) happens in AdvanceParticles. The legacy multiphase arrays
+   travel with the record; mf_alpha_pre receives the sorted fractions (the
+   start-of-step values the multiphase kernels read). MFidTable (written at :112,
+   never read) is not restated. Returns 0 on success. */
 int FN(orc_rearrange_data)(const sphmp_params* p, ST* s) {
     (void)p;
     const int n = s->n;
@@ -201,18 +204,11 @@ int FN(orc_rearrange_data)(const sphmp_params* p, ST* s) {
 #undef DUP
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++) {
-        if (s->mgcell[i] != UNDEF) {
-            int e = (int)s->midsort[i];
+        int e = (int)s->midsort[i];
 #define MV(field, k) for (int c = 0; c < (k); c++) s->field[(size_t)i * (k) + c] = old_##field[(size_t)e * (k) + c];
-            MV(pos, 3) MV(type, 1) MV(color, 4) MV(vel, 3) MV(veleval, 3) MV(pressure, 1) MV(dens, 1)
-            MV(restdens, 1) MV(mass, 1) MV(visc, 1) MV(bornid, 1) MV(accel, 3) MV(alpha, 3) MV(aprev, 3)
+        MV(pos, 3) MV(type, 1) MV(color, 4) MV(vel, 3) MV(veleval, 3) MV(pressure, 1) MV(dens, 1)
+        MV(restdens, 1) MV(mass, 1) MV(visc, 1) MV(bornid, 1) MV(accel, 3) MV(alpha, 3) MV(aprev, 3)
 #undef MV
-        } else {
-            s->mgcell[i] = UNDEF;
-            s->pos[3 * i + 0] = -1000;
-            s->pos[3 * i + 1] = -1000;
-            s->pos[3 * i + 2] = -1000;
-        }
         for (int k = 0; k < 3; k++) s->alpha_pre[3 * i + k] = s->alpha[3 * i + k];
     }
     free(old_pos); free(old_type); free(old_color); free(old_vel); free(old_veleval);

@@ -242,33 +242,78 @@ inline void swap_all(sphmp_ctx* c) {
     for (int f = 0; f < kNumFloat4Fields; f++) c->cur[f] ^= 1;
 }
 
+// Optional event marks between the stages of a step (for sphmp_step_profile).
+struct StageTimer {
+    static constexpr int kMax = 24;
+    cudaEvent_t ev[kMax + 1];
+    const char* name[kMax];
+    int n = 0;
+    bool ok = true;
+    StageTimer() {
+        for (int i = 0; i <= kMax; i++)
+            if (cudaEventCreate(&ev[i]) != cudaSuccess) ok = false;
+    }
+    ~StageTimer() {
+        for (int i = 0; i <= kMax; i++) cudaEventDestroy(ev[i]);
+    }
+    void start(cudaStream_t s) { cudaEventRecord(ev[0], s); }
+    void mark(cudaStream_t s, const char* nm) {
+        if (n >= kMax) return;
+        name[n] = nm;
+        cudaEventRecord(ev[++n], s);
+    }
+};
+
 // Queue one full step on the context stream (no host synchronisation).
-sphmp_status enqueue_step(sphmp_ctx* c, int schedule) {
+sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     const DevParams P = dev_params(c);
     const cudaStream_t s = c->stream;
+    auto mark = [&](const char* nm) {
+        if (T) T->mark(s, nm);
+    };
+    if (T) T->start(s);
     launch_hash(P, c->B, c->cur, s);
-    launch_grid_list(P, c->B, s);
+    mark("hash");
+    launch_cell_starts(P, c->B, s);
+    mark("cell_starts");
+    launch_cell_order(P, c->B, s);
+    mark("cell_order");
     launch_rearrange(P, c->B, c->cur, s);
+    mark("rearrange");
     swap_all(c);
     c->alpha_advanced = false;
     c->grid_valid = true;
     launch_density(P, c->B, c->cur, s);
+    mark("density");
     if (schedule == SPHMP_SCHEDULE_FUSED) {
         launch_force_drift(P, c->B, c->cur, true, P.multiphase != 0, s);
-        if (P.st_on) launch_surface_tension(P, c->B, c->cur, s);
+        mark("force_drift");
+        if (P.st_on) {
+            launch_surface_tension(P, c->B, c->cur, s);
+            mark("surface_tension");
+        }
         launch_pass_c(P, c->B, c->cur, s);
+        mark(P.multiphase ? "alpha_correct_advance" : "advance");
         swap_all(c);
     } else {
         if (P.multiphase) {
             launch_force_drift(P, c->B, c->cur, false, true, s);
+            mark("drift");
             launch_alpha_advance(P, c->B, c->cur, s);
+            mark("alpha_advance");
             c->cur[ALPHA] ^= 1;
             c->alpha_advanced = true;
             launch_correction(P, c->B, c->cur, c->cur[ALPHA] ^ 1, s);
+            mark("correction");
         }
         launch_force_drift(P, c->B, c->cur, true, false, s);
-        if (P.st_on) launch_surface_tension(P, c->B, c->cur, s);
+        mark("force");
+        if (P.st_on) {
+            launch_surface_tension(P, c->B, c->cur, s);
+            mark("surface_tension");
+        }
         launch_advance(P, c->B, c->cur, s);
+        mark("advance");
     }
     CHECK_LAUNCH("step");
     return SPHMP_OK;
@@ -663,6 +708,38 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
     for (int t = 0; t < nsteps; t++)
         if (sphmp_status st = enqueue_step(c, schedule)) return st;
     return SPHMP_OK;
+}
+
+int32_t sphmp_step_profile(sphmp_ctx* c, int32_t schedule, float* ms, char* names, int32_t nmax) {
+    if (need_ctx(c) != SPHMP_OK) return -SPHMP_ERR_INVALID_ARG;
+    if (!ms || nmax <= 0) {
+        fail(SPHMP_ERR_INVALID_ARG, "need an output array");
+        return -SPHMP_ERR_INVALID_ARG;
+    }
+    if (schedule != SPHMP_SCHEDULE_REFERENCE && schedule != SPHMP_SCHEDULE_FUSED) {
+        fail(SPHMP_ERR_INVALID_ARG, "unknown schedule %d", schedule);
+        return -SPHMP_ERR_INVALID_ARG;
+    }
+    StageTimer T;
+    if (!T.ok) {
+        fail(SPHMP_ERR_CUDA, "cudaEventCreate failed");
+        return -SPHMP_ERR_CUDA;
+    }
+    sphmp_status st = enqueue_step(c, schedule, &T);
+    if (st) return -st;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return -cuda_fail(e, "cudaStreamSynchronize");
+    const int n = T.n < nmax ? T.n : nmax;
+    for (int i = 0; i < n; i++) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, T.ev[i], T.ev[i + 1]);
+        ms[i] = t;
+        if (names) {
+            strncpy(names + 32 * i, T.name[i], 31);
+            names[32 * i + 31] = 0;
+        }
+    }
+    return n;
 }
 
 sphmp_status sphmp_conservation(sphmp_ctx* c, double* out, int32_t nout) {

@@ -99,6 +99,10 @@ enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
 // All take the current double-buffer selectors in `cur` (one per Field4).
 void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+// the two halves of launch_grid_list: cell starts (histogram scan), then the
+// scatter and per-cell stable ordering
+void launch_cell_starts(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_cell_order(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);

@@ -386,19 +386,18 @@ struct F4Set {
     float4* __restrict__ out[kNumFloat4Fields];
 };
 
+// Every slot, out-of-grid ones included, receives the record of its pre-sort slot:
+// the reference's `int cell != GRID_UNDEF` test (fluid_system_kern.cu:104-108)
+// compares against a 64-bit literal on LP64 hosts and is always true there.
+// Out-of-grid particles are parked at (-1000)^3 by the advance.
 __global__ void __launch_bounds__(kThreads) k_rearrange(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= P.n) return;
-    const bool undef = B.mgcell[s] == kUndef;
-    const uint32_t src = undef ? (uint32_t)s : B.midsort[s];
+    const uint32_t src = B.midsort[s];
 #pragma unroll
-    for (int f = 0; f < kNumFloat4Fields; f++) {
-        float4 v = S.in[f][src];
-        if (f == POS && undef) { v.x = -1000.f; v.y = -1000.f; v.z = -1000.f; }
-        S.out[f][s] = v;
-    }
+    for (int f = 0; f < kNumFloat4Fields; f++) S.out[f][s] = S.in[f][src];
 }
 
 // ---------------------------------------------------------------------------
@@ -1070,19 +1069,26 @@ void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaSt
     k_hash<<<blocks_for(P.n, kHashBlock), kHashBlock, 0, s>>>(P, B, B.f4[POS][cur[POS]]);
 }
 
-void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+void launch_cell_starts(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
     const int per = kScanBlock * kScanItems;
     const int nb = (P.G + per - 1) / per;
     const int nchunks = blocks_for(P.n, kHashBlock);
     k_scan_reduce<<<nb, kScanBlock, 0, s>>>(P, B);
     k_scan_top<<<1, kScanBlock, 0, s>>>(P, B, nb, nchunks);
     k_scan_apply<<<nb, kScanBlock, 0, s>>>(P, B);
+}
+
+void launch_cell_order(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
     if (P.n <= 0) return;
     k_scatter<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
-    const int warps = P.G;
-    const int grid = min(blocks_for(warps * 32), 152 * 16);
+    const int grid = min(blocks_for(P.G * 32), 152 * 16);
     k_cell_sort<<<grid, kThreads, 0, s>>>(P, B);
     k_big_cell_sort<<<64, 1024, 0, s>>>(P, B);
+}
+
+void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+    launch_cell_starts(P, B, s);
+    launch_cell_order(P, B, s);
 }
 
 void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {

@@ -71,6 +71,7 @@ def load():
         "sphmp_advance": (st, [ctx]),
         "sphmp_step": (st, [ctx, C.c_int32, C.c_int32, C.c_int32]),
         "sphmp_conservation": (st, [ctx, P(C.c_double), C.c_int32]),
+        "sphmp_step_profile": (C.c_int32, [ctx, C.c_int32, P(C.c_float), C.c_char_p, C.c_int32]),
         "sphmp_device_errors": (st, [ctx, P(C.c_uint32)]),
         "sphmp_last_error": (C.c_char_p, []),
         "sphmp_version": (C.c_char_p, []),
@@ -282,6 +283,16 @@ class Context:
 
     def step(self, nsteps=1, schedule=abi.SCHEDULE_FUSED, use_graph=True):
         check(self._lib.sphmp_step(self._ptr, int(nsteps), int(schedule), int(bool(use_graph))))
+
+    def step_profile(self, schedule=abi.SCHEDULE_FUSED):
+        """One eager step; returns [(stage name, milliseconds)] timed with CUDA events."""
+        ms = (C.c_float * 24)()
+        names = C.create_string_buffer(32 * 24)
+        n = self._lib.sphmp_step_profile(self._ptr, int(schedule), ms, names, 24)
+        if n < 0:
+            raise SphmpError(-n, last_error())
+        raw = names.raw
+        return [(raw[32 * i:32 * i + 32].split(b"\0")[0].decode(), float(ms[i])) for i in range(n)]
 
     def conservation(self):
         k = self.params.nphase

@@ -140,7 +140,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_params_default", "sphmp_setup_constants", "sphmp_setup_grid", "sphmp_add_fluid_volume",
     "sphmp_add_wall", "sphmp_add_open_box", "sphmp_boundary_spacing",
     "sphmp_create", "sphmp_destroy", "sphmp_set_params", "sphmp_get_params", "sphmp_set_stream",
-    "sphmp_sync", "sphmp_num_particles", "sphmp_upload_aos", "sphmp_download_aos", "sphmp_emit_aos",
+    "sphmp_sync", "sphmp_num_particles", "sphmp_step_profile", "sphmp_upload_aos", "sphmp_download_aos", "sphmp_emit_aos",
     "sphmp_upload_field", "sphmp_download_field", "sphmp_get_particle_index", "sphmp_get_grid_list",
     "sphmp_rearrange_data", "sphmp_compute_boundary_density", "sphmp_compute_pressure",
     "sphmp_compute_drift_vel", "sphmp_compute_alpha_advance", "sphmp_compute_correction",

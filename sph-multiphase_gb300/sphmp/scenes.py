@@ -6,8 +6,9 @@ densities of the workloads this library is measured on:
 
 * ``dam_break_2phase``  — 32x32x32 liquid block (d = 0.01 m, h = 0.02 m) with a gas
   sphere (r = 0.06 m at (0.16, 0.10, 0.16)) in a 0.64 m open box;
-* ``blobs_3phase``      — 128^3 block (d = 0.005 m, h = 0.01 m) in a 1.28 x 0.64 x 0.64 m
-  open box, phases from 64 random spherical blobs (radii 0.02-0.08 m);
+* ``blobs_3phase``      — 1,048,576 liquid particles on a 128 x 64 x 128 lattice (x, y, z;
+  d = 0.005 m, h = 0.01 m) in a 1.28 x 0.64 x 0.64 m open box, phases from 64 random
+  spherical blobs (radii 0.02-0.08 m);
 * ``small_block``       — parameterised small scenes for parity tests.
 
 Particles are generated with the library's own reference-equivalent generators
@@ -39,7 +40,8 @@ class Scene:
 
 def make_params(*, h, d, dt, box_min, box_max, nphase, dens, visc, simscale=1.0, gravity=(0.0, -9.81, 0.0),
                 eos=abi.EOS_LINEAR, eos_k=3.0, multiphase=1, headroom=None, bvisc=100.0, wall_layers=2):
-    """Parameters for a box [box_min, box_max] with `wall_layers` boundary layers at spacing d."""
+    """Parameters for a box [box_min, box_max] (sim units) with `wall_layers` boundary layers at spacing d.
+    Masses are rest density times (d * simscale)^3, the physical volume of a lattice site."""
     p = params_default()
     p.smoothradius = h
     p.simscale = simscale
@@ -54,17 +56,17 @@ def make_params(*, h, d, dt, box_min, box_max, nphase, dens, visc, simscale=1.0,
         kk = min(k, nphase - 1)
         p.densArr[k] = dens[kk]
         p.viscArr[k] = visc[kk]
-        p.massArr[k] = np.float32(dens[kk]) * np.float32(d) ** 3
+        p.massArr[k] = np.float32(dens[kk]) * np.float32(d * simscale) ** 3
     p.restdensity = dens[0]
     p.viscosity = visc[0]
     p.mass = p.massArr[0]
     p.bRestdensity = 1000.0
-    p.bmass = np.float32(1000.0) * np.float32(d) ** 3
+    p.bmass = np.float32(1000.0) * np.float32(d * simscale) ** 3
     p.bvisc = bvisc
     setup_constants(p)
     # grid: walls (thickness t) plus two cells of padding; extra headroom above the box
     t = (wall_layers - 0.5) * d
-    pad = t + 2.0 * p.cellsize
+    pad = t + 2.0 * p.cellsize / simscale
     hr = (box_max[1] - box_min[1]) * 0.5 if headroom is None else headroom
     for a in range(3):
         p.volmin[a] = box_min[a] - pad
@@ -109,15 +111,16 @@ def dam_break_2phase(seed=1, n_side=32, d=0.01, h=0.02, box=0.64, dt=2e-4, eos=a
     n_fluid = count
     pos = disp["pos"][:count]
     gas = np.sum((pos - np.asarray(gas_center, np.float32)) ** 2, axis=1) < gas_radius ** 2
-    _assign_phase(p, calc, gas, 1)
+    _assign_phase(p, calc, np.nonzero(gas)[0], 1)
     if walls:
         count = _walls(p, disp, calc, count, bmin, bmax, d)
     return _finish(p, disp, calc, count, n_fluid, f"dam_break_2phase_{n_side}")
 
 
-def blobs_3phase(seed=2, n_side=128, d=0.005, h=0.01, box=(1.28, 0.64, 0.64), dt=1e-4, eos=abi.EOS_LINEAR,
-                 eos_k=3.0, n_blobs=64, rmin=0.02, rmax=0.08, multiphase=1, walls=True):
-    """n_side^3 block filling the low-x half of the box; phases 0/1/2 (1000/800/1.2) from random blobs."""
+def blobs_3phase(seed=2, lattice=(128, 64, 128), d=0.005, h=0.01, box=(1.28, 0.64, 0.64), dt=1e-4,
+                 eos=abi.EOS_LINEAR, eos_k=3.0, n_blobs=64, rmin=0.02, rmax=0.08, multiphase=1, walls=True):
+    """A lattice block in the low-x corner of the box; phases 0/1/2 (1000/800/1.2 kg/m^3) from
+    random blobs (the last blob containing a particle wins, phase 0 elsewhere)."""
     bmin, bmax = (0.0, 0.0, 0.0), tuple(box)
     p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=3, dens=(1000.0, 800.0, 1.2),
                     visc=(0.2, 0.2, 0.2), eos=eos, eos_k=eos_k, multiphase=multiphase)
@@ -125,13 +128,13 @@ def blobs_3phase(seed=2, n_side=128, d=0.005, h=0.01, box=(1.28, 0.64, 0.64), dt
     if walls:
         nx, ny, nz = [int(b / d) + 8 for b in box]
         wall_est = 2 * (nx * nz + 2 * nx * ny + 2 * nz * ny) + 4096
-    cap = n_side ** 3 + wall_est
+    cap = int(np.prod(lattice)) + wall_est
     disp, calc = record_arrays(cap)
-    count = _block(p, disp, calc, 0, bmin, (n_side,) * 3, d, 0.1, seed)
+    count = _block(p, disp, calc, 0, bmin, lattice, d, 0.1, seed)
     n_fluid = count
     rng = np.random.default_rng(seed)
-    ext = n_side * d
-    centers = rng.uniform(0.0, ext, size=(n_blobs, 3)).astype(np.float32)
+    ext = np.asarray(lattice, np.float32) * np.float32(d)
+    centers = (rng.uniform(0.0, 1.0, size=(n_blobs, 3)) * ext).astype(np.float32)
     radii = rng.uniform(rmin, rmax, size=n_blobs).astype(np.float32)
     phases = rng.integers(0, 3, size=n_blobs)
     pos = disp["pos"][:count]
@@ -143,7 +146,8 @@ def blobs_3phase(seed=2, n_side=128, d=0.005, h=0.01, box=(1.28, 0.64, 0.64), dt
         _assign_phase(p, calc, np.nonzero(phase == k)[0], k)
     if walls:
         count = _walls(p, disp, calc, count, bmin, bmax, d)
-    return _finish(p, disp, calc, count, n_fluid, f"blobs_3phase_{n_side}")
+    name = "blobs_3phase_" + "x".join(str(v) for v in lattice)
+    return _finish(p, disp, calc, count, n_fluid, name)
 
 
 def small_block(seed=3, n=(12, 10, 8), d=0.01, h=0.02, box=None, dt=2e-4, nphase=2, eos=abi.EOS_TAIT,
