@@ -24,6 +24,9 @@ struct sphmp_ctx {
     int cur[kNumFloat4Fields] = {0, 0, 0, 0, 0};
     bool alpha_advanced = false;  // alpha4[cur] = advanced fractions, alpha4[cur^1] = start of step
     bool grid_valid = false;      // cell starts built for the current slot order
+    bool nbr_valid = false;       // neighbour list built by the density pass for the current positions
+    bool oct_built = false;       // the last grid list also built the octant order
+    bool oct_valid = false;       // octant order matches the current slot order and positions
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
@@ -105,6 +108,9 @@ DevParams dev_params(const sphmp_ctx* c) {
     P.ss = p.simscale;
     P.h = p.smoothradius;
     P.r2 = p.smoothradius * p.smoothradius;
+    P.r2list = P.r2 * (1.0f + 1.0e-5f);
+    P.use_list = c->nbr_valid ? 1 : 0;
+    P.use_oct = c->oct_valid ? 1 : 0;
     P.dt = p.dt;
     P.kpoly6 = p.kpoly6;
     P.kspikydiff = p.kspikydiff;
@@ -143,7 +149,8 @@ void free_buffers(sphmp_ctx* c) {
         for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
                     B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
-                    B.mass_raw, B.err, B.red, B.vtmp, c->stage};
+                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.pos4o, B.oidx, B.oct_start,
+                    c->stage};
     for (void* q : ptrs) cudaFree(q);
     memset(&c->B, 0, sizeof(c->B));
     c->stage = nullptr;
@@ -184,6 +191,11 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.err, 1));
     CK(dalloc(&B.red, 16));
     CK(dalloc(&B.vtmp, N));
+    CK(dalloc(&B.nbr, (size_t)kMaxNbr * N));
+    CK(dalloc(&B.nbr_cnt, N));
+    CK(dalloc(&B.pos4o, N));
+    CK(dalloc(&B.oidx, N));
+    CK(dalloc(&B.oct_start, 8 * G));
     c->stage_bytes = N * (sizeof(sphmp_display_pack) + sizeof(sphmp_calc_pack));
     if (c->stage_bytes < G * sizeof(int32_t)) c->stage_bytes = G * sizeof(int32_t);
     CK(cudaMalloc(&c->stage, c->stage_bytes));
@@ -276,44 +288,52 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     mark("hash");
     launch_cell_starts(P, c->B, s);
     mark("cell_starts");
-    launch_cell_order(P, c->B, s);
+    launch_cell_order(P, c->B, c->cur, s);
     mark("cell_order");
     launch_rearrange(P, c->B, c->cur, s);
     mark("rearrange");
     swap_all(c);
     c->alpha_advanced = false;
     c->grid_valid = true;
-    launch_density(P, c->B, c->cur, s);
+    c->oct_valid = true;
+    c->nbr_valid = false;
+    launch_density(dev_params(c), c->B, c->cur, s);
     mark("density");
+    c->nbr_valid = true;
+    const DevParams PL = dev_params(c);  // neighbour passes read the list
     if (schedule == SPHMP_SCHEDULE_FUSED) {
-        launch_force_drift(P, c->B, c->cur, true, P.multiphase != 0, s);
+        launch_force_drift(PL, c->B, c->cur, true, P.multiphase != 0, s);
         mark("force_drift");
         if (P.st_on) {
-            launch_surface_tension(P, c->B, c->cur, s);
+            launch_surface_tension(PL, c->B, c->cur, s);
             mark("surface_tension");
         }
-        launch_pass_c(P, c->B, c->cur, s);
+        launch_pass_c(PL, c->B, c->cur, s);
         mark(P.multiphase ? "alpha_correct_advance" : "advance");
         swap_all(c);
+        c->nbr_valid = false;  // positions moved
+        c->oct_valid = false;
     } else {
         if (P.multiphase) {
-            launch_force_drift(P, c->B, c->cur, false, true, s);
+            launch_force_drift(PL, c->B, c->cur, false, true, s);
             mark("drift");
-            launch_alpha_advance(P, c->B, c->cur, s);
+            launch_alpha_advance(PL, c->B, c->cur, s);
             mark("alpha_advance");
             c->cur[ALPHA] ^= 1;
             c->alpha_advanced = true;
-            launch_correction(P, c->B, c->cur, c->cur[ALPHA] ^ 1, s);
+            launch_correction(PL, c->B, c->cur, c->cur[ALPHA] ^ 1, s);
             mark("correction");
         }
-        launch_force_drift(P, c->B, c->cur, true, false, s);
+        launch_force_drift(PL, c->B, c->cur, true, false, s);
         mark("force");
         if (P.st_on) {
-            launch_surface_tension(P, c->B, c->cur, s);
+            launch_surface_tension(PL, c->B, c->cur, s);
             mark("surface_tension");
         }
-        launch_advance(P, c->B, c->cur, s);
+        launch_advance(PL, c->B, c->cur, s);
         mark("advance");
+        c->nbr_valid = false;
+        c->oct_valid = false;
     }
     CHECK_LAUNCH("step");
     return SPHMP_OK;
@@ -454,6 +474,9 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     CHECK_LAUNCH("unpack records");
     c->alpha_advanced = false;
     c->grid_valid = false;
+    c->nbr_valid = false;
+    c->oct_valid = false;
+    c->oct_built = false;
     drop_graph(c);
     CK(cudaStreamSynchronize(c->stream));
     return take_device_errors(c, nullptr);
@@ -535,6 +558,9 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
     if (void* arr = sort_array(c, field, &count)) {
         if (n < 0 || (size_t)n > count) return fail(SPHMP_ERR_CAPACITY, "n %d exceeds %zu entries", n, count);
         CK(cudaMemcpyAsync(arr, host, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+        c->nbr_valid = false;
+        c->oct_valid = false;
+        c->oct_built = false;
         if (field == SPHMP_F_MGRIDCNT) {
             // rebuild the cell starts (and mgridoff) from the uploaded counts
             CK(cudaMemcpyAsync(c->B.ccount, c->B.mgridcnt, sizeof(uint32_t) * (size_t)c->prm.gridtotal,
@@ -542,7 +568,7 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
             DevParams P = dev_params(c);
             const int saved = P.n;
             P.n = 0;  // scan only: no scatter / cell sort
-            launch_grid_list(P, c->B, c->stream);
+            launch_grid_list(P, c->B, c->cur, c->stream);
             P.n = saved;
             // cstart[G+1] must still be n
             const uint32_t nn = (uint32_t)c->n;
@@ -570,6 +596,11 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
     const DevParams P = dev_params(c);
     launch_unpack_field(P, c->B, c->cur, field, a_cur, a_pre, c->stage, n, c->stream);
     CHECK_LAUNCH("unpack field");
+    if (field == SPHMP_F_POS) {
+        c->nbr_valid = false;
+        c->oct_valid = false;
+        c->oct_built = false;
+    }
     drop_graph(c);
     CK(cudaStreamSynchronize(c->stream));
     return SPHMP_OK;
@@ -582,13 +613,17 @@ sphmp_status sphmp_get_particle_index(sphmp_ctx* c) {
     launch_hash(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("GetParticleIndex");
     c->grid_valid = false;
+    c->nbr_valid = false;
+    c->oct_valid = false;
+    c->oct_built = false;
     return SPHMP_OK;
 }
 
 sphmp_status sphmp_get_grid_list(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
-    launch_grid_list(dev_params(c), c->B, c->stream);
+    launch_grid_list(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("GetGridList");
+    c->oct_built = true;
     return SPHMP_OK;
 }
 
@@ -599,6 +634,9 @@ sphmp_status sphmp_rearrange_data(sphmp_ctx* c) {
     swap_all(c);
     c->alpha_advanced = false;
     c->grid_valid = true;
+    c->nbr_valid = false;
+    c->oct_valid = c->oct_built;
+    c->oct_built = false;
     return SPHMP_OK;
 }
 
@@ -607,6 +645,8 @@ sphmp_status sphmp_compute_boundary_density(sphmp_ctx* c) {
     if (sphmp_status st = need_grid(c)) return st;
     launch_boundary_volume(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("ComputeBoundaryDensity");
+    c->oct_valid = false;  // the octant-order copy of pos4 still holds the old volumes
+    c->nbr_valid = false;
     return SPHMP_OK;
 }
 
@@ -615,6 +655,7 @@ sphmp_status sphmp_compute_pressure(sphmp_ctx* c) {
     if (sphmp_status st = need_grid(c)) return st;
     launch_density(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("MfComputePressure");
+    c->nbr_valid = true;
     return SPHMP_OK;
 }
 
@@ -660,6 +701,8 @@ sphmp_status sphmp_advance(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     launch_advance(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("MfAdvance");
+    c->nbr_valid = false;
+    c->oct_valid = false;
     return SPHMP_OK;
 }
 

@@ -33,6 +33,7 @@ constexpr int kScanItems = 4;         // items per thread in the scan
 constexpr int kWarpSortMax = 256;     // cells up to this size are sorted by one warp
 constexpr int kCtaSortMax = 8192;     // larger cells up to this size are sorted by one CTA
 constexpr int kNumFloat4Fields = 5;   // pos4, vel4, vev4, alpha4, aprev4
+constexpr int kMaxNbr = 128;          // neighbour-list capacity per particle (more: the passes rescan)
 
 // Error bits accumulated in the device error word (1 << sphmp_status).
 constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
@@ -51,6 +52,9 @@ struct DevParams {
     float srad[3];   // search radius h/simscale in cell units per axis, plus a rounding margin
     float ss;        // simscale
     float h, r2;     // smoothing radius and its square
+    float r2list;    // squared radius of the neighbour list (r2 plus a rounding margin)
+    int use_list;    // 1: the neighbour list matches the current slot order
+    int use_oct;     // 1: the octant order matches the current slot order and positions
     float dt;
     float kpoly6, kspikydiff;
     float bvisc;
@@ -91,6 +95,13 @@ struct DevBuffers {
     uint32_t* err;      // device error word
     double* red;        // [16] FP64 reduction results
     float* vtmp;        // [cap] scratch (boundary volumes)
+    uint32_t* nbr;      // [kMaxNbr * cap] neighbour slots, column-major: entry k of slot s at k * cap + s
+    uint32_t* nbr_cnt;  // [cap] neighbours of slot s (> kMaxNbr: list overflowed, rescan)
+    // Octant order: inside every 2h cell, members grouped by the h-subcell (octant)
+    // they occupy, octant index (oy * 2 + oz) * 2 + ox. Covers the in-grid slots.
+    float4* pos4o;      // [cap] pos4 of the member at octant-order position o
+    uint32_t* oidx;     // [cap] slot of the member at octant-order position o
+    uint32_t* oct_start;// [8 * G] first octant-order position of bucket (cell, octant)
 };
 
 enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
@@ -98,11 +109,12 @@ enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
 // ---- launchers (sphmp_kernels.cu) ----
 // All take the current double-buffer selectors in `cur` (one per Field4).
 void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
-void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+// (reads the pre-sort positions pos4[cur[POS]] to build the octant order)
+void launch_grid_list(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 // the two halves of launch_grid_list: cell starts (histogram scan), then the
-// scatter and per-cell stable ordering
+// scatter, the per-cell stable ordering and the per-cell octant order
 void launch_cell_starts(const DevParams& P, const DevBuffers& B, cudaStream_t s);
-void launch_cell_order(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_cell_order(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);

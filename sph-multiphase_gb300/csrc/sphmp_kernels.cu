@@ -84,6 +84,23 @@ __device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_
 
 __device__ __forceinline__ void set_err(const DevBuffers& B, uint32_t bit) { atomicOr(B.err, bit); }
 
+// Visit the neighbour candidates of slot s: the list written by the density pass
+// when it is valid and did not overflow, otherwise the cell search. Every lane
+// of a warp walks its own list, so the per-neighbour work runs converged.
+template <class F>
+__device__ __forceinline__ void for_neighbours(const DevParams& P, const DevBuffers& B, int s, float x, float y,
+                                               float z, F&& f) {
+    if (P.use_list) {
+        const uint32_t cnt = B.nbr_cnt[s];
+        if (cnt <= (uint32_t)kMaxNbr) {
+            const uint32_t* __restrict__ col = B.nbr + s;
+            for (uint32_t k = 0; k < cnt; k++) f(__ldg(col + (size_t)k * P.cap));
+            return;
+        }
+    }
+    for_candidates(P, B.cstart, x, y, z, f);
+}
+
 // ---------------------------------------------------------------------------
 // Hash + histogram (GetParticleIndexCUDA)
 // ---------------------------------------------------------------------------
@@ -236,8 +253,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(const __grid_constant
             B.mgridoff[c] = v[k] ? (int32_t)run : 0;
             B.mgridcnt[c] = (int32_t)v[k];
             if (v[k] > (uint32_t)kWarpSortMax) {
-                if (v[k] > (uint32_t)kCtaSortMax) set_err(B, kErrCellOverflow);
-                else {
+                if (v[k] > (uint32_t)kCtaSortMax) {
+                    set_err(B, kErrCellOverflow);  // left unsorted; keep its octant ranges in bounds
+                    for (int b = 0; b < 8; b++) B.oct_start[(size_t)c * 8 + b] = run;
+                } else {
                     const uint32_t slot = atomicAdd(&B.big[0], 1u);
                     B.big[1 + slot] = (uint32_t)c;
                 }
@@ -306,8 +325,36 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[E]) {
     }
 }
 
+// Octant (h-subcell inside its 2h cell) of an in-grid position: bit 0 = x half,
+// bit 1 = z half, bit 2 = y half, from int(2 t) with t the reference's grid coordinate.
+__device__ __forceinline__ uint32_t octant_of(const DevParams& P, const float4 p) {
+    const int hx = __float2int_rz(2.f * grid_t(p.x, P.gmin[0], P.fac[0]));
+    const int hy = __float2int_rz(2.f * grid_t(p.y, P.gmin[1], P.fac[1]));
+    const int hz = __float2int_rz(2.f * grid_t(p.z, P.gmin[2], P.fac[2]));
+    return (uint32_t)(((hy & 1) * 2 + (hz & 1)) * 2 + (hx & 1));
+}
+
+// Write the octant order of cell c from the key (octant << shift | member index)
+// held at sorted position q (cellstart + q is its octant-order position).
+__device__ __forceinline__ void emit_octant(const DevBuffers& B, uint32_t c, uint32_t start, uint32_t cnt, uint32_t q,
+                                            uint32_t key, uint32_t prev_oct, int shift, const float4* __restrict__ pos_in,
+                                            uint32_t pre_slot) {
+    const uint32_t oct = key >> shift;
+    const uint32_t idx = key & ((1u << shift) - 1u);
+    if (q < cnt) {
+        B.pos4o[start + q] = pos_in[pre_slot];
+        B.oidx[start + q] = start + idx;
+    }
+    // bucket starts: every bucket in (prev_oct, oct] begins at q (8 marks past the end)
+    const uint32_t hi = q < cnt ? oct : 8u;
+    for (uint32_t b = prev_oct + 1; b <= hi && b < 8; b++) B.oct_start[(size_t)c * 8 + b] = start + q;
+    if (q == cnt - 1)
+        for (uint32_t b = oct + 1; b < 8; b++) B.oct_start[(size_t)c * 8 + b] = start + cnt;
+}
+
 template <int E>
-__device__ __forceinline__ void warp_sort_cell(const DevBuffers& B, uint32_t c, uint32_t start, uint32_t cnt) {
+__device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuffers& B, const float4* __restrict__ pos_in,
+                                               uint32_t* wsm, uint32_t c, uint32_t start, uint32_t cnt) {
     uint32_t v[E];
     const unsigned lane = lane_id();
 #pragma unroll
@@ -316,35 +363,76 @@ __device__ __forceinline__ void warp_sort_cell(const DevBuffers& B, uint32_t c, 
         v[r] = idx < cnt ? B.sidx[start + idx] : 0xFFFFFFFFu;
     }
     warp_bitonic<E>(v);
+    // stable order: pre-sort slots ascending
+    uint32_t key[E];
 #pragma unroll
     for (int r = 0; r < E; r++) {
         const uint32_t idx = lane * E + r;
+        wsm[idx] = v[r];
+        key[r] = 0xFFFFFFFFu;
         if (idx < cnt) {
             B.midsort[start + idx] = v[r];
             B.mgcell[start + idx] = c;
             B.mgndx[start + idx] = idx;
+            key[r] = (octant_of(P, pos_in[v[r]]) << 8) | idx;
         }
     }
+    // octant order: sort (octant, member index)
+    warp_bitonic<E>(key);
+    __syncwarp();
+    const uint32_t last_prev = __shfl_up_sync(0xffffffffu, key[E - 1], 1);
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const uint32_t q = lane * E + r;
+        const uint32_t pk = r > 0 ? key[r - 1] : (lane > 0 ? last_prev : 0xFFFFFFFFu);
+        const uint32_t prev_oct = (q == 0) ? 0xFFFFFFFFu : (pk == 0xFFFFFFFFu ? 8u : pk >> 8);
+        if (q <= cnt) {
+            const uint32_t k = key[r];
+            const uint32_t pre = q < cnt ? wsm[k & 255u] : 0u;
+            emit_octant(B, c, start, cnt, q, q < cnt ? k : (8u << 8), prev_oct, 8, pos_in, pre);
+        }
+    }
+    __syncwarp();
 }
 
 // One warp per cell (cells of up to kWarpSortMax members).
 __global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ DevParams P,
-                                                        const __grid_constant__ DevBuffers B) {
+                                                        const __grid_constant__ DevBuffers B,
+                                                        const float4* __restrict__ pos_in) {
+    __shared__ uint32_t sm[kThreads / 32][kWarpSortMax];
+    uint32_t* wsm = sm[threadIdx.x >> 5];
     const int nwarps = (gridDim.x * kThreads) >> 5;
     for (int c = (blockIdx.x * kThreads + threadIdx.x) >> 5; c < P.G; c += nwarps) {
         const uint32_t start = B.cstart[c];
         const uint32_t cnt = B.cstart[c + 1] - start;
         if (cnt == 0 || cnt > (uint32_t)kWarpSortMax) continue;
-        if (cnt <= 32) warp_sort_cell<1>(B, c, start, cnt);
-        else if (cnt <= 64) warp_sort_cell<2>(B, c, start, cnt);
-        else if (cnt <= 128) warp_sort_cell<4>(B, c, start, cnt);
-        else warp_sort_cell<8>(B, c, start, cnt);
+        if (cnt <= 32) warp_sort_cell<1>(P, B, pos_in, wsm, c, start, cnt);
+        else if (cnt <= 64) warp_sort_cell<2>(P, B, pos_in, wsm, c, start, cnt);
+        else if (cnt <= 128) warp_sort_cell<4>(P, B, pos_in, wsm, c, start, cnt);
+        else warp_sort_cell<8>(P, B, pos_in, wsm, c, start, cnt);
     }
 }
 
-// One CTA per large cell (kWarpSortMax < members <= kCtaSortMax): bitonic sort in shared memory.
+__device__ __forceinline__ void cta_bitonic(uint32_t* sm, uint32_t M) {
+    for (uint32_t k = 2; k <= M; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t t = threadIdx.x; t < M; t += blockDim.x) {
+                const uint32_t p = t ^ j;
+                if (p > t) {
+                    const bool asc = (t & k) == 0;
+                    const uint32_t a = sm[t], q = sm[p];
+                    if (asc ? (a > q) : (a < q)) { sm[t] = q; sm[p] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// One CTA per large cell (kWarpSortMax < members <= kCtaSortMax): bitonic sorts in shared memory.
 __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ DevParams P,
-                                                        const __grid_constant__ DevBuffers B) {
+                                                        const __grid_constant__ DevBuffers B,
+                                                        const float4* __restrict__ pos_in) {
     __shared__ uint32_t sm[kCtaSortMax];
     const uint32_t nbig = B.big[0];
     for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
@@ -355,23 +443,23 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
         while (M < cnt) M <<= 1;
         for (uint32_t k = threadIdx.x; k < M; k += blockDim.x) sm[k] = k < cnt ? B.sidx[start + k] : 0xFFFFFFFFu;
         __syncthreads();
-        for (uint32_t k = 2; k <= M; k <<= 1) {
-            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                for (uint32_t t = threadIdx.x; t < M; t += blockDim.x) {
-                    const uint32_t p = t ^ j;
-                    if (p > t) {
-                        const bool asc = (t & k) == 0;
-                        const uint32_t a = sm[t], q = sm[p];
-                        if (asc ? (a > q) : (a < q)) { sm[t] = q; sm[p] = a; }
-                    }
-                }
-                __syncthreads();
-            }
-        }
+        cta_bitonic(sm, M);
         for (uint32_t k = threadIdx.x; k < cnt; k += blockDim.x) {
             B.midsort[start + k] = sm[k];
             B.mgcell[start + k] = c;
             B.mgndx[start + k] = k;
+        }
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < M; k += blockDim.x)
+            sm[k] = k < cnt ? ((octant_of(P, pos_in[B.midsort[start + k]]) << 13) | k) : 0xFFFFFFFFu;
+        __syncthreads();
+        cta_bitonic(sm, M);
+        for (uint32_t q = threadIdx.x; q <= cnt && q < M + 1; q += blockDim.x) {
+            const uint32_t k = q < cnt ? sm[q] : (8u << 13);
+            const uint32_t pk = q == 0 ? 0xFFFFFFFFu : sm[q - 1];
+            const uint32_t prev_oct = q == 0 ? 0xFFFFFFFFu : (pk >> 13);
+            const uint32_t pre = q < cnt ? B.midsort[start + (k & 0x1FFFu)] : 0u;
+            emit_octant(B, c, start, cnt, q, k, prev_oct, 13, pos_in, pre);
         }
         __syncthreads();
     }
@@ -443,6 +531,83 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // Density + EOS pressure (MfComputePressureCUDA)
 // ---------------------------------------------------------------------------
 
+// Density + EOS with the octant order: one thread per in-grid particle, taken in
+// octant order so the lanes of a warp share cell and octant. The search visits
+// the h-subcells within h of the particle (at most 4 per axis, normally 3),
+// limited to the reference's 3x3x3 cells; along x, the subcells of one cell are
+// adjacent octant buckets, so each (y, z) subcell row is at most two ranges.
+// Writes 1/rho and p like k_density, plus the neighbour list.
+__global__ void __launch_bounds__(kThreads) k_density_oct(const __grid_constant__ DevParams P,
+                                                          const __grid_constant__ DevBuffers B,
+                                                          const float4* __restrict__ alpha4) {
+    const uint32_t nin = B.cstart[P.G];
+    const uint32_t o = blockIdx.x * kThreads + threadIdx.x;
+    if (o >= nin) return;
+    const uint32_t s = B.oidx[o];
+    const float4 pi = B.pos4o[o];
+    if (pi.w < 0.f) {
+        B.densp[s] = make_float2(-pi.w, 0.f);
+        B.nbr_cnt[s] = 0;
+        return;
+    }
+    const float rho0 = alpha4[s].w;
+    const float t[3] = {grid_t(pi.x, P.gmin[0], P.fac[0]), grid_t(pi.y, P.gmin[1], P.fac[1]),
+                        grid_t(pi.z, P.gmin[2], P.fac[2])};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int g2 = 2 * __float2int_rz(t[a]);
+        const float u = 2.f * t[a];
+        const float R = 2.f * P.srad[a];
+        lo[a] = max(g2 - 2, __float2int_rd(u - R));
+        hi[a] = min(g2 + 3, __float2int_rd(u + R));
+    }
+    Kahan sum;
+    uint32_t cnt = 0;
+    uint32_t* __restrict__ col = B.nbr + s;
+    for (int hy = lo[1]; hy <= hi[1]; hy++) {
+        const int cy = hy >> 1, oy = hy & 1;
+        for (int hz = lo[2]; hz <= hi[2]; hz++) {
+            const int cz = hz >> 1, oz = hz & 1;
+            const int rowc = (cy * P.rz + cz) * P.rx;
+            for (int cx = lo[0] >> 1; cx <= (hi[0] >> 1); cx++) {
+                const uint32_t c = (uint32_t)(rowc + cx);
+                const uint32_t ce = __ldg(&B.cstart[c + 1]);
+                if (__ldg(&B.cstart[c]) == ce) continue;
+                const int oxlo = max(lo[0] - 2 * cx, 0), oxhi = min(hi[0] - 2 * cx, 1);
+                const int bq = (oy * 2 + oz) * 2;
+                const uint32_t k0 = __ldg(&B.oct_start[(size_t)c * 8 + bq + oxlo]);
+                const uint32_t k1 = (bq + oxhi == 7) ? ce : __ldg(&B.oct_start[(size_t)c * 8 + bq + oxhi + 1]);
+                for (uint32_t k = k0; k < k1; k++) {
+                    const float4 pj = __ldg(&B.pos4o[k]);
+                    const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+                    const float dsq = dx * dx + dy * dy + dz * dz;
+                    if (dsq < P.r2) {
+                        const float cc = P.r2 - dsq;
+                        const float m = pj.w > 0.f ? pj.w : rho0 * (-pj.w);
+                        sum.add(cc * cc * cc * m);
+                        if (dsq > 0.f) {
+                            if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = __ldg(&B.oidx[k]);
+                            cnt++;
+                        }
+                    } else if (dsq < P.r2list) {
+                        if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = __ldg(&B.oidx[k]);
+                        cnt++;
+                    }
+                }
+            }
+        }
+    }
+    B.nbr_cnt[s] = cnt;
+    float rho = sum.s * P.kpoly6;
+    if (rho == 0.f) rho = 1.f;
+    float p;
+    if (P.eos == SPHMP_EOS_LINEAR) p = P.eos_k * (rho - rho0);
+    else p = 2.5f * rho0 * (powf(rho / rho0, 7.0f) - 1.0f);
+    if (p < 0.f) p = 0.f;
+    B.densp[s] = make_float2(1.f / rho, p);
+}
+
 __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ DevParams P,
                                                       const __grid_constant__ DevBuffers B,
                                                       const float4* __restrict__ pos4,
@@ -450,12 +615,15 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= P.n || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
-    if (pi.w < 0.f) {  // boundary: carries its volume, no pressure
+    if (pi.w < 0.f) {  // boundary: carries its volume, no pressure, needs no list
         B.densp[s] = make_float2(-pi.w, 0.f);
+        B.nbr_cnt[s] = 0;
         return;
     }
     const float rho0 = alpha4[s].w;
     Kahan sum;
+    uint32_t cnt = 0;
+    uint32_t* __restrict__ col = B.nbr + s;
     for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
@@ -465,7 +633,12 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
             const float m = pj.w > 0.f ? pj.w : rho0 * (-pj.w);
             sum.add(c * c * c * m);
         }
+        if (dsq > 0.f && dsq < P.r2list) {
+            if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = j;
+            cnt++;
+        }
     });
+    B.nbr_cnt[s] = cnt;
     float rho = sum.s * P.kpoly6;
     if (rho == 0.f) rho = 1.f;
     float p;
@@ -480,7 +653,7 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
 // ---------------------------------------------------------------------------
 
 template <bool FORCE, bool DRIFT, int NP>
-__global__ void __launch_bounds__(kThreads) k_force_drift(const __grid_constant__ DevParams P,
+__global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_constant__ DevParams P,
                                                           const __grid_constant__ DevBuffers B,
                                                           const float4* __restrict__ pos4,
                                                           const float4* __restrict__ vel4,
@@ -512,14 +685,14 @@ __global__ void __launch_bounds__(kThreads) k_force_drift(const __grid_constant_
             ag[k] = make_float3(0.f, 0.f, 0.f);
         }
     }
-    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+    for_neighbours(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
         const float dsq = dx * dx + dy * dy + dz * dz;
         if (!(dsq < P.r2 && dsq > 0.f)) return;
-        const float r = sqrtf(dsq);
-        const float c = P.h - r;
-        const float g1 = P.kspikydiff * c * c / r;
+        const float rinv = rsqrtf(dsq);  // 1/r; r = dsq/r
+        const float c = P.h - dsq * rinv;
+        const float g1 = P.kspikydiff * c * c * rinv;
         if (pj.w > 0.f) {  // fluid neighbour
             const float2 dpj = __ldg(&B.densp[j]);
             const float g = g1 * pj.w * dpj.x;
@@ -645,16 +818,16 @@ __device__ __forceinline__ void alpha_change(const DevParams& P, const DevBuffer
         um[k] = make_float3(u.x, u.y, u.z);
     }
     Kahan acc[NP];
-    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+    for_neighbours(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         if (pj.w < 0.f) return;  // boundary neighbours do not exchange volume fraction
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
         const float dsq = dx * dx + dy * dy + dz * dz;
         if (!(dsq < P.r2 && dsq > 0.f)) return;
-        const float r = sqrtf(dsq);
-        const float c = P.h - r;
+        const float rinv = rsqrtf(dsq);
+        const float c = P.h - dsq * rinv;
         const float2 dpj = __ldg(&B.densp[j]);
-        const float cm = P.kspikydiff * c * c / r * pj.w * dpj.x;
+        const float cm = P.kspikydiff * c * c * rinv * pj.w * dpj.x;
         const float4 vej = __ldg(&vev4[j]);
         const float dot1 = (vej.x - vei.x) * dx + (vej.y - vei.y) * dy + (vej.z - vei.z) * dz;
         const float4 aj = __ldg(&alpha4[j]);
@@ -810,7 +983,7 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
 // Fused alpha advance + correction + advance: reads the cur buffers, writes
 // every float4 field of every slot into the other buffer.
 template <int NP, bool MP>
-__global__ void __launch_bounds__(kThreads) k_pass_c(const __grid_constant__ DevParams P,
+__global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ DevParams P,
                                                      const __grid_constant__ DevBuffers B,
                                                      const __grid_constant__ F4Set S) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
@@ -1078,17 +1251,18 @@ void launch_cell_starts(const DevParams& P, const DevBuffers& B, cudaStream_t s)
     k_scan_apply<<<nb, kScanBlock, 0, s>>>(P, B);
 }
 
-void launch_cell_order(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+void launch_cell_order(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
     if (P.n <= 0) return;
+    const float4* pos_in = B.f4[POS][cur[POS]];
     k_scatter<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
     const int grid = min(blocks_for(P.G * 32), 152 * 16);
-    k_cell_sort<<<grid, kThreads, 0, s>>>(P, B);
-    k_big_cell_sort<<<64, 1024, 0, s>>>(P, B);
+    k_cell_sort<<<grid, kThreads, 0, s>>>(P, B, pos_in);
+    k_big_cell_sort<<<64, 1024, 0, s>>>(P, B, pos_in);
 }
 
-void launch_grid_list(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+void launch_grid_list(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
     launch_cell_starts(P, B, s);
-    launch_cell_order(P, B, s);
+    launch_cell_order(P, B, cur, s);
 }
 
 void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
@@ -1104,7 +1278,10 @@ void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* 
 
 void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
     if (P.n <= 0) return;
-    k_density<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[ALPHA][cur[ALPHA]]);
+    if (P.use_oct)
+        k_density_oct<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[ALPHA][cur[ALPHA]]);
+    else
+        k_density<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[ALPHA][cur[ALPHA]]);
 }
 
 template <bool F, bool D>

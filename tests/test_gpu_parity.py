@@ -38,12 +38,23 @@ def _scene(kind):
 KINDS = ["tait2", "tait3", "linear1", "simscale", "dam"]
 
 
-def _sorted_pair(kind):
+def _resort(p, s, ctx):
+    for st in ("orc_get_particle_index", "orc_get_grid_list", "orc_rearrange_data"):
+        O.call(st, p, s)
+    ctx.sort()
+
+
+def _sorted_pair(kind, resort=True):
+    """Both sides sorted with boundary volumes computed. With `resort`, a second
+    sort (idempotent on the slot order) rebuilds the device's octant order, so the
+    density runs its octant-order kernel; without it, the slot-order kernel."""
     sc = _scene(kind)
     s = oracle_state(sc)
     O.before_first_step(sc.params, s)
     ctx = device_ctx(sc)
     ctx.before_first_step()
+    if resort:
+        _resort(sc.params, s, ctx)
     ctx.sync()
     return sc, s, ctx
 
@@ -71,9 +82,10 @@ def test_sort_bit_exact(kind):
     ctx.close()
 
 
+@pytest.mark.parametrize("resort", [True, False], ids=["octant", "slot_order"])
 @pytest.mark.parametrize("kind", KINDS)
-def test_density_force_advance(kind):
-    sc, s, ctx = _sorted_pair(kind)
+def test_density_force_advance(kind, resort):
+    sc, s, ctx = _sorted_pair(kind, resort)
     p = sc.params
     O.call("orc_compute_pressure", p, s)
     ctx.compute_pressure()
