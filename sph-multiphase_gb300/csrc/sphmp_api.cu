@@ -27,6 +27,7 @@ struct sphmp_ctx {
     bool nbr_valid = false;       // neighbour list built by the density pass for the current positions
     bool oct_built = false;       // the last grid list also built the octant order
     bool oct_valid = false;       // octant order matches the current slot order and positions
+    int list_mode = 0;            // kind of list the last density pass wrote (DevParams::list_mode)
     int device = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
@@ -109,8 +110,7 @@ DevParams dev_params(const sphmp_ctx* c) {
     P.h = p.smoothradius;
     P.r2 = p.smoothradius * p.smoothradius;
     P.r2list = P.r2 * (1.0f + 1.0e-5f);
-    P.use_list = c->nbr_valid ? 1 : 0;
-    P.use_oct = c->oct_valid ? 1 : 0;
+    P.list_mode = c->nbr_valid ? c->list_mode : 0;
     P.dt = p.dt;
     P.kpoly6 = p.kpoly6;
     P.kspikydiff = p.kspikydiff;
@@ -150,7 +150,7 @@ void free_buffers(sphmp_ctx* c) {
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
                     B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
                     B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.pos4o, B.oidx, B.oct_start,
-                    c->stage};
+                    B.act, B.act_n, B.nbr16, c->stage};
     for (void* q : ptrs) cudaFree(q);
     memset(&c->B, 0, sizeof(c->B));
     c->stage = nullptr;
@@ -196,6 +196,10 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.pos4o, N));
     CK(dalloc(&B.oidx, N));
     CK(dalloc(&B.oct_start, 8 * G));
+    CK(dalloc(&B.act, G));
+    CK(dalloc(&B.act_n, 1));
+    CK(dalloc(&B.nbr16, (size_t)kMaxNbr * N));
+    CK(cudaMemset(B.act_n, 0, sizeof(uint32_t)));
     c->stage_bytes = N * (sizeof(sphmp_display_pack) + sizeof(sphmp_calc_pack));
     if (c->stage_bytes < G * sizeof(int32_t)) c->stage_bytes = G * sizeof(int32_t);
     CK(cudaMalloc(&c->stage, c->stage_bytes));
@@ -254,6 +258,28 @@ inline void swap_all(sphmp_ctx* c) {
     for (int f = 0; f < kNumFloat4Fields; f++) c->cur[f] ^= 1;
 }
 
+// Density pass: the cell-block kernel when the octant order of this sort is valid
+// (it writes stage-index lists), otherwise the slot-order kernel (slot lists).
+void run_density(sphmp_ctx* c, cudaStream_t s) {
+    const DevParams P = dev_params(c);
+    if (c->oct_valid) {
+        launch_density_oct(P, c->B, c->cur, s);
+        c->list_mode = 1;
+    } else {
+        launch_density(P, c->B, c->cur, s);
+        c->list_mode = 1;
+    }
+    c->nbr_valid = true;
+}
+
+inline bool block_lists(const sphmp_ctx* c) { return c->nbr_valid && c->list_mode == 2 && c->oct_valid; }
+
+void run_force_drift(sphmp_ctx* c, bool force, bool drift, cudaStream_t s) {
+    const DevParams P = dev_params(c);
+    if (block_lists(c)) launch_force_drift_blk(P, c->B, c->cur, force, drift, s);
+    else launch_force_drift(P, c->B, c->cur, force, drift, s);
+}
+
 // Optional event marks between the stages of a step (for sphmp_step_profile).
 struct StageTimer {
     static constexpr int kMax = 24;
@@ -297,40 +323,42 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     c->grid_valid = true;
     c->oct_valid = true;
     c->nbr_valid = false;
-    launch_density(dev_params(c), c->B, c->cur, s);
+    run_density(c, s);
     mark("density");
-    c->nbr_valid = true;
     const DevParams PL = dev_params(c);  // neighbour passes read the list
+    const bool blk = block_lists(c);
     if (schedule == SPHMP_SCHEDULE_FUSED) {
-        launch_force_drift(PL, c->B, c->cur, true, P.multiphase != 0, s);
+        run_force_drift(c, true, PL.multiphase != 0, s);
         mark("force_drift");
-        if (P.st_on) {
+        if (PL.st_on) {
             launch_surface_tension(PL, c->B, c->cur, s);
             mark("surface_tension");
         }
-        launch_pass_c(PL, c->B, c->cur, s);
-        mark(P.multiphase ? "alpha_correct_advance" : "advance");
+        if (blk) launch_pass_c_blk(PL, c->B, c->cur, s);
+        else launch_pass_c(PL, c->B, c->cur, s);
+        mark(PL.multiphase ? "alpha_correct_advance" : "advance");
         swap_all(c);
         c->nbr_valid = false;  // positions moved
         c->oct_valid = false;
     } else {
-        if (P.multiphase) {
-            launch_force_drift(PL, c->B, c->cur, false, true, s);
+        if (PL.multiphase) {
+            run_force_drift(c, false, true, s);
             mark("drift");
-            launch_alpha_advance(PL, c->B, c->cur, s);
+            if (blk) launch_alpha_advance_blk(PL, c->B, c->cur, s);
+            else launch_alpha_advance(PL, c->B, c->cur, s);
             mark("alpha_advance");
             c->cur[ALPHA] ^= 1;
             c->alpha_advanced = true;
-            launch_correction(PL, c->B, c->cur, c->cur[ALPHA] ^ 1, s);
+            launch_correction(dev_params(c), c->B, c->cur, c->cur[ALPHA] ^ 1, s);
             mark("correction");
         }
-        launch_force_drift(PL, c->B, c->cur, true, false, s);
+        run_force_drift(c, true, false, s);
         mark("force");
-        if (P.st_on) {
+        if (PL.st_on) {
             launch_surface_tension(PL, c->B, c->cur, s);
             mark("surface_tension");
         }
-        launch_advance(PL, c->B, c->cur, s);
+        launch_advance(dev_params(c), c->B, c->cur, s);
         mark("advance");
         c->nbr_valid = false;
         c->oct_valid = false;
@@ -653,16 +681,15 @@ sphmp_status sphmp_compute_boundary_density(sphmp_ctx* c) {
 sphmp_status sphmp_compute_pressure(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (sphmp_status st = need_grid(c)) return st;
-    launch_density(dev_params(c), c->B, c->cur, c->stream);
+    run_density(c, c->stream);
     CHECK_LAUNCH("MfComputePressure");
-    c->nbr_valid = true;
     return SPHMP_OK;
 }
 
 sphmp_status sphmp_compute_drift_vel(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (sphmp_status st = need_grid(c)) return st;
-    launch_force_drift(dev_params(c), c->B, c->cur, false, true, c->stream);
+    run_force_drift(c, false, true, c->stream);
     CHECK_LAUNCH("MfComputeDriftVel");
     return SPHMP_OK;
 }
@@ -672,7 +699,8 @@ sphmp_status sphmp_compute_alpha_advance(sphmp_ctx* c) {
     if (sphmp_status st = need_grid(c)) return st;
     if (c->alpha_advanced)
         return fail(SPHMP_ERR_STATE, "volume fractions already advanced in this step (re-sort first)");
-    launch_alpha_advance(dev_params(c), c->B, c->cur, c->stream);
+    if (block_lists(c)) launch_alpha_advance_blk(dev_params(c), c->B, c->cur, c->stream);
+    else launch_alpha_advance(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("MfComputeAlphaAdvance");
     c->cur[ALPHA] ^= 1;
     c->alpha_advanced = true;
@@ -691,7 +719,7 @@ sphmp_status sphmp_compute_force(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (sphmp_status st = need_grid(c)) return st;
     const DevParams P = dev_params(c);
-    launch_force_drift(P, c->B, c->cur, true, false, c->stream);
+    run_force_drift(c, true, false, c->stream);
     if (P.st_on) launch_surface_tension(P, c->B, c->cur, c->stream);
     CHECK_LAUNCH("MfComputeForce");
     return SPHMP_OK;

@@ -1,0 +1,393 @@
+// sphmp_device.cuh — device helpers and the per-pair physics of the multiphase
+// SPH step, shared by the slot-order kernels (sphmp_kernels.cu) and the
+// cell-block kernels (sphmp_cellblock.cu).
+//
+// The physics follows the reference kernels of ZP-Z/sph-multiphase:
+//   density / EOS      SPH_Solver/fluids/fluid_system_kern.cu:214-247, 279-318
+//   force              SPH_Solver/fluids/fluid_system_kern.cu:325-424
+//   drift velocity     SPH_Solver/fluids/multiphase.cu:19-166
+//   alpha advance      SPH_Solver/fluids/multiphase.cu:169-272
+//   correction         SPH_Solver/fluids/multiphase.cu:275-349
+//   advance            SPH_Solver/fluids/fluid_system_kern.cu:426-534
+// in FP32, with Kahan-compensated density and volume-fraction sums.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "sphmp_internal.h"
+
+namespace sphmp {
+namespace dev {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// Kahan-compensated float accumulator.
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ Kahan() : s(0.f), c(0.f) {}
+    __device__ __forceinline__ void add(float y) {
+        float yy = __fsub_rn(y, c);
+        float t = __fadd_rn(s, yy);
+        c = __fsub_rn(__fsub_rn(t, s), yy);
+        s = t;
+    }
+};
+
+// Grid coordinate in cell units, the reference's (pos - gridmin) * gridIdfac.
+__device__ __forceinline__ float grid_t(float p, float gmin, float fac) { return __fmul_rn(__fsub_rn(p, gmin), fac); }
+// int(t) is only defined inside the int range; outside it (and for NaN) the
+// particle is out of the grid.
+__device__ __forceinline__ bool t_ok(float t) { return t > -2147483520.f && t < 2147483520.f; }
+
+__device__ __forceinline__ uint32_t cell_key(const DevParams& P, float x, float y, float z) {
+    const float tx = grid_t(x, P.gmin[0], P.fac[0]);
+    const float ty = grid_t(y, P.gmin[1], P.fac[1]);
+    const float tz = grid_t(z, P.gmin[2], P.fac[2]);
+    if (!(t_ok(tx) && t_ok(ty) && t_ok(tz))) return kUndef;
+    const int gx = __float2int_rz(tx), gy = __float2int_rz(ty), gz = __float2int_rz(tz);
+    if (gx >= 1 && gx < P.rx - 1 && gy >= 1 && gy < P.ry - 1 && gz >= 1 && gz < P.rz - 1)
+        return (uint32_t)((gy * P.rz + gz) * P.rx + gx);
+    return kUndef;
+}
+
+// Octant (h-subcell inside its 2h cell) of an in-grid position: bit 0 = x half,
+// bit 1 = z half, bit 2 = y half, from int(2 t) with t the reference's grid coordinate.
+__device__ __forceinline__ uint32_t octant_of(const DevParams& P, const float4 p) {
+    const int hx = __float2int_rz(2.f * grid_t(p.x, P.gmin[0], P.fac[0]));
+    const int hy = __float2int_rz(2.f * grid_t(p.y, P.gmin[1], P.fac[1]));
+    const int hz = __float2int_rz(2.f * grid_t(p.z, P.gmin[2], P.fac[2]));
+    return (uint32_t)(((hy & 1) * 2 + (hz & 1)) * 2 + (hx & 1));
+}
+
+__device__ __forceinline__ void set_err(const DevBuffers& B, uint32_t bit) { atomicOr(B.err, bit); }
+
+// Visit the candidate slots of an in-grid particle at (x, y, z): along each axis
+// the cells within [t - R, t + R] (R = h in cell units plus a margin), limited
+// to the reference's +-1 cell. Cells along x are adjacent in the sorted order,
+// so each (y, z) row of cells is one contiguous slot range.
+template <class F>
+__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart, float x,
+                                               float y, float z, F&& f) {
+    const float t[3] = {grid_t(x, P.gmin[0], P.fac[0]), grid_t(y, P.gmin[1], P.fac[1]),
+                        grid_t(z, P.gmin[2], P.fac[2])};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int g = __float2int_rz(t[a]);
+        lo[a] = max(g - 1, __float2int_rd(t[a] - P.srad[a]));
+        hi[a] = min(g + 1, __float2int_rd(t[a] + P.srad[a]));
+    }
+    for (int yy = lo[1]; yy <= hi[1]; yy++) {
+        for (int zz = lo[2]; zz <= hi[2]; zz++) {
+            const int base = (yy * P.rz + zz) * P.rx;
+            const uint32_t j0 = __ldg(&cstart[base + lo[0]]);
+            const uint32_t j1 = __ldg(&cstart[base + hi[0] + 1]);
+            for (uint32_t j = j0; j < j1; j++) f(j);
+        }
+    }
+}
+
+// Visit the neighbour slots of slot s from the slot list written by the density
+// pass when it is valid and did not overflow, otherwise by the cell search.
+template <class F>
+__device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffers& B, int s, float x, float y,
+                                              float z, F&& f) {
+    if (P.list_mode != 0) {
+        const uint32_t raw = B.nbr_cnt[s];
+        const uint32_t cnt = raw & ~kListGlobal;
+        if ((P.list_mode == 1 || (raw & kListGlobal)) && cnt <= (uint32_t)kMaxNbr) {
+            const uint32_t* __restrict__ col = B.nbr + s;
+#pragma unroll 2
+            for (uint32_t k = 0; k < cnt; k++) f(__ldg(col + (size_t)k * P.cap));
+            return;
+        }
+    }
+    for_candidates(P, B.cstart, x, y, z, f);
+}
+
+// ---------------------------------------------------------------------------
+// Density + EOS (MfComputePressureCUDA)
+// ---------------------------------------------------------------------------
+
+// Tait (2.5 * rho0 * ((rho/rho0)^7 - 1), the 2.5 is a double literal in the
+// reference) or the linear extension, clamped at 0; rho == 0 reads as 1.
+__device__ __forceinline__ float2 density_result(const DevParams& P, float wsum, float rho0) {
+    float rho = wsum * P.kpoly6;
+    if (rho == 0.f) rho = 1.f;
+    float p;
+    if (P.eos == SPHMP_EOS_LINEAR) p = P.eos_k * (rho - rho0);
+    else p = 2.5f * rho0 * (powf(rho / rho0, 7.0f) - 1.0f);
+    if (p < 0.f) p = 0.f;
+    return make_float2(1.f / rho, p);
+}
+
+// ---------------------------------------------------------------------------
+// Force + drift velocity (MfComputeForceCUDA, MfComputeDriftVelCUDA)
+// ---------------------------------------------------------------------------
+
+// Accumulates the force (contributeForce_new) and / or the drift-velocity terms
+// (contributeDriftVel) of one in-grid fluid particle over its neighbours.
+// `pair` takes the neighbour's pos4, (1/rho, p), vel4 and alpha4.
+template <bool FORCE, bool DRIFT, int NP>
+struct ForceDrift {
+    static constexpr int K = NP > 0 ? NP : 1;
+    float4 pi, vi;
+    float idens, ipress, ivisc, rho0;
+    float ia[3];
+    float mc[K];
+    float relax_coef, invdens;
+    float fx, fy, fz;
+    float3 dv[K], ag[K];
+
+    __device__ __forceinline__ void init(const DevParams& P, float4 pi_, float4 vi_, float2 dpi, float4 ai) {
+        pi = pi_;
+        vi = vi_;
+        idens = dpi.x;
+        ipress = dpi.y;
+        ivisc = vi_.w;
+        rho0 = ai.w;
+        ia[0] = ai.x; ia[1] = ai.y; ia[2] = ai.z;
+        fx = fy = fz = 0.f;
+        relax_coef = invdens = 0.f;
+        if (DRIFT) {
+            relax_coef = P.relax / ivisc;
+            invdens = 1.f / rho0;
+#pragma unroll
+            for (int k = 0; k < NP; k++) {
+                mc[k] = ia[k] * P.dens_k[k] * invdens;
+                dv[k] = make_float3(0.f, 0.f, 0.f);
+                ag[k] = make_float3(0.f, 0.f, 0.f);
+            }
+        }
+    }
+
+    __device__ __forceinline__ void pair(const DevParams& P, const float4 pj, const float2 dpj, const float4 vj,
+                                         const float4 aj) {
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (!(dsq < P.r2 && dsq > 0.f)) return;
+        const float rinv = rsqrtf(dsq);  // 1/r; r = dsq/r
+        const float c = P.h - dsq * rinv;
+        const float g1 = P.kspikydiff * c * c * rinv;
+        if (pj.w > 0.f) {  // fluid neighbour
+            const float g = g1 * pj.w * dpj.x;
+            if (FORCE) {
+                const float pm = -0.5f * g * dpj.y * idens;
+                fx += dx * pm; fy += dy * pm; fz += dz * pm;
+                const float vm = g * (ivisc + vj.w) * idens;
+                fx += (vi.x - vj.x) * vm; fy += (vi.y - vj.y) * vm; fz += (vi.z - vj.z) * vm;
+            }
+            if (DRIFT) {
+                const float ja[3] = {aj.x, aj.y, aj.z};
+                float3 pg[K];
+                float3 psum = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    const float pm = g * (-ia[k] * ipress + ja[k] * dpj.y);
+                    pg[k] = make_float3(pm * dx, pm * dy, pm * dz);
+                    psum.x += pg[k].x * mc[k]; psum.y += pg[k].y * mc[k]; psum.z += pg[k].z * mc[k];
+                    const float ga = (ja[k] - ia[k]) * g;
+                    ag[k].x += ga * dx; ag[k].y += ga * dy; ag[k].z += ga * dz;
+                }
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    dv[k].x -= relax_coef * (pg[k].x - psum.x);
+                    dv[k].y -= relax_coef * (pg[k].y - psum.y);
+                    dv[k].z -= relax_coef * (pg[k].z - psum.z);
+                }
+            }
+        } else if (FORCE) {  // boundary neighbour, volume V_j = -w
+            const float V = -pj.w;
+            const float pm = -g1 * rho0 * V * ipress * idens * idens;
+            fx += dx * pm; fy += dy * pm; fz += dz * pm;
+            float pij = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
+            if (pij < 0.f) {
+                pij = pij / (dsq + P.r2 * 0.01f);
+                pij = pij * P.bvisc * P.h / 2.f / rho0;
+                pij = g1 * rho0 * V * pij;
+                fx += dx * pij; fy += dy * pij; fz += dz * pij;
+            }
+        }
+    }
+
+    // mfComputeDriftVel's closing terms (multiphase.cu:131-163) and the stores.
+    __device__ __forceinline__ void finish(const DevParams& P, const DevBuffers& B, int s, const float4 ap) {
+        if (FORCE) B.accel4[s] = make_float4(fx, fy, fz, 0.f);
+        if (DRIFT) {
+            const float cc = P.cont * P.cont2;
+            const float cs = P.cont * P.cont1 * P.sigma;
+            float3 out[K], st[K];
+            float dsum = 0.f;
+            float3 ssum = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < NP; k++) {
+                out[k] = make_float3(cc * dv[k].x, cc * dv[k].y, cc * dv[k].z);
+                const float temp = ia[k];
+                dsum += temp * P.dens_k[k] * P.dens_k[k] * invdens;
+                // `temp > 0.0001` in double is exactly `temp > 1e-4f` in float
+                st[k] = temp > 1e-4f ? make_float3(ag[k].x / temp, ag[k].y / temp, ag[k].z / temp)
+                                     : make_float3(0.f, 0.f, 0.f);
+                ssum.x += st[k].x * temp * P.dens_k[k] * invdens;
+                ssum.y += st[k].y * temp * P.dens_k[k] * invdens;
+                ssum.z += st[k].z * temp * P.dens_k[k] * invdens;
+            }
+#pragma unroll
+            for (int k = 0; k < NP; k++) {
+                const float tdiff = (P.dens_k[k] - dsum) * relax_coef;
+                out[k].x += ap.x * tdiff; out[k].y += ap.y * tdiff; out[k].z += ap.z * tdiff;
+                out[k].x -= cs * (st[k].x - ssum.x);
+                out[k].y -= cs * (st[k].y - ssum.y);
+                out[k].z -= cs * (st[k].z - ssum.z);
+                B.drift4[(size_t)k * P.cap + s] = make_float4(out[k].x, out[k].y, out[k].z, 0.f);
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Volume-fraction advance (MfComputeAlphaAdvanceCUDA)
+// ---------------------------------------------------------------------------
+
+// Alpha change of one in-grid fluid particle (contributeAlphaChange), Kahan-
+// compensated per phase. `pair` takes the neighbour's pos4, md = mass * (1/rho)
+// (zero for boundary neighbours, which exchange no volume fraction), veleval,
+// alpha4 and drift velocities.
+template <int NP>
+struct AlphaChange {
+    float4 pi, vei;
+    float ia[3];
+    float3 um[NP];
+    Kahan acc[NP];
+
+    __device__ __forceinline__ void init(const float4 pi_, const float4 vei_, const float4 ai, const float3* um_) {
+        pi = pi_;
+        vei = vei_;
+        ia[0] = ai.x; ia[1] = ai.y; ia[2] = ai.z;
+#pragma unroll
+        for (int k = 0; k < NP; k++) um[k] = um_[k];
+    }
+
+    __device__ __forceinline__ void pair(const DevParams& P, const float4 pj, const float md, const float4 vej,
+                                         const float4 aj, const float4* uj) {
+        if (!(pj.w > 0.f)) return;
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (!(dsq < P.r2 && dsq > 0.f)) return;
+        const float rinv = rsqrtf(dsq);
+        const float c = P.h - dsq * rinv;
+        const float cm = P.kspikydiff * c * c * rinv * md;
+        const float dot1 = (vej.x - vei.x) * dx + (vej.y - vei.y) * dy + (vej.z - vei.z) * dz;
+        const float ja[3] = {aj.x, aj.y, aj.z};
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            acc[k].add(-(0.5f * cm * (ja[k] + ia[k]) * dot1));
+            const float vx = ja[k] * uj[k].x + ia[k] * um[k].x;
+            const float vy = ja[k] * uj[k].y + ia[k] * um[k].y;
+            const float vz = ja[k] * uj[k].z + ia[k] * um[k].z;
+            acc[k].add(-(cm * (vx * dx + vy * dy + vz * dz)));
+        }
+    }
+
+    // dalpha * dt clamped at -0.99, added to the start-of-step fraction.
+    __device__ __forceinline__ void result(const DevParams& P, float (&out)[3]) const {
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            float ch = acc[k].s * P.dt;
+            // `ch < -0.99` in double is exactly `ch <= -0.99f` in float
+            if (ch <= -0.99f) ch = -0.99f;
+            out[k] = ch + ia[k];
+        }
+    }
+};
+
+// mfComputeCorrection (multiphase.cu:275-349) for one particle. `a` holds the
+// advanced fractions on entry and the corrected ones on exit; `apre` are the
+// start-of-step fractions (argmax fallback).
+template <int NP>
+__device__ __forceinline__ void correct(const DevParams& P, float (&a)[3], const float (&apre)[3], float dens,
+                                        float rho0, float& pmod, float& newrho0, float& newvisc) {
+    float before[3];
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        before[k] = a[k];
+        if (a[k] < 0.f) a[k] = 0.f;
+        sum += a[k];
+    }
+    const bool flag = sum > 0.f;
+    if (!flag) sum = 1.f;
+    int maxcat = 0;
+#pragma unroll
+    for (int k = 1; k < NP; k++)
+        if (apre[k] > apre[maxcat]) maxcat = k;
+    const float inv = 1.f / sum;
+    const float x = 1.f / (dens * rho0);
+    const float coef = -(6.f * powf(x, 7.0f) + 1.f) * P.pintstiff;
+    float pm = 0.f;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        a[k] = flag ? a[k] * inv : (k == maxcat ? 1.f : 0.f);
+        pm += coef * P.dens_k[k] * (a[k] - before[k]);
+    }
+    float nd = 0.f, nv = 0.f;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        nd += a[k] * P.dens_k[k];
+        nv += a[k] * P.visc_k[k];
+    }
+    pmod = pm;
+    newrho0 = nd;
+    newvisc = nv;
+}
+
+// AdvanceParticles (fluid_system_kern.cu:426-534) for one in-grid non-boundary
+// particle, with un-contracted float operations in the reference's order.
+__device__ __forceinline__ void advance_one(const DevParams& P, float4& p, float4& v, float4& ve, float4& ap,
+                                            const float4 acc) {
+    const float a[3] = {__fadd_rn(acc.x, P.grav[0]), __fadd_rn(acc.y, P.grav[1]), __fadd_rn(acc.z, P.grav[2])};
+    float* pp[3] = {&p.x, &p.y, &p.z};
+    float* vv[3] = {&v.x, &v.y, &v.z};
+    float* ee[3] = {&ve.x, &ve.y, &ve.z};
+    float* aa[3] = {&ap.x, &ap.y, &ap.z};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float v0 = *vv[k];
+        const float vn = __fadd_rn(__fmul_rn(a[k], P.dt), v0);
+        *pp[k] = __fadd_rn(*pp[k], __fdiv_rn(__fmul_rn(vn, P.dt), P.ss));
+        *ee[k] = __fmul_rn(__fadd_rn(v0, vn), 0.5f);
+        *vv[k] = vn;
+        *aa[k] = __fsub_rn(P.grav[k], a[k]);
+    }
+}
+
+// Fused alpha + correction + advance of one slot (reads in*, returns the new
+// values of the five float4 fields). `alpha_sum` runs the neighbour loop.
+template <int NP, bool MP, class AlphaSum>
+__device__ __forceinline__ void pass_c_slot(const DevParams& P, const DevBuffers& B, int s, bool undef, float4& p,
+                                            float4& v, float4& ve, float4& al, float4& ap, AlphaSum&& alpha_sum) {
+    if (p.w < 0.f) return;  // boundary: never advanced
+    if (undef) {
+        p.x = -1000.f; p.y = -1000.f; p.z = -1000.f;
+        v.x = 0.f; v.y = 0.f; v.z = 0.f;
+        return;
+    }
+    if (MP) {
+        const float ia[3] = {al.x, al.y, al.z};
+        float a[3] = {al.x, al.y, al.z};
+        alpha_sum(a);
+        float pmod, nr, nv;
+        correct<NP>(P, a, ia, B.densp[s].x, al.w, pmod, nr, nv);
+        al = make_float4(a[0], a[1], a[2], nr);
+        v.w = nv;
+        B.pmod[s] = pmod;
+    }
+    advance_one(P, p, v, ve, ap, B.accel4[s]);
+}
+
+}  // namespace dev
+}  // namespace sphmp

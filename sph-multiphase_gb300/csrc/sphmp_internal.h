@@ -34,6 +34,11 @@ constexpr int kWarpSortMax = 256;     // cells up to this size are sorted by one
 constexpr int kCtaSortMax = 8192;     // larger cells up to this size are sorted by one CTA
 constexpr int kNumFloat4Fields = 5;   // pos4, vel4, vev4, alpha4, aprev4
 constexpr int kMaxNbr = 128;          // neighbour-list capacity per particle (more: the passes rescan)
+constexpr int kBlk = 128;             // threads of a cell-block CTA
+constexpr int kStageDens = 1024;      // candidates a cell block stages for the density pass
+constexpr int kStageForce = 768;      // ... for the force + drift pass
+constexpr int kStagePassC = 640;      // ... for the alpha + correction + advance pass
+constexpr uint32_t kListGlobal = 0x80000000u;  // nbr_cnt flag: the list holds slots (nbr), not stage indices
 
 // Error bits accumulated in the device error word (1 << sphmp_status).
 constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
@@ -53,8 +58,7 @@ struct DevParams {
     float ss;        // simscale
     float h, r2;     // smoothing radius and its square
     float r2list;    // squared radius of the neighbour list (r2 plus a rounding margin)
-    int use_list;    // 1: the neighbour list matches the current slot order
-    int use_oct;     // 1: the octant order matches the current slot order and positions
+    int list_mode;   // 0: no list, 1: slot lists in nbr, 2: cell-block lists (nbr16 stage indices)
     float dt;
     float kpoly6, kspikydiff;
     float bvisc;
@@ -102,9 +106,20 @@ struct DevBuffers {
     float4* pos4o;      // [cap] pos4 of the member at octant-order position o
     uint32_t* oidx;     // [cap] slot of the member at octant-order position o
     uint32_t* oct_start;// [8 * G] first octant-order position of bucket (cell, octant)
+    // Cell blocks: every cell with members, and per-particle lists of indices into the
+    // block's staged candidates (the 4x4x4 h-subcells around the cell).
+    uint32_t* act;      // [G] cells with members (any order)
+    uint32_t* act_n;    // [1] number of entries in act
+    uint16_t* nbr16;    // [kMaxNbr * cap] stage indices, column-major like nbr
 };
 
 enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
+
+// Input and output buffers of the five float4 fields for one kernel launch.
+struct F4Set {
+    const float4* __restrict__ in[kNumFloat4Fields];
+    float4* __restrict__ out[kNumFloat4Fields];
+};
 
 // ---- launchers (sphmp_kernels.cu) ----
 // All take the current double-buffer selectors in `cur` (one per Field4).
@@ -118,6 +133,8 @@ void launch_cell_order(const DevParams& P, const DevBuffers& B, const int* cur, 
 void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// octant-order density (needs the octant order of this sort); writes slot lists
+void launch_density_oct(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_force_drift(const DevParams& P, const DevBuffers& B, const int* cur, bool force, bool drift,
                         cudaStream_t s);
 void launch_surface_tension(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
@@ -130,6 +147,16 @@ void launch_advance(const DevParams& P, const DevBuffers& B, const int* cur, cud
 // fused alpha + correction + advance: reads cur, writes cur^1 for all five float4 fields
 void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+
+// cell-block kernels (sphmp_cellblock.cu): need the octant order and the cell list of
+// the current sort; the density writes stage-index lists (list_mode 2) that the
+// other three read
+void launch_density_blk(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_force_drift_blk(const DevParams& P, const DevBuffers& B, const int* cur, bool force, bool drift,
+                            cudaStream_t s);
+void launch_pass_c_blk(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// alpha advance alone: new fractions into alpha4[cur^1]
+void launch_alpha_advance_blk(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 
 // transfers (staging buffers hold reference records)
 void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,

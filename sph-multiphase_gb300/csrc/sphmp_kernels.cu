@@ -16,90 +16,14 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "sphmp_device.cuh"
 #include "sphmp_internal.h"
 
 namespace sphmp {
 
 namespace {
 
-constexpr int kThreads = 256;
-
-__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
-__device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
-
-// Kahan-compensated float accumulator.
-struct Kahan {
-    float s, c;
-    __device__ __forceinline__ Kahan() : s(0.f), c(0.f) {}
-    __device__ __forceinline__ void add(float y) {
-        float yy = __fsub_rn(y, c);
-        float t = __fadd_rn(s, yy);
-        c = __fsub_rn(__fsub_rn(t, s), yy);
-        s = t;
-    }
-};
-
-// Grid coordinate in cell units, the reference's (pos - gridmin) * gridIdfac.
-__device__ __forceinline__ float grid_t(float p, float gmin, float fac) { return __fmul_rn(__fsub_rn(p, gmin), fac); }
-// int(t) is only defined inside the int range; outside it (and for NaN) the
-// particle is out of the grid.
-__device__ __forceinline__ bool t_ok(float t) { return t > -2147483520.f && t < 2147483520.f; }
-
-__device__ __forceinline__ uint32_t cell_key(const DevParams& P, float x, float y, float z) {
-    const float tx = grid_t(x, P.gmin[0], P.fac[0]);
-    const float ty = grid_t(y, P.gmin[1], P.fac[1]);
-    const float tz = grid_t(z, P.gmin[2], P.fac[2]);
-    if (!(t_ok(tx) && t_ok(ty) && t_ok(tz))) return kUndef;
-    const int gx = __float2int_rz(tx), gy = __float2int_rz(ty), gz = __float2int_rz(tz);
-    if (gx >= 1 && gx < P.rx - 1 && gy >= 1 && gy < P.ry - 1 && gz >= 1 && gz < P.rz - 1)
-        return (uint32_t)((gy * P.rz + gz) * P.rx + gx);
-    return kUndef;
-}
-
-// Visit the candidate slots of an in-grid particle at (x, y, z): along each axis
-// the cells within [t - R, t + R] (R = h in cell units plus a margin), limited
-// to the reference's +-1 cell. Cells along x are adjacent in the sorted order,
-// so each (y, z) row of cells is one contiguous slot range.
-template <class F>
-__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart, float x,
-                                               float y, float z, F&& f) {
-    const float t[3] = {grid_t(x, P.gmin[0], P.fac[0]), grid_t(y, P.gmin[1], P.fac[1]),
-                        grid_t(z, P.gmin[2], P.fac[2])};
-    int lo[3], hi[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int g = __float2int_rz(t[a]);
-        lo[a] = max(g - 1, __float2int_rd(t[a] - P.srad[a]));
-        hi[a] = min(g + 1, __float2int_rd(t[a] + P.srad[a]));
-    }
-    for (int yy = lo[1]; yy <= hi[1]; yy++) {
-        for (int zz = lo[2]; zz <= hi[2]; zz++) {
-            const int base = (yy * P.rz + zz) * P.rx;
-            const uint32_t j0 = __ldg(&cstart[base + lo[0]]);
-            const uint32_t j1 = __ldg(&cstart[base + hi[0] + 1]);
-            for (uint32_t j = j0; j < j1; j++) f(j);
-        }
-    }
-}
-
-__device__ __forceinline__ void set_err(const DevBuffers& B, uint32_t bit) { atomicOr(B.err, bit); }
-
-// Visit the neighbour candidates of slot s: the list written by the density pass
-// when it is valid and did not overflow, otherwise the cell search. Every lane
-// of a warp walks its own list, so the per-neighbour work runs converged.
-template <class F>
-__device__ __forceinline__ void for_neighbours(const DevParams& P, const DevBuffers& B, int s, float x, float y,
-                                               float z, F&& f) {
-    if (P.use_list) {
-        const uint32_t cnt = B.nbr_cnt[s];
-        if (cnt <= (uint32_t)kMaxNbr) {
-            const uint32_t* __restrict__ col = B.nbr + s;
-            for (uint32_t k = 0; k < cnt; k++) f(__ldg(col + (size_t)k * P.cap));
-            return;
-        }
-    }
-    for_candidates(P, B.cstart, x, y, z, f);
-}
+using namespace dev;
 
 // ---------------------------------------------------------------------------
 // Hash + histogram (GetParticleIndexCUDA)
@@ -233,6 +157,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_top(const __grid_constant__
         B.cstart[P.G] = nin;
         B.cstart[P.G + 1] = (uint32_t)P.n;
         B.big[0] = 0u;
+        *B.act_n = 0u;
     }
 }
 
@@ -252,6 +177,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(const __grid_constant
             B.cstart[c] = run;
             B.mgridoff[c] = v[k] ? (int32_t)run : 0;
             B.mgridcnt[c] = (int32_t)v[k];
+            if (v[k]) B.act[atomicAdd(B.act_n, 1u)] = (uint32_t)c;
             if (v[k] > (uint32_t)kWarpSortMax) {
                 if (v[k] > (uint32_t)kCtaSortMax) {
                     set_err(B, kErrCellOverflow);  // left unsorted; keep its octant ranges in bounds
@@ -323,15 +249,6 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[E]) {
             }
         }
     }
-}
-
-// Octant (h-subcell inside its 2h cell) of an in-grid position: bit 0 = x half,
-// bit 1 = z half, bit 2 = y half, from int(2 t) with t the reference's grid coordinate.
-__device__ __forceinline__ uint32_t octant_of(const DevParams& P, const float4 p) {
-    const int hx = __float2int_rz(2.f * grid_t(p.x, P.gmin[0], P.fac[0]));
-    const int hy = __float2int_rz(2.f * grid_t(p.y, P.gmin[1], P.fac[1]));
-    const int hz = __float2int_rz(2.f * grid_t(p.z, P.gmin[2], P.fac[2]));
-    return (uint32_t)(((hy & 1) * 2 + (hz & 1)) * 2 + (hx & 1));
 }
 
 // Write the octant order of cell c from the key (octant << shift | member index)
@@ -469,10 +386,6 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
 // Reorder (RearrageDataCUDA)
 // ---------------------------------------------------------------------------
 
-struct F4Set {
-    const float4* __restrict__ in[kNumFloat4Fields];
-    float4* __restrict__ out[kNumFloat4Fields];
-};
 
 // Every slot, out-of-grid ones included, receives the record of its pre-sort slot:
 // the reference's `int cell != GRID_UNDEF` test (fluid_system_kern.cu:104-108)
@@ -599,13 +512,7 @@ __global__ void __launch_bounds__(kThreads) k_density_oct(const __grid_constant_
         }
     }
     B.nbr_cnt[s] = cnt;
-    float rho = sum.s * P.kpoly6;
-    if (rho == 0.f) rho = 1.f;
-    float p;
-    if (P.eos == SPHMP_EOS_LINEAR) p = P.eos_k * (rho - rho0);
-    else p = 2.5f * rho0 * (powf(rho / rho0, 7.0f) - 1.0f);
-    if (p < 0.f) p = 0.f;
-    B.densp[s] = make_float2(1.f / rho, p);
+    B.densp[s] = density_result(P, sum.s, rho0);
 }
 
 __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ DevParams P,
@@ -639,26 +546,22 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
         }
     });
     B.nbr_cnt[s] = cnt;
-    float rho = sum.s * P.kpoly6;
-    if (rho == 0.f) rho = 1.f;
-    float p;
-    if (P.eos == SPHMP_EOS_LINEAR) p = P.eos_k * (rho - rho0);
-    else p = 2.5f * rho0 * (powf(rho / rho0, 7.0f) - 1.0f);
-    if (p < 0.f) p = 0.f;
-    B.densp[s] = make_float2(1.f / rho, p);
+    B.densp[s] = density_result(P, sum.s, rho0);
 }
 
 // ---------------------------------------------------------------------------
 // Force + drift velocity (MfComputeForceCUDA, MfComputeDriftVelCUDA)
 // ---------------------------------------------------------------------------
 
+// Slot-order force + drift: one thread per slot, neighbours gathered from global
+// memory through the slot list (or the cell search).
 template <bool FORCE, bool DRIFT, int NP>
 __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_constant__ DevParams P,
-                                                          const __grid_constant__ DevBuffers B,
-                                                          const float4* __restrict__ pos4,
-                                                          const float4* __restrict__ vel4,
-                                                          const float4* __restrict__ alpha4,
-                                                          const float4* __restrict__ aprev4) {
+                                                             const __grid_constant__ DevBuffers B,
+                                                             const float4* __restrict__ pos4,
+                                                             const float4* __restrict__ vel4,
+                                                             const float4* __restrict__ alpha4,
+                                                             const float4* __restrict__ aprev4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= P.n || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
@@ -666,107 +569,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_consta
         if (FORCE) B.accel4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    const float4 vi = vel4[s];
-    const float2 dpi = B.densp[s];
-    const float4 ai = alpha4[s];
-    const float idens = dpi.x, ipress = dpi.y, ivisc = vi.w, rho0 = ai.w;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    float ia[3] = {ai.x, ai.y, ai.z};
-    float mc[NP > 0 ? NP : 1];
-    float3 dv[NP > 0 ? NP : 1], ag[NP > 0 ? NP : 1];
-    float relax_coef = 0.f, invdens = 0.f;
-    if (DRIFT) {
-        relax_coef = P.relax / ivisc;
-        invdens = 1.f / rho0;
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            mc[k] = ia[k] * P.dens_k[k] * invdens;
-            dv[k] = make_float3(0.f, 0.f, 0.f);
-            ag[k] = make_float3(0.f, 0.f, 0.f);
-        }
-    }
-    for_neighbours(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+    ForceDrift<FORCE, DRIFT, NP> acc;
+    acc.init(P, pi, vel4[s], B.densp[s], alpha4[s]);
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        // every load first (list entries are almost always neighbours), so that
+        // consecutive neighbours' gathers overlap
         const float4 pj = __ldg(&pos4[j]);
-        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
-        const float dsq = dx * dx + dy * dy + dz * dz;
-        if (!(dsq < P.r2 && dsq > 0.f)) return;
-        const float rinv = rsqrtf(dsq);  // 1/r; r = dsq/r
-        const float c = P.h - dsq * rinv;
-        const float g1 = P.kspikydiff * c * c * rinv;
-        if (pj.w > 0.f) {  // fluid neighbour
-            const float2 dpj = __ldg(&B.densp[j]);
-            const float g = g1 * pj.w * dpj.x;
-            if (FORCE) {
-                const float4 vj = __ldg(&vel4[j]);
-                const float pm = -0.5f * g * dpj.y * idens;
-                fx += dx * pm; fy += dy * pm; fz += dz * pm;
-                const float vm = g * (ivisc + vj.w) * idens;
-                fx += (vi.x - vj.x) * vm; fy += (vi.y - vj.y) * vm; fz += (vi.z - vj.z) * vm;
-            }
-            if (DRIFT) {
-                const float4 aj = __ldg(&alpha4[j]);
-                const float ja[3] = {aj.x, aj.y, aj.z};
-                float3 pg[NP > 0 ? NP : 1];
-                float3 psum = make_float3(0.f, 0.f, 0.f);
-#pragma unroll
-                for (int k = 0; k < NP; k++) {
-                    const float pm = g * (-ia[k] * ipress + ja[k] * dpj.y);
-                    pg[k] = make_float3(pm * dx, pm * dy, pm * dz);
-                    psum.x += pg[k].x * mc[k]; psum.y += pg[k].y * mc[k]; psum.z += pg[k].z * mc[k];
-                    const float ga = (ja[k] - ia[k]) * g;
-                    ag[k].x += ga * dx; ag[k].y += ga * dy; ag[k].z += ga * dz;
-                }
-#pragma unroll
-                for (int k = 0; k < NP; k++) {
-                    dv[k].x -= relax_coef * (pg[k].x - psum.x);
-                    dv[k].y -= relax_coef * (pg[k].y - psum.y);
-                    dv[k].z -= relax_coef * (pg[k].z - psum.z);
-                }
-            }
-        } else if (FORCE) {  // boundary neighbour, volume V_j = -w
-            const float V = -pj.w;
-            const float4 vj = __ldg(&vel4[j]);
-            const float pm = -g1 * rho0 * V * ipress * idens * idens;
-            fx += dx * pm; fy += dy * pm; fz += dz * pm;
-            float pij = (vi.x - vj.x) * dx + (vi.y - vj.y) * dy + (vi.z - vj.z) * dz;
-            if (pij < 0.f) {
-                pij = pij / (dsq + P.r2 * 0.01f);
-                pij = pij * P.bvisc * P.h / 2.f / rho0;
-                pij = g1 * rho0 * V * pij;
-                fx += dx * pij; fy += dy * pij; fz += dz * pij;
-            }
-        }
+        const float2 dpj = __ldg(&B.densp[j]);
+        const float4 vj = FORCE ? __ldg(&vel4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 aj = DRIFT ? __ldg(&alpha4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        acc.pair(P, pj, dpj, vj, aj);
     });
-    if (FORCE) B.accel4[s] = make_float4(fx, fy, fz, 0.f);
-    if (DRIFT) {
-        const float4 ap = aprev4[s];
-        const float cc = P.cont * P.cont2;
-        const float cs = P.cont * P.cont1 * P.sigma;
-        float3 out[NP > 0 ? NP : 1], st[NP > 0 ? NP : 1];
-        float dsum = 0.f;
-        float3 ssum = make_float3(0.f, 0.f, 0.f);
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            out[k] = make_float3(cc * dv[k].x, cc * dv[k].y, cc * dv[k].z);
-            const float temp = ia[k];
-            dsum += temp * P.dens_k[k] * P.dens_k[k] * invdens;
-            // `temp > 0.0001` in double is exactly `temp > 1e-4f` in float
-            st[k] = temp > 1e-4f ? make_float3(ag[k].x / temp, ag[k].y / temp, ag[k].z / temp)
-                                 : make_float3(0.f, 0.f, 0.f);
-            ssum.x += st[k].x * temp * P.dens_k[k] * invdens;
-            ssum.y += st[k].y * temp * P.dens_k[k] * invdens;
-            ssum.z += st[k].z * temp * P.dens_k[k] * invdens;
-        }
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            const float tdiff = (P.dens_k[k] - dsum) * relax_coef;
-            out[k].x += ap.x * tdiff; out[k].y += ap.y * tdiff; out[k].z += ap.z * tdiff;
-            out[k].x -= cs * (st[k].x - ssum.x);
-            out[k].y -= cs * (st[k].y - ssum.y);
-            out[k].z -= cs * (st[k].z - ssum.z);
-            B.drift4[(size_t)k * P.cap + s] = make_float4(out[k].x, out[k].y, out[k].z, 0.f);
-        }
-    }
+    acc.finish(P, B, s, DRIFT ? aprev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
 }
 
 // Surface tension (reference SurfaceTension, fluid_system_kern.cu:569-625): all
@@ -804,111 +618,32 @@ __global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_const
 // Volume-fraction advance, correction, advection
 // ---------------------------------------------------------------------------
 
-// Sum of the alpha change over the neighbours of an in-grid fluid particle
-// (contributeAlphaChange, multiphase.cu:169-216), Kahan-compensated per phase.
+// Alpha change of slot s with neighbours gathered from global memory.
 template <int NP>
-__device__ __forceinline__ void alpha_change(const DevParams& P, const DevBuffers& B, const float4* __restrict__ pos4,
-                                             const float4* __restrict__ vev4, const float4* __restrict__ alpha4,
-                                             int s, const float4 pi, const float4 vei, const float (&ia)[3],
-                                             float (&change)[3]) {
+__device__ __forceinline__ void alpha_change_slot(const DevParams& P, const DevBuffers& B,
+                                                  const float4* __restrict__ pos4, const float4* __restrict__ vev4,
+                                                  const float4* __restrict__ alpha4, int s, const float4 pi,
+                                                  const float4 vei, const float4 ai, float (&out)[3]) {
     float3 um[NP];
 #pragma unroll
     for (int k = 0; k < NP; k++) {
         const float4 u = B.drift4[(size_t)k * P.cap + s];
         um[k] = make_float3(u.x, u.y, u.z);
     }
-    Kahan acc[NP];
-    for_neighbours(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+    AlphaChange<NP> acc;
+    acc.init(pi, vei, ai, um);
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        // every load first, so that consecutive neighbours' gathers overlap
         const float4 pj = __ldg(&pos4[j]);
-        if (pj.w < 0.f) return;  // boundary neighbours do not exchange volume fraction
-        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
-        const float dsq = dx * dx + dy * dy + dz * dz;
-        if (!(dsq < P.r2 && dsq > 0.f)) return;
-        const float rinv = rsqrtf(dsq);
-        const float c = P.h - dsq * rinv;
         const float2 dpj = __ldg(&B.densp[j]);
-        const float cm = P.kspikydiff * c * c * rinv * pj.w * dpj.x;
         const float4 vej = __ldg(&vev4[j]);
-        const float dot1 = (vej.x - vei.x) * dx + (vej.y - vei.y) * dy + (vej.z - vei.z) * dz;
         const float4 aj = __ldg(&alpha4[j]);
-        const float ja[3] = {aj.x, aj.y, aj.z};
+        float4 uj[NP];
 #pragma unroll
-        for (int k = 0; k < NP; k++) {
-            const float4 uj = __ldg(&B.drift4[(size_t)k * P.cap + j]);
-            acc[k].add(-(0.5f * cm * (ja[k] + ia[k]) * dot1));
-            const float vx = ja[k] * uj.x + ia[k] * um[k].x;
-            const float vy = ja[k] * uj.y + ia[k] * um[k].y;
-            const float vz = ja[k] * uj.z + ia[k] * um[k].z;
-            acc[k].add(-(cm * (vx * dx + vy * dy + vz * dz)));
-        }
+        for (int k = 0; k < NP; k++) uj[k] = __ldg(&B.drift4[(size_t)k * P.cap + j]);
+        acc.pair(P, pj, pj.w * dpj.x, vej, aj, uj);
     });
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        float ch = acc[k].s * P.dt;
-        // `ch < -0.99` in double is exactly `ch <= -0.99f` in float
-        if (ch <= -0.99f) ch = -0.99f;
-        change[k] = ch + ia[k];
-    }
-}
-
-// mfComputeCorrection (multiphase.cu:275-349) for one particle. `a` holds the
-// advanced fractions on entry and the corrected ones on exit; `apre` are the
-// start-of-step fractions (argmax fallback).
-template <int NP>
-__device__ __forceinline__ void correct(const DevParams& P, float (&a)[3], const float (&apre)[3], float dens,
-                                        float rho0, float& pmod, float& newrho0, float& newvisc) {
-    float before[3];
-    float sum = 0.f;
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        before[k] = a[k];
-        if (a[k] < 0.f) a[k] = 0.f;
-        sum += a[k];
-    }
-    const bool flag = sum > 0.f;
-    if (!flag) sum = 1.f;
-    int maxcat = 0;
-#pragma unroll
-    for (int k = 1; k < NP; k++)
-        if (apre[k] > apre[maxcat]) maxcat = k;
-    const float inv = 1.f / sum;
-    const float x = 1.f / (dens * rho0);
-    const float coef = -(6.f * powf(x, 7.0f) + 1.f) * P.pintstiff;
-    float pm = 0.f;
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        a[k] = flag ? a[k] * inv : (k == maxcat ? 1.f : 0.f);
-        pm += coef * P.dens_k[k] * (a[k] - before[k]);
-    }
-    float nd = 0.f, nv = 0.f;
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        nd += a[k] * P.dens_k[k];
-        nv += a[k] * P.visc_k[k];
-    }
-    pmod = pm;
-    newrho0 = nd;
-    newvisc = nv;
-}
-
-// AdvanceParticles (fluid_system_kern.cu:426-534) for one in-grid non-boundary
-// particle, with un-contracted float operations in the reference's order.
-__device__ __forceinline__ void advance_one(const DevParams& P, float4& p, float4& v, float4& ve, float4& ap,
-                                            const float4 acc) {
-    const float a[3] = {__fadd_rn(acc.x, P.grav[0]), __fadd_rn(acc.y, P.grav[1]), __fadd_rn(acc.z, P.grav[2])};
-    float* pp[3] = {&p.x, &p.y, &p.z};
-    float* vv[3] = {&v.x, &v.y, &v.z};
-    float* ee[3] = {&ve.x, &ve.y, &ve.z};
-    float* aa[3] = {&ap.x, &ap.y, &ap.z};
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const float v0 = *vv[k];
-        const float vn = __fadd_rn(__fmul_rn(a[k], P.dt), v0);
-        *pp[k] = __fadd_rn(*pp[k], __fdiv_rn(__fmul_rn(vn, P.dt), P.ss));
-        *ee[k] = __fmul_rn(__fadd_rn(v0, vn), 0.5f);
-        *vv[k] = vn;
-        *aa[k] = __fsub_rn(P.grav[k], a[k]);
-    }
+    acc.result(P, out);
 }
 
 // Separate alpha advance: new fractions into alpha4 out (restdens copied).
@@ -927,9 +662,8 @@ __global__ void __launch_bounds__(kThreads) k_alpha_advance(const __grid_constan
         alpha_out[s] = ai;
         return;
     }
-    const float ia[3] = {ai.x, ai.y, ai.z};
     float na[3] = {ai.x, ai.y, ai.z};
-    alpha_change<NP>(P, B, pos4, vev4, alpha_in, s, pi, vev4[s], ia, na);
+    alpha_change_slot<NP>(P, B, pos4, vev4, alpha_in, s, pi, vev4[s], ai, na);
     alpha_out[s] = make_float4(na[0], na[1], na[2], ai.w);
 }
 
@@ -980,33 +714,19 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
     aprev4[s] = ap;
 }
 
-// Fused alpha advance + correction + advance: reads the cur buffers, writes
-// every float4 field of every slot into the other buffer.
+// Fused alpha advance + correction + advance (slot order): reads the cur buffers,
+// writes every float4 field of every slot into the other buffer.
 template <int NP, bool MP>
 __global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ DevParams P,
-                                                     const __grid_constant__ DevBuffers B,
-                                                     const __grid_constant__ F4Set S) {
+                                                        const __grid_constant__ DevBuffers B,
+                                                        const __grid_constant__ F4Set S) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= P.n) return;
     float4 p = S.in[POS][s], v = S.in[VEL][s], ve = S.in[VEV][s], al = S.in[ALPHA][s], ap = S.in[APREV][s];
-    if (!(p.w < 0.f)) {
-        if (B.mgcell[s] == kUndef) {
-            p.x = -1000.f; p.y = -1000.f; p.z = -1000.f;
-            v.x = 0.f; v.y = 0.f; v.z = 0.f;
-        } else {
-            if (MP) {
-                const float ia[3] = {al.x, al.y, al.z};
-                float a[3] = {al.x, al.y, al.z};
-                alpha_change<NP>(P, B, S.in[POS], S.in[VEV], S.in[ALPHA], s, p, ve, ia, a);
-                float pmod, nr, nv;
-                correct<NP>(P, a, ia, B.densp[s].x, al.w, pmod, nr, nv);
-                al = make_float4(a[0], a[1], a[2], nr);
-                v.w = nv;
-                B.pmod[s] = pmod;
-            }
-            advance_one(P, p, v, ve, ap, B.accel4[s]);
-        }
-    }
+    const float4 pi = p, vei = ve, ai = al;
+    pass_c_slot<NP, MP>(P, B, s, B.mgcell[s] == kUndef, p, v, ve, al, ap, [&](float (&a)[3]) {
+        alpha_change_slot<NP>(P, B, S.in[POS], S.in[VEV], S.in[ALPHA], s, pi, vei, ai, a);
+    });
     S.out[POS][s] = p;
     S.out[VEL][s] = v;
     S.out[VEV][s] = ve;
@@ -1278,10 +998,12 @@ void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* 
 
 void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
     if (P.n <= 0) return;
-    if (P.use_oct)
-        k_density_oct<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[ALPHA][cur[ALPHA]]);
-    else
-        k_density<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[ALPHA][cur[ALPHA]]);
+    k_density<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[ALPHA][cur[ALPHA]]);
+}
+
+void launch_density_oct(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_density_oct<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[ALPHA][cur[ALPHA]]);
 }
 
 template <bool F, bool D>

@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libsphmp.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["sphmp_kernels.cu", "sphmp_api.cu"]
+CUDA_SOURCES = ["sphmp_kernels.cu", "sphmp_cellblock.cu", "sphmp_api.cu"]
 HOST_SOURCES = ["sphmp_host.cpp"]
 
 
@@ -36,7 +36,7 @@ def _nvcc():
 
 def _sources():
     out = [os.path.join(CSRC, f) for f in CUDA_SOURCES + HOST_SOURCES]
-    out += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    out += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     out += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     out.append(os.path.abspath(__file__))
     return out
