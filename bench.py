@@ -48,6 +48,41 @@ def _dist():
     return ws, rank, local
 
 
+class Replicas:
+    """Independent replicas, one per rank (the step has no data exchange): a
+    barrier around the timed region and the maximum of the per-rank times."""
+
+    def __init__(self, backend=None):
+        self.ws, self.rank, self.local = _dist()
+        self.dist = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as dist
+            if backend is None:
+                backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if not dist.is_initialized():
+                dist.init_process_group(backend)
+            self.dist = dist
+            self.device = "cuda" if backend == "nccl" else "cpu"
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, value):
+        if self.dist is None:
+            return float(value)
+        import torch
+        t = torch.tensor([float(value)], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
 def _peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -140,11 +175,11 @@ def cpu_sample(scene, steps, budget_s, threads=None):
         s.alpha[:, k] = scene.calc["restdens"] == np.float32(p.densArr[k])
     s.alpha_pre[:] = s.alpha
     O.before_first_step(p, s)
-    O.step(p, s, abi.SCHEDULE_FUSED, 1)  # warm-up (page-in, thread pool)
+    O.step(p, s, abi.SCHEDULE_REFERENCE, 1)  # warm-up (page-in, thread pool)
     done = 0
     t0 = time.perf_counter()
     while done < steps:
-        O.step(p, s, abi.SCHEDULE_FUSED, 1)
+        O.step(p, s, abi.SCHEDULE_REFERENCE, 1)
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
@@ -164,7 +199,8 @@ def run_reference(args):
         "steps": done, "warmup": 1, "ms_per_step": 1000.0 * dt / max(done, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": scene.name, "fluid_particles": scene.n_fluid,
-                   "boundary_particles": scene.n_boundary, "schedule": "fused", "eos": "linear k=3"},
+                   "boundary_particles": scene.n_boundary, "schedule": "reference call order",
+                   "eos": "linear k=3"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthr, "kind": "port",
                          "sample": f"{done} full steps of the {scene.n_fluid}-fluid-particle scene "
                                    f"(capped at {args.cpu_budget:.0f} s; requested {args.steps})"},
@@ -181,10 +217,8 @@ def run_gpu(args):
     import sphmp
     from sphmp import abi
 
-    ws, rank, local = _dist()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    rep = Replicas()
+    ws, rank, local = rep.ws, rep.rank, rep.local
     torch.cuda.set_device(local)
     dev_index = torch.cuda.current_device()
     scene = build_scene(args.seed + rank)
@@ -198,9 +232,7 @@ def run_gpu(args):
     ctx.step(args.warmup, abi.SCHEDULE_FUSED, use_graph=True)   # includes graph capture
     ctx.sync()
 
-    def barrier():
-        if ws > 1:
-            torch.distributed.barrier()
+    barrier = rep.barrier
 
     # ---- device-resident timed region ----
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -213,12 +245,8 @@ def run_gpu(args):
         ev1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
+    ms = rep.max(ev0.elapsed_time(ev1))
     ctx.sync()
-    if ws > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     n_in = int((ctx.download_field(abi.F_MGCELL) != abi.GRID_UNDEF).sum())
     cons = ctx.conservation()
 
@@ -264,11 +292,7 @@ def run_gpu(args):
         ctx2.step(1, abi.SCHEDULE_FUSED, use_graph=True)
         ctx2.download_aos(calc=False, out=(ho, None))
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = rep.max(time.perf_counter() - t0)
     ctx2.close()
 
     value = ws * n_fluid * args.steps / (ms * 1e-3)
@@ -299,8 +323,7 @@ def run_gpu(args):
                                           f"({dt:.1f} s, {nthr} threads)"}
     if rank == 0:
         print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    rep.close()
     return 0
 
 
