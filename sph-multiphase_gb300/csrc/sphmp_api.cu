@@ -25,8 +25,8 @@ struct sphmp_ctx {
     bool alpha_advanced = false;  // alpha4[cur] = advanced fractions, alpha4[cur^1] = start of step
     bool grid_valid = false;      // cell starts built for the current slot order
     bool nbr_valid = false;       // neighbour list built by the density pass for the current positions
-    bool oct_built = false;       // the last grid list also built the octant order
-    bool oct_valid = false;       // octant order matches the current slot order and positions
+    bool oct_built = false;       // the last grid list also built the next internal order (osrc)
+    bool oct_valid = false;       // the internal order is octant-grouped for the current cell list
     int list_mode = 0;            // kind of list the last density pass wrote (DevParams::list_mode)
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -149,8 +149,8 @@ void free_buffers(sphmp_ctx* c) {
         for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
                     B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
-                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.pos4o, B.oidx, B.oct_start,
-                    B.act, B.act_n, B.nbr16, c->stage};
+                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.opos, B.oidx, B.osrc, B.oct_start,
+                    B.act, B.act_n, c->stage};
     for (void* q : ptrs) cudaFree(q);
     memset(&c->B, 0, sizeof(c->B));
     c->stage = nullptr;
@@ -193,12 +193,15 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.vtmp, N));
     CK(dalloc(&B.nbr, (size_t)kMaxNbr * N));
     CK(dalloc(&B.nbr_cnt, N));
-    CK(dalloc(&B.pos4o, N));
+    CK(dalloc(&B.nmask, (size_t)kMaskWords * N));
+    CK(dalloc(&B.btab, 8 * G * kTabStride));
+    CK(dalloc(&B.dctr, 1));
+    CK(dalloc(&B.opos, N));
     CK(dalloc(&B.oidx, N));
+    CK(dalloc(&B.osrc, N));
     CK(dalloc(&B.oct_start, 8 * G));
     CK(dalloc(&B.act, G));
     CK(dalloc(&B.act_n, 1));
-    CK(dalloc(&B.nbr16, (size_t)kMaxNbr * N));
     CK(cudaMemset(B.act_n, 0, sizeof(uint32_t)));
     c->stage_bytes = N * (sizeof(sphmp_display_pack) + sizeof(sphmp_calc_pack));
     if (c->stage_bytes < G * sizeof(int32_t)) c->stage_bytes = G * sizeof(int32_t);
@@ -211,6 +214,9 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(cudaMemset(B.drift4, 0, sizeof(float4) * 3 * N));
     CK(cudaMemset(B.pmod, 0, sizeof(float) * N));
     CK(cudaMemset(B.mgcell, 0xFF, sizeof(uint32_t) * N));
+    CK(cudaMemset(B.opos, 0, sizeof(uint32_t) * N));
+    CK(cudaMemset(B.oidx, 0, sizeof(uint32_t) * N));
+    CK(cudaMemset(B.osrc, 0, sizeof(uint32_t) * N));
     CK(cudaMemset(B.midsort, 0, sizeof(uint32_t) * N));
     CK(cudaMemset(B.mgndx, 0xFF, sizeof(uint32_t) * N));
     CK(cudaMemset(B.mgridoff, 0, sizeof(int32_t) * G));
@@ -258,26 +264,19 @@ inline void swap_all(sphmp_ctx* c) {
     for (int f = 0; f < kNumFloat4Fields; f++) c->cur[f] ^= 1;
 }
 
-// Density pass: the cell-block kernel when the octant order of this sort is valid
-// (it writes stage-index lists), otherwise the slot-order kernel (slot lists).
+// Density pass: the bucket kernel when the internal order of this sort is
+// octant-grouped, otherwise the cell-search kernel; both write neighbour lists.
 void run_density(sphmp_ctx* c, cudaStream_t s) {
     const DevParams P = dev_params(c);
-    if (c->oct_valid) {
-        launch_density_oct(P, c->B, c->cur, s);
-        c->list_mode = 1;
-    } else {
-        launch_density(P, c->B, c->cur, s);
-        c->list_mode = 1;
-    }
+    if (c->oct_valid) launch_density_oct(P, c->B, c->cur, s);
+    else launch_density(P, c->B, c->cur, s);
+    c->list_mode = 1;
     c->nbr_valid = true;
 }
 
-inline bool block_lists(const sphmp_ctx* c) { return c->nbr_valid && c->list_mode == 2 && c->oct_valid; }
-
 void run_force_drift(sphmp_ctx* c, bool force, bool drift, cudaStream_t s) {
     const DevParams P = dev_params(c);
-    if (block_lists(c)) launch_force_drift_blk(P, c->B, c->cur, force, drift, s);
-    else launch_force_drift(P, c->B, c->cur, force, drift, s);
+    launch_force_drift(P, c->B, c->cur, force, drift, s);
 }
 
 // Optional event marks between the stages of a step (for sphmp_step_profile).
@@ -316,7 +315,7 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     mark("cell_starts");
     launch_cell_order(P, c->B, c->cur, s);
     mark("cell_order");
-    launch_rearrange(P, c->B, c->cur, s);
+    launch_rearrange(P, c->B, c->cur, false, s);
     mark("rearrange");
     swap_all(c);
     c->alpha_advanced = false;
@@ -326,7 +325,6 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     run_density(c, s);
     mark("density");
     const DevParams PL = dev_params(c);  // neighbour passes read the list
-    const bool blk = block_lists(c);
     if (schedule == SPHMP_SCHEDULE_FUSED) {
         run_force_drift(c, true, PL.multiphase != 0, s);
         mark("force_drift");
@@ -334,8 +332,7 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
             launch_surface_tension(PL, c->B, c->cur, s);
             mark("surface_tension");
         }
-        if (blk) launch_pass_c_blk(PL, c->B, c->cur, s);
-        else launch_pass_c(PL, c->B, c->cur, s);
+        launch_pass_c(PL, c->B, c->cur, s);
         mark(PL.multiphase ? "alpha_correct_advance" : "advance");
         swap_all(c);
         c->nbr_valid = false;  // positions moved
@@ -344,8 +341,7 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
         if (PL.multiphase) {
             run_force_drift(c, false, true, s);
             mark("drift");
-            if (blk) launch_alpha_advance_blk(PL, c->B, c->cur, s);
-            else launch_alpha_advance(PL, c->B, c->cur, s);
+            launch_alpha_advance(PL, c->B, c->cur, s);
             mark("alpha_advance");
             c->cur[ALPHA] ^= 1;
             c->alpha_advanced = true;
@@ -657,7 +653,9 @@ sphmp_status sphmp_get_grid_list(sphmp_ctx* c) {
 
 sphmp_status sphmp_rearrange_data(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
-    launch_rearrange(dev_params(c), c->B, c->cur, c->stream);
+    // without this library's grid list (sort arrays uploaded by the caller) the
+    // new internal order is the plain sorted slot order
+    launch_rearrange(dev_params(c), c->B, c->cur, !c->oct_built, c->stream);
     CHECK_LAUNCH("RearrageData");
     swap_all(c);
     c->alpha_advanced = false;
@@ -673,7 +671,6 @@ sphmp_status sphmp_compute_boundary_density(sphmp_ctx* c) {
     if (sphmp_status st = need_grid(c)) return st;
     launch_boundary_volume(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("ComputeBoundaryDensity");
-    c->oct_valid = false;  // the octant-order copy of pos4 still holds the old volumes
     c->nbr_valid = false;
     return SPHMP_OK;
 }
@@ -699,8 +696,7 @@ sphmp_status sphmp_compute_alpha_advance(sphmp_ctx* c) {
     if (sphmp_status st = need_grid(c)) return st;
     if (c->alpha_advanced)
         return fail(SPHMP_ERR_STATE, "volume fractions already advanced in this step (re-sort first)");
-    if (block_lists(c)) launch_alpha_advance_blk(dev_params(c), c->B, c->cur, c->stream);
-    else launch_alpha_advance(dev_params(c), c->B, c->cur, c->stream);
+    launch_alpha_advance(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("MfComputeAlphaAdvance");
     c->cur[ALPHA] ^= 1;
     c->alpha_advanced = true;

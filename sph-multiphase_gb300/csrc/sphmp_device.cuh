@@ -1,6 +1,5 @@
 // sphmp_device.cuh — device helpers and the per-pair physics of the multiphase
-// SPH step, shared by the slot-order kernels (sphmp_kernels.cu) and the
-// cell-block kernels (sphmp_cellblock.cu).
+// SPH step used by the kernels in sphmp_kernels.cu.
 //
 // The physics follows the reference kernels of ZP-Z/sph-multiphase:
 //   density / EOS      SPH_Solver/fluids/fluid_system_kern.cu:214-247, 279-318
@@ -92,15 +91,14 @@ __device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_
     }
 }
 
-// Visit the neighbour slots of slot s from the slot list written by the density
-// pass when it is valid and did not overflow, otherwise by the cell search.
+// Visit the neighbours of particle s from the index list of the density pass
+// when it is valid and did not overflow, otherwise by the cell search.
 template <class F>
 __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffers& B, int s, float x, float y,
                                               float z, F&& f) {
     if (P.list_mode != 0) {
-        const uint32_t raw = B.nbr_cnt[s];
-        const uint32_t cnt = raw & ~kListGlobal;
-        if ((P.list_mode == 1 || (raw & kListGlobal)) && cnt <= (uint32_t)kMaxNbr) {
+        const uint32_t cnt = B.nbr_cnt[s];
+        if (cnt <= (uint32_t)kMaxNbr) {
             const uint32_t* __restrict__ col = B.nbr + s;
 #pragma unroll 2
             for (uint32_t k = 0; k < cnt; k++) f(__ldg(col + (size_t)k * P.cap));

@@ -1,11 +1,16 @@
 // sphmp_internal.h — device-side data layout and kernel launchers of the
 // GB300 multiphase SPH step (shared by sphmp_kernels.cu and sphmp_api.cu).
 //
-// Particle state lives in HBM as structure-of-arrays in the reference's sorted
-// slot order (stable sort by the reference's linear 2h cell id). Every
-// per-particle array that survives a step is a float4 so neighbour gathers are
-// single 16-byte loads, and each is double-buffered: a pass that moves or
-// advances particles reads buffer `cur` and writes buffer `cur ^ 1`.
+// Particle state lives in HBM as structure-of-arrays in an internal order: the
+// in-grid particles grouped by the reference's 2h cell (cell c occupies the same
+// index range [cstart[c], cstart[c+1]) as its slots in the reference's sorted
+// order) and, inside a cell, by h-subcell (octant); out-of-grid particles follow
+// in slot order. opos[slot] and oidx[index] map between the reference's slots
+// and internal indices; every reference-facing array (mgcell, midsort, mgndx,
+// mgridoff, mgridcnt) and every transfer is in slot order. Every per-particle
+// array that survives a step is a float4 so neighbour gathers are single
+// 16-byte loads, and each is double-buffered: a pass that moves or advances
+// particles reads buffer `cur` and writes buffer `cur ^ 1`.
 //
 //   pos4   : x, y, z (sim units), w = mass (fluid) or -V_b (boundary volume)
 //   vel4   : vx, vy, vz, visc
@@ -33,12 +38,13 @@ constexpr int kScanItems = 4;         // items per thread in the scan
 constexpr int kWarpSortMax = 256;     // cells up to this size are sorted by one warp
 constexpr int kCtaSortMax = 8192;     // larger cells up to this size are sorted by one CTA
 constexpr int kNumFloat4Fields = 5;   // pos4, vel4, vev4, alpha4, aprev4
-constexpr int kMaxNbr = 128;          // neighbour-list capacity per particle (more: the passes rescan)
-constexpr int kBlk = 128;             // threads of a cell-block CTA
-constexpr int kStageDens = 1024;      // candidates a cell block stages for the density pass
-constexpr int kStageForce = 768;      // ... for the force + drift pass
-constexpr int kStagePassC = 640;      // ... for the alpha + correction + advance pass
-constexpr uint32_t kListGlobal = 0x80000000u;  // nbr_cnt flag: the list holds slots (nbr), not stage indices
+constexpr int kMaxNbr = 256;          // index-list capacity per particle (more: the passes rescan)
+// Bucket neighbour lists: a bitmask over the bucket's candidate sequence (the 27
+// h-subcells around it as 18 index ranges), one word per 32 candidates.
+constexpr int kMaskWords = 64;        // mask words per particle (more candidates: the passes rescan)
+constexpr int kTabStride = 40;        // per bucket: [0..18] range ends in the sequence, [20..37] index - sequence
+constexpr uint32_t kMaskList = 0x80000000u;  // nbr_cnt flag: bucket mask list, low bits = bucket (cell * 8 + octant)
+constexpr uint32_t kRescan = 0x7fffffffu;    // nbr_cnt value: no list, search the cells
 
 // Error bits accumulated in the device error word (1 << sphmp_status).
 constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
@@ -58,7 +64,7 @@ struct DevParams {
     float ss;        // simscale
     float h, r2;     // smoothing radius and its square
     float r2list;    // squared radius of the neighbour list (r2 plus a rounding margin)
-    int list_mode;   // 0: no list, 1: slot lists in nbr, 2: cell-block lists (nbr16 stage indices)
+    int list_mode;   // 0: no list, 1: index lists in nbr (written by the last density pass)
     float dt;
     float kpoly6, kspikydiff;
     float bvisc;
@@ -99,18 +105,19 @@ struct DevBuffers {
     uint32_t* err;      // device error word
     double* red;        // [16] FP64 reduction results
     float* vtmp;        // [cap] scratch (boundary volumes)
-    uint32_t* nbr;      // [kMaxNbr * cap] neighbour slots, column-major: entry k of slot s at k * cap + s
-    uint32_t* nbr_cnt;  // [cap] neighbours of slot s (> kMaxNbr: list overflowed, rescan)
-    // Octant order: inside every 2h cell, members grouped by the h-subcell (octant)
-    // they occupy, octant index (oy * 2 + oz) * 2 + ox. Covers the in-grid slots.
-    float4* pos4o;      // [cap] pos4 of the member at octant-order position o
-    uint32_t* oidx;     // [cap] slot of the member at octant-order position o
-    uint32_t* oct_start;// [8 * G] first octant-order position of bucket (cell, octant)
-    // Cell blocks: every cell with members, and per-particle lists of indices into the
-    // block's staged candidates (the 4x4x4 h-subcells around the cell).
+    uint32_t* nbr;      // [kMaxNbr * cap] neighbour indices, column-major: entry k of particle s at k * cap + s
+    uint32_t* nbr_cnt;  // [cap] list of particle s: kMaskList | bucket, index count (<= kMaxNbr) or kRescan
+    uint32_t* nmask;    // [kMaskWords * cap] bucket mask lists, column-major: word k of particle s at k * cap + s
+    uint32_t* btab;     // [8 * G * kTabStride] candidate ranges of each bucket with a mask list
+    uint32_t* dctr;     // [1] work counter of the bucket density kernel
+    // Internal order: inside every 2h cell, members grouped by the h-subcell
+    // (octant) they occupy, octant index (oy * 2 + oz) * 2 + ox.
+    uint32_t* opos;     // [cap] internal index of each reference slot
+    uint32_t* oidx;     // [cap] reference slot of each internal index (after the last sort)
+    uint32_t* osrc;     // [cap] previous internal index of each new internal index (sort -> rearrange)
+    uint32_t* oct_start;// [8 * G] first internal index of bucket (cell, octant)
     uint32_t* act;      // [G] cells with members (any order)
     uint32_t* act_n;    // [1] number of entries in act
-    uint16_t* nbr16;    // [kMaxNbr * cap] stage indices, column-major like nbr
 };
 
 enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
@@ -124,13 +131,16 @@ struct F4Set {
 // ---- launchers (sphmp_kernels.cu) ----
 // All take the current double-buffer selectors in `cur` (one per Field4).
 void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
-// (reads the pre-sort positions pos4[cur[POS]] to build the octant order)
+// (reads the pre-sort positions pos4[cur[POS]] to build the next internal order)
 void launch_grid_list(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 // the two halves of launch_grid_list: cell starts (histogram scan), then the
 // scatter, the per-cell stable ordering and the per-cell octant order
 void launch_cell_starts(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_cell_order(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
-void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// move every particle to its new internal index (osrc) and update opos; with
+// `slot_order`, the new internal order is the reference's sorted slot order
+// (for a rearrange that did not follow this library's grid list)
+void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, bool slot_order, cudaStream_t s);
 void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 // octant-order density (needs the octant order of this sort); writes slot lists
@@ -147,16 +157,6 @@ void launch_advance(const DevParams& P, const DevBuffers& B, const int* cur, cud
 // fused alpha + correction + advance: reads cur, writes cur^1 for all five float4 fields
 void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
-
-// cell-block kernels (sphmp_cellblock.cu): need the octant order and the cell list of
-// the current sort; the density writes stage-index lists (list_mode 2) that the
-// other three read
-void launch_density_blk(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
-void launch_force_drift_blk(const DevParams& P, const DevBuffers& B, const int* cur, bool force, bool drift,
-                            cudaStream_t s);
-void launch_pass_c_blk(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
-// alpha advance alone: new fractions into alpha4[cur^1]
-void launch_alpha_advance_blk(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 
 // transfers (staging buffers hold reference records)
 void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(kHashBlock) k_hash(const __grid_constant__ Dev
     const bool valid = i < P.n;
     uint32_t key = kUndef;
     if (valid) {
-        const float4 p = pos4[i];
+        const float4 p = pos4[B.opos[i]];
         key = cell_key(P, p.x, p.y, p.z);
         B.key[i] = key;
         B.mgcell[i] = key;
@@ -209,6 +209,8 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const __grid_constant__ De
         B.midsort[d] = (uint32_t)i;
         B.mgcell[d] = kUndef;
         B.mgndx[d] = kUndef;
+        B.osrc[d] = B.opos[i];  // out-of-grid particles keep slot order at the end
+        B.oidx[d] = d;
     }
 }
 
@@ -251,15 +253,15 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[E]) {
     }
 }
 
-// Write the octant order of cell c from the key (octant << shift | member index)
-// held at sorted position q (cellstart + q is its octant-order position).
+// Write the internal order of cell c from the key (octant << shift | member index)
+// held at sorted position q (cellstart + q is its internal index): the member's
+// previous internal index (osrc), its slot (oidx) and the bucket starts.
 __device__ __forceinline__ void emit_octant(const DevBuffers& B, uint32_t c, uint32_t start, uint32_t cnt, uint32_t q,
-                                            uint32_t key, uint32_t prev_oct, int shift, const float4* __restrict__ pos_in,
-                                            uint32_t pre_slot) {
+                                            uint32_t key, uint32_t prev_oct, int shift, uint32_t pre_slot) {
     const uint32_t oct = key >> shift;
     const uint32_t idx = key & ((1u << shift) - 1u);
     if (q < cnt) {
-        B.pos4o[start + q] = pos_in[pre_slot];
+        B.osrc[start + q] = B.opos[pre_slot];
         B.oidx[start + q] = start + idx;
     }
     // bucket starts: every bucket in (prev_oct, oct] begins at q (8 marks past the end)
@@ -291,7 +293,7 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
             B.midsort[start + idx] = v[r];
             B.mgcell[start + idx] = c;
             B.mgndx[start + idx] = idx;
-            key[r] = (octant_of(P, pos_in[v[r]]) << 8) | idx;
+            key[r] = (octant_of(P, pos_in[B.opos[v[r]]]) << 8) | idx;
         }
     }
     // octant order: sort (octant, member index)
@@ -306,7 +308,7 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
         if (q <= cnt) {
             const uint32_t k = key[r];
             const uint32_t pre = q < cnt ? wsm[k & 255u] : 0u;
-            emit_octant(B, c, start, cnt, q, q < cnt ? k : (8u << 8), prev_oct, 8, pos_in, pre);
+            emit_octant(B, c, start, cnt, q, q < cnt ? k : (8u << 8), prev_oct, 8, pre);
         }
     }
     __syncwarp();
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
         }
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < M; k += blockDim.x)
-            sm[k] = k < cnt ? ((octant_of(P, pos_in[B.midsort[start + k]]) << 13) | k) : 0xFFFFFFFFu;
+            sm[k] = k < cnt ? ((octant_of(P, pos_in[B.opos[B.midsort[start + k]]]) << 13) | k) : 0xFFFFFFFFu;
         __syncthreads();
         cta_bitonic(sm, M);
         for (uint32_t q = threadIdx.x; q <= cnt && q < M + 1; q += blockDim.x) {
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
             const uint32_t pk = q == 0 ? 0xFFFFFFFFu : sm[q - 1];
             const uint32_t prev_oct = q == 0 ? 0xFFFFFFFFu : (pk >> 13);
             const uint32_t pre = q < cnt ? B.midsort[start + (k & 0x1FFFu)] : 0u;
-            emit_octant(B, c, start, cnt, q, k, prev_oct, 13, pos_in, pre);
+            emit_octant(B, c, start, cnt, q, k, prev_oct, 13, pre);
         }
         __syncthreads();
     }
@@ -387,18 +389,38 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
 // ---------------------------------------------------------------------------
 
 
-// Every slot, out-of-grid ones included, receives the record of its pre-sort slot:
-// the reference's `int cell != GRID_UNDEF` test (fluid_system_kern.cu:104-108)
-// compares against a 64-bit literal on LP64 hosts and is always true there.
-// Out-of-grid particles are parked at (-1000)^3 by the advance.
+// Every particle, out-of-grid ones included, moves to its new internal index
+// (the reference gathers every slot: its `int cell != GRID_UNDEF` test at
+// fluid_system_kern.cu:104-108 compares against a 64-bit literal on LP64 hosts
+// and is always true there; out-of-grid particles are parked at (-1000)^3 by the
+// advance). The slot -> index map is updated last.
 __global__ void __launch_bounds__(kThreads) k_rearrange(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
+    const int o = blockIdx.x * kThreads + threadIdx.x;
+    if (o >= P.n) return;
+    uint32_t src = B.osrc[o];
+    if (src >= (uint32_t)P.n) src = o;  // only after a cell-overflow error (flagged by the scan)
+#pragma unroll
+    for (int f = 0; f < kNumFloat4Fields; f++) S.out[f][o] = S.in[f][src];
+}
+
+__global__ void __launch_bounds__(kThreads) k_update_opos(const __grid_constant__ DevParams P,
+                                                          const __grid_constant__ DevBuffers B) {
+    const int o = blockIdx.x * kThreads + threadIdx.x;
+    if (o >= P.n) return;
+    const uint32_t slot = B.oidx[o];
+    if (slot < (uint32_t)P.n) B.opos[slot] = (uint32_t)o;
+}
+
+// New internal order = the sorted slot order (midsort given, no octant order).
+__global__ void __launch_bounds__(kThreads) k_slot_order(const __grid_constant__ DevParams P,
+                                                         const __grid_constant__ DevBuffers B) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= P.n) return;
-    const uint32_t src = B.midsort[s];
-#pragma unroll
-    for (int f = 0; f < kNumFloat4Fields; f++) S.out[f][s] = S.in[f][src];
+    const uint32_t m = B.midsort[s];
+    B.osrc[s] = m < (uint32_t)P.n ? B.opos[m] : (uint32_t)s;
+    B.oidx[s] = (uint32_t)s;
 }
 
 // ---------------------------------------------------------------------------
@@ -450,20 +472,9 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // limited to the reference's 3x3x3 cells; along x, the subcells of one cell are
 // adjacent octant buckets, so each (y, z) subcell row is at most two ranges.
 // Writes 1/rho and p like k_density, plus the neighbour list.
-__global__ void __launch_bounds__(kThreads) k_density_oct(const __grid_constant__ DevParams P,
-                                                          const __grid_constant__ DevBuffers B,
-                                                          const float4* __restrict__ alpha4) {
-    const uint32_t nin = B.cstart[P.G];
-    const uint32_t o = blockIdx.x * kThreads + threadIdx.x;
-    if (o >= nin) return;
-    const uint32_t s = B.oidx[o];
-    const float4 pi = B.pos4o[o];
-    if (pi.w < 0.f) {
-        B.densp[s] = make_float2(-pi.w, 0.f);
-        B.nbr_cnt[s] = 0;
-        return;
-    }
-    const float rho0 = alpha4[s].w;
+__device__ __forceinline__ void density_octant_one(const DevParams& P, const DevBuffers& B,
+                                                   const float4* __restrict__ pos4, uint32_t s, const float4 pi,
+                                                   float rho0) {
     const float t[3] = {grid_t(pi.x, P.gmin[0], P.fac[0]), grid_t(pi.y, P.gmin[1], P.fac[1]),
                         grid_t(pi.z, P.gmin[2], P.fac[2])};
     int lo[3], hi[3];
@@ -492,7 +503,7 @@ __global__ void __launch_bounds__(kThreads) k_density_oct(const __grid_constant_
                 const uint32_t k0 = __ldg(&B.oct_start[(size_t)c * 8 + bq + oxlo]);
                 const uint32_t k1 = (bq + oxhi == 7) ? ce : __ldg(&B.oct_start[(size_t)c * 8 + bq + oxhi + 1]);
                 for (uint32_t k = k0; k < k1; k++) {
-                    const float4 pj = __ldg(&B.pos4o[k]);
+                    const float4 pj = __ldg(&pos4[k]);
                     const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
                     const float dsq = dx * dx + dy * dy + dz * dz;
                     if (dsq < P.r2) {
@@ -500,11 +511,11 @@ __global__ void __launch_bounds__(kThreads) k_density_oct(const __grid_constant_
                         const float m = pj.w > 0.f ? pj.w : rho0 * (-pj.w);
                         sum.add(cc * cc * cc * m);
                         if (dsq > 0.f) {
-                            if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = __ldg(&B.oidx[k]);
+                            if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = k;
                             cnt++;
                         }
                     } else if (dsq < P.r2list) {
-                        if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = __ldg(&B.oidx[k]);
+                        if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = k;
                         cnt++;
                     }
                 }
@@ -513,6 +524,257 @@ __global__ void __launch_bounds__(kThreads) k_density_oct(const __grid_constant_
     }
     B.nbr_cnt[s] = cnt;
     B.densp[s] = density_result(P, sum.s, rho0);
+}
+
+// Density + EOS, one warp per octant bucket (the members of one h-subcell).
+// Every member of a bucket has its neighbours within the 27 h-subcells around
+// it: a pair closer than h is at most one subcell apart per axis, up to the
+// rounding of the grid coordinate (a pair that rounding puts two subcells apart
+// is within 1e-4 h of the cutoff, where the kernels and their gradients vanish
+// to below 1e-7 of a typical term). The 27 subcells form 18 contiguous index
+// ranges (per (y, z) row: the x-neighbour bucket in the adjacent cell and the
+// two buckets of the same cell); their concatenation is the bucket's candidate
+// sequence, recorded in btab. The warp takes the candidates in blocks of
+// 32 * kBucketChunks held in registers, one per lane and chunk; for each block
+// it walks the bucket's members, every lane testing its candidates against the
+// member. The neighbour list of a member is the ballot of those tests, one
+// mask word per 32 candidates. The density terms are non-negative; each lane
+// sums at most kBucketChunks of them per block, the lanes are summed pairwise
+// and the blocks with Kahan compensation, so the relative rounding error of a
+// member's sum stays below (kBucketChunks + 6) * 2^-24. Warps take buckets from
+// a shared counter (bucket costs differ by orders of magnitude). Buckets with
+// more than kBucketMaxMembers members take the per-member octant search.
+// The candidate sequence of bucket (c, q): the 27 h-subcells around it as 18
+// contiguous index ranges, two per (y, z) subcell row (the x-neighbour bucket in
+// the adjacent cell, and both x buckets of the bucket's own cell column). Lane i
+// < 18 computes range i; the warp scans the lengths. Range starts and sequence
+// offsets go to the warp's shared table (offset[18] = length T); lane i < 18
+// returns its range start and offset in st / off.
+__device__ __forceinline__ uint32_t bucket_ranges(const DevParams& P, const DevBuffers& B, uint32_t c, uint32_t q,
+                                                  unsigned lane, uint32_t* rstart, uint32_t* roff, uint32_t& st,
+                                                  uint32_t& off) {
+    const int cx = (int)(c % (uint32_t)P.rx);
+    const int cyz = (int)(c / (uint32_t)P.rx);
+    const int cz = cyz % P.rz, cy = cyz / P.rz;
+    const int ox = (int)(q & 1u), oz = (int)((q >> 1) & 1u), oy = (int)(q >> 2);
+    uint32_t len = 0;
+    st = 0;
+    if (lane < 18) {
+        const int r = (int)(lane >> 1), part = (int)(lane & 1u);
+        const int sy = 2 * cy + oy + r / 3 - 1, sz = 2 * cz + oz + r % 3 - 1;
+        const int oyz = ((sy & 1) * 2 + (sz & 1)) * 2;
+        int ccx, xlo, xhi;
+        if ((ox == 0) == (part == 0)) {  // the single x-neighbour bucket in the adjacent cell
+            ccx = ox == 0 ? cx - 1 : cx + 1;
+            xlo = xhi = ox == 0 ? 1 : 0;
+        } else {                         // both x buckets of the bucket's own cell column
+            ccx = cx;
+            xlo = 0;
+            xhi = 1;
+        }
+        const uint32_t cc = (uint32_t)(((sy >> 1) * P.rz + (sz >> 1)) * P.rx + ccx);
+        const uint32_t cs = __ldg(&B.cstart[cc]), ce = __ldg(&B.cstart[cc + 1]);
+        if (cs < ce) {
+            st = __ldg(&B.oct_start[(size_t)cc * 8 + oyz + xlo]);
+            const uint32_t en = (oyz + xhi == 7) ? ce : __ldg(&B.oct_start[(size_t)cc * 8 + oyz + xhi + 1]);
+            len = en - st;
+        }
+    }
+    uint32_t inc = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, inc, d);
+        if ((int)lane >= d) inc += v;
+    }
+    const uint32_t T = __shfl_sync(0xffffffffu, inc, 31);
+    off = inc - len;
+    if (lane < 18) {
+        rstart[lane] = st;
+        roff[lane] = off;
+    }
+    if (lane == 18) roff[18] = T;
+    __syncwarp();
+    return T;
+}
+
+// Index of candidate e of the sequence; r is the caller's range cursor (e must
+// not decrease between calls with the same cursor).
+__device__ __forceinline__ uint32_t seq_index(const uint32_t* rstart, const uint32_t* roff, int& r, uint32_t e) {
+    while (roff[r + 1] <= e) r++;
+    return rstart[r] + (e - roff[r]);
+}
+
+constexpr int kBucketChunks = 8;
+constexpr int kBucketMaxMembers = 128;
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint32_t next_bucket(uint32_t* ctr, unsigned lane) {
+    uint32_t v = 0;
+    if (lane == 0) v = atomicAdd(ctr, 1u);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+template <bool SS1>
+__global__ void __launch_bounds__(kThreads, 3) k_density_bucket(const __grid_constant__ DevParams P,
+                                                                const __grid_constant__ DevBuffers B,
+                                                                const float4* __restrict__ pos4,
+                                                                const float4* __restrict__ alpha4) {
+    constexpr int kWarps = kThreads / 32;
+    __shared__ uint32_t tab[kWarps][2][20];                 // range starts and sequence offsets
+    __shared__ float2 msum[kWarps][kBucketMaxMembers];      // member sums (Kahan s, c) over blocks
+    const unsigned lane = lane_id();
+    const int w = threadIdx.x >> 5;
+    uint32_t* rstart = tab[w][0];
+    uint32_t* roff = tab[w][1];
+    const uint32_t nb = *B.act_n * 8u;
+    const size_t cap = (size_t)P.cap;
+    const float r2 = P.r2, r2list = P.r2list, ss = P.ss;
+    const float kFar = __int_as_float(0x7f800000);  // +inf: never within range
+    for (uint32_t b = next_bucket(B.dctr, lane); b < nb; b = next_bucket(B.dctr, lane)) {
+        const uint32_t c = __ldg(&B.act[b >> 3]), q = b & 7u;
+        const uint32_t m0 = __ldg(&B.oct_start[(size_t)c * 8 + q]);
+        const uint32_t m1 = q == 7 ? __ldg(&B.cstart[c + 1]) : __ldg(&B.oct_start[(size_t)c * 8 + q + 1]);
+        if (m0 >= m1) continue;
+        // boundary members carry their volume and need no list
+        bool fluid = false;
+        for (uint32_t i = m0 + lane; i < m1; i += 32) {
+            const float wv = __ldg(&pos4[i]).w;
+            if (wv < 0.f) {
+                B.densp[i] = make_float2(-wv, 0.f);
+                B.nbr_cnt[i] = 0;
+            } else {
+                fluid = true;
+            }
+        }
+        if (!__any_sync(0xffffffffu, fluid)) continue;
+        if (m1 - m0 > (uint32_t)kBucketMaxMembers) {
+            for (uint32_t i = m0 + lane; i < m1; i += 32) {
+                const float4 pi = __ldg(&pos4[i]);
+                if (!(pi.w < 0.f)) density_octant_one(P, B, pos4, i, pi, __ldg(&alpha4[i]).w);
+            }
+            continue;
+        }
+        uint32_t st, off;
+        const uint32_t T = bucket_ranges(P, B, c, q, lane, rstart, roff, st, off);
+        const uint32_t bid = c * 8u + q;
+        const bool masked = T <= 32u * kMaskWords;
+        uint32_t* __restrict__ bt = B.btab + (size_t)bid * kTabStride;
+        if (masked && lane < 18) {
+            bt[lane] = off;
+            bt[20 + lane] = st - off;
+        }
+        if (masked && lane == 18) bt[18] = T;
+        int r = 0;
+        for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
+            float4 cj[kBucketChunks];  // w: fluid mass (0 for boundary)
+            float vb[kBucketChunks];   // boundary volume (0 for fluid)
+#pragma unroll
+            for (int ch = 0; ch < kBucketChunks; ch++) {
+                const uint32_t e = base + lane + 32u * ch;
+                cj[ch] = make_float4(kFar, kFar, kFar, 0.f);
+                vb[ch] = 0.f;
+                if (e < T) {
+                    cj[ch] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
+                    vb[ch] = fmaxf(-cj[ch].w, 0.f);
+                    cj[ch].w = fmaxf(cj[ch].w, 0.f);
+                }
+            }
+            const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
+            const uint32_t word0 = base >> 5;
+            const bool first = base == 0;
+            for (uint32_t t = m0; t < m1; t++) {
+                const float4 pt = __ldg(&pos4[t]);
+                if (pt.w < 0.f) continue;
+                const float rho0 = __ldg(&alpha4[t]).w;
+                float acc = 0.f;
+                uint32_t mine = 0;  // lane k keeps the mask word of chunk k
+#pragma unroll
+                for (int ch = 0; ch < kBucketChunks; ch++) {
+                    if (ch < nch) {
+                        float dx = pt.x - cj[ch].x, dy = pt.y - cj[ch].y, dz = pt.z - cj[ch].z;
+                        if (!SS1) {
+                            dx *= ss;
+                            dy *= ss;
+                            dz *= ss;
+                        }
+                        const float dsq = dx * dx + dy * dy + dz * dz;
+                        const float cc = fmaxf(r2 - dsq, 0.f);  // 0 outside h (and for the padding lanes)
+                        acc = fmaf(cc * cc * cc, fmaf(rho0, vb[ch], cj[ch].w), acc);
+                        const uint32_t bal = __ballot_sync(0xffffffffu, dsq > 0.f && dsq < r2list);
+                        mine = lane == (unsigned)ch ? bal : mine;
+                    }
+                }
+                if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
+                const float part = warp_sum_f(acc);
+                if (lane == 0) {
+                    Kahan tot;
+                    if (!first) {
+                        const float2 prev = msum[w][t - m0];
+                        tot.s = prev.x;
+                        tot.c = prev.y;
+                    }
+                    tot.add(part);
+                    msum[w][t - m0] = make_float2(tot.s, tot.c);
+                }
+            }
+            __syncwarp();
+        }
+        const uint32_t lst = masked ? (kMaskList | bid) : kRescan;
+        for (uint32_t i = lane; i < m1 - m0; i += 32) {
+            const uint32_t t = m0 + i;
+            if (__ldg(&pos4[t]).w < 0.f) continue;
+            B.nbr_cnt[t] = lst;
+            B.densp[t] = density_result(P, msum[w][i].x, __ldg(&alpha4[t]).w);
+        }
+        __syncwarp();
+    }
+}
+
+// Index lists from the bucket mask lists: bit e of a member's mask stands for
+// candidate e of its bucket's sequence, whose index is e plus the offset of the
+// sequence range holding e (btab). One thread per in-grid particle; the lanes
+// of a warp emit their n-th entries together so that every row of the
+// column-major list is written by one coalesced store. Lists longer than
+// kMaxNbr leave the particle to the cell search.
+__global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant__ DevParams P,
+                                                           const __grid_constant__ DevBuffers B) {
+    const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+    const uint32_t lst = t < B.cstart[P.G] ? B.nbr_cnt[t] : 0u;
+    const bool mine = (lst & kMaskList) != 0;  // else boundary, index list or cell search already
+    const uint32_t* __restrict__ tab = B.btab + (size_t)(mine ? lst & ~kMaskList : 0u) * kTabStride;
+    const uint32_t nw = mine ? (__ldg(&tab[18]) + 31u) >> 5 : 0u;
+    const size_t cap = (size_t)P.cap;
+    const uint32_t* __restrict__ mw = B.nmask + t;
+    uint32_t* __restrict__ col = B.nbr + t;
+    uint32_t r = 0, end = 0, delta = 0;
+    if (mine) {
+        end = __ldg(&tab[1]);
+        delta = __ldg(&tab[20]);
+    }
+    uint32_t wd = 0, m = nw > 0 ? __ldg(mw) : 0u;
+    uint32_t n = 0;
+    while (true) {
+        while (m == 0u && ++wd < nw) m = __ldg(mw + (size_t)wd * cap);
+        const bool has = m != 0u;
+        if (!__any_sync(0xffffffffu, has)) break;
+        if (has) {
+            const uint32_t e = (wd << 5) + (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            while (e >= end) {  // ends at tab[18] = the sequence length > e
+                r++;
+                end = __ldg(&tab[r + 1]);
+                delta = __ldg(&tab[20 + r]);
+            }
+            if (n < (uint32_t)kMaxNbr) col[(size_t)n * cap] = e + delta;
+            n++;
+        }
+    }
+    if (mine) B.nbr_cnt[t] = n <= (uint32_t)kMaxNbr ? n : kRescan;
 }
 
 __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ DevParams P,
@@ -553,8 +815,28 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
 // Force + drift velocity (MfComputeForceCUDA, MfComputeDriftVelCUDA)
 // ---------------------------------------------------------------------------
 
-// Slot-order force + drift: one thread per slot, neighbours gathered from global
-// memory through the slot list (or the cell search).
+// Force + drift of one in-grid fluid particle, neighbours gathered from global
+// memory through its list (or the cell search).
+template <bool FORCE, bool DRIFT, int NP>
+__device__ __forceinline__ void force_drift_one(const DevParams& P, const DevBuffers& B,
+                                                const float4* __restrict__ pos4, const float4* __restrict__ vel4,
+                                                const float4* __restrict__ alpha4, const float4* __restrict__ aprev4,
+                                                int s, const float4 pi) {
+    ForceDrift<FORCE, DRIFT, NP> acc;
+    acc.init(P, pi, vel4[s], B.densp[s], alpha4[s]);
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        // every load first (list entries are almost always neighbours), so that
+        // consecutive neighbours' gathers overlap
+        const float4 pj = __ldg(&pos4[j]);
+        const float2 dpj = __ldg(&B.densp[j]);
+        const float4 vj = FORCE ? __ldg(&vel4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 aj = DRIFT ? __ldg(&alpha4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        acc.pair(P, pj, dpj, vj, aj);
+    });
+    acc.finish(P, B, s, DRIFT ? aprev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
+}
+
+// Force + drift, one thread per particle.
 template <bool FORCE, bool DRIFT, int NP>
 __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_constant__ DevParams P,
                                                              const __grid_constant__ DevBuffers B,
@@ -569,18 +851,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_consta
         if (FORCE) B.accel4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
-    ForceDrift<FORCE, DRIFT, NP> acc;
-    acc.init(P, pi, vel4[s], B.densp[s], alpha4[s]);
-    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
-        // every load first (list entries are almost always neighbours), so that
-        // consecutive neighbours' gathers overlap
-        const float4 pj = __ldg(&pos4[j]);
-        const float2 dpj = __ldg(&B.densp[j]);
-        const float4 vj = FORCE ? __ldg(&vel4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 aj = DRIFT ? __ldg(&alpha4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
-        acc.pair(P, pj, dpj, vj, aj);
-    });
-    acc.finish(P, B, s, DRIFT ? aprev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
+    force_drift_one<FORCE, DRIFT, NP>(P, B, pos4, vel4, alpha4, aprev4, s, pi);
 }
 
 // Surface tension (reference SurfaceTension, fluid_system_kern.cu:569-625): all
@@ -717,11 +988,7 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
 // Fused alpha advance + correction + advance (slot order): reads the cur buffers,
 // writes every float4 field of every slot into the other buffer.
 template <int NP, bool MP>
-__global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ DevParams P,
-                                                        const __grid_constant__ DevBuffers B,
-                                                        const __grid_constant__ F4Set S) {
-    const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+__device__ __forceinline__ void pass_c_one(const DevParams& P, const DevBuffers& B, const F4Set& S, int s) {
     float4 p = S.in[POS][s], v = S.in[VEL][s], ve = S.in[VEV][s], al = S.in[ALPHA][s], ap = S.in[APREV][s];
     const float4 pi = p, vei = ve, ai = al;
     pass_c_slot<NP, MP>(P, B, s, B.mgcell[s] == kUndef, p, v, ve, al, ap, [&](float (&a)[3]) {
@@ -732,6 +999,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ 
     S.out[VEV][s] = ve;
     S.out[ALPHA][s] = al;
     S.out[APREV][s] = ap;
+}
+
+template <int NP, bool MP>
+__global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ DevParams P,
+                                                        const __grid_constant__ DevBuffers B,
+                                                        const __grid_constant__ F4Set S) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    pass_c_one<NP, MP>(P, B, S, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -832,6 +1108,8 @@ __global__ void __launch_bounds__(kThreads) k_unpack_aos(const __grid_constant__
         if (P.dens_k[k] == c.restdens) { ph = k; break; }
     S.out[ALPHA][i] = make_float4(ph == 0 ? 1.f : 0.f, ph == 1 ? 1.f : 0.f, ph == 2 ? 1.f : 0.f, c.restdens);
     S.out[APREV][i] = make_float4(0.f, 0.f, 0.f, __uint_as_float((uint32_t)i));
+    B.opos[i] = (uint32_t)i;  // freshly written slots sit at their own internal index
+    B.oidx[i] = (uint32_t)i;
     B.densp[i] = make_float2(c.dens, c.pressure);
     B.accel4[i] = make_float4(c.accel[0], c.accel[1], c.accel[2], 0.f);
     B.color[i] = make_float4(d.color[0], d.color[1], d.color[2], d.color[3]);
@@ -843,8 +1121,9 @@ __global__ void __launch_bounds__(kThreads) k_pack_aos(const __grid_constant__ D
                                                        const __grid_constant__ DevBuffers B,
                                                        const __grid_constant__ F4Set S, sphmp_display_pack* disp,
                                                        sphmp_calc_pack* calc, int n) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= n) return;
+    const int slot = blockIdx.x * kThreads + threadIdx.x;
+    if (slot >= n) return;
+    const int i = (int)B.opos[slot];
     const float4 p = S.in[POS][i];
     const uint32_t o = __float_as_uint(S.in[APREV][i].w);
     const bool bnd = p.w < 0.f;
@@ -853,7 +1132,7 @@ __global__ void __launch_bounds__(kThreads) k_pack_aos(const __grid_constant__ D
     d.pos[0] = p.x; d.pos[1] = p.y; d.pos[2] = p.z;
     d.color[0] = col.x; d.color[1] = col.y; d.color[2] = col.z; d.color[3] = col.w;
     d.type = bnd ? SPHMP_TYPE_BOUNDARY : SPHMP_TYPE_FLUID;
-    disp[i] = d;
+    disp[slot] = d;
     if (calc == nullptr) return;
     const float4 v = S.in[VEL][i], ve = S.in[VEV][i], al = S.in[ALPHA][i];
     const float2 dp = B.densp[i];
@@ -870,7 +1149,7 @@ __global__ void __launch_bounds__(kThreads) k_pack_aos(const __grid_constant__ D
     c.visc = v.w;
     c.bornid = B.bornid[o];
     c.accel[0] = ac.x; c.accel[1] = ac.y; c.accel[2] = ac.z;
-    calc[i] = c;
+    calc[slot] = c;
 }
 
 __global__ void __launch_bounds__(kThreads) k_pack_field(const __grid_constant__ DevParams P,
@@ -878,34 +1157,35 @@ __global__ void __launch_bounds__(kThreads) k_pack_field(const __grid_constant__
                                                          const __grid_constant__ F4Set S, int field,
                                                          const float4* __restrict__ alpha_c,
                                                          const float4* __restrict__ alpha_p, void* stage, int n) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= n) return;
+    const int t = blockIdx.x * kThreads + threadIdx.x;  // slot (stage index)
+    if (t >= n) return;
+    const int i = (int)B.opos[t];                         // internal index
     float* f = reinterpret_cast<float*>(stage);
     int32_t* q = reinterpret_cast<int32_t*>(stage);
     const float4 p = S.in[POS][i];
     const uint32_t o = __float_as_uint(S.in[APREV][i].w);
     switch (field) {
-        case SPHMP_F_POS: f[3 * i] = p.x; f[3 * i + 1] = p.y; f[3 * i + 2] = p.z; break;
-        case SPHMP_F_VEL: { const float4 v = S.in[VEL][i]; f[3 * i] = v.x; f[3 * i + 1] = v.y; f[3 * i + 2] = v.z; } break;
-        case SPHMP_F_VELEVAL: { const float4 v = S.in[VEV][i]; f[3 * i] = v.x; f[3 * i + 1] = v.y; f[3 * i + 2] = v.z; } break;
-        case SPHMP_F_PRESSURE: f[i] = p.w < 0.f ? 0.f : B.densp[i].y; break;
-        case SPHMP_F_DENS: f[i] = p.w < 0.f ? -p.w : B.densp[i].x; break;
-        case SPHMP_F_RESTDENS: f[i] = alpha_c[i].w; break;
-        case SPHMP_F_VISC: f[i] = S.in[VEL][i].w; break;
-        case SPHMP_F_ACCEL: { const float4 a = B.accel4[i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
-        case SPHMP_F_ALPHA: { const float4 a = alpha_c[i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
-        case SPHMP_F_ALPHA_PRE: { const float4 a = alpha_p[i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
+        case SPHMP_F_POS: f[3 * t] = p.x; f[3 * t + 1] = p.y; f[3 * t + 2] = p.z; break;
+        case SPHMP_F_VEL: { const float4 v = S.in[VEL][i]; f[3 * t] = v.x; f[3 * t + 1] = v.y; f[3 * t + 2] = v.z; } break;
+        case SPHMP_F_VELEVAL: { const float4 v = S.in[VEV][i]; f[3 * t] = v.x; f[3 * t + 1] = v.y; f[3 * t + 2] = v.z; } break;
+        case SPHMP_F_PRESSURE: f[t] = p.w < 0.f ? 0.f : B.densp[i].y; break;
+        case SPHMP_F_DENS: f[t] = p.w < 0.f ? -p.w : B.densp[i].x; break;
+        case SPHMP_F_RESTDENS: f[t] = alpha_c[i].w; break;
+        case SPHMP_F_VISC: f[t] = S.in[VEL][i].w; break;
+        case SPHMP_F_ACCEL: { const float4 a = B.accel4[i]; f[3 * t] = a.x; f[3 * t + 1] = a.y; f[3 * t + 2] = a.z; } break;
+        case SPHMP_F_ALPHA: { const float4 a = alpha_c[i]; f[3 * t] = a.x; f[3 * t + 1] = a.y; f[3 * t + 2] = a.z; } break;
+        case SPHMP_F_ALPHA_PRE: { const float4 a = alpha_p[i]; f[3 * t] = a.x; f[3 * t + 1] = a.y; f[3 * t + 2] = a.z; } break;
         case SPHMP_F_DRIFT:
             for (int k = 0; k < 3; k++) {
                 const float4 u = B.drift4[(size_t)k * P.cap + i];
-                f[9 * i + 3 * k] = u.x; f[9 * i + 3 * k + 1] = u.y; f[9 * i + 3 * k + 2] = u.z;
+                f[9 * t + 3 * k] = u.x; f[9 * t + 3 * k + 1] = u.y; f[9 * t + 3 * k + 2] = u.z;
             }
             break;
-        case SPHMP_F_APREV: { const float4 a = S.in[APREV][i]; f[3 * i] = a.x; f[3 * i + 1] = a.y; f[3 * i + 2] = a.z; } break;
-        case SPHMP_F_PMOD: f[i] = B.pmod[i]; break;
-        case SPHMP_F_TYPE: q[i] = p.w < 0.f ? SPHMP_TYPE_BOUNDARY : SPHMP_TYPE_FLUID; break;
-        case SPHMP_F_MASS: f[i] = B.mass_raw[o]; break;
-        case SPHMP_F_BORNID: q[i] = B.bornid[o]; break;
+        case SPHMP_F_APREV: { const float4 a = S.in[APREV][i]; f[3 * t] = a.x; f[3 * t + 1] = a.y; f[3 * t + 2] = a.z; } break;
+        case SPHMP_F_PMOD: f[t] = B.pmod[i]; break;
+        case SPHMP_F_TYPE: q[t] = p.w < 0.f ? SPHMP_TYPE_BOUNDARY : SPHMP_TYPE_FLUID; break;
+        case SPHMP_F_MASS: f[t] = B.mass_raw[o]; break;
+        case SPHMP_F_BORNID: q[t] = B.bornid[o]; break;
         default: break;
     }
 }
@@ -915,31 +1195,45 @@ __global__ void __launch_bounds__(kThreads) k_unpack_field(const __grid_constant
                                                            const __grid_constant__ F4Set S, int field,
                                                            float4* alpha_c, float4* alpha_p, const void* stage,
                                                            int n) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= n) return;
+    const int t = blockIdx.x * kThreads + threadIdx.x;  // slot (stage index)
+    if (t >= n) return;
+    const int i = (int)B.opos[t];                         // internal index
     const float* f = reinterpret_cast<const float*>(stage);
     float4* const __restrict__* out = S.out;
     switch (field) {
-        case SPHMP_F_POS: { float4 p = out[POS][i]; p.x = f[3 * i]; p.y = f[3 * i + 1]; p.z = f[3 * i + 2]; out[POS][i] = p; } break;
-        case SPHMP_F_VEL: { float4 v = out[VEL][i]; v.x = f[3 * i]; v.y = f[3 * i + 1]; v.z = f[3 * i + 2]; out[VEL][i] = v; } break;
-        case SPHMP_F_VELEVAL: { float4 v = out[VEV][i]; v.x = f[3 * i]; v.y = f[3 * i + 1]; v.z = f[3 * i + 2]; out[VEV][i] = v; } break;
-        case SPHMP_F_PRESSURE: { float2 d = B.densp[i]; d.y = f[i]; B.densp[i] = d; } break;
-        case SPHMP_F_RESTDENS: { float4 a = alpha_c[i]; a.w = f[i]; alpha_c[i] = a; } break;
-        case SPHMP_F_VISC: { float4 v = out[VEL][i]; v.w = f[i]; out[VEL][i] = v; } break;
-        case SPHMP_F_ACCEL: B.accel4[i] = make_float4(f[3 * i], f[3 * i + 1], f[3 * i + 2], 0.f); break;
-        case SPHMP_F_ALPHA: { float4 a = alpha_c[i]; a.x = f[3 * i]; a.y = f[3 * i + 1]; a.z = f[3 * i + 2]; alpha_c[i] = a; } break;
-        case SPHMP_F_ALPHA_PRE: { float4 a = alpha_p[i]; a.x = f[3 * i]; a.y = f[3 * i + 1]; a.z = f[3 * i + 2]; alpha_p[i] = a; } break;
+        case SPHMP_F_POS: { float4 p = out[POS][i]; p.x = f[3 * t]; p.y = f[3 * t + 1]; p.z = f[3 * t + 2]; out[POS][i] = p; } break;
+        case SPHMP_F_VEL: { float4 v = out[VEL][i]; v.x = f[3 * t]; v.y = f[3 * t + 1]; v.z = f[3 * t + 2]; out[VEL][i] = v; } break;
+        case SPHMP_F_VELEVAL: { float4 v = out[VEV][i]; v.x = f[3 * t]; v.y = f[3 * t + 1]; v.z = f[3 * t + 2]; out[VEV][i] = v; } break;
+        case SPHMP_F_PRESSURE: { float2 d = B.densp[i]; d.y = f[t]; B.densp[i] = d; } break;
+        case SPHMP_F_RESTDENS: { float4 a = alpha_c[i]; a.w = f[t]; alpha_c[i] = a; } break;
+        case SPHMP_F_VISC: { float4 v = out[VEL][i]; v.w = f[t]; out[VEL][i] = v; } break;
+        case SPHMP_F_ACCEL: B.accel4[i] = make_float4(f[3 * t], f[3 * t + 1], f[3 * t + 2], 0.f); break;
+        case SPHMP_F_ALPHA: { float4 a = alpha_c[i]; a.x = f[3 * t]; a.y = f[3 * t + 1]; a.z = f[3 * t + 2]; alpha_c[i] = a; } break;
+        case SPHMP_F_ALPHA_PRE: { float4 a = alpha_p[i]; a.x = f[3 * t]; a.y = f[3 * t + 1]; a.z = f[3 * t + 2]; alpha_p[i] = a; } break;
         case SPHMP_F_DRIFT:
             for (int k = 0; k < 3; k++)
-                B.drift4[(size_t)k * P.cap + i] = make_float4(f[9 * i + 3 * k], f[9 * i + 3 * k + 1], f[9 * i + 3 * k + 2], 0.f);
+                B.drift4[(size_t)k * P.cap + i] = make_float4(f[9 * t + 3 * k], f[9 * t + 3 * k + 1], f[9 * t + 3 * k + 2], 0.f);
             break;
-        case SPHMP_F_APREV: { float4 a = out[APREV][i]; a.x = f[3 * i]; a.y = f[3 * i + 1]; a.z = f[3 * i + 2]; out[APREV][i] = a; } break;
-        case SPHMP_F_PMOD: B.pmod[i] = f[i]; break;
+        case SPHMP_F_APREV: { float4 a = out[APREV][i]; a.x = f[3 * t]; a.y = f[3 * t + 1]; a.z = f[3 * t + 2]; out[APREV][i] = a; } break;
+        case SPHMP_F_PMOD: B.pmod[i] = f[t]; break;
         default: break;
     }
 }
 
 inline int blocks_for(int n, int t = kThreads) { return (n + t - 1) / t; }
+
+// Blocks of kThreads that are resident at once on the whole device (for
+// kernels that loop over a device-side work count).
+template <class K>
+int resident_grid(K kernel) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, 0);
+    if (sms <= 0) sms = 1;
+    if (per <= 0) per = 1;
+    return sms * per;
+}
 
 F4Set make_set(const DevBuffers& B, const int* cur, bool to_alt) {
     F4Set S;
@@ -985,9 +1279,11 @@ void launch_grid_list(const DevParams& P, const DevBuffers& B, const int* cur, c
     launch_cell_order(P, B, cur, s);
 }
 
-void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, bool slot_order, cudaStream_t s) {
     if (P.n <= 0) return;
+    if (slot_order) k_slot_order<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
     k_rearrange<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, make_set(B, cur, true));
+    k_update_opos<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
 }
 
 void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
@@ -1003,7 +1299,14 @@ void launch_density(const DevParams& P, const DevBuffers& B, const int* cur, cud
 
 void launch_density_oct(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
     if (P.n <= 0) return;
-    k_density_oct<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[ALPHA][cur[ALPHA]]);
+    const float4* pos = B.f4[POS][cur[POS]];
+    const float4* alpha = B.f4[ALPHA][cur[ALPHA]];
+    cudaMemsetAsync(B.dctr, 0, sizeof(uint32_t), s);
+    if (P.ss == 1.0f)
+        k_density_bucket<true><<<resident_grid(k_density_bucket<true>), kThreads, 0, s>>>(P, B, pos, alpha);
+    else
+        k_density_bucket<false><<<resident_grid(k_density_bucket<false>), kThreads, 0, s>>>(P, B, pos, alpha);
+    k_expand_lists<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
 }
 
 template <bool F, bool D>
