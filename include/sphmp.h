@@ -285,6 +285,26 @@ sphmp_status sphmp_get_particle_index(sphmp_ctx* ctx);
 /* GetGridListCUDA (fluid_system_host.cu:161-185): stable key sort, cell
    offsets/counts and rank-in-cell. */
 sphmp_status sphmp_get_grid_list(sphmp_ctx* ctx);
+/* Allocation-free cell sort; no counterpart in the reference (its GetGridListCUDA
+   sorts the context's own arrays). For callers that must not let a library
+   allocate device memory (a host application owning the device through its own
+   pool, a frame loop that cannot take cudaMalloc's implicit synchronisation):
+   sorts n cell ids `cell` (GRID_UNDEF for out-of-grid particles) on `stream` (a
+   cudaStream_t, NULL for the default stream) into caller-owned device buffers:
+   midsort[n] (stable order), mgndx[n] (rank in cell, GRID_UNDEF out of grid),
+   gridoff[gridtotal] and gridcnt[gridtotal], with the values GetGridListCUDA
+   gives. Its only scratch is a 4.2 MB static device array, so n is limited to
+   SPHMP_NOALLOC_MAX_PARTICLES, gridtotal to SPHMP_NOALLOC_MAX_CELLS and one cell
+   to 4096 particles (larger inputs return SPHMP_ERR_CAPACITY or
+   SPHMP_ERR_CELL_OVERFLOW). The first call on a device looks the scratch up
+   (cudaGetSymbolAddress) with that device current: make it before any stream
+   capture. Calls on one device share the scratch: calls that overlap in time
+   race and must be serialised. Returns after synchronising `stream`. */
+#define SPHMP_NOALLOC_MAX_PARTICLES 262144
+#define SPHMP_NOALLOC_MAX_CELLS 262144
+sphmp_status sphmp_sort_cells_noalloc(const uint32_t* cell, int32_t n, int32_t gridtotal,
+                                      uint32_t* midsort, uint32_t* mgndx, int32_t* gridoff,
+                                      int32_t* gridcnt, void* stream);
 /* RearrageDataCUDA (fluid_system_host.cu:187-210): move every particle to its
    sorted slot; out-of-grid slots are parked at (-1000,-1000,-1000). */
 sphmp_status sphmp_rearrange_data(sphmp_ctx* ctx);

@@ -374,6 +374,8 @@ int field_width(int field) {
 
 }  // namespace
 
+sphmp_status sphmp::record_error(sphmp_status st, const char* msg) { return fail(st, "%s", msg); }
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

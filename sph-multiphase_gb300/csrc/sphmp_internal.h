@@ -128,6 +128,9 @@ struct F4Set {
     float4* __restrict__ out[kNumFloat4Fields];
 };
 
+// Record the text returned by sphmp_last_error on the calling thread (sphmp_api.cu).
+sphmp_status record_error(sphmp_status st, const char* msg);
+
 // ---- launchers (sphmp_kernels.cu) ----
 // All take the current double-buffer selectors in `cur` (one per Field4).
 void launch_hash(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);

@@ -145,7 +145,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_rearrange_data", "sphmp_compute_boundary_density", "sphmp_compute_pressure",
     "sphmp_compute_drift_vel", "sphmp_compute_alpha_advance", "sphmp_compute_correction",
     "sphmp_compute_force", "sphmp_advance", "sphmp_step", "sphmp_conservation",
-    "sphmp_device_errors", "sphmp_last_error", "sphmp_version",
+    "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
