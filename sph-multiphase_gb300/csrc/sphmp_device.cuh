@@ -131,6 +131,21 @@ __device__ __forceinline__ float2 density_result(const DevParams& P, float wsum,
 // Accumulates the force (contributeForce_new) and / or the drift-velocity terms
 // (contributeDriftVel) of one in-grid fluid particle over its neighbours.
 // `pair` takes the neighbour's pos4, (1/rho, p), vel4 and alpha4.
+// Neighbour record of particle s for the alpha pass, 80 contiguous bytes:
+//   {x, y, z, md}, {veleval xyz, alpha_0}, {alpha_1, alpha_2, u_0x, u_0y},
+//   {u_0z, u_1xyz}, {u_2xyz, 0}
+// with md = mass * (1/rho) for fluid particles and -1 for boundary particles
+// (which exchange no volume fraction), u_k the drift velocities.
+__device__ __forceinline__ void write_nrec(const DevBuffers& B, int s, const float4 p, float md, const float4 ve,
+                                           const float (&a)[3], const float (&u)[9]) {
+    float4* r = B.nrec + (size_t)s * kNrecFloat4;
+    r[0] = make_float4(p.x, p.y, p.z, md);
+    r[1] = make_float4(ve.x, ve.y, ve.z, a[0]);
+    r[2] = make_float4(a[1], a[2], u[0], u[1]);
+    r[3] = make_float4(u[2], u[3], u[4], u[5]);
+    r[4] = make_float4(u[6], u[7], u[8], 0.f);
+}
+
 template <bool FORCE, bool DRIFT, int NP>
 struct ForceDrift {
     static constexpr int K = NP > 0 ? NP : 1;
@@ -214,7 +229,11 @@ struct ForceDrift {
     }
 
     // mfComputeDriftVel's closing terms (multiphase.cu:131-163) and the stores.
-    __device__ __forceinline__ void finish(const DevParams& P, const DevBuffers& B, int s, const float4 ap) {
+    // `vev` (the particle's veleval) is only read when FORCE and DRIFT run
+    // together: that pass also writes the particle's neighbour record for the
+    // alpha pass (write_nrec).
+    __device__ __forceinline__ void finish(const DevParams& P, const DevBuffers& B, int s, const float4 ap,
+                                           const float4 vev = make_float4(0.f, 0.f, 0.f, 0.f)) {
         if (FORCE) B.accel4[s] = make_float4(fx, fy, fz, 0.f);
         if (DRIFT) {
             const float cc = P.cont * P.cont2;
@@ -243,9 +262,20 @@ struct ForceDrift {
                 out[k].z -= cs * (st[k].z - ssum.z);
                 B.drift4[(size_t)k * P.cap + s] = make_float4(out[k].x, out[k].y, out[k].z, 0.f);
             }
+            if (FORCE) {
+                float u[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    u[3 * k] = out[k].x;
+                    u[3 * k + 1] = out[k].y;
+                    u[3 * k + 2] = out[k].z;
+                }
+                write_nrec(B, s, pi, pi.w * idens, vev, ia, u);
+            }
         }
     }
 };
+
 
 // ---------------------------------------------------------------------------
 // Volume-fraction advance (MfComputeAlphaAdvanceCUDA)

@@ -39,6 +39,7 @@ constexpr int kWarpSortMax = 256;     // cells up to this size are sorted by one
 constexpr int kCtaSortMax = 8192;     // larger cells up to this size are sorted by one CTA
 constexpr int kNumFloat4Fields = 5;   // pos4, vel4, vev4, alpha4, aprev4
 constexpr int kMaxNbr = 256;          // index-list capacity per particle (more: the passes rescan)
+constexpr int kNrecFloat4 = 5;        // float4 per neighbour record of the alpha pass
 // Bucket neighbour lists: a bitmask over the bucket's candidate sequence (the 27
 // h-subcells around it as 18 index ranges), one word per 32 candidates.
 constexpr int kMaskWords = 64;        // mask words per particle (more candidates: the passes rescan)
@@ -110,6 +111,7 @@ struct DevBuffers {
     uint32_t* nmask;    // [kMaskWords * cap] bucket mask lists, column-major: word k of particle s at k * cap + s
     uint32_t* btab;     // [8 * G * kTabStride] candidate ranges of each bucket with a mask list
     uint32_t* dctr;     // [1] work counter of the bucket density kernel
+    float4* nrec;       // [kNrecFloat4 * cap] neighbour records of the alpha pass (written by force + drift)
     // Internal order: inside every 2h cell, members grouped by the h-subcell
     // (octant) they occupy, octant index (oy * 2 + oz) * 2 + ox.
     uint32_t* opos;     // [cap] internal index of each reference slot

@@ -821,7 +821,7 @@ template <bool FORCE, bool DRIFT, int NP>
 __device__ __forceinline__ void force_drift_one(const DevParams& P, const DevBuffers& B,
                                                 const float4* __restrict__ pos4, const float4* __restrict__ vel4,
                                                 const float4* __restrict__ alpha4, const float4* __restrict__ aprev4,
-                                                int s, const float4 pi) {
+                                                const float4* __restrict__ vev4, int s, const float4 pi) {
     ForceDrift<FORCE, DRIFT, NP> acc;
     acc.init(P, pi, vel4[s], B.densp[s], alpha4[s]);
     for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
@@ -833,25 +833,33 @@ __device__ __forceinline__ void force_drift_one(const DevParams& P, const DevBuf
         const float4 aj = DRIFT ? __ldg(&alpha4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
         acc.pair(P, pj, dpj, vj, aj);
     });
-    acc.finish(P, B, s, DRIFT ? aprev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
+    acc.finish(P, B, s, DRIFT ? aprev4[s] : make_float4(0.f, 0.f, 0.f, 0.f),
+               FORCE && DRIFT ? vev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
 }
 
-// Force + drift, one thread per particle.
+// Force + drift, one thread per particle. With both, it also writes every
+// in-grid particle's neighbour record for the fused alpha pass.
 template <bool FORCE, bool DRIFT, int NP>
 __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_constant__ DevParams P,
                                                              const __grid_constant__ DevBuffers B,
                                                              const float4* __restrict__ pos4,
                                                              const float4* __restrict__ vel4,
                                                              const float4* __restrict__ alpha4,
-                                                             const float4* __restrict__ aprev4) {
+                                                             const float4* __restrict__ aprev4,
+                                                             const float4* __restrict__ vev4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= P.n || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
     if (pi.w < 0.f) {
         if (FORCE) B.accel4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FORCE && DRIFT) {
+            const float a0[3] = {0.f, 0.f, 0.f};
+            const float u0[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            write_nrec(B, s, pi, -1.f, make_float4(0.f, 0.f, 0.f, 0.f), a0, u0);
+        }
         return;
     }
-    force_drift_one<FORCE, DRIFT, NP>(P, B, pos4, vel4, alpha4, aprev4, s, pi);
+    force_drift_one<FORCE, DRIFT, NP>(P, B, pos4, vel4, alpha4, aprev4, vev4, s, pi);
 }
 
 // Surface tension (reference SurfaceTension, fluid_system_kern.cu:569-625): all
@@ -987,12 +995,39 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
 
 // Fused alpha advance + correction + advance (slot order): reads the cur buffers,
 // writes every float4 field of every slot into the other buffer.
+// Alpha change of in-grid particle s with its neighbours' data from the
+// neighbour records the force + drift pass of this step wrote (five 16-byte
+// loads per neighbour instead of seven separate gathers).
+template <int NP>
+__device__ __forceinline__ void alpha_change_nrec(const DevParams& P, const DevBuffers& B, int s, const float4 pi,
+                                                  const float4 vei, const float4 ai, float (&out)[3]) {
+    float3 um[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        const float4 u = B.drift4[(size_t)k * P.cap + s];
+        um[k] = make_float3(u.x, u.y, u.z);
+    }
+    AlphaChange<NP> acc;
+    acc.init(pi, vei, ai, um);
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4* __restrict__ r = B.nrec + (size_t)j * kNrecFloat4;
+        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+        const float4 r4 = NP > 2 ? __ldg(r + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 uj[NP];
+        uj[0] = make_float4(r2.z, r2.w, r3.x, 0.f);
+        if (NP > 1) uj[NP > 1 ? 1 : 0] = make_float4(r3.y, r3.z, r3.w, 0.f);
+        if (NP > 2) uj[NP > 2 ? 2 : 0] = make_float4(r4.x, r4.y, r4.z, 0.f);
+        acc.pair(P, r0, r0.w, make_float4(r1.x, r1.y, r1.z, 0.f), make_float4(r1.w, r2.x, r2.y, 0.f), uj);
+    });
+    acc.result(P, out);
+}
+
 template <int NP, bool MP>
 __device__ __forceinline__ void pass_c_one(const DevParams& P, const DevBuffers& B, const F4Set& S, int s) {
     float4 p = S.in[POS][s], v = S.in[VEL][s], ve = S.in[VEV][s], al = S.in[ALPHA][s], ap = S.in[APREV][s];
     const float4 pi = p, vei = ve, ai = al;
     pass_c_slot<NP, MP>(P, B, s, B.mgcell[s] == kUndef, p, v, ve, al, ap, [&](float (&a)[3]) {
-        alpha_change_slot<NP>(P, B, S.in[POS], S.in[VEV], S.in[ALPHA], s, pi, vei, ai, a);
+        alpha_change_nrec<NP>(P, B, s, pi, vei, ai, a);
     });
     S.out[POS][s] = p;
     S.out[VEL][s] = v;
@@ -1315,15 +1350,16 @@ static void fd_dispatch(const DevParams& P, const DevBuffers& B, const int* cur,
     const float4* vel = B.f4[VEL][cur[VEL]];
     const float4* al = B.f4[ALPHA][cur[ALPHA]];
     const float4* ap = B.f4[APREV][cur[APREV]];
+    const float4* ve = B.f4[VEV][cur[VEV]];
     const int g = blocks_for(P.n);
     if (!D) {
-        k_force_drift<F, false, 0><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap);
+        k_force_drift<F, false, 0><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve);
         return;
     }
     switch (P.nphase) {
-        case 1: k_force_drift<F, true, 1><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap); break;
-        case 2: k_force_drift<F, true, 2><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap); break;
-        default: k_force_drift<F, true, 3><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap); break;
+        case 1: k_force_drift<F, true, 1><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve); break;
+        case 2: k_force_drift<F, true, 2><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve); break;
+        default: k_force_drift<F, true, 3><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve); break;
     }
 }
 
