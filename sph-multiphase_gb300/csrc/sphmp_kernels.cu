@@ -750,6 +750,12 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
     const uint32_t nw = mine ? (__ldg(&tab[18]) + 31u) >> 5 : 0u;
     const size_t cap = (size_t)P.cap;
     const uint32_t* __restrict__ mw = B.nmask + t;
+    // hits of this particle, then of the warp's busiest lane (the loop bound)
+    uint32_t cnt = 0;
+    for (uint32_t wd = 0; wd < nw; wd++) cnt += __popc(__ldg(mw + (size_t)wd * cap));
+    uint32_t rounds = min(cnt, (uint32_t)kMaxNbr);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
     uint32_t* __restrict__ col = B.nbr + t;
     uint32_t r = 0, end = 0, delta = 0;
     if (mine) {
@@ -757,12 +763,9 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
         delta = __ldg(&tab[20]);
     }
     uint32_t wd = 0, m = nw > 0 ? __ldg(mw) : 0u;
-    uint32_t n = 0;
-    while (true) {
-        while (m == 0u && ++wd < nw) m = __ldg(mw + (size_t)wd * cap);
-        const bool has = m != 0u;
-        if (!__any_sync(0xffffffffu, has)) break;
-        if (has) {
+    for (uint32_t n = 0; n < rounds; n++) {
+        if (n < cnt) {
+            while (m == 0u) m = __ldg(mw + (size_t)(++wd) * cap);
             const uint32_t e = (wd << 5) + (uint32_t)(__ffs(m) - 1);
             m &= m - 1u;
             while (e >= end) {  // ends at tab[18] = the sequence length > e
@@ -770,11 +773,10 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
                 end = __ldg(&tab[r + 1]);
                 delta = __ldg(&tab[20 + r]);
             }
-            if (n < (uint32_t)kMaxNbr) col[(size_t)n * cap] = e + delta;
-            n++;
+            col[(size_t)n * cap] = e + delta;
         }
     }
-    if (mine) B.nbr_cnt[t] = n <= (uint32_t)kMaxNbr ? n : kRescan;
+    if (mine) B.nbr_cnt[t] = cnt <= (uint32_t)kMaxNbr ? cnt : kRescan;
 }
 
 __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ DevParams P,
