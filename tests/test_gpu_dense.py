@@ -1,0 +1,90 @@
+"""GPU parity on tightly packed scenes, where the neighbour machinery leaves its
+common path: candidate sequences longer than one register block of the bucket
+density (256), index lists longer than their capacity (256 entries: the passes
+fall back to the cell search), sequences longer than the mask capacity (2048
+candidates: no mask list at all) and buckets with more than 128 members (the
+per-member octant search). Particles are lighter in proportion, so densities
+stay near rest density. Same tolerances as test_gpu_parity.py.
+"""
+import numpy as np
+import pytest
+from scipy.ndimage import uniform_filter
+
+import sphmp
+from helpers import UNDEF, bits_equal, device_ctx, download_state, field_err, in_grid_fluid, oracle_state
+from oracle import oracle as O
+from sphmp import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+H = 0.02
+
+# name -> (h / d, lattice): ~268, ~524 and ~736 neighbours per particle
+PACKINGS = {"blocks_and_overflow": (4.0, (20, 20, 20)), "unmasked": (5.0, (18, 18, 18)),
+            "big_buckets": (5.6, (17, 17, 17))}
+
+
+def _scene(name):
+    ratio, n = PACKINGS[name]
+    return scenes.small_block(seed=41, n=n, d=H / ratio, h=H, nphase=3, eos=abi.EOS_TAIT, velocity_scale=0.2)
+
+
+def _bucket_stats(sc):
+    """Members per h-subcell and candidates (27 subcells) seen by each fluid particle."""
+    p = sc.params
+    pos = sc.disp["pos"]
+    gmin = np.array(p.gridmin[:3], np.float32)
+    fac = np.array(p.gridIdfac[:3], np.float32)
+    res = np.array(p.gridres[:3])
+    sub = np.floor(2 * ((pos - gmin) * fac)).astype(np.int64)
+    cnt = np.zeros((2 * res[2], 2 * res[1], 2 * res[0]), np.int32)
+    np.add.at(cnt, (sub[:, 2], sub[:, 1], sub[:, 0]), 1)
+    seq = np.rint(uniform_filter(cnt.astype(np.float64), size=3, mode="constant") * 27)
+    fl = sc.disp["type"] == 0
+    at = (sub[fl, 2], sub[fl, 1], sub[fl, 0])
+    return cnt[at], seq[at]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build(built):
+    sphmp.load()
+
+
+def test_packings_reach_the_intended_paths():
+    occ, seq = _bucket_stats(_scene("blocks_and_overflow"))
+    assert seq.max() > 256 * 4 and seq.max() <= 2048 and occ.max() <= 128
+    occ, seq = _bucket_stats(_scene("unmasked"))
+    assert (seq > 2048).mean() > 0.3
+    occ, seq = _bucket_stats(_scene("big_buckets"))
+    assert (occ > 128).mean() > 0.3
+
+
+@pytest.mark.parametrize("schedule", [abi.SCHEDULE_FUSED, abi.SCHEDULE_REFERENCE], ids=["fused", "reference"])
+@pytest.mark.parametrize("name", list(PACKINGS))
+def test_dense_step_matches_oracle(name, schedule):
+    sc = _scene(name)
+    p = sc.params
+    s = oracle_state(sc)
+    O.before_first_step(p, s)
+    ctx = device_ctx(sc)
+    ctx.before_first_step()
+    # a first sort on both sides builds the device's octant order, as in a running simulation
+    for st in ("orc_get_particle_index", "orc_get_grid_list", "orc_rearrange_data"):
+        O.call(st, p, s)
+    ctx.sort()
+    O.step(p, s, schedule, 1)
+    ctx.step(1, schedule, use_graph=False)
+    ctx.sync()
+    assert ctx.device_errors() == 0
+    g = download_state(ctx)
+    for k in ("mgcell", "midsort", "mgridoff", "mgridcnt"):
+        assert bits_equal(g[k], getattr(s, k)), k
+    f = in_grid_fluid(s)
+    assert f.sum() > 1000
+    assert field_err(g["dens"][f], s.dens[f]) < RTOL
+    assert field_err(g["accel"][f], s.accel[f]) < RTOL
+    for k in ("pos", "vel", "veleval"):
+        assert field_err(g[k][f], getattr(s, k)[f]) < RTOL, k
+    assert field_err(g["alpha"][f][:, :3], s.alpha[f][:, :3], floor=1.0) < RTOL
+    ctx.close()
