@@ -243,6 +243,39 @@ sphmp_status sphmp_add_open_box(const sphmp_params* p, const float vmin[3], cons
 /* Boundary lattice spacing (bmass/bRestdensity)^(1/3)/simscale (AddShape.cpp:265-271). */
 float sphmp_boundary_spacing(const sphmp_params* p);
 
+/* ---- particle data formats (host only) ---- */
+
+/* Text frame dump of the reference's FluidSystem::outputFile
+   (SPH_Solver/fluids/FluidIOUtility.cpp:17-38): the count on the first line, then
+   per record "x y z mass restdens type" in printf %f / %d form. */
+sphmp_status sphmp_write_frame_text(const char* path, const sphmp_display_pack* disp,
+                                    const sphmp_calc_pack* calc, int32_t n);
+
+/* Header of a BINX-020 (.bi2) particle file (SPH_Solver/catpaw/BI2Reader.h:20-58). */
+typedef struct sphmp_bi2_info {
+    int32_t fmt, bitorder, full, data2d;
+    float dp, h, b, rhop0, gamma, massbound, massfluid, time;
+    int32_t np, nfixed, nmoving, nfloat, nfluidout, nbound, nfluid;
+} sphmp_bi2_info;
+
+/* Read a BINX-020 file as the reference's BI2Reader::GetInfo(false) does
+   (SPH_Solver/catpaw/BI2Reader.cpp:19-106), converting the byte order when it
+   differs from the host's. Fills `info`; when any of pos (3 floats per
+   particle), vel (3 floats) or rhop (1 float) is non-NULL, also fills those
+   arrays for info->np particles (cap >= np), with zero for particles the file
+   does not carry (the fixed ones of a short file, fluid that left). Unlike the
+   reference, a file that is not BINX-020 or has inconsistent counts is an error. */
+sphmp_status sphmp_read_bi2(const char* path, sphmp_bi2_info* info, float* pos, float* vel, float* rhop,
+                            int32_t cap);
+
+/* Append the particles of a .bi2 shape as fluid of `phase` (the reference's
+   FluidSystem::AddShape, SPH_Solver/fluids/fluid_system.cpp:809-835, which uses
+   scale 0.005, velocity (0, -1.5, 0) and the third phase): position (x, y, z)
+   of the file becomes (x, z, y) / scale + offs. */
+sphmp_status sphmp_add_bi2_shape(const sphmp_params* p, const float* pos, int32_t np, float scale,
+                                 const float offs[3], const float vel[3], int32_t phase,
+                                 sphmp_display_pack* disp, sphmp_calc_pack* calc, int32_t cap, int32_t* count);
+
 /* ---- context lifetime (reference FluidSetupCUDA / FluidClearCUDA, fluid_system_host.cu:79-144) ---- */
 
 /* Allocate device buffers for p->maxNum particles and p->gridtotal cells on the
@@ -339,6 +372,15 @@ int32_t sphmp_step_profile(sphmp_ctx* ctx, int32_t schedule, float* ms, char* na
    out[0] = total mass, out[1] = total volume sum(m/rho), out[2+k] = phase-k volume
    sum(alpha_k m/rho) for k < nphase, out[2+nphase] = max |sum_k alpha_k - 1|. */
 sphmp_status sphmp_conservation(sphmp_ctx* ctx, double* out, int32_t nout);
+
+/* Binary state checkpoint of a context (no counterpart in the reference): the
+   reference records of every particle plus its volume fractions and last-step
+   (g - a), everything a following step reads, so a context loaded from a
+   checkpoint continues bit for bit like the one that wrote it. Little-endian
+   hosts; sphmp_load_state replaces the context's particles (the phase count
+   must match, n must fit the capacity). */
+sphmp_status sphmp_save_state(sphmp_ctx* ctx, const char* path);
+sphmp_status sphmp_load_state(sphmp_ctx* ctx, const char* path);
 
 /* Device-side error word accumulated by the kernels since the last call (bit set of
    (1 << sphmp_status)); reading it clears it. */

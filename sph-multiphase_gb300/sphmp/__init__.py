@@ -76,6 +76,12 @@ def load():
         "sphmp_last_error": (C.c_char_p, []),
         "sphmp_version": (C.c_char_p, []),
         "sphmp_legacy_context": (ctx, []),
+        "sphmp_write_frame_text": (st, [C.c_char_p, vp, vp, C.c_int32]),
+        "sphmp_read_bi2": (st, [C.c_char_p, P(abi.Bi2Info), vp, vp, vp, C.c_int32]),
+        "sphmp_add_bi2_shape": (st, [P(Params), vp, C.c_int32, C.c_float, P(C.c_float), P(C.c_float), C.c_int32,
+                                     vp, vp, C.c_int32, P(C.c_int32)]),
+        "sphmp_save_state": (st, [ctx, C.c_char_p]),
+        "sphmp_load_state": (st, [ctx, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -306,7 +312,47 @@ class Context:
         check(self._lib.sphmp_device_errors(self._ptr, C.byref(bits)))
         return bits.value
 
+    def save_state(self, path):
+        check(self._lib.sphmp_save_state(self._ptr, os.fsencode(path)))
+
+    def load_state(self, path):
+        check(self._lib.sphmp_load_state(self._ptr, os.fsencode(path)))
+
+
+# ---------------------------------------------------------------------------
+# particle data formats (host only)
+# ---------------------------------------------------------------------------
+
+def write_frame_text(path, disp, calc, n=None):
+    """The reference's text frame dump (FluidSystem::outputFile)."""
+    n = len(disp) if n is None else n
+    check(load().sphmp_write_frame_text(os.fsencode(path), disp.ctypes.data, calc.ctypes.data, int(n)))
+
+
+def read_bi2(path, header_only=False):
+    """(info dict, pos[np,3], vel[np,3], rhop[np]) of a BINX-020 file."""
+    info = abi.Bi2Info()
+    L = load()
+    check(L.sphmp_read_bi2(os.fsencode(path), C.byref(info), None, None, None, 0))
+    if header_only:
+        return info.as_dict(), None, None, None
+    n = info.np
+    pos = np.zeros((n, 3), np.float32)
+    vel = np.zeros((n, 3), np.float32)
+    rhop = np.zeros(n, np.float32)
+    check(L.sphmp_read_bi2(os.fsencode(path), C.byref(info), pos.ctypes.data, vel.ctypes.data, rhop.ctypes.data, n))
+    return info.as_dict(), pos, vel, rhop
+
+
+def add_bi2_shape(p, disp, calc, count, pos, scale=0.005, offs=(0, 0, 0), vel=(0, -1.5, 0), phase=2):
+    """Append .bi2 shape particles as fluid (the reference's FluidSystem::AddShape); returns the new count."""
+    pos = np.ascontiguousarray(pos, np.float32)
+    n = C.c_int32(count)
+    check(load().sphmp_add_bi2_shape(C.byref(p), pos.ctypes.data, len(pos), float(scale), _f3(offs), _f3(vel),
+                                     int(phase), disp.ctypes.data, calc.ctypes.data, len(disp), C.byref(n)))
+    return n.value
+
 
 __all__ = ["abi", "Params", "DisplayPack", "CalcPack", "Context", "SphmpError", "load", "check", "last_error",
            "params_default", "setup_constants", "setup_grid", "boundary_spacing", "record_arrays",
-           "add_fluid_volume", "add_wall", "add_open_box"]
+           "add_fluid_volume", "add_wall", "add_open_box", "write_frame_text", "read_bi2", "add_bi2_shape"]

@@ -146,6 +146,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_compute_drift_vel", "sphmp_compute_alpha_advance", "sphmp_compute_correction",
     "sphmp_compute_force", "sphmp_advance", "sphmp_step", "sphmp_conservation",
     "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
+    "sphmp_write_frame_text", "sphmp_read_bi2", "sphmp_add_bi2_shape", "sphmp_save_state", "sphmp_load_state",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
@@ -153,3 +154,15 @@ EXPORTED_SYMBOLS = [
     "ComputeBoundaryDensity", "computeNumBlocks", "sphmp_legacy_context", "TransferToCUDA",
     "TransferFromCUDA", "EmitUpdateCUDA",
 ]
+
+
+class Bi2Info(C.Structure):
+    """sphmp_bi2_info: header of a BINX-020 (.bi2) particle file."""
+    _fields_ = [("fmt", C.c_int32), ("bitorder", C.c_int32), ("full", C.c_int32), ("data2d", C.c_int32),
+                ("dp", C.c_float), ("h", C.c_float), ("b", C.c_float), ("rhop0", C.c_float), ("gamma", C.c_float),
+                ("massbound", C.c_float), ("massfluid", C.c_float), ("time", C.c_float),
+                ("np", C.c_int32), ("nfixed", C.c_int32), ("nmoving", C.c_int32), ("nfloat", C.c_int32),
+                ("nfluidout", C.c_int32), ("nbound", C.c_int32), ("nfluid", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}

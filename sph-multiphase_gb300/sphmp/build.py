@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libsphmp.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["sphmp_kernels.cu", "sphmp_api.cu", "sphmp_noalloc.cu"]
-HOST_SOURCES = ["sphmp_host.cpp"]
+HOST_SOURCES = ["sphmp_host.cpp", "sphmp_io.cpp"]
 
 
 def _nvcc():
