@@ -303,6 +303,17 @@ sphmp_status sphmp_upload_aos(sphmp_ctx* ctx, const sphmp_display_pack* disp,
    (the reference's per-frame TransferFromCUDA copies display records only). */
 sphmp_status sphmp_download_aos(sphmp_ctx* ctx, sphmp_display_pack* disp,
                                 sphmp_calc_pack* calc, int32_t n);
+/* Asynchronous TransferFromCUDA: queue, after the work already on the context
+   stream, a download of the n display records into `disp` and return at once.
+   The copy runs on a separate stream, so it overlaps whatever is queued next
+   (the following steps); `disp` must stay valid and unread until
+   sphmp_download_wait (or sphmp_sync) returns, and should be pinned host memory
+   (pageable memory makes the copy synchronous). Two downloads can be in flight;
+   a third waits on the device for the first. No counterpart in the reference,
+   whose TransferFromCUDA is synchronous. */
+sphmp_status sphmp_download_display_async(sphmp_ctx* ctx, sphmp_display_pack* disp, int32_t n);
+/* Wait for every asynchronous download of the context. */
+sphmp_status sphmp_download_wait(sphmp_ctx* ctx);
 /* Append records into slots [start, end) and set num = end (EmitUpdateCUDA). */
 sphmp_status sphmp_emit_aos(sphmp_ctx* ctx, const sphmp_display_pack* disp,
                             const sphmp_calc_pack* calc, int32_t start, int32_t end);

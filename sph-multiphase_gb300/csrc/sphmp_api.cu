@@ -37,6 +37,13 @@ struct sphmp_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_n = -1;
     int graph_schedule = -1;
+    // asynchronous display downloads: two device staging buffers, copied to the
+    // host on a separate stream while the context stream runs on
+    cudaStream_t copy_stream = nullptr;
+    sphmp_display_pack* dl_stage[2] = {nullptr, nullptr};
+    cudaEvent_t dl_packed[2] = {nullptr, nullptr};
+    cudaEvent_t dl_done[2] = {nullptr, nullptr};
+    int dl_next = 0;
 };
 
 namespace {
@@ -423,6 +430,15 @@ sphmp_status sphmp_create(const sphmp_params* p, sphmp_ctx** out) {
 sphmp_status sphmp_destroy(sphmp_ctx* c) {
     if (!c) return SPHMP_OK;
     cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    for (int k = 0; k < 2; k++) {
+        cudaFree(c->dl_stage[k]);
+        if (c->dl_packed[k]) cudaEventDestroy(c->dl_packed[k]);
+        if (c->dl_done[k]) cudaEventDestroy(c->dl_done[k]);
+    }
     drop_graph(c);
     free_buffers(c);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -465,6 +481,7 @@ sphmp_status sphmp_set_stream(sphmp_ctx* c, void* stream) {
 sphmp_status sphmp_sync(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     CK(cudaStreamSynchronize(c->stream));
+    if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
     return take_device_errors(c, nullptr);
 }
 
@@ -539,6 +556,40 @@ sphmp_status sphmp_download_aos(sphmp_ctx* c, sphmp_display_pack* disp, sphmp_ca
             CK(cudaMemcpyAsync(calc, d_calc, sizeof(sphmp_calc_pack) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_download_display_async(sphmp_ctx* c, sphmp_display_pack* disp, int32_t n) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!disp) return fail(SPHMP_ERR_INVALID_ARG, "display pointer is NULL");
+    if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
+    if (!c->copy_stream) {  // first use: the copy stream, two staging buffers and their events
+        CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; k++) {
+            CK(cudaMalloc(&c->dl_stage[k], sizeof(sphmp_display_pack) * (size_t)(c->cap > 0 ? c->cap : 1)));
+            CK(cudaEventCreateWithFlags(&c->dl_packed[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&c->dl_done[k], cudaEventDisableTiming));
+            CK(cudaEventRecord(c->dl_done[k], c->copy_stream));
+        }
+    }
+    const int k = c->dl_next;
+    c->dl_next ^= 1;
+    // the staging buffer is free once the copy of two downloads ago has landed
+    CK(cudaStreamWaitEvent(c->stream, c->dl_done[k], 0));
+    launch_pack_aos(dev_params(c), c->B, c->cur, c->dl_stage[k], nullptr, n, c->stream);
+    CHECK_LAUNCH("pack display records");
+    CK(cudaEventRecord(c->dl_packed[k], c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->dl_packed[k], 0));
+    if (n > 0)
+        CK(cudaMemcpyAsync(disp, c->dl_stage[k], sizeof(sphmp_display_pack) * (size_t)n, cudaMemcpyDeviceToHost,
+                           c->copy_stream));
+    CK(cudaEventRecord(c->dl_done[k], c->copy_stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_download_wait(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
     return SPHMP_OK;
 }
 

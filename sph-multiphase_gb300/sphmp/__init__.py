@@ -81,6 +81,8 @@ def load():
         "sphmp_add_bi2_shape": (st, [P(Params), vp, C.c_int32, C.c_float, P(C.c_float), P(C.c_float), C.c_int32,
                                      vp, vp, C.c_int32, P(C.c_int32)]),
         "sphmp_save_state": (st, [ctx, C.c_char_p]),
+        "sphmp_download_display_async": (st, [ctx, vp, C.c_int32]),
+        "sphmp_download_wait": (st, [ctx]),
         "sphmp_load_state": (st, [ctx, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
@@ -311,6 +313,14 @@ class Context:
         bits = C.c_uint32(0)
         check(self._lib.sphmp_device_errors(self._ptr, C.byref(bits)))
         return bits.value
+
+    def download_display_async(self, disp, n=None):
+        """Queue a download of the display records into `disp` (pinned numpy memory); see download_wait."""
+        n = self.n if n is None else n
+        check(self._lib.sphmp_download_display_async(self._ptr, disp.ctypes.data, int(n)))
+
+    def download_wait(self):
+        check(self._lib.sphmp_download_wait(self._ptr))
 
     def save_state(self, path):
         check(self._lib.sphmp_save_state(self._ptr, os.fsencode(path)))

@@ -128,3 +128,35 @@ def test_checkpoint_continues_bit_for_bit(tmp_path):
     with pytest.raises(sphmp.SphmpError):
         c.load_state(path)
     c.close()
+
+
+@pytest.mark.gpu
+def test_async_display_download_matches_sync():
+    """Two contexts run the same steps; one downloads synchronously, the other
+    through the asynchronous path into two alternating pinned buffers."""
+    import torch
+    sc = scenes.small_block(seed=9, n=(12, 10, 9), nphase=2, eos=abi.EOS_TAIT, velocity_scale=0.3)
+    a = sphmp.Context(sc.params)
+    b = sphmp.Context(sc.params)
+    for ctx in (a, b):
+        ctx.upload_aos(sc.disp, sc.calc)
+        ctx.before_first_step()
+    pinned = [torch.empty(sc.n * 32, dtype=torch.uint8, pin_memory=True) for _ in range(2)]
+    bufs = [t.numpy().view(abi.display_dtype()) for t in pinned]
+    want = []
+    for k in range(5):
+        a.step(1, abi.SCHEDULE_FUSED, use_graph=True)
+        want.append(a.download_aos(calc=False).copy())
+    got = []
+    for k in range(5):
+        b.step(1, abi.SCHEDULE_FUSED, use_graph=True)
+        b.download_display_async(bufs[k & 1])
+        if k & 1:  # both buffers in flight: collect them
+            b.download_wait()
+            got += [bufs[0].copy(), bufs[1].copy()]
+    b.download_wait()
+    got.append(bufs[0].copy())
+    for k in range(5):
+        assert want[k].tobytes() == got[k].tobytes(), k
+    a.close()
+    b.close()
