@@ -175,3 +175,84 @@ def small_block(seed=3, n=(12, 10, 8), d=0.01, h=0.02, box=None, dt=2e-4, nphase
     if walls:
         count = _walls(p, disp, calc, count, bmin, bmax, d)
     return _finish(p, disp, calc, count, n_fluid, "small_block")
+
+
+def bubble_scene(seed, n_particles, d=0.01, h=0.02, dt=2e-4, eos=abi.EOS_LINEAR, eos_k=3.0, jitter=0.05,
+                 multiphase=1):
+    """One scene of the batched configuration: a near-cubic liquid lattice of about `n_particles` sites at
+    spacing d with +-jitter*d jitter, 1-4 gas bubbles of radius U(3h, 8h) (liquid 1000, gas 1.2 kg/m^3),
+    in an open box 1.5x the block."""
+    rng = np.random.default_rng(seed)
+    side = n_particles ** (1.0 / 3.0)
+    nx = max(4, int(round(side)))
+    nz = max(4, int(round(side)))
+    ny = max(4, int(round(n_particles / (nx * nz))))
+    box = tuple(max(c * d * 1.5, 4 * h) for c in (nx, ny, nz))
+    bmin, bmax = (0.0, 0.0, 0.0), box
+    p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=2, dens=(1000.0, 1.2), visc=(0.2, 0.2),
+                    eos=eos, eos_k=eos_k, multiphase=multiphase)
+    cap = nx * ny * nz + int(2 * 2 * sum(box[a] * box[b] for a in range(3) for b in range(a + 1, 3)) / d ** 2 * 1.6) \
+        + 2048
+    disp, calc = record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, (nx, ny, nz), d, jitter, seed)
+    n_fluid = count
+    ext = np.array([nx, ny, nz], np.float32) * np.float32(d)
+    pos = disp["pos"][:count]
+    gas = np.zeros(count, bool)
+    for _ in range(int(rng.integers(1, 5))):
+        c = (rng.uniform(0.2, 0.8, 3) * ext).astype(np.float32)
+        r = np.float32(rng.uniform(3 * h, 8 * h))
+        gas |= np.sum((pos - c) ** 2, axis=1) < r * r
+    _assign_phase(p, calc, np.nonzero(gas)[0], 1)
+    count = _walls(p, disp, calc, count, bmin, bmax, d)
+    return _finish(p, disp, calc, count, n_fluid, f"bubbles_{nx}x{ny}x{nz}")
+
+
+def tile(scene_list, gap_cells=2):
+    """Independent scenes in one domain, so that every pass covers all of them in one launch: each scene
+    is moved into its own tile of a 3D arrangement (x fastest, then z, then y), tiles separated by
+    `gap_cells` empty grid cells, all offsets whole multiples of the cell size. Every scene keeps its
+    own grid padding (two cells outside its walls), so no particle of one scene is ever within h of
+    another's. The scenes must share their physics (h, dt, phases, EOS, simscale); the combined grid
+    covers every tile. One difference from running a scene alone: a particle that leaves its walls
+    stays in the combined grid instead of reaching that scene's grid border. Returns the combined
+    Scene and, per scene, (first record, record count, offset)."""
+    p0 = scene_list[0].params
+    cell = float(p0.cellsize) / float(p0.simscale)
+    ext = np.array([[s.params.volmax[a] - s.params.volmin[a] for a in range(3)] for s in scene_list], np.float64)
+    pitch = np.ceil(ext.max(axis=0) / cell) * cell + gap_cells * cell
+    k = len(scene_list)
+    nx = int(np.ceil(k ** (1.0 / 3.0) - 1e-9))
+    nz = nx
+    disp_all, calc_all, layout = [], [], []
+    first = 0
+    n_fluid = 0
+    for i, s in enumerate(scene_list):
+        ix, iz, iy = i % nx, (i // nx) % nz, i // (nx * nz)
+        corner = np.array([ix, iy, iz], np.float64) * pitch
+        off = (corner - np.array([s.params.volmin[a] for a in range(3)], np.float64))
+        off = (np.round(off / cell) * cell).astype(np.float32)
+        d = s.disp.copy()
+        c = s.calc.copy()
+        d["pos"] += off
+        c["bornid"] += first
+        disp_all.append(d)
+        calc_all.append(c)
+        layout.append((first, len(d), off))
+        first += len(d)
+        n_fluid += s.n_fluid
+    disp = np.concatenate(disp_all)
+    calc = np.concatenate(calc_all)
+    p = p0.copy()
+    lo = np.min([np.array([s.params.volmin[a] for a in range(3)]) + o for s, (_, _, o) in zip(scene_list, layout)],
+                axis=0)
+    hi = np.max([np.array([s.params.volmax[a] for a in range(3)]) + o for s, (_, _, o) in zip(scene_list, layout)],
+                axis=0)
+    for a in range(3):
+        p.volmin[a] = lo[a]
+        p.volmax[a] = hi[a]
+    setup_grid(p)
+    p.num = len(disp)
+    p.maxNum = len(disp)
+    return Scene(params=p, disp=disp, calc=calc, n_fluid=n_fluid, n_boundary=len(disp) - n_fluid,
+                 name=f"tiled_{k}"), layout
