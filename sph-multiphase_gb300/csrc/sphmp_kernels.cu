@@ -4,12 +4,13 @@
 //  * the hash reproduces InitialSort (SPH_Solver/fluids/fluid_system_kern.cu:36-64)
 //    with the same float operations, so cell ids are bit-identical;
 //  * the sort reproduces thrust::sort_by_key's stable order (fluid_system_host.cu:164-166)
-//    by ranking every cell's members by their pre-sort slot;
+//    by ranking every cell's members by their pre-sort slot, and also builds the
+//    internal order of the particle state (cells as sorted, members grouped by
+//    h-subcell inside each cell);
 //  * neighbour sums follow the reference formulas (fluid_system_kern.cu:183-424,
-//    multiphase.cu:19-349) in FP32; density and volume-fraction sums are Kahan-
-//    compensated. Only the 8 (of 27) cells that can hold a particle within h are
-//    visited: with cells of 2h the search sphere spans at most two cells per
-//    axis, chosen by which half of its cell the particle sits in.
+//    multiphase.cu:19-349) in FP32 over the pairs closer than h, found by the
+//    bucket density kernel (one warp per h-subcell, the 27 h-subcells around it)
+//    and kept as index lists for the force, drift and volume-fraction passes;
 //  * the advance reproduces AdvanceParticles (fluid_system_kern.cu:426-534) with
 //    un-contracted float operations, so it is bit-identical given the same accel.
 #include <cuda_runtime.h>
@@ -466,12 +467,12 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // Density + EOS pressure (MfComputePressureCUDA)
 // ---------------------------------------------------------------------------
 
-// Density + EOS with the octant order: one thread per in-grid particle, taken in
-// octant order so the lanes of a warp share cell and octant. The search visits
-// the h-subcells within h of the particle (at most 4 per axis, normally 3),
-// limited to the reference's 3x3x3 cells; along x, the subcells of one cell are
+// Density + EOS of one in-grid particle by its own search over the internal
+// order (the bucket kernel's path for buckets with too many members): the
+// h-subcells within h of the particle (at most 4 per axis, normally 3), limited
+// to the reference's 3x3x3 cells; along x, the subcells of one cell are
 // adjacent octant buckets, so each (y, z) subcell row is at most two ranges.
-// Writes 1/rho and p like k_density, plus the neighbour list.
+// Writes 1/rho and p like k_density, plus the neighbour index list.
 __device__ __forceinline__ void density_octant_one(const DevParams& P, const DevBuffers& B,
                                                    const float4* __restrict__ pos4, uint32_t s, const float4 pi,
                                                    float rho0) {
@@ -899,7 +900,8 @@ __global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_const
 // Volume-fraction advance, correction, advection
 // ---------------------------------------------------------------------------
 
-// Alpha change of slot s with neighbours gathered from global memory.
+// Alpha change of particle s with neighbours gathered from global memory (the
+// separate alpha-advance pass of the reference call order).
 template <int NP>
 __device__ __forceinline__ void alpha_change_slot(const DevParams& P, const DevBuffers& B,
                                                   const float4* __restrict__ pos4, const float4* __restrict__ vev4,
@@ -995,8 +997,8 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
     aprev4[s] = ap;
 }
 
-// Fused alpha advance + correction + advance (slot order): reads the cur buffers,
-// writes every float4 field of every slot into the other buffer.
+// Fused alpha advance + correction + advance, one thread per particle: reads the
+// cur buffers, writes every float4 field of every particle into the other buffer.
 // Alpha change of in-grid particle s with its neighbours' data from the
 // neighbour records the force + drift pass of this step wrote (five 16-byte
 // loads per neighbour instead of seven separate gathers).
