@@ -997,8 +997,6 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
     aprev4[s] = ap;
 }
 
-// Fused alpha advance + correction + advance, one thread per particle: reads the
-// cur buffers, writes every float4 field of every particle into the other buffer.
 // Alpha change of in-grid particle s with its neighbours' data from the
 // neighbour records the force + drift pass of this step wrote (five 16-byte
 // loads per neighbour instead of seven separate gathers).
@@ -1040,6 +1038,8 @@ __device__ __forceinline__ void pass_c_one(const DevParams& P, const DevBuffers&
     S.out[APREV][s] = ap;
 }
 
+// Fused alpha advance + correction + advance, one thread per particle: reads the
+// cur buffers, writes every float4 field of every particle into the other buffer.
 template <int NP, bool MP>
 __global__ void __launch_bounds__(kThreads, 3) k_pass_c(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
