@@ -240,6 +240,24 @@ sphmp_status sphmp_add_wall(const sphmp_params* p, const float vmin[3], const fl
 sphmp_status sphmp_add_open_box(const sphmp_params* p, const float vmin[3], const float vmax[3],
                                 float thickness, sphmp_display_pack* disp, sphmp_calc_pack* calc,
                                 int32_t cap, int32_t* count);
+/* A disk emitter (the reference's ParticleEmitter, SPH_Solver/fluids/fluid_system.h:30-40). */
+typedef struct sphmp_emitter {
+    float position[3];
+    float dir[3];      /* unit emission direction */
+    float vel;         /* emission speed */
+    float radius;
+    float spacing;
+} sphmp_emitter;
+/* Append `layers` emitted disks (FluidSystem::EmitParticles / EmitImmediate /
+   InsertParticles, SPH_Solver/fluids/fluid_system.cpp:619-700) as fluid of `phase`:
+   lattice sites within `radius` of the centre in the plane normal to dir, with
+   a seeded in-plane jitter of +-jitter/2 spacings (the reference uses 1 and
+   rand()), layer k shifted by k spacings along +y, velocity dir * vel, colour
+   (frame/200, 0.5, 0.8, 0.5). Upload the new records with sphmp_emit_aos
+   (EmitUpdateCUDA). */
+sphmp_status sphmp_emit_disk(const sphmp_params* p, const sphmp_emitter* e, int32_t layers, int32_t phase,
+                             int32_t frame, float jitter, uint64_t seed, sphmp_display_pack* disp,
+                             sphmp_calc_pack* calc, int32_t cap, int32_t* count);
 /* Boundary lattice spacing (bmass/bRestdensity)^(1/3)/simscale (AddShape.cpp:265-271). */
 float sphmp_boundary_spacing(const sphmp_params* p);
 

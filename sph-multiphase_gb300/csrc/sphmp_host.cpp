@@ -209,4 +209,68 @@ sphmp_status sphmp_add_open_box(const sphmp_params* p, const float mn[3], const 
     return SPHMP_OK;
 }
 
+// FluidSystem::EmitParticles / ParticleEmitter::EmitImmediate / InsertParticles
+// (SPH_Solver/fluids/fluid_system.cpp:619-700): a disk of radius e->radius on a
+// lattice of e->spacing in the plane normal to e->dir, each site moved by a
+// uniform in-plane jitter of +-jitter/2 spacings (the reference draws +-1/2 from
+// rand(); here a seeded stream), rotated so the lattice's y axis becomes dir,
+// shifted to e->position; `layers` disks, layer k shifted by k spacings along
+// +y as the reference's two calls are. Records as InsertParticles: velocity and
+// veleval dir * vel, colour (frame/200, 0.5, 0.8, 0.5), the phase's rest
+// density, mass and viscosity.
+sphmp_status sphmp_emit_disk(const sphmp_params* p, const sphmp_emitter* e, int32_t layers, int32_t phase,
+                             int32_t frame, float jitter, uint64_t seed, sphmp_display_pack* disp,
+                             sphmp_calc_pack* calc, int32_t cap, int32_t* count) {
+    if (!p || !e || !disp || !calc || !count || layers < 0) return SPHMP_ERR_INVALID_ARG;
+    if (!(e->spacing > 0.0f) || !(e->radius >= 0.0f) || phase < 0 || phase >= SPHMP_MAX_PHASES)
+        return SPHMP_ERR_INVALID_ARG;
+    const float* dir = e->dir;
+    // rotation with columns (newx, dir, newz), identity when dir is (anti)parallel to y
+    float m[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
+    float nx[3] = {dir[1] * 0.f - dir[2] * 1.f, dir[2] * 0.f - dir[0] * 0.f, dir[0] * 1.f - dir[1] * 0.f};
+    const float nn = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
+    if (nn > 0.001f) {
+        const float inv = sqrtf(nn);
+        for (int a = 0; a < 3; a++) nx[a] = nx[a] / inv;
+        const float nz[3] = {nx[1] * dir[2] - nx[2] * dir[1], nx[2] * dir[0] - nx[0] * dir[2],
+                             nx[0] * dir[1] - nx[1] * dir[0]};
+        for (int a = 0; a < 3; a++) {
+            m[a][0] = nx[a];
+            m[a][1] = dir[a];
+            m[a][2] = nz[a];
+        }
+    }
+    const int res = (int)(e->radius / e->spacing);
+    uint64_t ctr = 0;
+    for (int layer = 0; layer < layers; layer++) {
+        const float centre[3] = {e->position[0], e->position[1] + (float)layer * e->spacing, e->position[2]};
+        for (int i = -res; i <= res; i++) {
+            for (int j = -res; j <= res; j++) {
+                const float jx = uniform01(seed, ctr++) * jitter * e->spacing - jitter * e->spacing * 0.5f;
+                const float jz = uniform01(seed, ctr++) * jitter * e->spacing - jitter * e->spacing * 0.5f;
+                const float t[3] = {(float)i * e->spacing + jx, 0.0f, (float)j * e->spacing + jz};
+                if (t[0] * t[0] + t[1] * t[1] + t[2] * t[2] > e->radius * e->radius) continue;
+                const int32_t n = *count;
+                if (n >= cap) return SPHMP_ERR_CAPACITY;
+                sphmp_display_pack* d = disp + n;
+                sphmp_calc_pack* c = calc + n;
+                init_record(d, c, n);
+                for (int a = 0; a < 3; a++)
+                    d->pos[a] = m[a][0] * t[0] + m[a][1] * t[1] + m[a][2] * t[2] + centre[a];
+                d->color[0] = (float)frame / 200.0f;
+                d->color[1] = 0.5f;
+                d->color[2] = 0.8f;
+                d->color[3] = 0.5f;
+                d->type = SPHMP_TYPE_FLUID;
+                for (int a = 0; a < 3; a++) c->vel[a] = c->veleval[a] = dir[a] * e->vel;
+                c->restdens = p->densArr[phase];
+                c->mass = p->massArr[phase];
+                c->visc = p->viscArr[phase];
+                *count = n + 1;
+            }
+        }
+    }
+    return SPHMP_OK;
+}
+
 }  // extern "C"

@@ -176,6 +176,7 @@ sphmp_status sphmp_add_bi2_shape(const sphmp_params* p, const float* pos, int32_
         sphmp_calc_pack& c = calc[k];
         memset(&d, 0, sizeof(d));
         memset(&c, 0, sizeof(c));
+        c.deformGrad[0] = c.deformGrad[4] = c.deformGrad[8] = 1.0f;  // as AddParticle
         const float x = pos[3 * i] / scale, z = pos[3 * i + 1] / scale, y = pos[3 * i + 2] / scale;
         d.pos[0] = x + offs[0];
         d.pos[1] = y + offs[1];

@@ -83,6 +83,8 @@ def load():
         "sphmp_save_state": (st, [ctx, C.c_char_p]),
         "sphmp_download_display_async": (st, [ctx, vp, C.c_int32]),
         "sphmp_download_wait": (st, [ctx]),
+        "sphmp_emit_disk": (st, [P(Params), P(abi.Emitter), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
+                                 vp, vp, C.c_int32, P(C.c_int32)]),
         "sphmp_load_state": (st, [ctx, C.c_char_p]),
     }
     for name, (res, args) in sig.items():
@@ -354,6 +356,20 @@ def read_bi2(path, header_only=False):
     return info.as_dict(), pos, vel, rhop
 
 
+def emit_disk(p, disp, calc, count, position, direction, speed, radius, spacing, layers=2, phase=0, frame=0,
+              jitter=1.0, seed=0):
+    """Append emitted disks (the reference's EmitParticles); returns the new count."""
+    e = abi.Emitter()
+    for a in range(3):
+        e.position[a] = position[a]
+        e.dir[a] = direction[a]
+    e.vel, e.radius, e.spacing = speed, radius, spacing
+    n = C.c_int32(count)
+    check(load().sphmp_emit_disk(C.byref(p), C.byref(e), int(layers), int(phase), int(frame), float(jitter),
+                                 int(seed), disp.ctypes.data, calc.ctypes.data, len(disp), C.byref(n)))
+    return n.value
+
+
 def add_bi2_shape(p, disp, calc, count, pos, scale=0.005, offs=(0, 0, 0), vel=(0, -1.5, 0), phase=2):
     """Append .bi2 shape particles as fluid (the reference's FluidSystem::AddShape); returns the new count."""
     pos = np.ascontiguousarray(pos, np.float32)
@@ -365,4 +381,4 @@ def add_bi2_shape(p, disp, calc, count, pos, scale=0.005, offs=(0, 0, 0), vel=(0
 
 __all__ = ["abi", "Params", "DisplayPack", "CalcPack", "Context", "SphmpError", "load", "check", "last_error",
            "params_default", "setup_constants", "setup_grid", "boundary_spacing", "record_arrays",
-           "add_fluid_volume", "add_wall", "add_open_box", "write_frame_text", "read_bi2", "add_bi2_shape"]
+           "add_fluid_volume", "add_wall", "add_open_box", "write_frame_text", "read_bi2", "add_bi2_shape", "emit_disk"]

@@ -147,7 +147,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_compute_force", "sphmp_advance", "sphmp_step", "sphmp_conservation",
     "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
     "sphmp_write_frame_text", "sphmp_read_bi2", "sphmp_add_bi2_shape", "sphmp_save_state", "sphmp_load_state",
-    "sphmp_download_display_async", "sphmp_download_wait",
+    "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
@@ -167,3 +167,9 @@ class Bi2Info(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Emitter(C.Structure):
+    """sphmp_emitter: a disk emitter (position, unit direction, speed, radius, lattice spacing)."""
+    _fields_ = [("position", C.c_float * 3), ("dir", C.c_float * 3), ("vel", C.c_float), ("radius", C.c_float),
+                ("spacing", C.c_float)]

@@ -160,3 +160,34 @@ def test_async_display_download_matches_sync():
         assert want[k].tobytes() == got[k].tobytes(), k
     a.close()
     b.close()
+
+
+def test_emit_disk_follows_emit_particles():
+    """EmitParticles (SPH_Solver/fluids/fluid_system.cpp:619-700): a disk normal to dir,
+    two layers along +y, velocity dir * vel."""
+    p = scenes.make_params(h=0.02, d=0.01, dt=1e-4, box_min=(0, 0, 0), box_max=(1, 1, 1), nphase=2,
+                           dens=(1000.0, 800.0), visc=(0.2, 0.3))
+    s, r = 0.01, 0.045
+    disp, calc = sphmp.record_arrays(500)
+    n = sphmp.emit_disk(p, disp, calc, 4, (0.5, 0.8, 0.5), (0, -1, 0), 1.0, r, s, layers=2, phase=1, frame=50,
+                        jitter=0.0)
+    res = int(np.float32(r) / np.float32(s))
+    sites = [(i, j) for i in range(-res, res + 1) for j in range(-res, res + 1)
+             if (np.float32(i * s)) ** 2 + (np.float32(j * s)) ** 2 <= np.float32(r) ** 2]
+    assert n == 4 + 2 * len(sites)
+    pos = disp["pos"][4:n]
+    assert np.allclose(pos[:len(sites), 1], 0.8) and np.allclose(pos[len(sites):, 1], 0.81)
+    assert np.allclose(np.sort(pos[:len(sites), 0] - 0.5), np.sort([i * s for i, _ in sites]), atol=1e-6)
+    assert np.allclose(calc["vel"][4:n], [0, -1, 0]) and np.allclose(calc["veleval"][4:n], [0, -1, 0])
+    assert np.allclose(disp["color"][4:n], [0.25, 0.5, 0.8, 0.5])
+    assert np.all(calc["restdens"][4:n] == np.float32(800.0)) and np.all(calc["visc"][4:n] == np.float32(0.3))
+    assert np.array_equal(calc["bornid"][4:n], np.arange(4, n))
+    # a sideways emitter lays its disk in the plane normal to dir
+    disp2, calc2 = sphmp.record_arrays(500)
+    m = sphmp.emit_disk(p, disp2, calc2, 0, (0.3, 0.4, 0.5), (1, 0, 0), 2.0, r, s, layers=1, jitter=1.0, seed=7)
+    assert m > 0 and np.all(disp2["pos"][:m, 0] == np.float32(0.3))
+    assert np.all(np.sum((disp2["pos"][:m] - np.float32([0.3, 0.4, 0.5])) ** 2, axis=1) <= r * r * 1.0001)
+    assert np.allclose(calc2["vel"][:m], [2, 0, 0])
+    with pytest.raises(sphmp.SphmpError) as e:
+        sphmp.emit_disk(p, disp2, calc2, 495, (0.3, 0.4, 0.5), (1, 0, 0), 2.0, r, s)
+    assert e.value.status == abi.ERR_CAPACITY
