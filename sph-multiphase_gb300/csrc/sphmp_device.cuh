@@ -91,6 +91,13 @@ __device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_
     }
 }
 
+// Rows of the column-major neighbour lists are streamed from DRAM (the lists
+// outgrow L2); the walk asks L2 for the row kListPrefetch entries ahead, so the
+// index load of a row rarely waits on DRAM.
+constexpr uint32_t kListPrefetch = 8;
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // Visit the neighbours of particle s from the index list of the density pass
 // when it is valid and did not overflow, otherwise by the cell search.
 template <class F>
@@ -100,8 +107,13 @@ __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffe
         const uint32_t cnt = B.nbr_cnt[s];
         if (cnt <= (uint32_t)kMaxNbr) {
             const uint32_t* __restrict__ col = B.nbr + s;
+            const size_t cap = (size_t)P.cap;
+            for (uint32_t k = 0; k < kListPrefetch && k < cnt; k++) prefetch_l2(col + (size_t)k * cap);
 #pragma unroll 2
-            for (uint32_t k = 0; k < cnt; k++) f(__ldg(col + (size_t)k * P.cap));
+            for (uint32_t k = 0; k < cnt; k++) {
+                if (k + kListPrefetch < cnt) prefetch_l2(col + (size_t)(k + kListPrefetch) * cap);
+                f(__ldg(col + (size_t)k * cap));
+            }
             return;
         }
     }
