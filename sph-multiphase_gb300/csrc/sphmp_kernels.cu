@@ -621,7 +621,7 @@ __device__ __forceinline__ uint32_t next_bucket(uint32_t* ctr, unsigned lane) {
 }
 
 template <bool SS1>
-__global__ void __launch_bounds__(kThreads, 3) k_density_bucket(const __grid_constant__ DevParams P,
+__global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_constant__ DevParams P,
                                                                 const __grid_constant__ DevBuffers B,
                                                                 const float4* __restrict__ pos4,
                                                                 const float4* __restrict__ alpha4) {
