@@ -1041,7 +1041,7 @@ __device__ __forceinline__ void pass_c_one(const DevParams& P, const DevBuffers&
 // Fused alpha advance + correction + advance, one thread per particle: reads the
 // cur buffers, writes every float4 field of every particle into the other buffer.
 template <int NP, bool MP>
-__global__ void __launch_bounds__(kThreads, 3) k_pass_c(const __grid_constant__ DevParams P,
+__global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
