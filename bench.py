@@ -170,8 +170,9 @@ def build_scene(seed):
     return scenes.blobs_3phase(seed=seed, eos=abi.EOS_LINEAR, eos_k=3.0)
 
 
-def cpu_sample(scene, steps, budget_s, threads=None):
-    """Time the CPU oracle on the bench scene; returns (particle-steps/s, steps done, seconds, threads)."""
+def cpu_sample(scene, steps, budget_s, threads=None, warmup=1):
+    """Time the CPU oracle on the bench scene after `warmup` untimed steps (their own budget of
+    budget_s); returns (particle-steps/s, steps done, seconds, threads, warm-up steps done)."""
     from oracle import oracle as O
     from sphmp import abi
     O.build()
@@ -185,7 +186,13 @@ def cpu_sample(scene, steps, budget_s, threads=None):
         s.alpha[:, k] = scene.calc["restdens"] == np.float32(p.densArr[k])
     s.alpha_pre[:] = s.alpha
     O.before_first_step(p, s)
-    O.step(p, s, abi.SCHEDULE_REFERENCE, 1)  # warm-up (page-in, thread pool)
+    warm = 0
+    tw = time.perf_counter()
+    while warm < max(1, warmup):  # page-in, thread pool
+        O.step(p, s, abi.SCHEDULE_REFERENCE, 1)
+        warm += 1
+        if time.perf_counter() - tw > budget_s:
+            break
     done = 0
     t0 = time.perf_counter()
     while done < steps:
@@ -194,7 +201,7 @@ def cpu_sample(scene, steps, budget_s, threads=None):
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return scene.n_fluid * done / dt, done, dt, nthr
+    return scene.n_fluid * done / dt, done, dt, nthr, warm
 
 
 def run_reference(args):
@@ -203,10 +210,11 @@ def run_reference(args):
         return 0
     scene = build_scene(args.seed)
     # warm-up steps are part of the sample's own warm-up; the timed part is bounded
-    value, done, dt, nthr = cpu_sample(scene, max(1, args.steps), budget_s=args.cpu_budget)
+    value, done, dt, nthr, warm = cpu_sample(scene, max(1, args.steps), budget_s=args.cpu_budget,
+                                             warmup=args.warmup)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-        "steps": done, "warmup": 1, "ms_per_step": 1000.0 * dt / max(done, 1), "higher_is_better": True,
+        "steps": done, "warmup": warm, "ms_per_step": 1000.0 * dt / max(done, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": scene.name, "fluid_particles": scene.n_fluid,
                    "boundary_particles": scene.n_boundary, "schedule": "reference call order",
@@ -345,7 +353,7 @@ def run_gpu(args):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        v, done, dt, nthr = cpu_sample(scene, args.cpu_steps, budget_s=args.cpu_budget)
+        v, done, dt, nthr, _ = cpu_sample(scene, args.cpu_steps, budget_s=args.cpu_budget)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthr, "kind": "port",
                                 "sample": f"{done} fused steps of the same scene on the CPU oracle "
                                           f"({dt:.1f} s, {nthr} threads)"}
