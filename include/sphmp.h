@@ -66,7 +66,13 @@ typedef enum sphmp_schedule {
        neighbour passes. The force reads the mixture rest density and viscosity
        from before this step's correction (the correction lands one step later
        in the force); everything else is identical to the reference order. */
-    SPHMP_SCHEDULE_FUSED = 1
+    SPHMP_SCHEDULE_FUSED = 1,
+    /* the legacy multiphase step as RunSimulateMultiCUDAFull writes it
+       (SPH_Solver/fluids/fluid_system.cpp:375-420): sort, density, drift, alpha
+       advance, correction, then the project-U force (ComputeForce_projectu,
+       SPH_Solver/fluids/multiphase.cu:488-616) in place of MfComputeForce, then
+       the advance; needs `multiphase` = 1. */
+    SPHMP_SCHEDULE_PROJECTU = 2
 } sphmp_schedule;
 
 /*
@@ -154,7 +160,9 @@ typedef struct sphmp_params {
     float mf_cont1;              /* simData.cont1 (diffusion term switch) */
     float mf_cont2;              /* simData.cont2 (pressure term switch) */
     float mf_pintstiff;          /* simData.pintstiff (pressure-correction stiffness) */
-    int32_t reserved[5];
+    float mf_omega;              /* simData.omega: boundary pressure factor of the project-U force */
+    float mf_visc_factor;        /* simData.visc_factor: boundary viscosity factor of the project-U force */
+    int32_t reserved[3];
 } sphmp_params;
 
 /* Byte-compatible copies of the reference records (SPH_Solver/common_header.h:112-137). */
@@ -209,7 +217,9 @@ typedef enum sphmp_field {
     SPHMP_F_MGNDX = 18,    /* uint32[n] rank inside its cell (GRID_UNDEF for out-of-grid slots) */
     SPHMP_F_MGRIDOFF = 19, /* int32[gridtotal] first slot of each occupied cell, 0 if empty */
     SPHMP_F_MGRIDCNT = 20, /* int32[gridtotal] particle count per cell */
-    SPHMP_F_COUNT = 21
+    SPHMP_F_VELXCOR = 21,  /* float[3n] mf_velxcor: XSPH velocity correction of the project-U force
+                              (0 for boundary and out-of-grid slots); download only */
+    SPHMP_F_COUNT = 22
 } sphmp_field;
 
 typedef struct sphmp_ctx sphmp_ctx;
@@ -383,6 +393,14 @@ sphmp_status sphmp_compute_correction(sphmp_ctx* ctx);
 /* MfComputeForceCUDA (fluid_system_host.cu:421-438), plus the reference
    SurfaceTension term (fluid_system_kern.cu:605-625) when enabled. */
 sphmp_status sphmp_compute_force(sphmp_ctx* ctx);
+/* ComputeForce_projectu (kernel SPH_Solver/fluids/multiphase.cu:488-616; its host
+   wrapper ComputeForceCUDA_ProjectU, fluid_system_host.cu:396-419, has the launch
+   commented out): pressure with p_i + p_j, viscosity on veleval, boundary terms
+   scaled by mf_omega / mf_visc_factor, the drift-velocity tensor term of every
+   phase, written to accel; the XSPH velocity correction to SPHMP_F_VELXCOR. Reads
+   the start-of-step fractions and this step's drift velocities. Adds the
+   SurfaceTension term when enabled. */
+sphmp_status sphmp_compute_force_projectu(sphmp_ctx* ctx);
 /* MfAdvanceCUDA (fluid_system_host.cu:385-394). */
 sphmp_status sphmp_advance(sphmp_ctx* ctx);
 

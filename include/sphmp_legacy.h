@@ -49,6 +49,9 @@ void MfComputeAlphaAdvanceCUDA(void);
 void MfComputeCorrectionCUDA(void);
 /* MfComputeForceCUDA (fluid_system_host.cu:421-438) */
 void MfComputeForceCUDA(void);
+/* ComputeForceCUDA_ProjectU (fluid_system_host.cu:396-419; decl fluid_system_host.cuh:77).
+   Runs the ComputeForce_projectu kernel, whose launch the reference comments out. */
+void ComputeForceCUDA_ProjectU(void);
 /* MfAdvanceCUDA (fluid_system_host.cu:385-394) */
 void MfAdvanceCUDA(void);
 /* ComputeBoundaryDensity (fluid_system_host.cu:510-513) */

@@ -76,7 +76,7 @@ def _state_struct(R):
         ("mass", P(R)), ("visc", P(R)), ("bornid", P(C.c_int32)), ("accel", P(R)),
         ("alpha", P(R)), ("alpha_pre", P(R)), ("drift", P(R)), ("aprev", P(R)), ("pmod", P(R)),
         ("mgcell", P(C.c_uint32)), ("midsort", P(C.c_uint32)), ("mgndx", P(C.c_uint32)),
-        ("mgridoff", P(C.c_int32)), ("mgridcnt", P(C.c_int32)),
+        ("mgridoff", P(C.c_int32)), ("mgridcnt", P(C.c_int32)), ("velxcor", P(R)),
     ]})
 
 
@@ -86,7 +86,7 @@ StateF64 = _state_struct(C.c_double)
 # per-particle real-valued fields and their trailing shapes
 REAL_FIELDS = {"pos": (3,), "vel": (3,), "veleval": (3,), "pressure": (), "dens": (), "restdens": (),
                "mass": (), "visc": (), "accel": (3,), "alpha": (3,), "alpha_pre": (3,), "drift": (3, 3),
-               "aprev": (3,), "pmod": ()}
+               "aprev": (3,), "pmod": (), "velxcor": (3,)}
 INT_FIELDS = {"type": np.int32, "bornid": np.int32, "mgcell": np.uint32, "midsort": np.uint32,
               "mgndx": np.uint32}
 GRID_FIELDS = ("mgridoff", "mgridcnt")
@@ -138,7 +138,7 @@ _REF = None
 _FUNCS = ["orc_get_particle_index", "orc_get_grid_list", "orc_rearrange_data",
           "orc_compute_boundary_volume", "orc_compute_pressure", "orc_compute_force",
           "orc_surface_tension", "orc_advance", "orc_compute_drift_vel", "orc_compute_alpha_advance",
-          "orc_compute_correction", "orc_before_first_step"]
+          "orc_compute_correction", "orc_compute_force_projectu", "orc_before_first_step"]
 
 
 def lib():
@@ -171,7 +171,7 @@ def ref_lib():
         for f in ["ref_get_particle_index", "ref_get_grid_list", "ref_rearrange_data",
                   "ref_compute_boundary_volume", "ref_compute_pressure", "ref_compute_force",
                   "ref_surface_tension", "ref_advance", "ref_compute_drift_vel",
-                  "ref_compute_alpha_advance", "ref_compute_correction"]:
+                  "ref_compute_alpha_advance", "ref_compute_correction", "ref_compute_force_projectu"]:
             getattr(L, f).argtypes = [C.POINTER(abi.Params), C.POINTER(StateF32)]
         L.ref_set_num_threads.argtypes = [C.c_int]
         _REF = L

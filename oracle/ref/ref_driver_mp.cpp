@@ -1,5 +1,5 @@
 /* ref_driver_mp.cpp — runs the reference's drift-flux kernels (SPH_Solver/fluids/
- * multiphase.cu:18-349, compiled unmodified as host C++ against the legacy layout in
+ * multiphase.cu:18-349) and its project-U force (:488-616), compiled unmodified as host C++ against the legacy layout in
  * shim_legacy/) on the CPU, as the pin for the oracle restatement. TEST
  * INFRASTRUCTURE ONLY; built into oracle/_ref/ by oracle/ref/build_ref.sh.
  *
@@ -22,6 +22,7 @@ legacy_FluidParams simData;
 __global__ void mfComputeDriftVel(bufList buf, int pnum);
 __global__ void mfComputeAlphaAdvance(bufList buf, int pnum);
 __global__ void mfComputeCorrection(bufList buf, int pnum);
+__global__ void ComputeForce_projectu(bufList buf, int pnum);
 
 void svdecomp3(float*, float*, float*, float) { abort(); }
 
@@ -52,10 +53,14 @@ static void set_sim(const sphmp_params* p) {
     simData.mf_dt = p->dt;
     simData.tohydro = FLT_MAX; /* the granular "becomes water" flip never fires */
     simData.pintstiff = p->mf_pintstiff;
+    simData.omega = p->mf_omega;
+    simData.visc_factor = p->mf_visc_factor;
 }
 
+/* `force_out`: mforce is the force output (the project-U force) rather than the
+   previous step's g - a that the drift velocity reads. */
 template <class K>
-static void run(K kernel, const sphmp_params* p, orc_state_f32* s) {
+static void run(K kernel, const sphmp_params* p, orc_state_f32* s, bool force_out = false) {
     set_sim(p);
     const int n = s->n;
     std::vector<int> isbound(n), mftype(n);
@@ -77,7 +82,8 @@ static void run(K kernel, const sphmp_params* p, orc_state_f32* s) {
     b.mf_alpha = s->alpha;
     b.mf_alpha_pre = s->alpha_pre;
     b.mf_vel_phrel = (cfloat3*)s->drift;
-    b.mforce = (cfloat3*)s->aprev;
+    b.mforce = (cfloat3*)(force_out ? s->accel : s->aprev);
+    b.mf_velxcor = (cfloat3*)s->velxcor;
     b.misbound = isbound.data();
     b.MFtype = mftype.data();
     b.mgrid = mgrid.data();
@@ -103,5 +109,9 @@ void ref_compute_drift_vel(const sphmp_params* p, orc_state_f32* s) { run(mfComp
 void ref_compute_alpha_advance(const sphmp_params* p, orc_state_f32* s) { run(mfComputeAlphaAdvance, p, s); }
 /* MfComputeCorrectionCUDA (fluid_system_host.cu:374-383) */
 void ref_compute_correction(const sphmp_params* p, orc_state_f32* s) { run(mfComputeCorrection, p, s); }
+/* ComputeForceCUDA_ProjectU (its launch is commented out at fluid_system_host.cu:399) */
+void ref_compute_force_projectu(const sphmp_params* p, orc_state_f32* s) {
+    run(ComputeForce_projectu, p, s, true);
+}
 
 } /* extern "C" */

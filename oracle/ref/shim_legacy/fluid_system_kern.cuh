@@ -54,8 +54,9 @@ struct legacy_bufList {
     int* mgridoff;
     float* mf_pressure_modify;
     uint* mclr;
-    /* granular / project-U arrays (never touched by the oracle) */
+    /* project-U output (XSPH correction) */
     cfloat3* mf_velxcor;
+    /* granular arrays (never touched by the oracle) */
     cfloat3* mf_alphagrad;
     float* last_mpress;
     float* MFpepsilon;

@@ -653,6 +653,106 @@ void FN(orc_compute_correction)(const sphmp_params* p, ST* s) {
     }
 }
 
+/* ComputeForce_projectu + contributeForce_projectu (multiphase.cu:488-616; the
+   launch in ComputeForceCUDA_ProjectU, fluid_system_host.cu:396-419, is commented
+   out). For every in-grid non-boundary slot, per neighbour cell, over 0 < r^2 < h^2:
+   fluid j: pressure -0.5 g (p_i + p_j) D_i x_ij, viscosity g (nu_i + nu_j) D_i
+   (ve_i - ve_j), drift tensor sum_k (g (u_jk.x_ij) a_jk u_jk + g (u_ik.x_ij) a_ik u_ik)
+   rho_k D_i, with g = kspikydiff (h - r)^2 / r m_j D_j and D the stored inverse
+   density; boundary j: pressure -g1 rho0_i m_j / rho0_j p_i D_i^2 x_ij omega and,
+   when (ve_i - ve_j).x_ij < 0, the artificial viscosity times visc_factor; every
+   j adds the XSPH term -(ve_i - ve_j) cx^3 m_j 2/(1/D_j + 1/D_i) kpoly6 0.5 to
+   velxcor (cx = (r2 - r^2) d2, a double literal 0.5). Per-cell force sums are
+   added to the total, velxcor accumulates directly; mforce is accel here.
+   Boundary and out-of-grid slots are left untouched, as in the reference. */
+void FN(orc_compute_force_projectu)(const sphmp_params* p, ST* s) {
+    const int np = p->nphase;
+    const R ss = (R)p->simscale;
+    const R h = (R)p->smoothradius;
+    const R d2 = ss * ss;
+    R r2h = h;
+    r2h = r2h * r2h;
+    const R r2 = r2h / d2;
+    const R spikykern = (R)p->kspikydiff;
+    const R poly6 = (R)p->kpoly6;
+    const R omega = (R)p->mf_omega, vfac = (R)p->mf_visc_factor;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == 1) continue;
+        uint32_t gc = s->mgcell[i];
+        if (gc == UNDEF) continue;
+        const R ipos[3] = {s->pos[3 * i + 0], s->pos[3 * i + 1], s->pos[3 * i + 2]};
+        const R ive[3] = {s->veleval[3 * i + 0], s->veleval[3 * i + 1], s->veleval[3 * i + 2]};
+        const R ipress = s->pressure[i];
+        const R idens = s->dens[i];
+        const R ivisc = s->visc[i];
+        R alpha_pre[3], ivmk[3][3];
+        for (int k = 0; k < np; k++) {
+            alpha_pre[k] = s->alpha_pre[3 * i + k];
+            for (int a = 0; a < 3; a++) ivmk[k][a] = s->drift[9 * i + 3 * k + a];
+        }
+        R force[3] = {0, 0, 0};
+        R* xc = &s->velxcor[3 * i];
+        xc[0] = xc[1] = xc[2] = 0;
+        for (int c = 0; c < p->neighbornum; c++) {
+            uint32_t cell = gc + (uint32_t)p->neighborid[c];
+            if (s->mgridcnt[cell] == 0) continue;
+            int cfirst = s->mgridoff[cell];
+            int clast = cfirst + s->mgridcnt[cell];
+            R cf[3] = {0, 0, 0};
+            for (int j = cfirst; j < clast; j++) {
+                R d[3] = {ipos[0] - s->pos[3 * j + 0], ipos[1] - s->pos[3 * j + 1], ipos[2] - s->pos[3 * j + 2]};
+                R dsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                d[0] *= ss; d[1] *= ss; d[2] *= ss;
+                if (!(dsq < r2 && dsq > 0)) continue;
+                const R cx = (r2 - dsq) * d2;
+                dsq = RSQRT(dsq * d2);
+                const R cc = (h - dsq);
+                const R cmterm1 = spikykern * cc * cc / dsq;
+                const R cmterm = spikykern * cc * cc / dsq * s->mass[j] * s->dens[j];
+                R vmr[3];
+                if (s->type[j] != 1) {
+                    const R pmterm = (R)-0.5f * cmterm * (ipress + s->pressure[j]) * idens;
+                    for (int a = 0; a < 3; a++) cf[a] += pmterm * d[a];
+                    for (int a = 0; a < 3; a++) vmr[a] = ive[a] - s->veleval[3 * j + a];
+                    const R vmterm = cmterm * (ivisc + s->visc[j]) * idens;
+                    for (int a = 0; a < 3; a++) cf[a] += vmterm * vmr[a];
+                } else {
+                    const R pmterm =
+                        -cmterm1 * s->restdens[i] * s->mass[j] / s->restdens[j] * (ipress)*s->dens[i] * s->dens[i];
+                    for (int a = 0; a < 3; a++) cf[a] += pmterm * d[a] * omega;
+                    for (int a = 0; a < 3; a++) vmr[a] = ive[a] - s->veleval[3 * j + a];
+                    R pi_ij = vmr[0] * d[0] + vmr[1] * d[1] + vmr[2] * d[2];
+                    if (pi_ij < 0) {
+                        pi_ij = (R)((double)pi_ij / ((double)(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) + (double)r2 * 0.01));
+                        pi_ij = pi_ij * (R)2 * h * (ivisc + s->visc[j]) * idens / (R)2;
+                        pi_ij = -cmterm1 * s->restdens[i] * s->mass[j] / s->restdens[j] * pi_ij;
+                        for (int a = 0; a < 3; a++) cf[a] += pi_ij * d[a] * vfac;
+                    }
+                }
+                if (s->type[j] != 1) {
+                    for (int k = 0; k < np; k++) {
+                        const R* uj = &s->drift[9 * j + 3 * k];
+                        const R tj = cmterm * (uj[0] * d[0] + uj[1] * d[1] + uj[2] * d[2]) * s->alpha_pre[3 * j + k];
+                        const R ti = cmterm * (ivmk[k][0] * d[0] + ivmk[k][1] * d[1] + ivmk[k][2] * d[2]) * alpha_pre[k];
+                        for (int a = 0; a < 3; a++)
+                            cf[a] += (tj * uj[a] + ti * ivmk[k][a]) * (R)p->densArr[k] * idens;
+                    }
+                }
+                const R ave = (R)2 / ((R)1 / s->dens[j] + (R)1 / idens);
+                const R xterm = (R)((double)(cx * cx * cx * s->mass[j] * ave * poly6) * 0.5);
+                for (int a = 0; a < 3; a++) xc[a] += -vmr[a] * xterm;
+            }
+            force[0] += cf[0];
+            force[1] += cf[1];
+            force[2] += cf[2];
+        }
+        s->accel[3 * i + 0] = force[0];
+        s->accel[3 * i + 1] = force[1];
+        s->accel[3 * i + 2] = force[2];
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* Step composition                                                            */
 /* ------------------------------------------------------------------------- */
@@ -668,7 +768,9 @@ int FN(orc_before_first_step)(const sphmp_params* p, ST* s) {
 
 /* One step: RunSimpleSPH (fluid_system.cpp:514-539) with the legacy multiphase calls
    inserted where RunSimulateMultiCUDAFull (:375-420) places them. The fused schedule
-   evaluates the force before the alpha advance and correction. */
+   evaluates the force before the alpha advance and correction; the project-U
+   schedule is RunSimulateMultiCUDAFull itself (ComputeForceCUDA_ProjectU in place
+   of MfComputeForceCUDA). */
 int FN(orc_step)(const sphmp_params* p, ST* s, int schedule, int nsteps) {
     for (int t = 0; t < nsteps; t++) {
         FN(orc_get_particle_index)(p, s);
@@ -689,7 +791,8 @@ int FN(orc_step)(const sphmp_params* p, ST* s, int schedule, int nsteps) {
                 FN(orc_compute_alpha_advance)(p, s);
                 FN(orc_compute_correction)(p, s);
             }
-            FN(orc_compute_force)(p, s);
+            if (schedule == SPHMP_SCHEDULE_PROJECTU) FN(orc_compute_force_projectu)(p, s);
+            else FN(orc_compute_force)(p, s);
             if (p->surface_tension) FN(orc_surface_tension)(p, s);
         }
         FN(orc_advance)(p, s);

@@ -50,7 +50,8 @@ extern "C" {
     uint32_t* midsort;  /* [n] */                                                 \
     uint32_t* mgndx;    /* [n] */                                                 \
     int32_t* mgridoff;  /* [gridtotal] */                                         \
-    int32_t* mgridcnt;  /* [gridtotal] */
+    int32_t* mgridcnt;  /* [gridtotal] */                                         \
+    R* velxcor;         /* [3n] mf_velxcor (project-U force) */
 
 typedef struct orc_state_f32 { ORC_STATE_FIELDS(float) } orc_state_f32;
 typedef struct orc_state_f64 { ORC_STATE_FIELDS(double) } orc_state_f64;
@@ -67,6 +68,7 @@ typedef struct orc_state_f64 { ORC_STATE_FIELDS(double) } orc_state_f64;
     void orc_compute_drift_vel##SFX(const sphmp_params* p, ST* s);                   \
     void orc_compute_alpha_advance##SFX(const sphmp_params* p, ST* s);               \
     void orc_compute_correction##SFX(const sphmp_params* p, ST* s);                  \
+    void orc_compute_force_projectu##SFX(const sphmp_params* p, ST* s);              \
     int orc_step##SFX(const sphmp_params* p, ST* s, int schedule, int nsteps);       \
     int orc_before_first_step##SFX(const sphmp_params* p, ST* s);
 

@@ -134,6 +134,8 @@ DevParams dev_params(const sphmp_ctx* c) {
     P.cont1 = p.mf_cont1;
     P.cont2 = p.mf_cont2;
     P.pintstiff = p.mf_pintstiff;
+    P.omega = p.mf_omega;
+    P.visc_factor = p.mf_visc_factor;
     P.eos = p.eos;
     P.eos_k = p.eos_stiffness;
     P.st_on = p.surface_tension;
@@ -154,7 +156,7 @@ void free_buffers(sphmp_ctx* c) {
     DevBuffers& B = c->B;
     for (int f = 0; f < kNumFloat4Fields; f++)
         for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
-    void* ptrs[] = {B.densp, B.accel4, B.drift4, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
+    void* ptrs[] = {B.densp, B.accel4, B.drift4, B.velxcor, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
                     B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
                     B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
                     B.act, B.act_n, c->stage};
@@ -177,6 +179,7 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.densp, N));
     CK(dalloc(&B.accel4, N));
     CK(dalloc(&B.drift4, 3 * N));
+    CK(dalloc(&B.velxcor, N));
     CK(dalloc(&B.pmod, N));
     CK(dalloc(&B.mgcell, N));
     CK(dalloc(&B.midsort, N));
@@ -220,6 +223,7 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(cudaMemset(B.densp, 0, sizeof(float2) * N));
     CK(cudaMemset(B.accel4, 0, sizeof(float4) * N));
     CK(cudaMemset(B.drift4, 0, sizeof(float4) * 3 * N));
+    CK(cudaMemset(B.velxcor, 0, sizeof(float4) * N));
     CK(cudaMemset(B.pmod, 0, sizeof(float) * N));
     CK(cudaMemset(B.mgcell, 0xFF, sizeof(uint32_t) * N));
     CK(cudaMemset(B.opos, 0, sizeof(uint32_t) * N));
@@ -356,8 +360,13 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
             launch_correction(dev_params(c), c->B, c->cur, c->cur[ALPHA] ^ 1, s);
             mark("correction");
         }
-        run_force_drift(c, true, false, s);
-        mark("force");
+        if (schedule == SPHMP_SCHEDULE_PROJECTU) {
+            launch_force_projectu(PL, c->B, c->cur, c->cur[ALPHA] ^ 1, s);
+            mark("force_projectu");
+        } else {
+            run_force_drift(c, true, false, s);
+            mark("force");
+        }
         if (PL.st_on) {
             launch_surface_tension(PL, c->B, c->cur, s);
             mark("surface_tension");
@@ -371,10 +380,19 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     return SPHMP_OK;
 }
 
+sphmp_status check_schedule(const sphmp_ctx* c, int schedule) {
+    if (schedule != SPHMP_SCHEDULE_REFERENCE && schedule != SPHMP_SCHEDULE_FUSED &&
+        schedule != SPHMP_SCHEDULE_PROJECTU)
+        return fail(SPHMP_ERR_INVALID_ARG, "unknown schedule %d", schedule);
+    if (schedule == SPHMP_SCHEDULE_PROJECTU && !c->prm.multiphase)
+        return fail(SPHMP_ERR_INVALID_ARG, "the project-U schedule is the multiphase step (set multiphase = 1)");
+    return SPHMP_OK;
+}
+
 int field_width(int field) {
     switch (field) {
         case SPHMP_F_POS: case SPHMP_F_VEL: case SPHMP_F_VELEVAL: case SPHMP_F_ACCEL:
-        case SPHMP_F_ALPHA: case SPHMP_F_ALPHA_PRE: case SPHMP_F_APREV: return 3;
+        case SPHMP_F_ALPHA: case SPHMP_F_ALPHA_PRE: case SPHMP_F_APREV: case SPHMP_F_VELXCOR: return 3;
         case SPHMP_F_DRIFT: return 9;
         default: return 1;
     }
@@ -630,7 +648,8 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
     if (sphmp_status st = need_ctx(c)) return st;
     if (!host) return fail(SPHMP_ERR_INVALID_ARG, "host pointer is NULL");
     if (field < 0 || field >= SPHMP_F_COUNT) return fail(SPHMP_ERR_INVALID_ARG, "unknown field %d", field);
-    if (field == SPHMP_F_DENS || field == SPHMP_F_TYPE || field == SPHMP_F_MASS || field == SPHMP_F_BORNID)
+    if (field == SPHMP_F_DENS || field == SPHMP_F_TYPE || field == SPHMP_F_MASS || field == SPHMP_F_BORNID ||
+        field == SPHMP_F_VELXCOR)
         return fail(SPHMP_ERR_INVALID_ARG, "field %d is download-only (upload it with sphmp_upload_aos)", field);
     size_t count = 0;
     if (void* arr = sort_array(c, field, &count)) {
@@ -775,6 +794,17 @@ sphmp_status sphmp_compute_force(sphmp_ctx* c) {
     return SPHMP_OK;
 }
 
+sphmp_status sphmp_compute_force_projectu(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    const DevParams P = dev_params(c);
+    const int pre = c->alpha_advanced ? c->cur[ALPHA] ^ 1 : c->cur[ALPHA];
+    launch_force_projectu(P, c->B, c->cur, pre, c->stream);
+    if (P.st_on) launch_surface_tension(P, c->B, c->cur, c->stream);
+    CHECK_LAUNCH("ComputeForce_projectu");
+    return SPHMP_OK;
+}
+
 sphmp_status sphmp_advance(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     launch_advance(dev_params(c), c->B, c->cur, c->stream);
@@ -787,8 +817,7 @@ sphmp_status sphmp_advance(sphmp_ctx* c) {
 sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t use_graph) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (nsteps < 0) return fail(SPHMP_ERR_INVALID_ARG, "nsteps < 0");
-    if (schedule != SPHMP_SCHEDULE_REFERENCE && schedule != SPHMP_SCHEDULE_FUSED)
-        return fail(SPHMP_ERR_INVALID_ARG, "unknown schedule %d", schedule);
+    if (sphmp_status st = check_schedule(c, schedule)) return st;
     if (nsteps == 0) return SPHMP_OK;
     // A fused step leaves every double buffer where it found it, so one captured
     // step replays for all later steps. The reference schedule flips buffers an
@@ -837,10 +866,7 @@ int32_t sphmp_step_profile(sphmp_ctx* c, int32_t schedule, float* ms, char* name
         fail(SPHMP_ERR_INVALID_ARG, "need an output array");
         return -SPHMP_ERR_INVALID_ARG;
     }
-    if (schedule != SPHMP_SCHEDULE_REFERENCE && schedule != SPHMP_SCHEDULE_FUSED) {
-        fail(SPHMP_ERR_INVALID_ARG, "unknown schedule %d", schedule);
-        return -SPHMP_ERR_INVALID_ARG;
-    }
+    if (sphmp_status st = check_schedule(c, schedule)) return -st;
     StageTimer T;
     if (!T.ok) {
         fail(SPHMP_ERR_CUDA, "cudaEventCreate failed");
@@ -953,6 +979,7 @@ void MfComputeDriftVelCUDA(void) { legacy_run("MfComputeDriftVelCUDA", sphmp_com
 void MfComputeAlphaAdvanceCUDA(void) { legacy_run("MfComputeAlphaAdvanceCUDA", sphmp_compute_alpha_advance); }
 void MfComputeCorrectionCUDA(void) { legacy_run("MfComputeCorrectionCUDA", sphmp_compute_correction); }
 void MfComputeForceCUDA(void) { legacy_run("MfComputeForceCUDA", sphmp_compute_force); }
+void ComputeForceCUDA_ProjectU(void) { legacy_run("MfComputeForceCUDA", sphmp_compute_force_projectu); }
 void MfAdvanceCUDA(void) { legacy_run("MfAdvanceCUDA", sphmp_advance); }
 void ComputeBoundaryDensity(void) { legacy_run("ComputeBoundaryDensity", sphmp_compute_boundary_density); }
 

@@ -7,6 +7,7 @@
 //   drift velocity     SPH_Solver/fluids/multiphase.cu:19-166
 //   alpha advance      SPH_Solver/fluids/multiphase.cu:169-272
 //   correction         SPH_Solver/fluids/multiphase.cu:275-349
+//   project-U force    SPH_Solver/fluids/multiphase.cu:488-616
 //   advance            SPH_Solver/fluids/fluid_system_kern.cu:426-534
 // in FP32, with Kahan-compensated density and volume-fraction sums.
 #pragma once
@@ -288,6 +289,91 @@ struct ForceDrift {
     }
 };
 
+
+// ---------------------------------------------------------------------------
+// Project-U force (ComputeForce_projectu)
+// ---------------------------------------------------------------------------
+
+// contributeForce_projectu (multiphase.cu:488-575) for one in-grid fluid
+// particle: fluid neighbours give pressure with p_i + p_j, viscosity on
+// veleval and the drift-velocity tensor of every phase; boundary neighbours
+// give pressure (rest-density ratio, times omega) and, when approaching, the
+// artificial viscosity (times visc_factor); every neighbour gives the XSPH
+// term -(ve_i - ve_j) (h^2 - r^2)^3 m_j (2 / (1/D_j + 1/D_i)) kpoly6 / 2, with
+// D the stored inverse density (the boundary volume for boundary particles).
+// `pair` takes the neighbour's pos4, (1/rho, p), veleval, viscosity, rest
+// density, raw mass, start-of-step fractions and drift velocities.
+template <int NP>
+struct ProjectU {
+    float4 pi, vei;
+    float idens, ipress, ivisc, rho0;
+    float ia[3];
+    float3 um[NP];
+    float fx, fy, fz;
+    float xx, xy, xz;
+
+    __device__ __forceinline__ void init(float4 pi_, float4 vei_, float2 dpi, float visc, float rho0_,
+                                         float4 apre, const float3* um_) {
+        pi = pi_;
+        vei = vei_;
+        idens = dpi.x;
+        ipress = dpi.y;
+        ivisc = visc;
+        rho0 = rho0_;
+        ia[0] = apre.x; ia[1] = apre.y; ia[2] = apre.z;
+#pragma unroll
+        for (int k = 0; k < NP; k++) um[k] = um_[k];
+        fx = fy = fz = 0.f;
+        xx = xy = xz = 0.f;
+    }
+
+    __device__ __forceinline__ void pair(const DevParams& P, const float4 pj, const float2 dpj, const float4 vej,
+                                         float viscj, float rho0j, float mj, const float4 aj, const float4* uj) {
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (!(dsq < P.r2 && dsq > 0.f)) return;
+        const float rinv = rsqrtf(dsq);
+        const float c = P.h - dsq * rinv;
+        const float g1 = P.kspikydiff * c * c * rinv;
+        const float vx = vei.x - vej.x, vy = vei.y - vej.y, vz = vei.z - vej.z;
+        float dj;  // the neighbour's stored inverse density (boundary: volume)
+        if (pj.w > 0.f) {
+            dj = dpj.x;
+            const float g = g1 * mj * dj;
+            const float pm = -0.5f * g * (ipress + dpj.y) * idens;
+            fx += dx * pm; fy += dy * pm; fz += dz * pm;
+            const float vm = g * (ivisc + viscj) * idens;
+            fx += vx * vm; fy += vy * vm; fz += vz * vm;
+            const float ja[3] = {aj.x, aj.y, aj.z};
+#pragma unroll
+            for (int k = 0; k < NP; k++) {
+                const float tj = g * (uj[k].x * dx + uj[k].y * dy + uj[k].z * dz) * ja[k];
+                const float ti = g * (um[k].x * dx + um[k].y * dy + um[k].z * dz) * ia[k];
+                const float f = P.dens_k[k] * idens;
+                fx += (tj * uj[k].x + ti * um[k].x) * f;
+                fy += (tj * uj[k].y + ti * um[k].y) * f;
+                fz += (tj * uj[k].z + ti * um[k].z) * f;
+            }
+        } else {
+            dj = -pj.w;
+            const float gb = g1 * rho0 * mj / rho0j;
+            const float pm = -gb * ipress * idens * idens * P.omega;
+            fx += dx * pm; fy += dy * pm; fz += dz * pm;
+            float pij = vx * dx + vy * dy + vz * dz;
+            if (pij < 0.f) {
+                // the reference adds r2 in unscaled units (simData.r2 / d2) to the scaled distance
+                pij = pij / (dsq + P.r2 / (P.ss * P.ss) * 0.01f);
+                pij = pij * 2.f * P.h * (ivisc + viscj) * idens / 2.f;
+                pij = -gb * pij * P.visc_factor;
+                fx += dx * pij; fy += dy * pij; fz += dz * pij;
+            }
+        }
+        const float cx = P.r2 - dsq;
+        const float ave = 2.f / (1.f / dj + 1.f / idens);
+        const float xt = cx * cx * cx * mj * ave * P.kpoly6 * 0.5f;
+        xx -= vx * xt; xy -= vy * xt; xz -= vz * xt;
+    }
+};
 
 // ---------------------------------------------------------------------------
 // Volume-fraction advance (MfComputeAlphaAdvanceCUDA)

@@ -69,6 +69,10 @@ sphmp_status sphmp_params_default(sphmp_params* p) {
     p->mf_cont1 = 1.0f;
     p->mf_cont2 = 1.0f;
     p->mf_pintstiff = 0.03f;
+    // simData.omega and simData.visc_factor of the project-U force are set by no
+    // remaining reference code; 1 leaves the boundary terms unscaled.
+    p->mf_omega = 1.0f;
+    p->mf_visc_factor = 1.0f;
     return SPHMP_OK;
 }
 

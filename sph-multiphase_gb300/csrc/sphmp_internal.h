@@ -20,7 +20,8 @@
 //            (bits of a uint32: the slot the particle was uploaded to)
 //
 // Per-step arrays (single buffer): densp (1/rho or V_b, pressure), accel4,
-// drift4 (phase-major: drift of phase k for slot i at [k * cap + i]), pmod.
+// drift4 (phase-major: drift of phase k for slot i at [k * cap + i]), pmod,
+// velxcor (XSPH correction of the project-U force).
 // Per-origin arrays (never moved): color, bornid, raw calc mass.
 #pragma once
 
@@ -74,6 +75,7 @@ struct DevParams {
     int multiphase;
     float dens_k[3], visc_k[3];
     float relax, sigma, cont, cont1, cont2, pintstiff;
+    float omega, visc_factor;  // boundary factors of the project-U force
     int eos;
     float eos_k;
     int st_on;
@@ -86,6 +88,7 @@ struct DevBuffers {
     float2* densp;
     float4* accel4;
     float4* drift4;   // [3 * cap]
+    float4* velxcor;  // [cap] XSPH velocity correction of the project-U force
     float* pmod;
     uint32_t* mgcell;   // sorted cell id per slot (unsorted key after the hash)
     uint32_t* midsort;  // pre-sort slot of each sorted slot
@@ -153,6 +156,8 @@ void launch_density_oct(const DevParams& P, const DevBuffers& B, const int* cur,
 void launch_force_drift(const DevParams& P, const DevBuffers& B, const int* cur, bool force, bool drift,
                         cudaStream_t s);
 void launch_surface_tension(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// project-U force: start-of-step fractions in alpha4[pre], rest densities in alpha4[cur[ALPHA]]
+void launch_force_projectu(const DevParams& P, const DevBuffers& B, const int* cur, int pre, cudaStream_t s);
 // alpha advance: reads alpha4[cur], writes alpha4[cur^1] (new fractions, same restdens)
 void launch_alpha_advance(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 // correction: fractions in alpha4[cur[ALPHA]], start-of-step fractions in alpha4[pre]; in place

@@ -896,6 +896,57 @@ __global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_const
     B.accel4[s] = a;
 }
 
+// Project-U force (ComputeForce_projectu, multiphase.cu:578-616), one thread
+// per particle: writes accel (the reference's mforce) and the XSPH correction of
+// every in-grid fluid particle. In-grid boundary particles get accel 0, as in the
+// force pass; boundary and out-of-grid particles get a zero correction (the
+// reference leaves both untouched for them).
+template <int NP>
+__global__ void __launch_bounds__(kThreads) k_force_projectu(const __grid_constant__ DevParams P,
+                                                             const __grid_constant__ DevBuffers B,
+                                                             const float4* __restrict__ pos4,
+                                                             const float4* __restrict__ vel4,
+                                                             const float4* __restrict__ vev4,
+                                                             const float4* __restrict__ alpha_cur,
+                                                             const float4* __restrict__ alpha_pre,
+                                                             const float4* __restrict__ aprev4) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= P.n) return;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 pi = pos4[s];
+    if (B.mgcell[s] == kUndef || pi.w < 0.f) {
+        if (B.mgcell[s] != kUndef) B.accel4[s] = zero;
+        B.velxcor[s] = zero;
+        return;
+    }
+    float3 um[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        const float4 u = B.drift4[(size_t)k * P.cap + s];
+        um[k] = make_float3(u.x, u.y, u.z);
+    }
+    ProjectU<NP> acc;
+    acc.init(pi, vev4[s], B.densp[s], vel4[s].w, alpha_cur[s].w, alpha_pre[s], um);
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        const float2 dpj = __ldg(&B.densp[j]);
+        const float4 vej = __ldg(&vev4[j]);
+        const float viscj = __ldg(&vel4[j].w);
+        const float4 aj = __ldg(&alpha_pre[j]);
+        float4 uj[NP];
+#pragma unroll
+        for (int k = 0; k < NP; k++) uj[k] = __ldg(&B.drift4[(size_t)k * P.cap + j]);
+        float mj = pj.w, rho0j = 1.f;
+        if (pj.w < 0.f) {  // boundary: raw mass (per origin) and rest density
+            mj = __ldg(&B.mass_raw[__float_as_uint(__ldg(&aprev4[j].w))]);
+            rho0j = __ldg(&alpha_cur[j].w);
+        }
+        acc.pair(P, pj, dpj, vej, viscj, rho0j, mj, aj, uj);
+    });
+    B.accel4[s] = make_float4(acc.fx, acc.fy, acc.fz, 0.f);
+    B.velxcor[s] = make_float4(acc.xx, acc.xy, acc.xz, 0.f);
+}
+
 // ---------------------------------------------------------------------------
 // Volume-fraction advance, correction, advection
 // ---------------------------------------------------------------------------
@@ -1222,6 +1273,7 @@ __global__ void __launch_bounds__(kThreads) k_pack_field(const __grid_constant__
             break;
         case SPHMP_F_APREV: { const float4 a = S.in[APREV][i]; f[3 * t] = a.x; f[3 * t + 1] = a.y; f[3 * t + 2] = a.z; } break;
         case SPHMP_F_PMOD: f[t] = B.pmod[i]; break;
+        case SPHMP_F_VELXCOR: { const float4 x = B.velxcor[i]; f[3 * t] = x.x; f[3 * t + 1] = x.y; f[3 * t + 2] = x.z; } break;
         case SPHMP_F_TYPE: q[t] = p.w < 0.f ? SPHMP_TYPE_BOUNDARY : SPHMP_TYPE_FLUID; break;
         case SPHMP_F_MASS: f[t] = B.mass_raw[o]; break;
         case SPHMP_F_BORNID: q[t] = B.bornid[o]; break;
@@ -1378,6 +1430,22 @@ void launch_force_drift(const DevParams& P, const DevBuffers& B, const int* cur,
 void launch_surface_tension(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
     if (P.n <= 0) return;
     k_surface_tension<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]]);
+}
+
+void launch_force_projectu(const DevParams& P, const DevBuffers& B, const int* cur, int pre, cudaStream_t s) {
+    if (P.n <= 0) return;
+    const float4* pos = B.f4[POS][cur[POS]];
+    const float4* vel = B.f4[VEL][cur[VEL]];
+    const float4* vev = B.f4[VEV][cur[VEV]];
+    const float4* ac = B.f4[ALPHA][cur[ALPHA]];
+    const float4* ap = B.f4[ALPHA][pre];
+    const float4* apv = B.f4[APREV][cur[APREV]];
+    const int g = blocks_for(P.n);
+    switch (P.nphase) {
+        case 1: k_force_projectu<1><<<g, kThreads, 0, s>>>(P, B, pos, vel, vev, ac, ap, apv); break;
+        case 2: k_force_projectu<2><<<g, kThreads, 0, s>>>(P, B, pos, vel, vev, ac, ap, apv); break;
+        default: k_force_projectu<3><<<g, kThreads, 0, s>>>(P, B, pos, vel, vev, ac, ap, apv); break;
+    }
 }
 
 void launch_alpha_advance(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {

@@ -68,6 +68,7 @@ def load():
         "sphmp_compute_alpha_advance": (st, [ctx]),
         "sphmp_compute_correction": (st, [ctx]),
         "sphmp_compute_force": (st, [ctx]),
+        "sphmp_compute_force_projectu": (st, [ctx]),
         "sphmp_advance": (st, [ctx]),
         "sphmp_step": (st, [ctx, C.c_int32, C.c_int32, C.c_int32]),
         "sphmp_conservation": (st, [ctx, P(C.c_double), C.c_int32]),
@@ -165,7 +166,7 @@ def add_open_box(p, disp, calc, count, vmin, vmax, thickness):
 
 FIELD_SHAPES = {
     abi.F_POS: (3,), abi.F_VEL: (3,), abi.F_VELEVAL: (3,), abi.F_ACCEL: (3,), abi.F_ALPHA: (3,),
-    abi.F_ALPHA_PRE: (3,), abi.F_APREV: (3,), abi.F_DRIFT: (3, 3),
+    abi.F_ALPHA_PRE: (3,), abi.F_APREV: (3,), abi.F_DRIFT: (3, 3), abi.F_VELXCOR: (3,),
 }
 FIELD_DTYPES = {abi.F_TYPE: np.int32, abi.F_BORNID: np.int32, abi.F_MGCELL: np.uint32, abi.F_MIDSORT: np.uint32,
                 abi.F_MGNDX: np.uint32, abi.F_MGRIDOFF: np.int32, abi.F_MGRIDCNT: np.int32}
@@ -282,6 +283,9 @@ class Context:
 
     def compute_force(self):
         check(self._lib.sphmp_compute_force(self._ptr))
+
+    def compute_force_projectu(self):
+        check(self._lib.sphmp_compute_force_projectu(self._ptr))
 
     def advance(self):
         check(self._lib.sphmp_advance(self._ptr))

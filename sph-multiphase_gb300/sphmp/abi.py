@@ -31,12 +31,14 @@ EOS_TAIT = 0
 EOS_LINEAR = 1
 SCHEDULE_REFERENCE = 0
 SCHEDULE_FUSED = 1
+SCHEDULE_PROJECTU = 2
 
 # sphmp_field
 F_POS, F_VEL, F_VELEVAL, F_PRESSURE, F_DENS, F_RESTDENS, F_VISC, F_ACCEL = range(8)
 F_ALPHA, F_ALPHA_PRE, F_DRIFT, F_APREV, F_PMOD, F_TYPE, F_MASS, F_BORNID = range(8, 16)
 F_MGCELL, F_MIDSORT, F_MGNDX, F_MGRIDOFF, F_MGRIDCNT = range(16, 21)
-F_COUNT = 21
+F_VELXCOR = 21
+F_COUNT = 22
 
 _f3 = C.c_float * 3
 
@@ -68,7 +70,8 @@ class Params(C.Structure):
         ("nphase", C.c_int32), ("multiphase", C.c_int32), ("surface_tension", C.c_int32),
         ("eos", C.c_int32), ("eos_stiffness", C.c_float), ("mf_relax", C.c_float),
         ("mf_diffusion", C.c_float), ("mf_cont", C.c_float), ("mf_cont1", C.c_float),
-        ("mf_cont2", C.c_float), ("mf_pintstiff", C.c_float), ("reserved", C.c_int32 * 5),
+        ("mf_cont2", C.c_float), ("mf_pintstiff", C.c_float), ("mf_omega", C.c_float),
+        ("mf_visc_factor", C.c_float), ("reserved", C.c_int32 * 3),
     ]
 
     def copy(self):
@@ -144,14 +147,15 @@ EXPORTED_SYMBOLS = [
     "sphmp_upload_field", "sphmp_download_field", "sphmp_get_particle_index", "sphmp_get_grid_list",
     "sphmp_rearrange_data", "sphmp_compute_boundary_density", "sphmp_compute_pressure",
     "sphmp_compute_drift_vel", "sphmp_compute_alpha_advance", "sphmp_compute_correction",
-    "sphmp_compute_force", "sphmp_advance", "sphmp_step", "sphmp_conservation",
+    "sphmp_compute_force", "sphmp_compute_force_projectu", "sphmp_advance", "sphmp_step", "sphmp_conservation",
     "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
     "sphmp_write_frame_text", "sphmp_read_bi2", "sphmp_add_bi2_shape", "sphmp_save_state", "sphmp_load_state",
     "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
-    "MfComputeAlphaAdvanceCUDA", "MfComputeCorrectionCUDA", "MfComputeForceCUDA", "MfAdvanceCUDA",
+    "MfComputeAlphaAdvanceCUDA", "MfComputeCorrectionCUDA", "MfComputeForceCUDA", "ComputeForceCUDA_ProjectU",
+    "MfAdvanceCUDA",
     "ComputeBoundaryDensity", "computeNumBlocks", "sphmp_legacy_context", "TransferToCUDA",
     "TransferFromCUDA", "EmitUpdateCUDA",
 ]

@@ -23,7 +23,7 @@ sys.path[:0] = [REPO, os.path.join(REPO, "sph-multiphase_gb300"), os.path.join(R
 from oracle import oracle as O  # noqa: E402
 from sphmp import abi, scenes  # noqa: E402
 
-from golden_stages import STAGES, prepare_multiphase, state_arrays  # noqa: E402
+from golden_stages import SIDE_STAGES, STAGES, prepare_multiphase, state_arrays  # noqa: E402
 
 
 def fixtures():
@@ -53,6 +53,13 @@ def fixtures():
     sc.params.surfaceTensionK = 1.0
     sc.params.surfaceTensionFluidC = 0.05
     out.append(("surface_tension", sc))
+    # liquid phases only (no gas next to liquid), so that the project-U force, which
+    # squares drift velocities, stays finite; boundary factors other than 1
+    sc = scenes.small_block(seed=26, n=(6, 6, 5), nphase=3, eos=abi.EOS_TAIT, velocity_scale=0.4,
+                            dens=(1000.0, 800.0, 900.0), phase_frac=0.5, box=(0.08, 0.08, 0.08))
+    sc.params.mf_omega = 0.7
+    sc.params.mf_visc_factor = 1.3
+    out.append(("projectu_liquids", sc))
     return out
 
 
@@ -70,6 +77,12 @@ def main():
             if stage == "multiphase_inputs":
                 prepare_multiphase(p, s, seed=zlib.crc32(name.encode()) % 1000)
             elif stage == "surface_tension" and not p.surface_tension:
+                continue
+            elif stage in SIDE_STAGES:
+                t = s.copy()
+                O.call_ref("ref_" + stage, p, t)
+                for f in fields:
+                    rec[f"{stage}__{f}"] = getattr(t, f).copy()
                 continue
             else:
                 O.call_ref("ref_" + stage, p, s)

@@ -4,6 +4,9 @@ import numpy as np
 from oracle import oracle as O
 
 # (stage, fields saved after it). "multiphase_inputs" seeds alpha / alpha_pre / aprev.
+# Stages in SIDE_STAGES run on a copy of the state: the chain goes on from the
+# state before them (the project-U force replaces MfComputeForce's accel only in
+# its own schedule, so the advance keeps reading the MfComputeForce result).
 STAGES = [
     ("get_particle_index", ["mgcell", "midsort"]),
     ("get_grid_list", ["mgcell", "midsort", "mgridoff", "mgridcnt", "mgndx"]),
@@ -16,8 +19,10 @@ STAGES = [
     ("compute_drift_vel", ["drift"]),
     ("compute_alpha_advance", ["alpha"]),
     ("compute_correction", ["alpha", "restdens", "visc", "pmod"]),
+    ("compute_force_projectu", ["accel", "velxcor"]),
     ("advance", ["pos", "vel", "veleval"]),
 ]
+SIDE_STAGES = {"compute_force_projectu"}
 
 
 def state_arrays(s):

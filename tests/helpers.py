@@ -83,7 +83,8 @@ def download_state(ctx, n=None):
                       ("alpha", F.F_ALPHA), ("alpha_pre", F.F_ALPHA_PRE), ("drift", F.F_DRIFT),
                       ("aprev", F.F_APREV), ("pmod", F.F_PMOD), ("type", F.F_TYPE), ("mass", F.F_MASS),
                       ("bornid", F.F_BORNID), ("mgcell", F.F_MGCELL), ("midsort", F.F_MIDSORT),
-                      ("mgndx", F.F_MGNDX), ("mgridoff", F.F_MGRIDOFF), ("mgridcnt", F.F_MGRIDCNT)]:
+                      ("mgndx", F.F_MGNDX), ("mgridoff", F.F_MGRIDOFF), ("mgridcnt", F.F_MGRIDCNT),
+                      ("velxcor", F.F_VELXCOR)]:
         out[name] = ctx.download_field(fid, None if name in ("mgridoff", "mgridcnt") else n)
     return out
 

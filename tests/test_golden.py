@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from golden_stages import STAGES, load_fixture
+from golden_stages import SIDE_STAGES, STAGES, load_fixture
 from helpers import bits_equal, field_err
 from oracle import oracle as O
 
@@ -16,7 +16,9 @@ UNDEF = 0xFFFFFFFF
 
 
 def test_fixtures_present():
-    assert len(GOLDEN) >= 5
+    assert len(GOLDEN) >= 6
+    # the fixture whose project-U force is finite everywhere (liquid phases only)
+    assert any(os.path.basename(g) == "projectu_liquids.npz" for g in GOLDEN)
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(g)[:-4] for g in GOLDEN])
@@ -29,9 +31,10 @@ def test_oracle_matches_reference_golden(path, built):
             continue
         if stage == "surface_tension" and not p.surface_tension:
             continue
-        O.call("orc_" + stage, p, s)
+        t = s.copy() if stage in SIDE_STAGES else s
+        O.call("orc_" + stage, p, t)
         for f in fields:
-            assert bits_equal(getattr(s, f), z[f"{stage}__{f}"]), f"{stage}: {f}"
+            assert bits_equal(getattr(t, f), z[f"{stage}__{f}"]), f"{stage}: {f}"
 
 
 @pytest.mark.gpu
@@ -57,19 +60,23 @@ def test_gpu_matches_reference_golden(path, built):
          "mgndx": abi.F_MGNDX, "pos": abi.F_POS, "type": abi.F_TYPE, "vel": abi.F_VEL, "veleval": abi.F_VELEVAL,
          "restdens": abi.F_RESTDENS, "mass": abi.F_MASS, "visc": abi.F_VISC, "bornid": abi.F_BORNID,
          "dens": abi.F_DENS, "pressure": abi.F_PRESSURE, "accel": abi.F_ACCEL, "drift": abi.F_DRIFT,
-         "alpha": abi.F_ALPHA, "alpha_pre": abi.F_ALPHA_PRE, "aprev": abi.F_APREV, "pmod": abi.F_PMOD}
+         "alpha": abi.F_ALPHA, "alpha_pre": abi.F_ALPHA_PRE, "aprev": abi.F_APREV, "pmod": abi.F_PMOD,
+         "velxcor": abi.F_VELXCOR}
     run = {"get_particle_index": ctx.get_particle_index, "get_grid_list": ctx.get_grid_list,
            "rearrange_data": ctx.rearrange_data, "compute_boundary_volume": ctx.compute_boundary_density,
            "compute_pressure": ctx.compute_pressure, "compute_force": ctx.compute_force,
            "surface_tension": lambda: None, "compute_drift_vel": ctx.compute_drift_vel,
            "compute_alpha_advance": ctx.compute_alpha_advance, "compute_correction": ctx.compute_correction,
-           "advance": ctx.advance}
+           "compute_force_projectu": ctx.compute_force_projectu, "advance": ctx.advance}
     exact = {"get_particle_index", "get_grid_list", "rearrange_data", "advance"}
     # (the density after the boundary-volume pass runs the slot-order kernel: the volumes
     # changed after the octant order was built)
     # floating-point stages start from the reference's own inputs, so each is measured alone
     feed = {"compute_alpha_advance": [("compute_drift_vel", "drift", abi.F_DRIFT)],
             "compute_correction": [("compute_alpha_advance", "alpha", abi.F_ALPHA)],
+            "compute_force_projectu": [("compute_drift_vel", "drift", abi.F_DRIFT),
+                                       ("compute_correction", "restdens", abi.F_RESTDENS),
+                                       ("compute_correction", "visc", abi.F_VISC)],
             "advance": [("surface_tension" if p.surface_tension else "compute_force", "accel", abi.F_ACCEL)]}
     mgcell = None
     for stage, fields in STAGES:
@@ -87,6 +94,10 @@ def test_gpu_matches_reference_golden(path, built):
             mgcell = z[f"{stage}__mgcell"]
         m = np.ones(s.n, bool) if mgcell is None else mgcell != UNDEF
         fl = m & (z["rearrange_data__type"] == 0)
+        if stage in SIDE_STAGES and not all(np.isfinite(z[f"{stage}__{f}"][fl]).all() for f in fields):
+            # gas next to liquid under the Tait EOS: the squared drift velocities
+            # overflow float in the reference too; only fixtures where it stays finite count
+            continue
         for f in fields:
             ref = z[f"{stage}__{f}"]
             got = ctx.download_field(F[f])

@@ -32,6 +32,12 @@ def _scene(kind):
                                   simscale=0.5, h=0.01, d=0.01)
     if kind == "dam":
         return scenes.dam_break_2phase(seed=15, n_side=16, box=0.32)
+    if kind == "liquids3":  # no gas next to liquid: the project-U force stays finite
+        sc = scenes.small_block(seed=16, n=(14, 12, 13), nphase=3, eos=abi.EOS_TAIT, velocity_scale=0.4,
+                                dens=(1000.0, 800.0, 900.0), phase_frac=0.5)
+        sc.params.mf_omega = 0.7
+        sc.params.mf_visc_factor = 1.3
+        return sc
     raise KeyError(kind)
 
 
@@ -144,6 +150,74 @@ def test_multiphase_passes(kind):
     assert field_err(g["restdens"][f], s.restdens[f]) < RTOL
     assert field_err(g["visc"][f], s.visc[f]) < RTOL
     assert field_err(g["pmod"][f], s.pmod[f], floor=1e-6) < 1e-4
+    ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["liquids3", "dam"])
+def test_projectu_pass(kind):
+    """ComputeForce_projectu on identical inputs: drift velocities, start-of-step
+    fractions and the corrected rest densities and viscosities of the oracle."""
+    sc, s, ctx = _sorted_pair(kind)
+    p = sc.params
+    rng = np.random.default_rng(4)
+    a = s.alpha.copy()
+    k = p.nphase
+    a[:, :k] = a[:, :k] * 0.7 + 0.3 * rng.random((s.n, k)).astype(np.float32)
+    a[:, :k] /= a[:, :k].sum(1, keepdims=True)
+    s.alpha[:] = a
+    s.alpha_pre[:] = a
+    s.aprev[:] = rng.normal(0, 3.0, (s.n, 3)).astype(np.float32)
+    fl = s.type == 0  # moving fluid (the dam starts at rest), so the XSPH term is not zero
+    s.veleval[fl] = rng.normal(0, 0.3, (int(fl.sum()), 3)).astype(np.float32)
+    upload_state_fields(ctx, s, ["alpha_pre", "aprev", "veleval"])
+    O.call("orc_compute_pressure", p, s)
+    ctx.compute_pressure()
+    for st in ("orc_compute_drift_vel", "orc_compute_alpha_advance", "orc_compute_correction"):
+        O.call(st, p, s)
+    ctx.compute_drift_vel()
+    ctx.compute_alpha_advance()
+    ctx.compute_correction()
+    upload_state_fields(ctx, s, ["drift", "restdens", "visc"])
+    O.call("orc_compute_force_projectu", p, s)
+    ctx.compute_force_projectu()
+    g = download_state(ctx)
+    f = in_grid_fluid(s)
+    assert np.isfinite(s.accel[f]).all() and np.abs(s.velxcor[f]).max() > 0
+    assert field_err(g["accel"][f], s.accel[f]) < RTOL
+    assert field_err(g["velxcor"][f], s.velxcor[f]) < RTOL
+    # boundary and out-of-grid slots carry no correction
+    assert not g["velxcor"][~f].any()
+    ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["liquids3", "dam"])
+def test_projectu_step(kind):
+    """One step of the legacy multiphase schedule with the project-U force."""
+    sc, s, ctx = _sorted_pair(kind)
+    p = sc.params
+    O.step(p, s, abi.SCHEDULE_PROJECTU, 1)
+    ctx.step(1, abi.SCHEDULE_PROJECTU, use_graph=True)
+    ctx.sync()
+    g = download_state(ctx)
+    for key in ("mgcell", "midsort", "mgridoff", "mgridcnt"):
+        assert bits_equal(g[key], getattr(s, key)), key
+    f = in_grid_fluid(s)
+    assert field_err(g["accel"][f], s.accel[f]) < RTOL
+    assert field_err(g["velxcor"][f], s.velxcor[f]) < RTOL
+    for key in ("pos", "vel", "veleval"):
+        assert field_err(g[key][f], getattr(s, key)[f]) < RTOL, key
+    kk = p.nphase
+    assert field_err(g["alpha"][f][:, :kk], s.alpha[f][:, :kk], floor=1.0) < RTOL
+    ctx.close()
+
+
+def test_projectu_schedule_needs_multiphase():
+    sc = _scene("liquids3")
+    sc.params.multiphase = 0
+    ctx = device_ctx(sc)
+    with pytest.raises(sphmp.SphmpError) as e:
+        ctx.step(1, abi.SCHEDULE_PROJECTU)
+    assert e.value.status == abi.ERR_INVALID_ARG
     ctx.close()
 
 

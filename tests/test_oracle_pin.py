@@ -18,6 +18,8 @@ SCENES = {
     "simscale": lambda: scenes.small_block(seed=34, n=(10, 10, 10), nphase=2, eos=abi.EOS_TAIT, simscale=0.25,
                                            h=0.005, d=0.01, velocity_scale=0.2),
     "dam": lambda: scenes.dam_break_2phase(seed=35, n_side=14, box=0.3, eos=abi.EOS_TAIT),
+    "liquids3": lambda: scenes.small_block(seed=36, n=(10, 9, 11), nphase=3, eos=abi.EOS_TAIT, velocity_scale=0.4,
+                                           dens=(1000.0, 800.0, 900.0), phase_frac=0.5),
 }
 
 
@@ -29,6 +31,9 @@ def test_every_stage_bit_identical(name, built):
         p.surface_tension = 1
         p.surfaceTensionK = 1.0
         p.surfaceTensionFluidC = 0.05
+    if name == "liquids3":  # the project-U boundary factors away from 1
+        p.mf_omega = 0.7
+        p.mf_visc_factor = 1.3
     a = O.state_from_aos(sc.disp, sc.calc, p.gridtotal)
     a.bornid[:] = np.arange(a.n)
     b = a.copy()
