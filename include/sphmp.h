@@ -268,6 +268,20 @@ typedef struct sphmp_emitter {
 sphmp_status sphmp_emit_disk(const sphmp_params* p, const sphmp_emitter* e, int32_t layers, int32_t phase,
                              int32_t frame, float jitter, uint64_t seed, sphmp_display_pack* disp,
                              sphmp_calc_pack* calc, int32_t cap, int32_t* count);
+/* Device-side emission (FluidSystem::EmitParticles, SPH_Solver/fluids/fluid_system.cpp:619-641,
+   where the host inserts particles every emitInterval frames and re-uploads them with
+   EmitUpdateCUDA): from now on every sphmp_step starts by appending, when its frame
+   (steps since this call, from 0) is a multiple of `interval`, the particles that
+   sphmp_emit_disk(params, e, layers, phase, frame, jitter, seed + frame, ...) would
+   produce, bit for bit, after the active slots, and the particle count grows on the
+   device, inside the captured step graph (no host round trip, no re-capture). The
+   kernels then run over the capacity and bound themselves by the device count;
+   sphmp_num_particles, the transfers and sphmp_sync read the count back. At capacity
+   the remaining sites are dropped, as the reference's AddParticle does, and
+   sphmp_device_errors reports SPHMP_ERR_CAPACITY. `e` NULL or interval <= 0 turns
+   the emitter off. */
+sphmp_status sphmp_set_device_emitter(sphmp_ctx* ctx, const sphmp_emitter* e, int32_t layers, int32_t phase,
+                                      int32_t interval, float jitter, uint64_t seed);
 /* Boundary lattice spacing (bmass/bRestdensity)^(1/3)/simscale (AddShape.cpp:265-271). */
 float sphmp_boundary_spacing(const sphmp_params* p);
 

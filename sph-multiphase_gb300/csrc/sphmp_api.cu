@@ -11,6 +11,7 @@
 #include <string>
 
 #include "sphmp.h"
+#include "sphmp_emit.h"
 #include "sphmp_internal.h"
 #include "sphmp_legacy.h"
 
@@ -44,6 +45,12 @@ struct sphmp_ctx {
     cudaEvent_t dl_packed[2] = {nullptr, nullptr};
     cudaEvent_t dl_done[2] = {nullptr, nullptr};
     int dl_next = 0;
+    // device-side emission: while `emit_on`, every step starts with the emitter
+    // kernel, the kernels run over the capacity and bound themselves by the device
+    // count, and `n` is re-read from the device after steps (`n_stale`)
+    bool emit_on = false;
+    bool n_stale = false;
+    DevEmitter emitter{};
 };
 
 namespace {
@@ -101,7 +108,7 @@ DevParams dev_params(const sphmp_ctx* c) {
     const sphmp_params& p = c->prm;
     DevParams P;
     memset(&P, 0, sizeof(P));
-    P.n = c->n;
+    P.n = c->emit_on ? c->cap : c->n;
     P.cap = c->cap;
     P.G = p.gridtotal;
     P.rx = p.gridres[0];
@@ -159,7 +166,7 @@ void free_buffers(sphmp_ctx* c) {
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.velxcor, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
                     B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
                     B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
-                    B.act, B.act_n, c->stage};
+                    B.act, B.act_n, B.nact, B.frame, c->stage};
     for (void* q : ptrs) cudaFree(q);
     memset(&c->B, 0, sizeof(c->B));
     c->stage = nullptr;
@@ -214,6 +221,10 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.act, G));
     CK(dalloc(&B.act_n, 1));
     CK(cudaMemset(B.act_n, 0, sizeof(uint32_t)));
+    CK(dalloc(&B.nact, 1));
+    CK(dalloc(&B.frame, 1));
+    CK(cudaMemset(B.nact, 0, sizeof(int32_t)));
+    CK(cudaMemset(B.frame, 0, sizeof(int32_t)));
     c->stage_bytes = N * (sizeof(sphmp_display_pack) + sizeof(sphmp_calc_pack));
     if (c->stage_bytes < G * sizeof(int32_t)) c->stage_bytes = G * sizeof(int32_t);
     CK(cudaMalloc(&c->stage, c->stage_bytes));
@@ -255,6 +266,7 @@ sphmp_status take_device_errors(sphmp_ctx* c, uint32_t* bits_out) {
                                    : s == SPHMP_ERR_NOT_FINITE     ? "non-finite particle position"
                                    : s == SPHMP_ERR_BAD_MASS       ? "fluid particle with mass <= 0 or not finite"
                                    : s == SPHMP_ERR_CELL_OVERFLOW  ? "a grid cell holds more than 8192 particles"
+                                   : s == SPHMP_ERR_CAPACITY       ? "device-side emission reached the capacity"
                                                                    : "device error";
                 return fail((sphmp_status)s, "device reported: %s", what);
             }
@@ -269,6 +281,18 @@ inline sphmp_status need_ctx(const sphmp_ctx* c) {
 
 inline sphmp_status need_grid(const sphmp_ctx* c) {
     if (!c->grid_valid) return fail(SPHMP_ERR_STATE, "no cell list for the current slot order (run the sort first)");
+    return SPHMP_OK;
+}
+
+// The particle count after steps that may have emitted on the device.
+sphmp_status refresh_n(sphmp_ctx* c) {
+    if (!c->n_stale) return SPHMP_OK;
+    int32_t n = 0;
+    CK(cudaMemcpyAsync(&n, c->B.nact, sizeof(n), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->n = n;
+    c->prm.num = n;
+    c->n_stale = false;
     return SPHMP_OK;
 }
 
@@ -321,6 +345,11 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
         if (T) T->mark(s, nm);
     };
     if (T) T->start(s);
+    if (c->emit_on) {
+        launch_emit(P, c->B, c->cur, c->emitter, s);
+        c->n_stale = true;
+        mark("emit");
+    }
     launch_hash(P, c->B, c->cur, s);
     mark("hash");
     launch_cell_starts(P, c->B, s);
@@ -441,6 +470,7 @@ sphmp_status sphmp_create(const sphmp_params* p, sphmp_ctx** out) {
         delete c;
         return st;
     }
+    launch_set_count(c->B, c->n, c->stream);
     *out = c;
     return SPHMP_OK;
 }
@@ -469,6 +499,7 @@ sphmp_status sphmp_set_params(sphmp_ctx* c, const sphmp_params* p) {
     if (sphmp_status st = validate_params(p)) return st;
     if (p->maxNum > c->cap) return fail(SPHMP_ERR_CAPACITY, "maxNum %d exceeds the allocated capacity %d", p->maxNum, c->cap);
     if (p->gridtotal > c->gcap) return fail(SPHMP_ERR_CAPACITY, "gridtotal %d exceeds the allocated %d cells", p->gridtotal, c->gcap);
+    if (sphmp_status st = refresh_n(c)) return st;
     const bool grid_changed = memcmp(p->gridres, c->prm.gridres, sizeof(p->gridres)) != 0 ||
                               memcmp(p->gridmin, c->prm.gridmin, sizeof(p->gridmin)) != 0 ||
                               memcmp(p->gridIdfac, c->prm.gridIdfac, sizeof(p->gridIdfac)) != 0;
@@ -483,6 +514,7 @@ sphmp_status sphmp_set_params(sphmp_ctx* c, const sphmp_params* p) {
 sphmp_status sphmp_get_params(const sphmp_ctx* c, sphmp_params* p) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (!p) return fail(SPHMP_ERR_INVALID_ARG, "params is NULL");
+    if (sphmp_status st = refresh_n(const_cast<sphmp_ctx*>(c))) return st;
     *p = c->prm;
     p->num = c->n;
     return SPHMP_OK;
@@ -499,11 +531,16 @@ sphmp_status sphmp_set_stream(sphmp_ctx* c, void* stream) {
 sphmp_status sphmp_sync(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     CK(cudaStreamSynchronize(c->stream));
+    if (sphmp_status st = refresh_n(c)) return st;
     if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
     return take_device_errors(c, nullptr);
 }
 
-int32_t sphmp_num_particles(const sphmp_ctx* c) { return c ? c->n : 0; }
+int32_t sphmp_num_particles(const sphmp_ctx* c) {
+    if (!c) return 0;
+    if (refresh_n(const_cast<sphmp_ctx*>(c))) return -1;
+    return c->n;
+}
 
 sphmp_status sphmp_device_errors(sphmp_ctx* c, uint32_t* bits) {
     if (sphmp_status st = need_ctx(c)) return st;
@@ -531,6 +568,8 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     }
     c->n = end;
     c->prm.num = end;
+    c->n_stale = false;
+    launch_set_count(c->B, end, c->stream);
     const DevParams P = dev_params(c);
     launch_unpack_aos(P, c->B, c->cur, d_disp, d_calc, start, end, c->stream);
     CHECK_LAUNCH("unpack records");
@@ -553,6 +592,7 @@ sphmp_status sphmp_upload_aos(sphmp_ctx* c, const sphmp_display_pack* disp, cons
 sphmp_status sphmp_emit_aos(sphmp_ctx* c, const sphmp_display_pack* disp, const sphmp_calc_pack* calc,
                             int32_t start, int32_t end) {
     if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = refresh_n(c)) return st;
     if (start != c->n) return fail(SPHMP_ERR_INVALID_ARG, "emission must append at slot %d (got start %d)", c->n, start);
     return upload_records(c, disp, calc, start, end);
 }
@@ -560,6 +600,7 @@ sphmp_status sphmp_emit_aos(sphmp_ctx* c, const sphmp_display_pack* disp, const 
 sphmp_status sphmp_download_aos(sphmp_ctx* c, sphmp_display_pack* disp, sphmp_calc_pack* calc, int32_t n) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (!disp) return fail(SPHMP_ERR_INVALID_ARG, "display pointer is NULL");
+    if (sphmp_status st = refresh_n(c)) return st;
     if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
     auto* d_disp = reinterpret_cast<sphmp_display_pack*>(c->stage);
     auto* d_calc = calc ? reinterpret_cast<sphmp_calc_pack*>(reinterpret_cast<char*>(c->stage) +
@@ -580,6 +621,7 @@ sphmp_status sphmp_download_aos(sphmp_ctx* c, sphmp_display_pack* disp, sphmp_ca
 sphmp_status sphmp_download_display_async(sphmp_ctx* c, sphmp_display_pack* disp, int32_t n) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (!disp) return fail(SPHMP_ERR_INVALID_ARG, "display pointer is NULL");
+    if (sphmp_status st = refresh_n(c)) return st;
     if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
     if (!c->copy_stream) {  // first use: the copy stream, two staging buffers and their events
         CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
@@ -626,6 +668,7 @@ sphmp_status sphmp_download_field(sphmp_ctx* c, int32_t field, void* host, int32
     if (sphmp_status st = need_ctx(c)) return st;
     if (!host) return fail(SPHMP_ERR_INVALID_ARG, "host pointer is NULL");
     if (field < 0 || field >= SPHMP_F_COUNT) return fail(SPHMP_ERR_INVALID_ARG, "unknown field %d", field);
+    if (sphmp_status st = refresh_n(c)) return st;
     size_t count = 0;
     if (void* arr = sort_array(c, field, &count)) {
         if (n < 0 || (size_t)n > count) return fail(SPHMP_ERR_CAPACITY, "n %d exceeds %zu entries", n, count);
@@ -648,6 +691,7 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
     if (sphmp_status st = need_ctx(c)) return st;
     if (!host) return fail(SPHMP_ERR_INVALID_ARG, "host pointer is NULL");
     if (field < 0 || field >= SPHMP_F_COUNT) return fail(SPHMP_ERR_INVALID_ARG, "unknown field %d", field);
+    if (sphmp_status st = refresh_n(c)) return st;
     if (field == SPHMP_F_DENS || field == SPHMP_F_TYPE || field == SPHMP_F_MASS || field == SPHMP_F_BORNID ||
         field == SPHMP_F_VELXCOR)
         return fail(SPHMP_ERR_INVALID_ARG, "field %d is download-only (upload it with sphmp_upload_aos)", field);
@@ -805,6 +849,50 @@ sphmp_status sphmp_compute_force_projectu(sphmp_ctx* c) {
     return SPHMP_OK;
 }
 
+sphmp_status sphmp_set_device_emitter(sphmp_ctx* c, const sphmp_emitter* e, int32_t layers, int32_t phase,
+                                      int32_t interval, float jitter, uint64_t seed) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = refresh_n(c)) return st;
+    if (!e || interval <= 0) {
+        c->emit_on = false;
+        drop_graph(c);
+        return SPHMP_OK;
+    }
+    if (!(e->spacing > 0.0f) || !(e->radius >= 0.0f) || layers < 0 || phase < 0 || phase >= SPHMP_MAX_PHASES)
+        return fail(SPHMP_ERR_INVALID_ARG, "emitter needs spacing > 0, radius >= 0, layers >= 0, phase in [0, 3)");
+    const sphmp_params& p = c->prm;
+    if (!(p.massArr[phase] > 0.0f) || !isfinite(p.massArr[phase]))
+        return fail(SPHMP_ERR_BAD_MASS, "phase %d has mass %g (massArr)", phase, (double)p.massArr[phase]);
+    DevEmitter E{};
+    emit_rotation(e->dir, E.rot);
+    for (int a = 0; a < 3; a++) {
+        E.pos[a] = e->position[a];
+        E.dir[a] = e->dir[a];
+    }
+    E.vel = e->vel;
+    E.radius = e->radius;
+    E.spacing = e->spacing;
+    E.jitter = jitter;
+    E.mass = p.massArr[phase];
+    E.restdens = p.densArr[phase];
+    E.visc = p.viscArr[phase];
+    E.seed = seed;
+    E.res = (int)(e->radius / e->spacing);
+    E.layers = layers;
+    E.interval = interval;
+    E.onehot = 0;  // sphmp_upload_aos's rule: the first phase with this rest density
+    for (int k = 0; k < p.nphase; k++)
+        if (p.densArr[k] == E.restdens) {
+            E.onehot = k;
+            break;
+        }
+    c->emitter = E;
+    c->emit_on = true;
+    drop_graph(c);
+    CK(cudaMemsetAsync(c->B.frame, 0, sizeof(int32_t), c->stream));
+    return SPHMP_OK;
+}
+
 sphmp_status sphmp_advance(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
     launch_advance(dev_params(c), c->B, c->cur, c->stream);
@@ -823,7 +911,9 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
     // step replays for all later steps. The reference schedule flips buffers an
     // odd number of times per step and runs eagerly.
     if (use_graph && schedule == SPHMP_SCHEDULE_FUSED) {
-        if (!c->graph || c->graph_n != c->n || c->graph_schedule != schedule) {
+        // with a device emitter the graph runs over the capacity and serves any count
+        const int key = c->emit_on ? -2 : c->n;
+        if (!c->graph || c->graph_n != key || c->graph_schedule != schedule) {
             drop_graph(c);
             cudaStream_t cap = c->stream;
             CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
@@ -847,10 +937,11 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
                 c->graph = nullptr;
                 return cuda_fail(e, "cudaGraphInstantiate");
             }
-            c->graph_n = c->n;
+            c->graph_n = key;
             c->graph_schedule = schedule;
         }
         for (int t = 0; t < nsteps; t++) CK(cudaGraphLaunch(c->graph, c->stream));
+        if (c->emit_on) c->n_stale = true;
         c->alpha_advanced = false;
         c->grid_valid = true;
         return SPHMP_OK;

@@ -8,21 +8,11 @@
 #include <string.h>
 
 #include "sphmp.h"
+#include "sphmp_emit.h"
 
 namespace {
 
-// splitmix64: seeded, platform-independent stream for the lattice jitter.
-inline uint64_t splitmix64(uint64_t x) {
-    x += 0x9E3779B97F4A7C15ull;
-    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-    return x ^ (x >> 31);
-}
-
-// uniform float in [0, 1) from counter `i` of stream `seed` (24 random bits)
-inline float uniform01(uint64_t seed, uint64_t i) {
-    return (float)(splitmix64(seed * 0x100000001B3ull + i) >> 40) * (1.0f / 16777216.0f);
-}
+using sphmp::uniform01;
 
 // AddParticle (SPH_Solver/fluids/fluid_system.cpp:702-717): a fresh record.
 void init_record(sphmp_display_pack* d, sphmp_calc_pack* c, int32_t n) {
@@ -229,21 +219,8 @@ sphmp_status sphmp_emit_disk(const sphmp_params* p, const sphmp_emitter* e, int3
     if (!(e->spacing > 0.0f) || !(e->radius >= 0.0f) || phase < 0 || phase >= SPHMP_MAX_PHASES)
         return SPHMP_ERR_INVALID_ARG;
     const float* dir = e->dir;
-    // rotation with columns (newx, dir, newz), identity when dir is (anti)parallel to y
-    float m[3][3] = {{1.f, 0.f, 0.f}, {0.f, 1.f, 0.f}, {0.f, 0.f, 1.f}};
-    float nx[3] = {dir[1] * 0.f - dir[2] * 1.f, dir[2] * 0.f - dir[0] * 0.f, dir[0] * 1.f - dir[1] * 0.f};
-    const float nn = nx[0] * nx[0] + nx[1] * nx[1] + nx[2] * nx[2];
-    if (nn > 0.001f) {
-        const float inv = sqrtf(nn);
-        for (int a = 0; a < 3; a++) nx[a] = nx[a] / inv;
-        const float nz[3] = {nx[1] * dir[2] - nx[2] * dir[1], nx[2] * dir[0] - nx[0] * dir[2],
-                             nx[0] * dir[1] - nx[1] * dir[0]};
-        for (int a = 0; a < 3; a++) {
-            m[a][0] = nx[a];
-            m[a][1] = dir[a];
-            m[a][2] = nz[a];
-        }
-    }
+    float m[3][3];
+    sphmp::emit_rotation(dir, m);
     const int res = (int)(e->radius / e->spacing);
     uint64_t ctr = 0;
     for (int layer = 0; layer < layers; layer++) {

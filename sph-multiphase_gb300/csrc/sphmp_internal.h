@@ -53,10 +53,12 @@ constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
 constexpr uint32_t kErrType = 1u << SPHMP_ERR_UNSUPPORTED_TYPE;
 constexpr uint32_t kErrNotFinite = 1u << SPHMP_ERR_NOT_FINITE;
 constexpr uint32_t kErrBadMass = 1u << SPHMP_ERR_BAD_MASS;
+constexpr uint32_t kErrCapacity = 1u << SPHMP_ERR_CAPACITY;
 
 // Scalars every kernel needs, passed by value.
 struct DevParams {
-    int n;           // active slots
+    int n;           // launch size: the active slots, or the capacity while a device emitter runs
+                     // (kernels bound themselves by the device counter, active_n)
     int cap;         // capacity (stride of phase-major arrays)
     int G;           // grid cells
     int rx, ry, rz;  // grid resolution
@@ -123,7 +125,29 @@ struct DevBuffers {
     uint32_t* oct_start;// [8 * G] first internal index of bucket (cell, octant)
     uint32_t* act;      // [G] cells with members (any order)
     uint32_t* act_n;    // [1] number of entries in act
+    int32_t* nact;      // [1] active slots (device-side emission grows it inside a step)
+    int32_t* frame;     // [1] steps since the device emitter was set
+    uint32_t* esum;     // [1] scratch of the emission kernel
 };
+
+// Device-side disk emitter (the reference's EmitParticles, run before the sort
+// of every step whose frame is a multiple of `interval`).
+struct DevEmitter {
+    float rot[3][3];   // columns (newx, dir, newz) of EmitImmediate's rotation
+    float pos[3];
+    float dir[3];
+    float vel, radius, spacing, jitter;
+    float mass, restdens, visc;  // of the emitted phase (massArr, densArr, viscArr)
+    unsigned long long seed;
+    int res;           // sites per half axis: int(radius / spacing)
+    int layers, interval;
+    int onehot;        // volume-fraction phase: the first whose rest density is `restdens`
+};
+
+#ifdef __CUDACC__
+// The active slot count every kernel bounds itself by.
+__device__ __forceinline__ int active_n(const DevBuffers& B) { return *B.nact; }
+#endif
 
 enum Field4 { POS = 0, VEL = 1, VEV = 2, ALPHA = 3, APREV = 4 };
 
@@ -167,6 +191,10 @@ void launch_advance(const DevParams& P, const DevBuffers& B, const int* cur, cud
 // fused alpha + correction + advance: reads cur, writes cur^1 for all five float4 fields
 void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// set the device counter of active slots
+void launch_set_count(const DevBuffers& B, int n, cudaStream_t s);
+// device-side emission into the current buffers (one block)
+void launch_emit(const DevParams& P, const DevBuffers& B, const int* cur, const DevEmitter& E, cudaStream_t s);
 
 // transfers (staging buffers hold reference records)
 void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,

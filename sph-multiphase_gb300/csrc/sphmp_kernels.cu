@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include "sphmp_device.cuh"
+#include "sphmp_emit.h"
 #include "sphmp_internal.h"
 
 namespace sphmp {
@@ -39,7 +40,7 @@ __global__ void __launch_bounds__(kHashBlock) k_hash(const __grid_constant__ Dev
                                                      const float4* __restrict__ pos4) {
     __shared__ uint32_t wcount[kHashBlock / 32];
     const int i = blockIdx.x * kHashBlock + threadIdx.x;
-    const bool valid = i < P.n;
+    const bool valid = i < active_n(B);
     uint32_t key = kUndef;
     if (valid) {
         const float4 p = pos4[B.opos[i]];
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_top(const __grid_constant__
     }
     if (threadIdx.x == 0) {
         B.cstart[P.G] = nin;
-        B.cstart[P.G + 1] = (uint32_t)P.n;
+        B.cstart[P.G + 1] = (uint32_t)active_n(B);
         B.big[0] = 0u;
         *B.act_n = 0u;
     }
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(const __grid_constant
 __global__ void __launch_bounds__(kThreads) k_scatter(const __grid_constant__ DevParams P,
                                                       const __grid_constant__ DevBuffers B) {
     const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= P.n) return;
+    if (i >= active_n(B)) return;
     const uint32_t key = B.key[i];
     const uint32_t r = B.arank[i];
     if (key != kUndef) {
@@ -399,9 +400,9 @@ __global__ void __launch_bounds__(kThreads) k_rearrange(const __grid_constant__ 
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
     const int o = blockIdx.x * kThreads + threadIdx.x;
-    if (o >= P.n) return;
+    if (o >= active_n(B)) return;
     uint32_t src = B.osrc[o];
-    if (src >= (uint32_t)P.n) src = o;  // only after a cell-overflow error (flagged by the scan)
+    if (src >= (uint32_t)active_n(B)) src = o;  // only after a cell-overflow error (flagged by the scan)
 #pragma unroll
     for (int f = 0; f < kNumFloat4Fields; f++) S.out[f][o] = S.in[f][src];
 }
@@ -409,18 +410,18 @@ __global__ void __launch_bounds__(kThreads) k_rearrange(const __grid_constant__ 
 __global__ void __launch_bounds__(kThreads) k_update_opos(const __grid_constant__ DevParams P,
                                                           const __grid_constant__ DevBuffers B) {
     const int o = blockIdx.x * kThreads + threadIdx.x;
-    if (o >= P.n) return;
+    if (o >= active_n(B)) return;
     const uint32_t slot = B.oidx[o];
-    if (slot < (uint32_t)P.n) B.opos[slot] = (uint32_t)o;
+    if (slot < (uint32_t)active_n(B)) B.opos[slot] = (uint32_t)o;
 }
 
 // New internal order = the sorted slot order (midsort given, no octant order).
 __global__ void __launch_bounds__(kThreads) k_slot_order(const __grid_constant__ DevParams P,
                                                          const __grid_constant__ DevBuffers B) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     const uint32_t m = B.midsort[s];
-    B.osrc[s] = m < (uint32_t)P.n ? B.opos[m] : (uint32_t)s;
+    B.osrc[s] = m < (uint32_t)active_n(B) ? B.opos[m] : (uint32_t)s;
     B.oidx[s] = (uint32_t)s;
 }
 
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume(const __grid_const
                                                               const __grid_constant__ DevBuffers B,
                                                               const float4* __restrict__ pos4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    if (s >= active_n(B) || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
     if (!(pi.w < 0.f)) return;
     Kahan sum;
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
                                                                     const __grid_constant__ DevBuffers B,
                                                                     float4* __restrict__ pos4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    if (s >= active_n(B) || B.mgcell[s] == kUndef) return;
     float4 p = pos4[s];
     if (!(p.w < 0.f)) return;
     p.w = -B.vtmp[s];
@@ -785,7 +786,7 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
                                                       const float4* __restrict__ pos4,
                                                       const float4* __restrict__ alpha4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    if (s >= active_n(B) || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
     if (pi.w < 0.f) {  // boundary: carries its volume, no pressure, needs no list
         B.densp[s] = make_float2(-pi.w, 0.f);
@@ -851,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_consta
                                                              const float4* __restrict__ aprev4,
                                                              const float4* __restrict__ vev4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n || B.mgcell[s] == kUndef) return;
+    if (s >= active_n(B) || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
     if (pi.w < 0.f) {
         if (FORCE) B.accel4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -871,7 +872,7 @@ __global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_const
                                                               const __grid_constant__ DevBuffers B,
                                                               const float4* __restrict__ pos4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     const uint32_t gc = B.mgcell[s];
     if (gc == kUndef) return;
     const float4 pi = pos4[s];
@@ -911,7 +912,7 @@ __global__ void __launch_bounds__(kThreads) k_force_projectu(const __grid_consta
                                                              const float4* __restrict__ alpha_pre,
                                                              const float4* __restrict__ aprev4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 pi = pos4[s];
     if (B.mgcell[s] == kUndef || pi.w < 0.f) {
@@ -989,7 +990,7 @@ __global__ void __launch_bounds__(kThreads) k_alpha_advance(const __grid_constan
                                                             const float4* __restrict__ alpha_in,
                                                             float4* __restrict__ alpha_out) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     const float4 ai = alpha_in[s];
     const float4 pi = pos4[s];
     if (B.mgcell[s] == kUndef || pi.w < 0.f) {
@@ -1009,7 +1010,7 @@ __global__ void __launch_bounds__(kThreads) k_correction(const __grid_constant__
                                                          float4* __restrict__ vel4,
                                                          const float4* __restrict__ pos4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     if (B.mgcell[s] == kUndef || pos4[s].w < 0.f) return;
     const float4 ac = alpha_cur[s];
     const float4 ap = alpha_pre[s];
@@ -1029,7 +1030,7 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
                                                       const __grid_constant__ DevBuffers B, float4* pos4,
                                                       float4* vel4, float4* vev4, float4* aprev4) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     float4 p = pos4[s];
     if (p.w < 0.f) return;
     float4 v = vel4[s];
@@ -1096,7 +1097,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ 
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
     const int s = blockIdx.x * kThreads + threadIdx.x;
-    if (s >= P.n) return;
+    if (s >= active_n(B)) return;
     pass_c_one<NP, MP>(P, B, S, s);
 }
 
@@ -1116,7 +1117,8 @@ __global__ void __launch_bounds__(kThreads) k_conservation(const __grid_constant
                                                            const float4* __restrict__ alpha4) {
     __shared__ double sh[6][kThreads / 32];
     double acc[6] = {0, 0, 0, 0, 0, 0};  // mass, volume, vol_k (3), max |sum alpha - 1|
-    for (int s = blockIdx.x * kThreads + threadIdx.x; s < P.n; s += gridDim.x * kThreads) {
+    const int n = active_n(B);
+    for (int s = blockIdx.x * kThreads + threadIdx.x; s < n; s += gridDim.x * kThreads) {
         if (B.mgcell[s] == kUndef) continue;
         const float4 p = pos4[s];
         if (p.w < 0.f) continue;
@@ -1153,6 +1155,102 @@ __global__ void __launch_bounds__(kThreads) k_conservation(const __grid_constant
         double m = 0.0;
         for (int w = 0; w < kThreads / 32; w++) m = fmax(m, sh[5][w]);
         atomicMax(reinterpret_cast<unsigned long long*>(&B.red[5]), (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Active count and device-side emission
+// ---------------------------------------------------------------------------
+
+__global__ void k_set_count(const __grid_constant__ DevBuffers B, int n) { *B.nact = n; }
+
+// FluidSystem::EmitParticles (SPH_Solver/fluids/fluid_system.cpp:619-641) on the
+// device, one block: at every frame that is a multiple of E.interval, the sites
+// of `layers` disks (EmitImmediate, :644-673; InsertParticles, :676-700) are
+// appended after the active slots and the device count grows; at capacity the
+// remaining sites are dropped (AddParticle returns -1 there) and the capacity
+// error bit is set. The sites, their jitter (stream E.seed + frame, two draws
+// per site in (layer, i, j) order) and every record field are computed with the
+// operations of the host generator sphmp_emit_disk in the same order, without
+// contraction, so the records are the ones sphmp_emit_disk + sphmp_emit_aos
+// would upload; a block-wide scan keeps the slot order of the accepted sites.
+__global__ void __launch_bounds__(kScanBlock) k_emit(const __grid_constant__ DevParams P,
+                                                     const __grid_constant__ DevBuffers B,
+                                                     const __grid_constant__ F4Set S,
+                                                     const __grid_constant__ DevEmitter E) {
+    __shared__ int sh_frame, sh_base;
+    if (threadIdx.x == 0) {
+        sh_frame = *B.frame;
+        sh_base = *B.nact;
+    }
+    __syncthreads();
+    const int f = sh_frame;
+    if (E.interval <= 0 || f % E.interval != 0) {
+        if (threadIdx.x == 0) *B.frame = f + 1;
+        return;
+    }
+    const uint32_t base = (uint32_t)sh_base;
+    const uint32_t room = (uint32_t)P.cap - base;
+    const int side = 2 * E.res + 1;
+    const uint32_t per_layer = (uint32_t)(side * side);
+    const uint32_t m = per_layer * (uint32_t)E.layers;
+    const uint64_t seed = E.seed + (uint64_t)f;
+    const float js = __fmul_rn(E.jitter, E.spacing);
+    const float jh = __fmul_rn(js, 0.5f);
+    const float r2 = __fmul_rn(E.radius, E.radius);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t written = 0;
+    for (uint32_t c0 = 0; c0 < m; c0 += kScanBlock) {
+        const uint32_t k = c0 + threadIdx.x;
+        bool ok = false;
+        float t0 = 0.f, t2 = 0.f;
+        int layer = 0;
+        if (k < m) {
+            layer = (int)(k / per_layer);
+            const uint32_t rem = k - (uint32_t)layer * per_layer;
+            const int i = (int)(rem / (uint32_t)side) - E.res;
+            const int j = (int)(rem % (uint32_t)side) - E.res;
+            const float jx = __fsub_rn(__fmul_rn(__fmul_rn(uniform01(seed, 2ull * k), E.jitter), E.spacing), jh);
+            const float jz = __fsub_rn(__fmul_rn(__fmul_rn(uniform01(seed, 2ull * k + 1ull), E.jitter), E.spacing), jh);
+            t0 = __fadd_rn(__fmul_rn((float)i, E.spacing), jx);
+            t2 = __fadd_rn(__fmul_rn((float)j, E.spacing), jz);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(t0, t0), __fmul_rn(0.f, 0.f)), __fmul_rn(t2, t2));
+            ok = !(d2 > r2);
+        }
+        uint32_t total;
+        const uint32_t off = block_excl_scan(ok ? 1u : 0u, &total);
+        const uint32_t q = written + off;
+        if (ok && q < room) {
+            const uint32_t idx = base + q;
+            const float centre[3] = {E.pos[0], __fadd_rn(E.pos[1], __fmul_rn((float)layer, E.spacing)), E.pos[2]};
+            float x[3], v[3];
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                x[a] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(E.rot[a][0], t0), __fmul_rn(E.rot[a][1], 0.f)),
+                                           __fmul_rn(E.rot[a][2], t2)),
+                                 centre[a]);
+                v[a] = __fmul_rn(E.dir[a], E.vel);
+            }
+            S.out[POS][idx] = make_float4(x[0], x[1], x[2], E.mass);
+            S.out[VEL][idx] = make_float4(v[0], v[1], v[2], E.visc);
+            S.out[VEV][idx] = make_float4(v[0], v[1], v[2], 0.f);
+            S.out[ALPHA][idx] = make_float4(E.onehot == 0 ? 1.f : 0.f, E.onehot == 1 ? 1.f : 0.f,
+                                            E.onehot == 2 ? 1.f : 0.f, E.restdens);
+            S.out[APREV][idx] = make_float4(0.f, 0.f, 0.f, __uint_as_float(idx));
+            B.opos[idx] = idx;
+            B.oidx[idx] = idx;
+            B.densp[idx] = make_float2(0.f, 0.f);
+            B.accel4[idx] = zero;
+            B.color[idx] = make_float4(__fdiv_rn((float)f, 200.0f), 0.5f, 0.8f, 0.5f);
+            B.bornid[idx] = (int32_t)idx;
+            B.mass_raw[idx] = E.mass;
+        }
+        written += total;
+    }
+    if (threadIdx.x == 0) {
+        if (written > room) set_err(B, kErrCapacity);
+        *B.nact = (int)(base + min(written, room));
+        *B.frame = f + 1;
     }
 }
 
@@ -1502,6 +1600,12 @@ void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur
     if (P.n <= 0) return;
     k_conservation<<<min(blocks_for(P.n), 152 * 8), kThreads, 0, s>>>(P, B, B.f4[POS][cur[POS]],
                                                                       B.f4[ALPHA][cur[ALPHA]]);
+}
+
+void launch_set_count(const DevBuffers& B, int n, cudaStream_t s) { k_set_count<<<1, 1, 0, s>>>(B, n); }
+
+void launch_emit(const DevParams& P, const DevBuffers& B, const int* cur, const DevEmitter& E, cudaStream_t s) {
+    k_emit<<<1, kScanBlock, 0, s>>>(P, B, make_set(B, cur, false), E);
 }
 
 void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,

@@ -84,6 +84,8 @@ def load():
         "sphmp_save_state": (st, [ctx, C.c_char_p]),
         "sphmp_download_display_async": (st, [ctx, vp, C.c_int32]),
         "sphmp_download_wait": (st, [ctx]),
+        "sphmp_set_device_emitter": (st, [ctx, P(abi.Emitter), C.c_int32, C.c_int32, C.c_int32, C.c_float,
+                                         C.c_uint64]),
         "sphmp_emit_disk": (st, [P(Params), P(abi.Emitter), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
                                  vp, vp, C.c_int32, P(C.c_int32)]),
         "sphmp_load_state": (st, [ctx, C.c_char_p]),
@@ -289,6 +291,18 @@ class Context:
 
     def advance(self):
         check(self._lib.sphmp_advance(self._ptr))
+
+    def set_device_emitter(self, position, direction, speed, radius, spacing, layers=2, phase=0, interval=22,
+                           jitter=1.0, seed=0):
+        """Emit disks on the device inside every step whose frame is a multiple of
+        `interval` (see sphmp_set_device_emitter); interval 0 turns it off."""
+        e = abi.Emitter()
+        for a in range(3):
+            e.position[a] = position[a]
+            e.dir[a] = direction[a]
+        e.vel, e.radius, e.spacing = speed, radius, spacing
+        check(self._lib.sphmp_set_device_emitter(self._ptr, C.byref(e), int(layers), int(phase), int(interval),
+                                                 float(jitter), int(seed)))
 
     def before_first_step(self):
         """Sort, then boundary volumes (reference FluidSystem::BeforeFirstStep)."""

@@ -150,7 +150,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_compute_force", "sphmp_compute_force_projectu", "sphmp_advance", "sphmp_step", "sphmp_conservation",
     "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
     "sphmp_write_frame_text", "sphmp_read_bi2", "sphmp_add_bi2_shape", "sphmp_save_state", "sphmp_load_state",
-    "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk",
+    "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk", "sphmp_set_device_emitter",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
