@@ -419,7 +419,9 @@ sphmp_status sphmp_compute_force_projectu(sphmp_ctx* ctx);
 sphmp_status sphmp_advance(sphmp_ctx* ctx);
 
 /* nsteps full steps (sort ... advance) in the given sphmp_schedule. Steps run
-   from a captured CUDA graph when `use_graph` is 1. */
+   from a captured CUDA graph when `use_graph` is 1 (one step per graph for the
+   fused schedule, two for the others, whose steps flip the double buffers an
+   odd number of times; an odd remainder runs eagerly). */
 sphmp_status sphmp_step(sphmp_ctx* ctx, int32_t nsteps, int32_t schedule, int32_t use_graph);
 
 /* Run one step eagerly with a CUDA event recorded on the context stream between

@@ -28,6 +28,7 @@ struct sphmp_ctx {
     bool nbr_valid = false;       // neighbour list built by the density pass for the current positions
     bool oct_built = false;       // the last grid list also built the next internal order (osrc)
     bool oct_valid = false;       // the internal order is octant-grouped for the current cell list
+    bool pos_sorted = false;      // positions unchanged since the cell list was built from them
     int list_mode = 0;            // kind of list the last density pass wrote (DevParams::list_mode)
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -125,6 +126,7 @@ DevParams dev_params(const sphmp_ctx* c) {
     P.r2 = p.smoothradius * p.smoothradius;
     P.r2list = P.r2 * (1.0f + 1.0e-5f);
     P.list_mode = c->nbr_valid ? c->list_mode : 0;
+    P.narrow = c->pos_sorted ? 1 : 0;
     P.dt = p.dt;
     P.kpoly6 = p.kpoly6;
     P.kspikydiff = p.kspikydiff;
@@ -362,7 +364,9 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     c->alpha_advanced = false;
     c->grid_valid = true;
     c->oct_valid = true;
+    c->oct_built = false;
     c->nbr_valid = false;
+    c->pos_sorted = true;
     run_density(c, s);
     mark("density");
     const DevParams PL = dev_params(c);  // neighbour passes read the list
@@ -378,6 +382,7 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
         swap_all(c);
         c->nbr_valid = false;  // positions moved
         c->oct_valid = false;
+        c->pos_sorted = false;
     } else {
         if (PL.multiphase) {
             run_force_drift(c, false, true, s);
@@ -404,6 +409,7 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
         mark("advance");
         c->nbr_valid = false;
         c->oct_valid = false;
+        c->pos_sorted = false;
     }
     CHECK_LAUNCH("step");
     return SPHMP_OK;
@@ -578,6 +584,7 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     c->nbr_valid = false;
     c->oct_valid = false;
     c->oct_built = false;
+    c->pos_sorted = false;
     drop_graph(c);
     CK(cudaStreamSynchronize(c->stream));
     return take_device_errors(c, nullptr);
@@ -702,6 +709,7 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
         c->nbr_valid = false;
         c->oct_valid = false;
         c->oct_built = false;
+        c->pos_sorted = false;
         if (field == SPHMP_F_MGRIDCNT) {
             // rebuild the cell starts (and mgridoff) from the uploaded counts
             CK(cudaMemcpyAsync(c->B.ccount, c->B.mgridcnt, sizeof(uint32_t) * (size_t)c->prm.gridtotal,
@@ -741,6 +749,7 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
         c->nbr_valid = false;
         c->oct_valid = false;
         c->oct_built = false;
+        c->pos_sorted = false;
     }
     drop_graph(c);
     CK(cudaStreamSynchronize(c->stream));
@@ -780,6 +789,7 @@ sphmp_status sphmp_rearrange_data(sphmp_ctx* c) {
     c->nbr_valid = false;
     c->oct_valid = c->oct_built;
     c->oct_built = false;
+    c->pos_sorted = true;
     return SPHMP_OK;
 }
 
@@ -899,6 +909,7 @@ sphmp_status sphmp_advance(sphmp_ctx* c) {
     CHECK_LAUNCH("MfAdvance");
     c->nbr_valid = false;
     c->oct_valid = false;
+    c->pos_sorted = false;
     return SPHMP_OK;
 }
 
@@ -908,9 +919,11 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
     if (sphmp_status st = check_schedule(c, schedule)) return st;
     if (nsteps == 0) return SPHMP_OK;
     // A fused step leaves every double buffer where it found it, so one captured
-    // step replays for all later steps. The reference schedule flips buffers an
-    // odd number of times per step and runs eagerly.
-    if (use_graph && schedule == SPHMP_SCHEDULE_FUSED) {
+    // step replays for all later steps. The reference and project-U schedules flip
+    // every buffer an odd number of times per step, so their graph holds two
+    // steps; an odd remainder runs eagerly.
+    const int per = schedule == SPHMP_SCHEDULE_FUSED ? 1 : 2;
+    if (use_graph && nsteps >= per) {
         // with a device emitter the graph runs over the capacity and serves any count
         const int key = c->emit_on ? -2 : c->n;
         if (!c->graph || c->graph_n != key || c->graph_schedule != schedule) {
@@ -919,7 +932,8 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
             CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
             int saved[kNumFloat4Fields];
             memcpy(saved, c->cur, sizeof(saved));
-            sphmp_status st = enqueue_step(c, schedule);
+            sphmp_status st = SPHMP_OK;
+            for (int k = 0; k < per && !st; k++) st = enqueue_step(c, schedule);
             cudaGraph_t g = nullptr;
             cudaError_t e = cudaStreamEndCapture(cap, &g);
             if (st) {
@@ -929,7 +943,7 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
             if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
             if (memcmp(saved, c->cur, sizeof(saved)) != 0) {
                 cudaGraphDestroy(g);
-                return fail(SPHMP_ERR_STATE, "internal: fused step did not restore buffer selectors");
+                return fail(SPHMP_ERR_STATE, "internal: captured steps did not restore buffer selectors");
             }
             e = cudaGraphInstantiate(&c->graph, g, 0);
             cudaGraphDestroy(g);
@@ -940,10 +954,18 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
             c->graph_n = key;
             c->graph_schedule = schedule;
         }
-        for (int t = 0; t < nsteps; t++) CK(cudaGraphLaunch(c->graph, c->stream));
+        for (int t = 0; t + per <= nsteps; t += per) CK(cudaGraphLaunch(c->graph, c->stream));
         if (c->emit_on) c->n_stale = true;
-        c->alpha_advanced = false;
+        // the state a step leaves behind (as enqueue_step sets it)
+        c->alpha_advanced = schedule != SPHMP_SCHEDULE_FUSED && c->prm.multiphase;
         c->grid_valid = true;
+        c->nbr_valid = false;
+        c->oct_valid = false;
+        c->oct_built = false;
+        c->pos_sorted = false;
+        c->list_mode = 1;
+        for (int t = 0; t < nsteps % per; t++)
+            if (sphmp_status st = enqueue_step(c, schedule)) return st;
         return SPHMP_OK;
     }
     for (int t = 0; t < nsteps; t++)

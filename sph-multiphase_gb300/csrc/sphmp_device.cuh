@@ -66,21 +66,40 @@ __device__ __forceinline__ uint32_t octant_of(const DevParams& P, const float4 p
 
 __device__ __forceinline__ void set_err(const DevBuffers& B, uint32_t bit) { atomicOr(B.err, bit); }
 
-// Visit the candidate slots of an in-grid particle at (x, y, z): along each axis
-// the cells within [t - R, t + R] (R = h in cell units plus a margin), limited
-// to the reference's +-1 cell. Cells along x are adjacent in the sorted order,
-// so each (y, z) row of cells is one contiguous slot range.
+// Grid coordinates (x, y, z) of an in-grid cell id, (gy * rz + gz) * rx + gx.
+__device__ __forceinline__ void cell_coords(const DevParams& P, uint32_t cell, int (&g)[3]) {
+    g[0] = (int)(cell % (uint32_t)P.rx);
+    const uint32_t yz = cell / (uint32_t)P.rx;
+    g[2] = (int)(yz % (uint32_t)P.rz);
+    g[1] = (int)(yz / (uint32_t)P.rz);
+}
+
+// Visit the candidate slots of an in-grid particle at (x, y, z) registered in
+// cell `cell` by the last sort: the reference's 3x3x3 cells around that cell
+// (contributeDensity and the other neighbour loops scan gc + neighborid[c]).
+// While the positions are the ones the sort binned (P.narrow), the block is
+// narrowed along each axis to the cells within [t - R, t + R] of the position
+// (R = h in cell units plus a margin), which hold every particle within h of
+// it; after the particles have moved (a pass called without a new sort) the
+// whole block is scanned, as the reference does. The stored cell lies in the
+// grid's interior, so every cell visited exists. Cells along x are adjacent in
+// the sorted order, so each (y, z) row of cells is one contiguous slot range.
 template <class F>
-__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart, float x,
-                                               float y, float z, F&& f) {
+__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart,
+                                               uint32_t cell, float x, float y, float z, F&& f) {
     const float t[3] = {grid_t(x, P.gmin[0], P.fac[0]), grid_t(y, P.gmin[1], P.fac[1]),
                         grid_t(z, P.gmin[2], P.fac[2])};
+    int g[3];
+    cell_coords(P, cell, g);
     int lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const int g = __float2int_rz(t[a]);
-        lo[a] = max(g - 1, __float2int_rd(t[a] - P.srad[a]));
-        hi[a] = min(g + 1, __float2int_rd(t[a] + P.srad[a]));
+        lo[a] = g[a] - 1;
+        hi[a] = g[a] + 1;
+        if (P.narrow) {
+            lo[a] = max(lo[a], __float2int_rd(t[a] - P.srad[a]));
+            hi[a] = min(hi[a], __float2int_rd(t[a] + P.srad[a]));
+        }
     }
     for (int yy = lo[1]; yy <= hi[1]; yy++) {
         for (int zz = lo[2]; zz <= hi[2]; zz++) {
@@ -118,7 +137,7 @@ __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffe
             return;
         }
     }
-    for_candidates(P, B.cstart, x, y, z, f);
+    for_candidates(P, B.cstart, B.mgcell[s], x, y, z, f);
 }
 
 // ---------------------------------------------------------------------------

@@ -69,6 +69,8 @@ struct DevParams {
     float h, r2;     // smoothing radius and its square
     float r2list;    // squared radius of the neighbour list (r2 plus a rounding margin)
     int list_mode;   // 0: no list, 1: index lists in nbr (written by the last density pass)
+    int narrow;      // 1: positions are the ones the cell lists were built from (the cell
+                     // search may skip the cells beyond h of the current position)
     float dt;
     float kpoly6, kspikydiff;
     float bvisc;

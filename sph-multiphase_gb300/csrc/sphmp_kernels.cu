@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume(const __grid_const
     const float4 pi = pos4[s];
     if (!(pi.w < 0.f)) return;
     Kahan sum;
-    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+    for_candidates(P, B.cstart, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         if (!(pj.w < 0.f)) return;
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // Density + EOS of one in-grid particle by its own search over the internal
 // order (the bucket kernel's path for buckets with too many members): the
 // h-subcells within h of the particle (at most 4 per axis, normally 3), limited
-// to the reference's 3x3x3 cells; along x, the subcells of one cell are
+// to the reference's 3x3x3 cells around its cell in this sort; along x, the subcells of one cell are
 // adjacent octant buckets, so each (y, z) subcell row is at most two ranges.
 // Writes 1/rho and p like k_density, plus the neighbour index list.
 __device__ __forceinline__ void density_octant_one(const DevParams& P, const DevBuffers& B,
@@ -479,14 +479,20 @@ __device__ __forceinline__ void density_octant_one(const DevParams& P, const Dev
                                                    float rho0) {
     const float t[3] = {grid_t(pi.x, P.gmin[0], P.fac[0]), grid_t(pi.y, P.gmin[1], P.fac[1]),
                         grid_t(pi.z, P.gmin[2], P.fac[2])};
+    int g[3];
+    cell_coords(P, B.mgcell[s], g);  // the particle's cell in this sort: interior, so all 27 exist
     int lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const int g2 = 2 * __float2int_rz(t[a]);
+        const int g2 = 2 * g[a];
         const float u = 2.f * t[a];
         const float R = 2.f * P.srad[a];
-        lo[a] = max(g2 - 2, __float2int_rd(u - R));
-        hi[a] = min(g2 + 3, __float2int_rd(u + R));
+        lo[a] = g2 - 2;
+        hi[a] = g2 + 3;
+        if (P.narrow) {
+            lo[a] = max(lo[a], __float2int_rd(u - R));
+            hi[a] = min(hi[a], __float2int_rd(u + R));
+        }
     }
     Kahan sum;
     uint32_t cnt = 0;
@@ -797,7 +803,7 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
     Kahan sum;
     uint32_t cnt = 0;
     uint32_t* __restrict__ col = B.nbr + s;
-    for_candidates(P, B.cstart, pi.x, pi.y, pi.z, [&](uint32_t j) {
+    for_candidates(P, B.cstart, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
         const float dsq = dx * dx + dy * dy + dz * dz;

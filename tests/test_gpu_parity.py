@@ -256,6 +256,66 @@ def test_graph_matches_eager():
         assert bits_equal(res[0][k], res[1][k]), k
 
 
+@pytest.mark.parametrize("schedule", [abi.SCHEDULE_REFERENCE, abi.SCHEDULE_PROJECTU], ids=["reference", "projectu"])
+def test_two_step_graph_matches_eager(schedule):
+    """The reference-order schedules replay a captured pair of steps (an odd
+    remainder runs eagerly): five steps, bit-identical to five eager steps."""
+    sc = _scene("liquids3")
+    res = []
+    for use_graph in (False, True):
+        ctx = device_ctx(sc)
+        ctx.before_first_step()
+        ctx.step(2, schedule, use_graph=use_graph)
+        ctx.step(3, schedule, use_graph=use_graph)
+        ctx.sync()
+        res.append(download_state(ctx))
+        ctx.close()
+    for k in ("pos", "vel", "veleval", "alpha", "alpha_pre", "accel", "velxcor", "mgcell", "midsort"):
+        assert bits_equal(res[0][k], res[1][k]), k
+
+
+def test_pass_after_graph_steps_uses_fresh_neighbours():
+    """A per-pass call after graph-replayed steps sees the state a step leaves
+    (no neighbour list from before the steps): same bits as after eager steps."""
+    sc = _scene("tait3")
+    res = []
+    for use_graph in (False, True):
+        ctx = device_ctx(sc)
+        ctx.before_first_step()
+        ctx.step(1, abi.SCHEDULE_FUSED, use_graph=use_graph)  # with a graph: captured here
+        ctx.compute_pressure()  # neighbour lists for the current positions
+        ctx.step(1, abi.SCHEDULE_FUSED, use_graph=use_graph)  # replayed: the positions move
+        ctx.compute_force()
+        ctx.sync()
+        res.append(download_state(ctx))
+        ctx.close()
+    assert bits_equal(res[0]["accel"], res[1]["accel"])
+
+
+def test_passes_after_advance_without_resort_match_oracle():
+    """MfComputePressure / MfComputeForce called after an advance with no new sort:
+    the neighbour loops scan the 27 cells around each particle's cell from the
+    last sort (gc + neighborid, as the reference does), with positions that have
+    moved since. Several steps of this, against the oracle doing the same."""
+    sc, s, ctx = _sorted_pair("tait3")
+    p = sc.params
+    for _ in range(3):
+        O.step(p, s, abi.SCHEDULE_FUSED, 1)
+        ctx.step(1, abi.SCHEDULE_FUSED, use_graph=False)
+        for st in ("orc_compute_pressure", "orc_compute_force"):
+            O.call(st, p, s)
+        ctx.compute_pressure()
+        ctx.compute_force()
+        ctx.sync()
+        g = download_state(ctx)
+        f = in_grid_fluid(s)
+        assert field_err(g["dens"][f], s.dens[f]) < RTOL
+        assert field_err(g["accel"][f], s.accel[f]) < RTOL
+        upload_state_fields(ctx, s, ["pos", "vel", "veleval", "accel"])
+        ctx.upload_field(abi.F_ALPHA, s.alpha)
+    ctx.close()
+
+
 def test_multi_step_tracks_oracle():
     """Ten fused steps: bit-identical sorts while positions stay bit-identical is not
     guaranteed, so compare particles by bornid with a loose bound."""
