@@ -29,6 +29,7 @@ struct sphmp_ctx {
     bool oct_built = false;       // the last grid list also built the next internal order (osrc)
     bool oct_valid = false;       // the internal order is octant-grouped for the current cell list
     bool pos_sorted = false;      // positions unchanged since the cell list was built from them
+    int hash_n = -1;              // particle count the cell keys were computed for (-1: none)
     int list_mode = 0;            // kind of list the last density pass wrote (DevParams::list_mode)
     int device = 0;
     cudaStream_t own_stream = nullptr;
@@ -354,6 +355,7 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     }
     launch_hash(P, c->B, c->cur, s);
     mark("hash");
+    c->hash_n = c->emit_on ? -1 : c->n;  // with an emitter the count is only known on the device
     launch_cell_starts(P, c->B, s);
     mark("cell_starts");
     launch_cell_order(P, c->B, c->cur, s);
@@ -575,6 +577,7 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     c->n = end;
     c->prm.num = end;
     c->n_stale = false;
+    c->hash_n = -1;
     launch_set_count(c->B, end, c->stream);
     const DevParams P = dev_params(c);
     launch_unpack_aos(P, c->B, c->cur, d_disp, d_calc, start, end, c->stream);
@@ -760,8 +763,10 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
 
 sphmp_status sphmp_get_particle_index(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = refresh_n(c)) return st;
     launch_hash(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("GetParticleIndex");
+    c->hash_n = c->n;
     c->grid_valid = false;
     c->nbr_valid = false;
     c->oct_valid = false;
@@ -771,6 +776,10 @@ sphmp_status sphmp_get_particle_index(sphmp_ctx* c) {
 
 sphmp_status sphmp_get_grid_list(sphmp_ctx* c) {
     if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = refresh_n(c)) return st;
+    // the scatter places every slot by its cell key and rank: both must exist for the current count
+    if (c->hash_n != c->n)
+        return fail(SPHMP_ERR_STATE, "no cell keys for the current %d particles (run GetParticleIndex first)", c->n);
     launch_grid_list(dev_params(c), c->B, c->cur, c->stream);
     CHECK_LAUNCH("GetGridList");
     c->oct_built = true;
@@ -964,6 +973,7 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
         c->oct_built = false;
         c->pos_sorted = false;
         c->list_mode = 1;
+        c->hash_n = c->emit_on ? -1 : c->n;
         for (int t = 0; t < nsteps % per; t++)
             if (sphmp_status st = enqueue_step(c, schedule)) return st;
         return SPHMP_OK;

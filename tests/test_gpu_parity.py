@@ -384,6 +384,24 @@ def test_fp64_oracle_error():
 # edge cases
 # ---------------------------------------------------------------------------
 
+def test_grid_list_needs_keys_for_the_current_count():
+    """GetGridList scatters every slot by the cell key and rank of GetParticleIndex:
+    without keys for the current particle count it is refused, not run."""
+    sc = _scene("tait2")
+    ctx = device_ctx(sc)
+    with pytest.raises(sphmp.SphmpError) as e:
+        ctx.get_grid_list()
+    assert e.value.status == abi.ERR_STATE
+    ctx.get_particle_index()
+    ctx.get_grid_list()
+    n0 = sc.n - 100
+    ctx.upload_aos(sc.disp[:n0], sc.calc[:n0])  # the count changed since the keys
+    with pytest.raises(sphmp.SphmpError) as e:
+        ctx.get_grid_list()
+    assert e.value.status == abi.ERR_STATE
+    ctx.close()
+
+
 def test_empty_context():
     sc = _scene("tait2")
     p = sc.params.copy()
