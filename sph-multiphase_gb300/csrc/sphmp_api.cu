@@ -663,6 +663,33 @@ sphmp_status sphmp_download_wait(sphmp_ctx* c) {
     return SPHMP_OK;
 }
 
+// Uploaded sort arrays are indexed with on the device: a cell id must be an
+// interior cell (the neighbour loops visit its 3x3x3 block) or GRID_UNDEF, and
+// the per-cell counts must be non-negative and add up to at most n.
+static sphmp_status check_sort_upload(const sphmp_ctx* c, int field, const void* host, int32_t n) {
+    const sphmp_params& p = c->prm;
+    if (field == SPHMP_F_MGCELL) {
+        const uint32_t* v = static_cast<const uint32_t*>(host);
+        for (int32_t i = 0; i < n; i++) {
+            if (v[i] == SPHMP_GRID_UNDEF) continue;
+            const uint32_t x = v[i] % (uint32_t)p.gridres[0], yz = v[i] / (uint32_t)p.gridres[0];
+            const uint32_t z = yz % (uint32_t)p.gridres[2], y = yz / (uint32_t)p.gridres[2];
+            if (v[i] >= (uint32_t)p.gridtotal || x < 1 || x + 2 > (uint32_t)p.gridres[0] || z < 1 ||
+                z + 2 > (uint32_t)p.gridres[2] || y < 1 || y + 2 > (uint32_t)p.gridres[1])
+                return fail(SPHMP_ERR_INVALID_ARG, "mgcell[%d] = %u is not an interior cell of the grid", i, v[i]);
+        }
+    } else if (field == SPHMP_F_MGRIDCNT) {
+        const int32_t* v = static_cast<const int32_t*>(host);
+        int64_t sum = 0;
+        for (int32_t i = 0; i < n; i++) {
+            if (v[i] < 0) return fail(SPHMP_ERR_INVALID_ARG, "mgridcnt[%d] = %d < 0", i, v[i]);
+            sum += v[i];
+        }
+        if (sum > c->n) return fail(SPHMP_ERR_INVALID_ARG, "mgridcnt adds up to %lld > %d particles", (long long)sum, c->n);
+    }
+    return SPHMP_OK;
+}
+
 static void* sort_array(sphmp_ctx* c, int field, size_t* count) {
     switch (field) {
         case SPHMP_F_MGCELL: *count = c->n; return c->B.mgcell;
@@ -708,6 +735,7 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
     size_t count = 0;
     if (void* arr = sort_array(c, field, &count)) {
         if (n < 0 || (size_t)n > count) return fail(SPHMP_ERR_CAPACITY, "n %d exceeds %zu entries", n, count);
+        if (sphmp_status st = check_sort_upload(c, field, host, n)) return st;
         CK(cudaMemcpyAsync(arr, host, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
         c->nbr_valid = false;
         c->oct_valid = false;

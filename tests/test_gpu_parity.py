@@ -402,6 +402,29 @@ def test_grid_list_needs_keys_for_the_current_count():
     ctx.close()
 
 
+def test_sort_array_uploads_are_checked():
+    """Caller-supplied sort arrays are indexed with on the device: border or
+    out-of-range cell ids and negative or excess counts are refused."""
+    sc, s, ctx = _sorted_pair("tait2")
+    p = sc.params
+    mgcell = ctx.download_field(abi.F_MGCELL).astype(np.uint32)
+    ctx.upload_field(abi.F_MGCELL, mgcell)  # its own cells: accepted
+    for bad in (0, p.gridres[0] - 1, p.gridtotal, p.gridtotal + 5):  # border cells, beyond the grid
+        m = mgcell.copy()
+        m[7] = bad
+        with pytest.raises(sphmp.SphmpError) as e:
+            ctx.upload_field(abi.F_MGCELL, m)
+        assert e.value.status == abi.ERR_INVALID_ARG
+    cnt = ctx.download_field(abi.F_MGRIDCNT).astype(np.int32)
+    for k, v in ((3, -1), (5, sc.n + 1)):
+        c2 = cnt.copy()
+        c2[k] = v
+        with pytest.raises(sphmp.SphmpError) as e:
+            ctx.upload_field(abi.F_MGRIDCNT, c2)
+        assert e.value.status == abi.ERR_INVALID_ARG
+    ctx.close()
+
+
 def test_empty_context():
     sc = _scene("tait2")
     p = sc.params.copy()
