@@ -511,10 +511,16 @@ sphmp_status sphmp_set_params(sphmp_ctx* c, const sphmp_params* p) {
     const bool grid_changed = memcmp(p->gridres, c->prm.gridres, sizeof(p->gridres)) != 0 ||
                               memcmp(p->gridmin, c->prm.gridmin, sizeof(p->gridmin)) != 0 ||
                               memcmp(p->gridIdfac, c->prm.gridIdfac, sizeof(p->gridIdfac)) != 0;
+    // neighbour lists and the octant buckets hold for the radius they were built with
+    const bool radius_changed = p->smoothradius != c->prm.smoothradius || p->simscale != c->prm.simscale;
     c->prm = *p;
     c->prm.maxNum = c->cap;
     c->prm.num = c->n;
     if (grid_changed) c->grid_valid = false;
+    if (grid_changed || radius_changed) {
+        c->nbr_valid = false;
+        c->oct_valid = false;
+    }
     drop_graph(c);
     return SPHMP_OK;
 }
