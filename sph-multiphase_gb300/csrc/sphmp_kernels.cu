@@ -468,72 +468,6 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // Density + EOS pressure (MfComputePressureCUDA)
 // ---------------------------------------------------------------------------
 
-// Density + EOS of one in-grid particle by its own search over the internal
-// order (the bucket kernel's path for buckets with too many members): the
-// h-subcells within h of the particle (at most 4 per axis, normally 3), limited
-// to the reference's 3x3x3 cells around its cell in this sort; along x, the subcells of one cell are
-// adjacent octant buckets, so each (y, z) subcell row is at most two ranges.
-// Writes 1/rho and p like k_density, plus the neighbour index list.
-__device__ __forceinline__ void density_octant_one(const DevParams& P, const DevBuffers& B,
-                                                   const float4* __restrict__ pos4, uint32_t s, const float4 pi,
-                                                   float rho0) {
-    const float t[3] = {grid_t(pi.x, P.gmin[0], P.fac[0]), grid_t(pi.y, P.gmin[1], P.fac[1]),
-                        grid_t(pi.z, P.gmin[2], P.fac[2])};
-    int g[3];
-    cell_coords(P, B.mgcell[s], g);  // the particle's cell in this sort: interior, so all 27 exist
-    int lo[3], hi[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int g2 = 2 * g[a];
-        const float u = 2.f * t[a];
-        const float R = 2.f * P.srad[a];
-        lo[a] = g2 - 2;
-        hi[a] = g2 + 3;
-        if (P.narrow) {
-            lo[a] = max(lo[a], __float2int_rd(u - R));
-            hi[a] = min(hi[a], __float2int_rd(u + R));
-        }
-    }
-    Kahan sum;
-    uint32_t cnt = 0;
-    uint32_t* __restrict__ col = B.nbr + s;
-    for (int hy = lo[1]; hy <= hi[1]; hy++) {
-        const int cy = hy >> 1, oy = hy & 1;
-        for (int hz = lo[2]; hz <= hi[2]; hz++) {
-            const int cz = hz >> 1, oz = hz & 1;
-            const int rowc = (cy * P.rz + cz) * P.rx;
-            for (int cx = lo[0] >> 1; cx <= (hi[0] >> 1); cx++) {
-                const uint32_t c = (uint32_t)(rowc + cx);
-                const uint32_t ce = __ldg(&B.cstart[c + 1]);
-                if (__ldg(&B.cstart[c]) == ce) continue;
-                const int oxlo = max(lo[0] - 2 * cx, 0), oxhi = min(hi[0] - 2 * cx, 1);
-                const int bq = (oy * 2 + oz) * 2;
-                const uint32_t k0 = __ldg(&B.oct_start[(size_t)c * 8 + bq + oxlo]);
-                const uint32_t k1 = (bq + oxhi == 7) ? ce : __ldg(&B.oct_start[(size_t)c * 8 + bq + oxhi + 1]);
-                for (uint32_t k = k0; k < k1; k++) {
-                    const float4 pj = __ldg(&pos4[k]);
-                    const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
-                    const float dsq = dx * dx + dy * dy + dz * dz;
-                    if (dsq < P.r2) {
-                        const float cc = P.r2 - dsq;
-                        const float m = pj.w > 0.f ? pj.w : rho0 * (-pj.w);
-                        sum.add(cc * cc * cc * m);
-                        if (dsq > 0.f) {
-                            if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = k;
-                            cnt++;
-                        }
-                    } else if (dsq < P.r2list) {
-                        if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = k;
-                        cnt++;
-                    }
-                }
-            }
-        }
-    }
-    B.nbr_cnt[s] = cnt;
-    B.densp[s] = density_result(P, sum.s, rho0);
-}
-
 // Density + EOS, one warp per octant bucket (the members of one h-subcell).
 // Every member of a bucket has its neighbours within the 27 h-subcells around
 // it: a pair closer than h is at most one subcell apart per axis, up to the
@@ -551,7 +485,7 @@ __device__ __forceinline__ void density_octant_one(const DevParams& P, const Dev
 // and the blocks with Kahan compensation, so the relative rounding error of a
 // member's sum stays below (kBucketChunks + 6) * 2^-24. Warps take buckets from
 // a shared counter (bucket costs differ by orders of magnitude). Buckets with
-// more than kBucketMaxMembers members take the per-member octant search.
+// more than kBucketMaxMembers members are taken in windows of that many.
 // The candidate sequence of bucket (c, q): the 27 h-subcells around it as 18
 // contiguous index ranges, two per (y, z) subcell row (the x-neighbour bucket in
 // the adjacent cell, and both x buckets of the bucket's own cell column). Lane i
@@ -660,13 +594,6 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
             }
         }
         if (!__any_sync(0xffffffffu, fluid)) continue;
-        if (m1 - m0 > (uint32_t)kBucketMaxMembers) {
-            for (uint32_t i = m0 + lane; i < m1; i += 32) {
-                const float4 pi = __ldg(&pos4[i]);
-                if (!(pi.w < 0.f)) density_octant_one(P, B, pos4, i, pi, __ldg(&alpha4[i]).w);
-            }
-            continue;
-        }
         uint32_t st, off;
         const uint32_t T = bucket_ranges(P, B, c, q, lane, rstart, roff, st, off);
         const uint32_t bid = c * 8u + q;
@@ -677,69 +604,73 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
             bt[20 + lane] = st - off;
         }
         if (masked && lane == 18) bt[18] = T;
-        int r = 0;
-        for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
-            float4 cj[kBucketChunks];  // w: fluid mass (0 for boundary)
-            float vb[kBucketChunks];   // boundary volume (0 for fluid)
-#pragma unroll
-            for (int ch = 0; ch < kBucketChunks; ch++) {
-                const uint32_t e = base + lane + 32u * ch;
-                cj[ch] = make_float4(kFar, kFar, kFar, 0.f);
-                vb[ch] = 0.f;
-                if (e < T) {
-                    cj[ch] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
-                    vb[ch] = fmaxf(-cj[ch].w, 0.f);
-                    cj[ch].w = fmaxf(cj[ch].w, 0.f);
-                }
-            }
-            const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
-            const uint32_t word0 = base >> 5;
-            const bool first = base == 0;
-            for (uint32_t t = m0; t < m1; t++) {
-                const float4 pt = __ldg(&pos4[t]);
-                if (pt.w < 0.f) continue;
-                const float rho0 = __ldg(&alpha4[t]).w;
-                float acc = 0.f;
-                uint32_t mine = 0;  // lane k keeps the mask word of chunk k
+        const uint32_t lst = masked ? (kMaskList | bid) : kRescan;
+        // the members in windows of kBucketMaxMembers (more than one only in squeezed regions)
+        for (uint32_t w0 = m0; w0 < m1; w0 += (uint32_t)kBucketMaxMembers) {
+            const uint32_t w1 = min(m1, w0 + (uint32_t)kBucketMaxMembers);
+            int r = 0;
+            for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
+                float4 cj[kBucketChunks];  // w: fluid mass (0 for boundary)
+                float vb[kBucketChunks];   // boundary volume (0 for fluid)
 #pragma unroll
                 for (int ch = 0; ch < kBucketChunks; ch++) {
-                    if (ch < nch) {
-                        float dx = pt.x - cj[ch].x, dy = pt.y - cj[ch].y, dz = pt.z - cj[ch].z;
-                        if (!SS1) {
-                            dx *= ss;
-                            dy *= ss;
-                            dz *= ss;
+                    const uint32_t e = base + lane + 32u * ch;
+                    cj[ch] = make_float4(kFar, kFar, kFar, 0.f);
+                    vb[ch] = 0.f;
+                    if (e < T) {
+                        cj[ch] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
+                        vb[ch] = fmaxf(-cj[ch].w, 0.f);
+                        cj[ch].w = fmaxf(cj[ch].w, 0.f);
+                    }
+                }
+                const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
+                const uint32_t word0 = base >> 5;
+                const bool first = base == 0;
+                for (uint32_t t = w0; t < w1; t++) {
+                    const float4 pt = __ldg(&pos4[t]);
+                    if (pt.w < 0.f) continue;
+                    const float rho0 = __ldg(&alpha4[t]).w;
+                    float acc = 0.f;
+                    uint32_t mine = 0;  // lane k keeps the mask word of chunk k
+#pragma unroll
+                    for (int ch = 0; ch < kBucketChunks; ch++) {
+                        if (ch < nch) {
+                            float dx = pt.x - cj[ch].x, dy = pt.y - cj[ch].y, dz = pt.z - cj[ch].z;
+                            if (!SS1) {
+                                dx *= ss;
+                                dy *= ss;
+                                dz *= ss;
+                            }
+                            const float dsq = dx * dx + dy * dy + dz * dz;
+                            const float cc = fmaxf(r2 - dsq, 0.f);  // 0 outside h (and for the padding lanes)
+                            acc = fmaf(cc * cc * cc, fmaf(rho0, vb[ch], cj[ch].w), acc);
+                            const uint32_t bal = __ballot_sync(0xffffffffu, dsq > 0.f && dsq < r2list);
+                            mine = lane == (unsigned)ch ? bal : mine;
                         }
-                        const float dsq = dx * dx + dy * dy + dz * dz;
-                        const float cc = fmaxf(r2 - dsq, 0.f);  // 0 outside h (and for the padding lanes)
-                        acc = fmaf(cc * cc * cc, fmaf(rho0, vb[ch], cj[ch].w), acc);
-                        const uint32_t bal = __ballot_sync(0xffffffffu, dsq > 0.f && dsq < r2list);
-                        mine = lane == (unsigned)ch ? bal : mine;
+                    }
+                    if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
+                    const float part = warp_sum_f(acc);
+                    if (lane == 0) {
+                        Kahan tot;
+                        if (!first) {
+                            const float2 prev = msum[w][t - w0];
+                            tot.s = prev.x;
+                            tot.c = prev.y;
+                        }
+                        tot.add(part);
+                        msum[w][t - w0] = make_float2(tot.s, tot.c);
                     }
                 }
-                if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
-                const float part = warp_sum_f(acc);
-                if (lane == 0) {
-                    Kahan tot;
-                    if (!first) {
-                        const float2 prev = msum[w][t - m0];
-                        tot.s = prev.x;
-                        tot.c = prev.y;
-                    }
-                    tot.add(part);
-                    msum[w][t - m0] = make_float2(tot.s, tot.c);
-                }
+                __syncwarp();
+            }
+            for (uint32_t i = lane; i < w1 - w0; i += 32) {
+                const uint32_t t = w0 + i;
+                if (__ldg(&pos4[t]).w < 0.f) continue;
+                B.nbr_cnt[t] = lst;
+                B.densp[t] = density_result(P, msum[w][i].x, __ldg(&alpha4[t]).w);
             }
             __syncwarp();
         }
-        const uint32_t lst = masked ? (kMaskList | bid) : kRescan;
-        for (uint32_t i = lane; i < m1 - m0; i += 32) {
-            const uint32_t t = m0 + i;
-            if (__ldg(&pos4[t]).w < 0.f) continue;
-            B.nbr_cnt[t] = lst;
-            B.densp[t] = density_result(P, msum[w][i].x, __ldg(&alpha4[t]).w);
-        }
-        __syncwarp();
     }
 }
 

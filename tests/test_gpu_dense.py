@@ -3,7 +3,7 @@ common path: candidate sequences longer than one register block of the bucket
 density (256), index lists longer than their capacity (256 entries: the passes
 fall back to the cell search), sequences longer than the mask capacity (2048
 candidates: no mask list at all) and buckets with more than 128 members (the
-per-member octant search). Particles are lighter in proportion, so densities
+member windows of 128). Particles are lighter in proportion, so densities
 stay near rest density. Same tolerances as test_gpu_parity.py.
 """
 import numpy as np
