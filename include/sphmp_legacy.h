@@ -39,6 +39,14 @@ void GetParticleIndexCUDA(void);
 void GetGridListCUDA(void);
 /* RearrageDataCUDA (fluid_system_host.cu:187-210; the reference's spelling) */
 void RearrageDataCUDA(void);
+/* The legacy names of the three sort steps, as the legacy multiphase step calls
+   them (fluid_system.cpp:382-384 and 427-429, InitialSortCUDA(0x0, 0x0, 0x0),
+   SortGridCUDA(0x0), CountingSortFullCUDA_(0x0)): the same as GetParticleIndexCUDA,
+   GetGridListCUDA and RearrageDataCUDA. The pointer arguments (host mirrors of the
+   older code) are ignored. */
+void InitialSortCUDA(uint32_t* gcell, uint32_t* ccell, int* gcnt);
+void SortGridCUDA(int* goff);
+void CountingSortFullCUDA_(uint32_t* ggrid);
 /* MfComputePressureCUDA (fluid_system_host.cu:337-348) */
 void MfComputePressureCUDA(void);
 /* MfComputeDriftVelCUDA (decl fluid_system_host.cuh:62) */

@@ -1131,6 +1131,9 @@ void FluidSetupCUDA(const sphmp_params* params) {
 void GetParticleIndexCUDA(void) { legacy_run("InsertParticlesCUDA", sphmp_get_particle_index); }
 void GetGridListCUDA(void) { legacy_run("Sort Grid", sphmp_get_grid_list); }
 void RearrageDataCUDA(void) { legacy_run("Sorting Failed", sphmp_rearrange_data); }
+void InitialSortCUDA(uint32_t*, uint32_t*, int*) { GetParticleIndexCUDA(); }
+void SortGridCUDA(int*) { GetGridListCUDA(); }
+void CountingSortFullCUDA_(uint32_t*) { RearrageDataCUDA(); }
 void MfComputePressureCUDA(void) { legacy_run("MfComputePressureCUDA", sphmp_compute_pressure); }
 void MfComputeDriftVelCUDA(void) { legacy_run("MfComputeDriftVelCUDA", sphmp_compute_drift_vel); }
 void MfComputeAlphaAdvanceCUDA(void) { legacy_run("MfComputeAlphaAdvanceCUDA", sphmp_compute_alpha_advance); }

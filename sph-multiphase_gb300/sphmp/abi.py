@@ -153,7 +153,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk", "sphmp_set_device_emitter",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
-    "GetGridListCUDA", "RearrageDataCUDA", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
+    "GetGridListCUDA", "RearrageDataCUDA", "InitialSortCUDA", "SortGridCUDA", "CountingSortFullCUDA_", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
     "MfComputeAlphaAdvanceCUDA", "MfComputeCorrectionCUDA", "MfComputeForceCUDA", "ComputeForceCUDA_ProjectU",
     "MfAdvanceCUDA",
     "ComputeBoundaryDensity", "computeNumBlocks", "sphmp_legacy_context", "TransferToCUDA",
