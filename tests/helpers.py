@@ -102,3 +102,36 @@ def upload_state_fields(ctx, s, names):
 def in_grid_fluid(s_or_dict):
     get = (lambda k: s_or_dict[k]) if isinstance(s_or_dict, dict) else (lambda k: getattr(s_or_dict, k))
     return (get("mgcell") != UNDEF) & (get("type") == 0)
+
+
+def build_c_host(out_dir):
+    """Compile tests/c_host/legacy_host.cpp against include/ and link libsphmp.so, as
+    a C++ host application of the reference would; returns the executable's path."""
+    import os
+    import subprocess
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(sphmp.load()._name)
+    exe = os.path.join(str(out_dir), "legacy_host")
+    cmd = [os.environ.get("CXX", "g++"), "-std=c++14", "-O1", "-Wall", "-Wextra", "-Werror",
+           "-I", os.path.join(repo, "include"), os.path.join(repo, "tests", "c_host", "legacy_host.cpp"),
+           "-o", exe, "-L", libdir, "-lsphmp", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def write_c_host_inputs(out_dir, scene):
+    """params.bin, display.bin, calc.bin for legacy_host (boundary accel/pressure zeroed, as the
+    oracle state starts); returns the three paths."""
+    import os
+    calc = scene.calc[:scene.n].copy()
+    bnd = scene.disp["type"][:scene.n] == abi.TYPE_BOUNDARY
+    calc["accel"][bnd] = 0
+    calc["pressure"][bnd] = 0
+    paths = [os.path.join(str(out_dir), f) for f in ("params.bin", "display.bin", "calc.bin")]
+    with open(paths[0], "wb") as f:
+        f.write(bytes(scene.params))
+    np.ascontiguousarray(scene.disp[:scene.n]).tofile(paths[1])
+    calc.tofile(paths[2])
+    return paths
+

@@ -20,7 +20,9 @@ import numpy as np
 import pytest
 
 import sphmp
-from helpers import field_err, in_grid_fluid, oracle_state
+import subprocess
+
+from helpers import build_c_host, field_err, in_grid_fluid, oracle_state, write_c_host_inputs
 from oracle import oracle as O
 from sphmp import abi, scenes
 
@@ -118,3 +120,25 @@ def test_legacy_multiphase_sequence_with_projectu(legacy):
             getattr(L, name)()
         O.step(p, s, abi.SCHEDULE_PROJECTU, 1)
         _check(L, sc, s)
+
+
+def test_cpp_host_program(built, tmp_path):
+    """The same BeforeFirstStep + RunSimpleSPH sequence from a compiled C++ host
+    (tests/c_host/legacy_host.cpp, linked with -lsphmp), three steps."""
+    exe = build_c_host(tmp_path)
+    sc = scenes.small_block(seed=73, n=(12, 10, 9), nphase=2, eos=abi.EOS_TAIT, velocity_scale=0.3, multiphase=0,
+                            dens=(1000.0, 800.0, 900.0))
+    args = write_c_host_inputs(tmp_path, sc)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([exe, *args, str(sc.n), "3", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    disp = np.fromfile(out, dtype=abi.display_dtype())
+    p = sc.params
+    s = oracle_state(sc)
+    O.before_first_step(p, s)
+    O.step(p, s, abi.SCHEDULE_REFERENCE, 3)
+    f = in_grid_fluid(s)
+    assert f.sum() > 500
+    assert field_err(disp["pos"][f], s.pos[f]) < RTOL
+    assert np.array_equal(disp["type"], s.type)
+

@@ -182,3 +182,30 @@ def test_param_carrier_prefix_layout():
             "gridtotal": 360, "surfaceTensionK": 452, "fBlending": 460, "nphase": 464}
     for k, v in offs.items():
         assert getattr(abi.Params, k).offset == v, k
+
+
+@pytest.mark.parametrize("header", ["sphmp.h", "sphmp_legacy.h"])
+@pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++11")])
+def test_headers_compile_as_c_and_cpp(header, lang, std):
+    cc = "gcc" if lang == "c" else "g++"
+    r = subprocess.run([cc, "-x", lang, std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                        os.path.join(REPO, "include"), os.path.join(REPO, "include", header)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_cpp_host_links_and_fails_loudly_without_a_device(lib, tmp_path):
+    """A C++ host in the reference's shape links against the library; with no GPU,
+    FluidSetupCUDA reports it and the program stops (no CPU fallback)."""
+    import torch
+
+    from helpers import build_c_host, write_c_host_inputs
+    exe = build_c_host(tmp_path)
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (tests/test_gpu_legacy.py runs the program)")
+    sc = scenes.small_block(seed=3, n=(4, 4, 4), walls=False)
+    args = write_c_host_inputs(tmp_path, sc)
+    r = subprocess.run([exe, *args, str(sc.n), "1", str(tmp_path / "out.bin")], capture_output=True, text=True)
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    assert "CUDA ERROR: FluidSetupCUDA" in r.stderr and "no CUDA device" in r.stderr
+
