@@ -331,7 +331,11 @@ sphmp_status sphmp_get_params(const sphmp_ctx* ctx, sphmp_params* p);
 /* Run all later work of this context on `stream` (a cudaStream_t; NULL = the
    context's own stream). */
 sphmp_status sphmp_set_stream(sphmp_ctx* ctx, void* stream);
+/* Wait for the context's work; returns the first device error recorded since the
+   last check (and clears it). */
 sphmp_status sphmp_sync(sphmp_ctx* ctx);
+/* Active particle slots (read back from the device after steps with a device
+   emitter, which waits for the context's stream); 0 for NULL, -1 if that read fails. */
 int32_t sphmp_num_particles(const sphmp_ctx* ctx);
 
 /* ---- host transfers (reference TransferToCUDA / TransferFromCUDA / EmitUpdateCUDA,

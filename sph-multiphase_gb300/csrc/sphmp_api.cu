@@ -913,6 +913,10 @@ sphmp_status sphmp_set_device_emitter(sphmp_ctx* c, const sphmp_emitter* e, int3
     }
     if (!(e->spacing > 0.0f) || !(e->radius >= 0.0f) || layers < 0 || phase < 0 || phase >= SPHMP_MAX_PHASES)
         return fail(SPHMP_ERR_INVALID_ARG, "emitter needs spacing > 0, radius >= 0, layers >= 0, phase in [0, 3)");
+    const double side = 2.0 * (double)(int)(e->radius / e->spacing) + 1.0;
+    if (side * side * (double)layers > 1.0e9)
+        return fail(SPHMP_ERR_INVALID_ARG, "emitter has %.3g lattice sites per emission (at most 1e9)",
+                    side * side * (double)layers);
     const sphmp_params& p = c->prm;
     if (!(p.massArr[phase] > 0.0f) || !isfinite(p.massArr[phase]))
         return fail(SPHMP_ERR_BAD_MASS, "phase %d has mass %g (massArr)", phase, (double)p.massArr[phase]);

@@ -89,3 +89,19 @@ def test_device_emission_stops_at_capacity(built):
     dev.sync()
     assert dev.n == sc.n + 60 and dev.device_errors() == 0
     dev.close()
+
+
+def test_device_emitter_rejects_bad_settings(built):
+    sc, disp, calc = _scene(spare=10)
+    dev = sphmp.Context(sc.params)
+    dev.upload_aos(disp[:sc.n], calc[:sc.n])
+    bad = [dict(EMITTER, spacing=0.0), dict(EMITTER, radius=-1.0), dict(EMITTER, radius=100.0, spacing=1e-4)]
+    for e in bad:
+        with pytest.raises(sphmp.SphmpError) as err:
+            dev.set_device_emitter(**e, interval=3)
+        assert err.value.status == abi.ERR_INVALID_ARG
+    with pytest.raises(sphmp.SphmpError) as err:
+        dev.set_device_emitter(**EMITTER, phase=5, interval=3)
+    assert err.value.status == abi.ERR_INVALID_ARG
+    dev.close()
+
