@@ -39,16 +39,16 @@ bubbles and with the same lattice all liquid, after 600 plain steps, 16 steps of
 8 dt against 128 plain steps, particles matched by bornid: rms and max relative
 density error and rms velocity error of the liquid, and the wall time of both.
 
---workload device_ref times the reference's own GPU kernels (fluid_system_kern.cu
-built unmodified for sm_103a, driven with the reference's launch sequence by
-oracle/ref_gpu.py; checked against the oracle in tests/test_gpu_device_ref.py)
-beside this library on the same 2^20-particle lattice with the reference's only
+--workload device_ref measures the 2^20-particle lattice with the reference's only
 EOS (Tait) and liquid phases (1000 / 800 kg/m^3: Tait diverges next to the
-1.2 kg/m^3 gas), plain SPH (RunSimpleSPH: sort, density, force, advance). The
-reference is timed as its wrappers run (a host synchronisation after every call)
-and stream-ordered; the library in the reference call order and fused, both
-replayed from captured graphs. Needs oracle/_ref/sph_ref_kern.cubin (built where
-the reference checkout exists).
+1.2 kg/m^3 gas), plain SPH (RunSimpleSPH: sort, density, force, advance), in two
+arms: this library (reference call order and fused, captured graphs), and with
+--impl reference the reference's own GPU kernels (fluid_system_kern.cu built
+unmodified for sm_103a, driven with the reference's launch sequence by
+oracle/ref_gpu.py, checked against the oracle in tests/test_gpu_device_ref.py),
+timed as its wrappers run (a host synchronisation after every call) and
+stream-ordered. The reference arm needs oracle/_ref/sph_ref_kern.cubin (built
+where the reference checkout exists).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
        [--workload batched|large_step|device_ref]
@@ -523,82 +523,117 @@ def run_large_step(args):
     return 0
 
 
-def run_device_ref(args):
+def device_ref_scene(seed):
+    """The benchmark lattice with the reference's only EOS (Tait) and liquid phases:
+    the 1.2 kg/m^3 gas blobs become phase-0 liquid (Tait diverges next to them)."""
+    import numpy as np
+    from sphmp import abi, scenes
+    sc = scenes.blobs_3phase(seed=seed, eos=abi.EOS_TAIT, multiphase=0)
+    gas = sc.calc["restdens"][:sc.n] == np.float32(sc.params.densArr[2])
+    sc.calc["restdens"][:sc.n][gas] = sc.params.densArr[0]
+    sc.calc["mass"][:sc.n][gas] = sc.params.massArr[0]
+    calc = sc.calc[:sc.n].copy()
+    bnd = sc.disp["type"][:sc.n] == abi.TYPE_BOUNDARY
+    calc["accel"][bnd] = 0  # as the oracle state starts
+    calc["pressure"][bnd] = 0
+    return sc, np.ascontiguousarray(sc.disp[:sc.n]), calc
+
+
+DEVICE_REF_METRIC = "particle-steps/s at 1M, Tait liquid lattice, plain SPH (1 GB300)"
+
+
+def device_ref_config(sc, what):
+    return {"workload": "blobs_128x64x128_liquid_tait", "fluid_particles": sc.n_fluid,
+            "boundary_particles": sc.n_boundary, "eos": "Tait (the reference's)", "phases": "1000 / 800 kg/m^3 blobs",
+            "step": "plain SPH (RunSimpleSPH: sort, density + pressure, force, advance)", "timed": what}
+
+
+def _timed(stream, fn):
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    fn()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def run_device_ref_library(args):
+    """This library on the device-ref scene (the sphmp arm of --workload device_ref)."""
     import numpy as np
     import torch
 
     import sphmp
-    from oracle import ref_gpu
-    from sphmp import abi, scenes
+    from sphmp import abi
 
-    if not ref_gpu.available():
-        print(json.dumps({"workload": "device_ref", "unavailable": "oracle/_ref/sph_ref_kern.cubin not built "
-                          "(the reference checkout is needed at build time)"}))
-        return 0
-    sc = scenes.blobs_3phase(seed=args.seed, eos=abi.EOS_TAIT, multiphase=0)
-    gas = sc.calc["restdens"][:sc.n] == np.float32(sc.params.densArr[2])
-    sc.calc["restdens"][:sc.n][gas] = sc.params.densArr[0]
-    sc.calc["mass"][:sc.n][gas] = sc.params.massArr[0]
-    p = sc.params
-    calc = sc.calc[:sc.n].copy()
-    bnd = sc.disp["type"][:sc.n] == abi.TYPE_BOUNDARY
-    calc["accel"][bnd] = 0
-    calc["pressure"][bnd] = 0
-    disp = np.ascontiguousarray(sc.disp[:sc.n])
+    sc, disp, calc = device_ref_scene(args.seed)
     K, W = args.steps, args.warmup
     stream = torch.cuda.Stream()
-
-    def timed(fn):
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        fn()
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        return ev0.elapsed_time(ev1)
-
     res = {}
     with ClockSampler(torch.cuda.current_device()) as clk:
-        R = ref_gpu.RefGPU(p, disp, calc, stream=stream)
-        R.before_first_step()
-        R.step(W)
-        R.sync_each = True
-        res["device_ref"] = timed(lambda: R.step(K))
-        R.sync_each = False
-        R.step(W)
-        res["device_ref_stream_ordered"] = timed(lambda: R.step(K))
-        d, _ = R.records(abi.display_dtype(), abi.calc_dtype())
-        ref_finite = bool(np.isfinite(d["pos"]).all())
-        R.close()
-        ctx = sphmp.Context(p)
+        ctx = sphmp.Context(sc.params)
         ctx.set_stream(stream.cuda_stream)
         ctx.upload_aos(disp, calc)
         ctx.before_first_step()
-        for name, sched in (("sphmp_reference_order", abi.SCHEDULE_REFERENCE), ("sphmp_fused", abi.SCHEDULE_FUSED)):
+        for name, sched in (("reference_order", abi.SCHEDULE_REFERENCE), ("fused", abi.SCHEDULE_FUSED)):
             ctx.step(W, sched, use_graph=True)
-            res[name] = timed(lambda: ctx.step(K, sched, use_graph=True))
+            res[name] = _timed(stream, lambda: ctx.step(K, sched, use_graph=True))
         ctx.sync()
-        ours_finite = bool(np.isfinite(ctx.download_field(abi.F_POS)).all())
+        finite = bool(np.isfinite(ctx.download_field(abi.F_POS)).all())
         ctx.close()
     nf = sc.n_fluid
-    out = {k: {"value": nf * K / (ms * 1e-3), "ms_per_step": ms / K} for k, ms in res.items()}
-    line = {
-        "metric": "particle-steps/s on one GB300: the reference's own GPU kernels against this library",
-        "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": W, "higher_is_better": True, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": "blobs_128x64x128_liquid_tait", "fluid_particles": nf, "boundary_particles": sc.n_boundary,
-                   "eos": "Tait (the reference's)", "phases": "1000 / 800 kg/m^3 blobs", "step": "plain SPH "
-                   "(RunSimpleSPH: sort, density + pressure, force, advance)", "device_ref_sort": "stable key sort "
-                   "(torch.sort) in place of thrust::sort_by_key",
-                   "device_ref_sync": "device_ref: host synchronisation after every call, as the reference's "
-                   "wrappers; device_ref_stream_ordered: none"},
-        "results": out,
-        "speedup_vs_device_ref": {k: out[k]["value"] / out["device_ref"]["value"] for k in
-                                  ("sphmp_reference_order", "sphmp_fused", "device_ref_stream_ordered")},
-        "finite": {"device_ref": ref_finite, "sphmp": ours_finite},
-        "clocks": clk.summary(),
-    }
+    line = {"metric": DEVICE_REF_METRIC, "value": nf * K / (res["reference_order"] * 1e-3), "unit": UNIT,
+            "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": res["reference_order"] / K,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": device_ref_config(sc, "reference call order, captured graph (value); fused schedule (fused)"),
+            "fused": {"value": nf * K / (res["fused"] * 1e-3), "ms_per_step": res["fused"] / K},
+            "finite": finite, "gpu_launches": KERNELS_PER_FUSED_STEP * K,  # the reference-order step: 13 kernels too
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+def run_device_ref_reference(args):
+    """The reference's own GPU kernels on the device-ref scene (the reference arm of
+    --workload device_ref): fluid_system_kern.cu built for sm_103a, driven by
+    oracle/ref_gpu.py with the reference's launch sequence."""
+    import numpy as np
+    import torch
+
+    from oracle import ref_gpu
+    from sphmp import abi
+
+    if not ref_gpu.available():
+        print(json.dumps({"impl": "reference", "workload": "device_ref",
+                          "unavailable": "oracle/_ref/sph_ref_kern.cubin not built (needs the reference checkout "
+                                         "at build time)"}))
+        return 0
+    sc, disp, calc = device_ref_scene(args.seed)
+    K, W = args.steps, args.warmup
+    stream = torch.cuda.Stream()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        R = ref_gpu.RefGPU(sc.params, disp, calc, stream=stream)
+        R.before_first_step()
+        R.step(W)
+        R.sync_each = True
+        ms = _timed(stream, lambda: R.step(K))
+        R.sync_each = False
+        R.step(W)
+        ms_async = _timed(stream, lambda: R.step(K))
+        d, _ = R.records(abi.display_dtype(), abi.calc_dtype())
+        finite = bool(np.isfinite(d["pos"]).all())
+        R.close()
+    nf = sc.n_fluid
+    line = {"metric": DEVICE_REF_METRIC, "value": nf * K / (ms * 1e-3), "unit": UNIT, "impl": "reference",
+            "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic",
+            "config": device_ref_config(sc, "the reference's kernels with a host synchronisation after every call, "
+                                            "as its wrappers (value); stream-ordered (stream_ordered); "
+                                            "thrust::sort_by_key replaced by the same stable key sort (torch.sort)"),
+            "stream_ordered": {"value": nf * K / (ms_async * 1e-3), "ms_per_step": ms_async / K},
+            "finite": finite, "clocks": clk.summary()}
     print(json.dumps(line))
     return 0
 
@@ -617,19 +652,19 @@ def main():
     ap.add_argument("--profile-every", type=int, default=100, help="steps between per-stage timing samples")
     ap.add_argument("--workload", default="blobs", choices=["blobs", "batched", "large_step", "device_ref"],
                     help="blobs: the headline 2^20-particle scene; batched: 512 tiled bubble scenes; "
-                         "large_step: one 8 dt step against 8 plain steps; device_ref: the reference's own GPU "
-                         "kernels beside this library")
+                         "large_step: one 8 dt step against 8 plain steps; device_ref: the Tait liquid lattice "
+                         "(with --impl reference: the reference's own GPU kernels)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "device_ref":
+        return run_device_ref_reference(args) if args.impl == "reference" else run_device_ref_library(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
     if args.workload == "large_step":
         return run_large_step(args)
-    if args.workload == "device_ref":
-        return run_device_ref(args)
     return run_gpu(args)
 
 
