@@ -6,8 +6,8 @@ Builds and loads:
   * libsphref.so  — the reference's own kernel sources compiled as host C++
     (oracle/ref/build_ref.sh), when they were built on this machine.
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
-module. The CUDA product never does.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg and its
+reference arm (--impl reference) import this module. The CUDA product never does.
 """
 import ctypes as C
 import os
