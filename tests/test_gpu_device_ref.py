@@ -8,7 +8,7 @@ built (it needs the reference checkout at build time)."""
 import numpy as np
 import pytest
 
-from helpers import bits_equal, field_err, in_grid_fluid, oracle_state
+from helpers import bits_equal, device_ctx, download_state, field_err, in_grid_fluid, oracle_state
 from oracle import oracle as O
 from oracle import ref_gpu
 from sphmp import abi, scenes
@@ -50,3 +50,44 @@ def test_device_ref_matches_oracle(built):
         O.step(p, s, abi.SCHEDULE_REFERENCE, 1)
         _compare(R, s)
     R.close()
+
+
+@pytest.mark.slow
+def test_library_matches_device_ref_at_full_size(built):
+    """The library against the reference's own GPU kernels on the benchmark lattice
+    (1,048,576 fluid + 267,030 boundary particles) with the reference's Tait EOS and
+    liquid phases: the first sort (GetParticleIndex .. RearrageData) bit for bit on
+    every slot, then one RunSimpleSPH step in the reference call order: sort arrays
+    bit for bit, densities, positions and velocities within RTOL."""
+    sc = scenes.blobs_3phase(seed=2, eos=abi.EOS_TAIT, multiphase=0)
+    gas = sc.calc["restdens"][:sc.n] == np.float32(sc.params.densArr[2])
+    sc.calc["restdens"][:sc.n][gas] = sc.params.densArr[0]
+    sc.calc["mass"][:sc.n][gas] = sc.params.massArr[0]
+    p = sc.params
+    calc = sc.calc[:sc.n].copy()
+    bnd = sc.disp["type"][:sc.n] == abi.TYPE_BOUNDARY
+    calc["accel"][bnd] = 0
+    calc["pressure"][bnd] = 0
+    R = ref_gpu.RefGPU(p, sc.disp[:sc.n], calc)
+    R.before_first_step()
+    ctx = device_ctx(sc)
+    ctx.before_first_step()
+    for step in range(2):
+        srt = R.sort_arrays()
+        g = download_state(ctx)
+        for k in ("mgcell", "midsort", "mgridoff", "mgridcnt"):
+            assert bits_equal(srt[k], g[k]), (step, k)
+        if step == 1:
+            d, c = R.records(abi.display_dtype(), abi.calc_dtype())
+            f = in_grid_fluid(g)
+            assert f.sum() > 1_000_000
+            assert field_err(g["dens"][f], c["dens"][f]) < RTOL
+            for k, ref in (("pos", d["pos"]), ("vel", c["vel"])):
+                assert field_err(g[k][f], ref[f]) < RTOL, k
+            break
+        R.step(1)
+        ctx.step(1, abi.SCHEDULE_REFERENCE, use_graph=False)
+        ctx.sync()
+    R.close()
+    ctx.close()
+
