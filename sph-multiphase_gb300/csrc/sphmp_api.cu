@@ -167,7 +167,7 @@ void free_buffers(sphmp_ctx* c) {
     for (int f = 0; f < kNumFloat4Fields; f++)
         for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.velxcor, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
-                    B.key, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
+                    B.key, B.octk, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
                     B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
                     B.act, B.act_n, B.nact, B.frame, c->stage};
     for (void* q : ptrs) cudaFree(q);
@@ -197,6 +197,7 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.mgridoff, G));
     CK(dalloc(&B.mgridcnt, G));
     CK(dalloc(&B.key, N));
+    CK(dalloc(&B.octk, N));
     CK(dalloc(&B.arank, N));
     CK(dalloc(&B.sidx, N));
     CK(dalloc(&B.ccount, G + 1));

@@ -100,6 +100,7 @@ struct DevBuffers {
     int32_t* mgridoff;  // [G]
     int32_t* mgridcnt;  // [G]
     uint32_t* key;      // [cap] unsorted cell key per slot
+    uint8_t* octk;      // [cap] octant (h-subcell inside the cell) per slot, in-grid slots only
     uint32_t* arank;    // [cap] rank inside the bin (atomic order; exact for out-of-grid)
     uint32_t* sidx;     // [cap] scatter target (pre-sort slots grouped by cell)
     uint32_t* ccount;   // [G + 1] histogram, bin G = out-of-grid

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(kHashBlock) k_hash(const __grid_constant__ Dev
         key = cell_key(P, p.x, p.y, p.z);
         B.key[i] = key;
         B.mgcell[i] = key;
+        if (key != kUndef) B.octk[i] = (uint8_t)octant_of(P, p);  // for the per-cell octant order
     }
     const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
     const bool und = valid && key == kUndef;
@@ -295,7 +296,7 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
             B.midsort[start + idx] = v[r];
             B.mgcell[start + idx] = c;
             B.mgndx[start + idx] = idx;
-            key[r] = (octant_of(P, pos_in[B.opos[v[r]]]) << 8) | idx;
+            key[r] = ((uint32_t)B.octk[v[r]] << 8) | idx;
         }
     }
     // octant order: sort (octant, member index)
@@ -323,7 +324,9 @@ __global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ 
     __shared__ uint32_t sm[kThreads / 32][kWarpSortMax];
     uint32_t* wsm = sm[threadIdx.x >> 5];
     const int nwarps = (gridDim.x * kThreads) >> 5;
-    for (int c = (blockIdx.x * kThreads + threadIdx.x) >> 5; c < P.G; c += nwarps) {
+    const uint32_t nact = *B.act_n;  // the occupied cells, listed by the scan
+    for (uint32_t a = (blockIdx.x * kThreads + threadIdx.x) >> 5; a < nact; a += (uint32_t)nwarps) {
+        const uint32_t c = B.act[a];
         const uint32_t start = B.cstart[c];
         const uint32_t cnt = B.cstart[c + 1] - start;
         if (cnt == 0 || cnt > (uint32_t)kWarpSortMax) continue;
@@ -372,7 +375,7 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
         }
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < M; k += blockDim.x)
-            sm[k] = k < cnt ? ((octant_of(P, pos_in[B.opos[B.midsort[start + k]]]) << 13) | k) : 0xFFFFFFFFu;
+            sm[k] = k < cnt ? (((uint32_t)B.octk[B.midsort[start + k]] << 13) | k) : 0xFFFFFFFFu;
         __syncthreads();
         cta_bitonic(sm, M);
         for (uint32_t q = threadIdx.x; q <= cnt && q < M + 1; q += blockDim.x) {
