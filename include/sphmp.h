@@ -45,7 +45,8 @@ typedef enum sphmp_status {
     SPHMP_ERR_STATE = 7,           /* call order violated (e.g. force before sort) */
     SPHMP_ERR_NO_DEVICE = 8,       /* no CUDA device / extension not loadable */
     SPHMP_ERR_BAD_MASS = 9,        /* fluid particle with mass <= 0 */
-    SPHMP_ERR_GRID = 10            /* grid parameters inconsistent (res < 3, total overflow) */
+    SPHMP_ERR_GRID = 10,           /* grid parameters inconsistent (res < 3, total overflow) */
+    SPHMP_ERR_TIMEOUT = 11         /* a bounded device wait ran out (a tensor-core chain did not complete) */
 } sphmp_status;
 
 /* Equation of state used by the density pass. */

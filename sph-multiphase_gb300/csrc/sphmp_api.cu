@@ -13,6 +13,7 @@
 #include "sphmp.h"
 #include "sphmp_emit.h"
 #include "sphmp_internal.h"
+#include "sphmp_learned.h"
 #include "sphmp_legacy.h"
 
 using namespace sphmp;
@@ -53,6 +54,15 @@ struct sphmp_ctx {
     bool emit_on = false;
     bool n_stale = false;
     DevEmitter emitter{};
+    // learned large step (allocated by the first corrected step): per row of the
+    // internal order, the features, bornid (-1: no features), network outputs
+    // and applied corrections of the last corrected step
+    float* lfeat = nullptr;
+    int32_t* lids = nullptr;
+    float* ly = nullptr;
+    float* lcorr = nullptr;
+    int lrows = 0;
+    void* xstage = nullptr;  // sphmp_copy_state: fractions and (g - a) of the source
 };
 
 namespace {
@@ -271,6 +281,7 @@ sphmp_status take_device_errors(sphmp_ctx* c, uint32_t* bits_out) {
                                    : s == SPHMP_ERR_BAD_MASS       ? "fluid particle with mass <= 0 or not finite"
                                    : s == SPHMP_ERR_CELL_OVERFLOW  ? "a grid cell holds more than 8192 particles"
                                    : s == SPHMP_ERR_CAPACITY       ? "device-side emission reached the capacity"
+                                   : s == SPHMP_ERR_TIMEOUT        ? "a tensor-core wait of the corrector ran out"
                                                                    : "device error";
                 return fail((sphmp_status)s, "device reported: %s", what);
             }
@@ -341,8 +352,16 @@ struct StageTimer {
     }
 };
 
-// Queue one full step on the context stream (no host synchronisation).
-sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
+// A corrected large step: the network and the step length it corrects.
+struct LargeStep {
+    sphmp_corrector* cor;
+    float dt;
+};
+
+// Queue one full step on the context stream (no host synchronisation). With
+// `L` (fused schedule only), the features are taken after the density pass and
+// the network's correction is applied to the step's result.
+sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr, const LargeStep* L = nullptr) {
     const DevParams P = dev_params(c);
     const cudaStream_t s = c->stream;
     auto mark = [&](const char* nm) {
@@ -374,6 +393,13 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
     mark("density");
     const DevParams PL = dev_params(c);  // neighbour passes read the list
     if (schedule == SPHMP_SCHEDULE_FUSED) {
+        if (L) {
+            const float* gv = c->prm.gravity;
+            const float gabs = sqrtf(gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]);
+            const float vs = sqrtf(fmaxf(gabs, 1e-3f) * c->prm.smoothradius);
+            launch_features(PL, c->B, c->cur, c->lfeat, c->lids, vs, L->dt, s);
+            mark("features");
+        }
         run_force_drift(c, true, PL.multiphase != 0, s);
         mark("force_drift");
         if (PL.st_on) {
@@ -383,6 +409,12 @@ sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr) {
         launch_pass_c(PL, c->B, c->cur, s);
         mark(PL.multiphase ? "alpha_correct_advance" : "advance");
         swap_all(c);
+        if (L) {
+            CK(corrector_forward_on(L->cor, c->lfeat, PL.n, c->ly, c->B.err, s));
+            launch_apply_correction(PL, c->B, c->cur, c->ly, corrector_out_scale(L->cor), c->lids, L->dt, c->lcorr, s);
+            c->lrows = PL.n;
+            mark("correction");
+        }
         c->nbr_valid = false;  // positions moved
         c->oct_valid = false;
         c->pos_sorted = false;
@@ -498,6 +530,8 @@ sphmp_status sphmp_destroy(sphmp_ctx* c) {
     }
     drop_graph(c);
     free_buffers(c);
+    void* lbufs[] = {c->lfeat, c->lids, c->ly, c->lcorr, c->xstage};
+    for (void* q : lbufs) cudaFree(q);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SPHMP_OK;
@@ -567,9 +601,10 @@ sphmp_status sphmp_device_errors(sphmp_ctx* c, uint32_t* bits) {
 
 // ---- transfers ----
 
+// Records [start, end) from the host, or (`staged`) already in the staging buffer.
 static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp, const sphmp_calc_pack* calc,
-                                   int start, int end) {
-    if (!disp || !calc) return fail(SPHMP_ERR_INVALID_ARG, "record pointers are NULL");
+                                   int start, int end, bool staged = false) {
+    if (!staged && (!disp || !calc)) return fail(SPHMP_ERR_INVALID_ARG, "record pointers are NULL");
     if (start < 0 || end < start) return fail(SPHMP_ERR_INVALID_ARG, "bad range [%d, %d)", start, end);
     if (end > c->cap) return fail(SPHMP_ERR_CAPACITY, "%d particles exceed the capacity %d", end, c->cap);
     const int m = end - start;
@@ -577,7 +612,7 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     auto* d_calc = reinterpret_cast<sphmp_calc_pack*>(reinterpret_cast<char*>(c->stage) +
                                                       sizeof(sphmp_display_pack) * (size_t)c->cap);
     if (take_device_errors(c, nullptr) == SPHMP_ERR_CUDA) return SPHMP_ERR_CUDA;  // clear stale bits
-    if (m > 0) {
+    if (m > 0 && !staged) {
         CK(cudaMemcpyAsync(d_disp, disp, sizeof(sphmp_display_pack) * (size_t)m, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemcpyAsync(d_calc, calc, sizeof(sphmp_calc_pack) * (size_t)m, cudaMemcpyHostToDevice, c->stream));
     }
@@ -731,6 +766,33 @@ sphmp_status sphmp_download_field(sphmp_ctx* c, int32_t field, void* host, int32
     return SPHMP_OK;
 }
 
+// A per-particle field (slot order, n entries) from device memory `dev` into the state.
+static sphmp_status unpack_field_staged(sphmp_ctx* c, int field, const void* dev, int n) {
+    if (field == SPHMP_F_ALPHA && !c->alpha_advanced) {
+        // keep the start-of-step fractions in the other buffer, then overwrite the current ones
+        CK(cudaMemcpyAsync(c->B.f4[ALPHA][c->cur[ALPHA] ^ 1], c->B.f4[ALPHA][c->cur[ALPHA]],
+                           sizeof(float4) * (size_t)c->cap, cudaMemcpyDeviceToDevice, c->stream));
+        c->cur[ALPHA] ^= 1;
+        CK(cudaMemcpyAsync(c->B.f4[ALPHA][c->cur[ALPHA]], c->B.f4[ALPHA][c->cur[ALPHA] ^ 1],
+                           sizeof(float4) * (size_t)c->cap, cudaMemcpyDeviceToDevice, c->stream));
+        c->alpha_advanced = true;
+    }
+    const int a_cur = c->cur[ALPHA];
+    const int a_pre = c->alpha_advanced ? a_cur ^ 1 : a_cur;
+    const DevParams P = dev_params(c);
+    launch_unpack_field(P, c->B, c->cur, field, a_cur, a_pre, dev, n, c->stream);
+    CHECK_LAUNCH("unpack field");
+    if (field == SPHMP_F_POS) {
+        c->nbr_valid = false;
+        c->oct_valid = false;
+        c->oct_built = false;
+        c->pos_sorted = false;
+    }
+    drop_graph(c);
+    CK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
 sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, int32_t n) {
     if (sphmp_status st = need_ctx(c)) return st;
     if (!host) return fail(SPHMP_ERR_INVALID_ARG, "host pointer is NULL");
@@ -768,30 +830,8 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
         return SPHMP_OK;
     }
     if (n < 0 || n > c->n) return fail(SPHMP_ERR_CAPACITY, "n %d outside [0, %d]", n, c->n);
-    if (field == SPHMP_F_ALPHA && !c->alpha_advanced) {
-        // keep the start-of-step fractions in the other buffer, then overwrite the current ones
-        CK(cudaMemcpyAsync(c->B.f4[ALPHA][c->cur[ALPHA] ^ 1], c->B.f4[ALPHA][c->cur[ALPHA]],
-                           sizeof(float4) * (size_t)c->cap, cudaMemcpyDeviceToDevice, c->stream));
-        c->cur[ALPHA] ^= 1;
-        CK(cudaMemcpyAsync(c->B.f4[ALPHA][c->cur[ALPHA]], c->B.f4[ALPHA][c->cur[ALPHA] ^ 1],
-                           sizeof(float4) * (size_t)c->cap, cudaMemcpyDeviceToDevice, c->stream));
-        c->alpha_advanced = true;
-    }
-    const int a_cur = c->cur[ALPHA];
-    const int a_pre = c->alpha_advanced ? a_cur ^ 1 : a_cur;
     CK(cudaMemcpyAsync(c->stage, host, sizeof(float) * (size_t)field_width(field) * n, cudaMemcpyHostToDevice, c->stream));
-    const DevParams P = dev_params(c);
-    launch_unpack_field(P, c->B, c->cur, field, a_cur, a_pre, c->stage, n, c->stream);
-    CHECK_LAUNCH("unpack field");
-    if (field == SPHMP_F_POS) {
-        c->nbr_valid = false;
-        c->oct_valid = false;
-        c->oct_built = false;
-        c->pos_sorted = false;
-    }
-    drop_graph(c);
-    CK(cudaStreamSynchronize(c->stream));
-    return SPHMP_OK;
+    return unpack_field_staged(c, field, c->stage, n);
 }
 
 // ---- per-pass entry points ----
@@ -1049,6 +1089,73 @@ int32_t sphmp_step_profile(sphmp_ctx* c, int32_t schedule, float* ms, char* name
         }
     }
     return n;
+}
+
+sphmp_status sphmp_step_large(sphmp_ctx* c, sphmp_corrector* cor, int32_t factor, int32_t nsteps) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (factor < 1 || nsteps < 0) return fail(SPHMP_ERR_INVALID_ARG, "factor must be >= 1 and nsteps >= 0");
+    if (cor && corrector_device(cor) != c->device)
+        return fail(SPHMP_ERR_INVALID_ARG, "the corrector lives on another device");
+    if (nsteps == 0) return SPHMP_OK;
+    if (cor && !c->lfeat) {
+        const size_t N = (size_t)c->cap;
+        CK(cudaMalloc(&c->lfeat, sizeof(float) * SPHMP_LC_FEATURES * N));
+        CK(cudaMalloc(&c->lids, sizeof(int32_t) * N));
+        CK(cudaMalloc(&c->ly, sizeof(float) * 4 * N));
+        CK(cudaMalloc(&c->lcorr, sizeof(float) * 4 * N));
+    }
+    const float dt0 = c->prm.dt;
+    c->prm.dt = dt0 * (float)factor;
+    const LargeStep L{cor, c->prm.dt};
+    sphmp_status st = SPHMP_OK;
+    for (int t = 0; t < nsteps && !st; t++) st = enqueue_step(c, SPHMP_SCHEDULE_FUSED, nullptr, cor ? &L : nullptr);
+    c->prm.dt = dt0;
+    return st;
+}
+
+sphmp_status sphmp_learned_features(sphmp_ctx* c, float* feat, int32_t* ids, float* corr, int32_t* count) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!c->lfeat || c->lrows <= 0) return fail(SPHMP_ERR_STATE, "no corrected large step has run");
+    const size_t n = (size_t)c->lrows;
+    if (feat) CK(cudaMemcpyAsync(feat, c->lfeat, sizeof(float) * SPHMP_LC_FEATURES * n, cudaMemcpyDeviceToDevice, c->stream));
+    if (ids) CK(cudaMemcpyAsync(ids, c->lids, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
+    if (corr) CK(cudaMemcpyAsync(corr, c->lcorr, sizeof(float) * 4 * n, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (count) *count = c->lrows;
+    return take_device_errors(c, nullptr);
+}
+
+sphmp_status sphmp_copy_state(sphmp_ctx* dst, sphmp_ctx* src) {
+    if (!dst || !src) return fail(SPHMP_ERR_INVALID_ARG, "context is NULL");
+    if (dst == src) return fail(SPHMP_ERR_INVALID_ARG, "source and destination are the same context");
+    if (dst->device != src->device) return fail(SPHMP_ERR_INVALID_ARG, "contexts on different devices");
+    if (dst->prm.nphase != src->prm.nphase) return fail(SPHMP_ERR_INVALID_ARG, "phase counts differ");
+    if (sphmp_status st = refresh_n(src)) return st;
+    const int n = src->n;
+    if (n > dst->cap) return fail(SPHMP_ERR_CAPACITY, "%d particles exceed the destination's capacity %d", n, dst->cap);
+    if (!dst->xstage) CK(cudaMalloc(&dst->xstage, sizeof(float) * 6 * (size_t)(dst->cap > 0 ? dst->cap : 1)));
+    CK(cudaStreamSynchronize(dst->stream));  // the destination's staging buffers are idle
+    auto* d_disp = reinterpret_cast<sphmp_display_pack*>(dst->stage);
+    auto* d_calc = reinterpret_cast<sphmp_calc_pack*>(reinterpret_cast<char*>(dst->stage) +
+                                                      sizeof(sphmp_display_pack) * (size_t)dst->cap);
+    float* xa = static_cast<float*>(dst->xstage);
+    float* xg = xa + 3 * (size_t)dst->cap;
+    // what sphmp_save_state writes: the records in slot order, the fractions, g - a
+    const DevParams PS = dev_params(src);
+    const int a_cur = src->cur[ALPHA];
+    const int a_pre = src->alpha_advanced ? a_cur ^ 1 : a_cur;
+    launch_pack_aos(PS, src->B, src->cur, d_disp, d_calc, n, src->stream);
+    launch_pack_field(PS, src->B, src->cur, SPHMP_F_ALPHA, a_cur, a_pre, xa, n, src->stream);
+    launch_pack_field(PS, src->B, src->cur, SPHMP_F_APREV, a_cur, a_pre, xg, n, src->stream);
+    CHECK_LAUNCH("pack state");
+    CK(cudaStreamSynchronize(src->stream));
+    // what sphmp_load_state does with them
+    if (sphmp_status st = upload_records(dst, nullptr, nullptr, 0, n, true)) return st;
+    if (n > 0) {
+        if (sphmp_status st = unpack_field_staged(dst, SPHMP_F_ALPHA, xa, n)) return st;
+        if (sphmp_status st = unpack_field_staged(dst, SPHMP_F_APREV, xg, n)) return st;
+    }
+    return SPHMP_OK;
 }
 
 sphmp_status sphmp_conservation(sphmp_ctx* c, double* out, int32_t nout) {

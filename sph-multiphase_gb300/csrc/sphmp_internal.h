@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include "sphmp.h"
+#include "sphmp_learned.h"
 
 namespace sphmp {
 
@@ -199,6 +200,14 @@ void launch_set_count(const DevBuffers& B, int n, cudaStream_t s);
 // device-side emission into the current buffers (one block)
 void launch_emit(const DevParams& P, const DevBuffers& B, const int* cur, const DevEmitter& E, cudaStream_t s);
 
+// learned large step (sphmp_learned.cu): the corrector's features of every
+// in-grid fluid particle after the density pass (feat [n][48], ids = bornid or
+// -1), and the correction of the step's result by the network outputs y [n][4]
+void launch_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids, float vs,
+                     float dt_large, cudaStream_t s);
+void launch_apply_correction(const DevParams& P, const DevBuffers& B, const int* cur, const float* y,
+                             const float* out_scale, const int32_t* ids, float dt_large, float* corr, cudaStream_t s);
+
 // transfers (staging buffers hold reference records)
 void launch_unpack_aos(const DevParams& P, const DevBuffers& B, const int* cur, const sphmp_display_pack* d,
                        const sphmp_calc_pack* c, int start, int end, cudaStream_t s);
@@ -209,5 +218,10 @@ void launch_pack_field(const DevParams& P, const DevBuffers& B, const int* cur, 
                        int alpha_pre, void* stage, int n, cudaStream_t s);
 void launch_unpack_field(const DevParams& P, const DevBuffers& B, const int* cur, int field, int alpha_cur,
                          int alpha_pre, const void* stage, int n, cudaStream_t s);
+
+// the corrector network as the large step uses it (sphmp_learned.cu)
+cudaError_t corrector_forward_on(sphmp_corrector* c, const float* x, int n, float* y, uint32_t* err, cudaStream_t s);
+const float* corrector_out_scale(const sphmp_corrector* c);  // device [4]
+int corrector_device(const sphmp_corrector* c);
 
 }  // namespace sphmp

@@ -1,0 +1,459 @@
+// sphmp_learned.cu — the learned large-step corrector: the per-particle feature
+// kernel, the correction kernel, and the network object (sphmp_corrector:
+// parameters, Adam state, training buffers) with its C ABI
+// (include/sphmp_learned.h). The network kernels are in sphmp_mlp.cu.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "sphmp.h"
+#include "sphmp_device.cuh"
+#include "sphmp_internal.h"
+#include "sphmp_learned.h"
+#include "sphmp_mlp.h"
+
+using namespace sphmp;
+using bf16 = __nv_bfloat16;
+
+// ---------------------------------------------------------------------------
+// Features and correction (one thread per particle of the internal order)
+// ---------------------------------------------------------------------------
+
+namespace sphmp {
+namespace {
+
+using dev::for_slot_list;
+
+// Features of an in-grid fluid particle, from the state after the density pass
+// of a step (pos, vel, 1/rho and p, fractions and rest density, g - a of the
+// last advance) over its neighbours closer than h. With w = (1 - r^2/h^2)^3,
+// g = (1 - r/h)^2, x_ij = x_i - x_j (metres), u = unit x_ij, vs = sqrt(|g| h):
+//   0-2  v_i / vs                     3   rho_i / rho0_i - 1
+//   4    p_i / (rho0_i vs^2)          5-7 alpha_i
+//   8-10 (g - a)_i dt_large / vs      11  sum_fluid w
+//   12-14 sum_fluid w x_ij / h        15-17 sum_fluid w (v_j - v_i) / vs
+//   18   sum_fluid w (rho_j/rho0_j - rho_i/rho0_i)
+//   19   sum_fluid w (p_j - p_i) / (rho0_i vs^2)
+//   20-22 sum_fluid w (alpha_j - alpha_i)
+//   23-28 sum_fluid w x x^T / h^2 (xx, yy, zz, xy, xz, yz)
+//   29-31 sum_fluid g u               32  sum_fluid g (v_j - v_i).u / vs
+//   33-35 sum_fluid g ((v_j - v_i) x u) / vs
+//   36-38 sum_fluid g (p_i + p_j) u / (rho0_i vs^2)
+//   39   fluid neighbours / 32        40  sum_boundary w
+//   41-43 sum_boundary w x_ij / h     44  boundary neighbours / 32
+//   45-47 sum_fluid g (alpha_j0 - alpha_i0) u
+__global__ void __launch_bounds__(128) k_features(const __grid_constant__ DevParams P,
+                                                  const __grid_constant__ DevBuffers B,
+                                                  const float4* __restrict__ pos4, const float4* __restrict__ vel4,
+                                                  const float4* __restrict__ alpha4,
+                                                  const float4* __restrict__ aprev4, float vs, float dt_large,
+                                                  float* __restrict__ feat, int32_t* __restrict__ ids) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= active_n(B)) return;
+    const float4 pi = pos4[s];
+    float4* out = reinterpret_cast<float4*>(feat + (size_t)s * mlp::kFeatures);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!(pi.w > 0.f) || B.mgcell[s] == kUndef) {
+        for (int i = 0; i < mlp::kFeatures / 4; i++) out[i] = zero;
+        ids[s] = -1;
+        return;
+    }
+    const float4 vi = vel4[s], ai = alpha4[s], gi = aprev4[s];
+    const float2 di = B.densp[s];
+    const float rhoi = 1.f / di.x, rho0 = ai.w;
+    const float ivs = 1.f / vs, ips = 1.f / (rho0 * vs * vs), ih = 1.f / P.h;
+    const float reli = rhoi / rho0;
+    float f[mlp::kFeatures];
+#pragma unroll
+    for (int k = 0; k < mlp::kFeatures; k++) f[k] = 0.f;
+    f[0] = vi.x * ivs; f[1] = vi.y * ivs; f[2] = vi.z * ivs;
+    f[3] = reli - 1.f;
+    f[4] = di.y * ips;
+    f[5] = ai.x; f[6] = P.nphase > 1 ? ai.y : 0.f; f[7] = P.nphase > 2 ? ai.z : 0.f;
+    f[8] = gi.x * dt_large * ivs; f[9] = gi.y * dt_large * ivs; f[10] = gi.z * dt_large * ivs;
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
+        const float dsq = dx * dx + dy * dy + dz * dz;
+        if (!(dsq < P.r2 && dsq > 0.f)) return;
+        const float r = sqrtf(dsq);
+        const float q2 = dsq / P.r2, q = r * ih;
+        const float w = (1.f - q2) * (1.f - q2) * (1.f - q2);
+        const float g = (1.f - q) * (1.f - q);
+        const float ux = dx / r, uy = dy / r, uz = dz / r;
+        if (pj.w < 0.f) {  // boundary
+            f[40] += w;
+            f[41] += w * dx * ih; f[42] += w * dy * ih; f[43] += w * dz * ih;
+            f[44] += 1.f / 32.f;
+            return;
+        }
+        const float4 vj = __ldg(&vel4[j]), aj = __ldg(&alpha4[j]);
+        const float2 dj = __ldg(&B.densp[j]);
+        const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
+        f[11] += w;
+        f[12] += w * dx * ih; f[13] += w * dy * ih; f[14] += w * dz * ih;
+        f[15] += w * dvx * ivs; f[16] += w * dvy * ivs; f[17] += w * dvz * ivs;
+        f[18] += w * (1.f / (dj.x * aj.w) - reli);
+        f[19] += w * (dj.y - di.y) * ips;
+        f[20] += w * (aj.x - ai.x);
+        f[21] += w * (P.nphase > 1 ? aj.y - ai.y : 0.f);
+        f[22] += w * (P.nphase > 2 ? aj.z - ai.z : 0.f);
+        f[23] += w * dx * dx * ih * ih; f[24] += w * dy * dy * ih * ih; f[25] += w * dz * dz * ih * ih;
+        f[26] += w * dx * dy * ih * ih; f[27] += w * dx * dz * ih * ih; f[28] += w * dy * dz * ih * ih;
+        f[29] += g * ux; f[30] += g * uy; f[31] += g * uz;
+        f[32] += g * (dvx * ux + dvy * uy + dvz * uz) * ivs;
+        f[33] += g * (dvy * uz - dvz * uy) * ivs;
+        f[34] += g * (dvz * ux - dvx * uz) * ivs;
+        f[35] += g * (dvx * uy - dvy * ux) * ivs;
+        const float pp = g * (di.y + dj.y) * ips;
+        f[36] += pp * ux; f[37] += pp * uy; f[38] += pp * uz;
+        f[39] += 1.f / 32.f;
+        const float da = g * (aj.x - ai.x);
+        f[45] += da * ux; f[46] += da * uy; f[47] += da * uz;
+    });
+#pragma unroll
+    for (int i = 0; i < mlp::kFeatures / 4; i++) out[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
+    ids[s] = B.bornid[__float_as_uint(gi.w)];
+}
+
+// Apply the network's outputs (times out_scale) to the step's result.
+__global__ void __launch_bounds__(256) k_apply_correction(const __grid_constant__ DevParams P,
+                                                          const __grid_constant__ DevBuffers B, float4* pos4,
+                                                          float4* vel4, float4* vev4, const float4* __restrict__ y,
+                                                          const float* __restrict__ out_scale,
+                                                          const int32_t* __restrict__ ids, float half_dt_over_ss,
+                                                          float4* __restrict__ corr) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= active_n(B)) return;
+    if (ids[s] < 0) {
+        corr[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const float4 o = y[s];
+    const float cx = o.x * out_scale[0], cy = o.y * out_scale[1], cz = o.z * out_scale[2];
+    const float cd = fmaxf(o.w * out_scale[3], -0.5f);
+    float4 v = vel4[s], e = vev4[s], p = pos4[s];
+    v.x += cx; v.y += cy; v.z += cz;
+    e.x += cx; e.y += cy; e.z += cz;
+    p.x += cx * half_dt_over_ss; p.y += cy * half_dt_over_ss; p.z += cz * half_dt_over_ss;
+    vel4[s] = v;
+    vev4[s] = e;
+    pos4[s] = p;
+    float2 d = B.densp[s];
+    d.x = d.x / (1.f + cd);
+    B.densp[s] = d;
+    corr[s] = make_float4(cx, cy, cz, cd);
+}
+
+}  // namespace
+
+void launch_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids, float vs,
+                     float dt_large, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_features<<<(P.n + 127) / 128, 128, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[VEL][cur[VEL]],
+                                                 B.f4[ALPHA][cur[ALPHA]], B.f4[APREV][cur[APREV]], vs, dt_large,
+                                                 feat, ids);
+}
+
+void launch_apply_correction(const DevParams& P, const DevBuffers& B, const int* cur, const float* y,
+                             const float* out_scale, const int32_t* ids, float dt_large, float* corr,
+                             cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_apply_correction<<<(P.n + 255) / 256, 256, 0, s>>>(
+        P, B, B.f4[POS][cur[POS]], B.f4[VEL][cur[VEL]], B.f4[VEV][cur[VEV]], reinterpret_cast<const float4*>(y),
+        out_scale, ids, 0.5f * dt_large / P.ss, reinterpret_cast<float4*>(corr));
+}
+
+}  // namespace sphmp
+
+// ---------------------------------------------------------------------------
+// The network object
+// ---------------------------------------------------------------------------
+
+struct sphmp_corrector {
+    int max_batch = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    int adam_step = 0;
+    // parameters
+    float* params = nullptr;  // [kParams] FP32 master
+    float* grads = nullptr;
+    float* adam_m = nullptr;
+    float* adam_v = nullptr;
+    bf16 *w1 = nullptr, *w2 = nullptr, *w3 = nullptr, *w4 = nullptr, *w2t = nullptr, *w3t = nullptr, *w4t = nullptr;
+    float* bias = nullptr;      // [3 * 128 + 16]
+    float* norm = nullptr;      // fshift [48], fscale [48], out_scale [4]
+    uint32_t* err = nullptr;
+    // training buffers (max_batch rows)
+    float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *y = nullptr, *dh = nullptr;
+    bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
+    bf16 *dz = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
+    float* part = nullptr;      // split-K partials
+    float* loss_part = nullptr;
+    float* loss = nullptr;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+thread_local char g_lerr[256];
+
+sphmp_status lfail(sphmp_status st, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_lerr, sizeof(g_lerr), fmt, ap);
+    va_end(ap);
+    return record_error(st, g_lerr);
+}
+
+#define LCK(call)                                                                      \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) return lfail(SPHMP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kSplitK = 64;  // K chunks of the weight-gradient GEMMs (K = batch)
+
+template <class T>
+sphmp_status lalloc(sphmp_corrector* c, T** p, size_t count) {
+    void* q = nullptr;
+    LCK(cudaMalloc(&q, sizeof(T) * (count ? count : 1)));
+    LCK(cudaMemset(q, 0, sizeof(T) * (count ? count : 1)));
+    c->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return SPHMP_OK;
+}
+
+mlp::Packed packed(const sphmp_corrector* c) {
+    return mlp::Packed{c->w1, c->w2, c->w3, c->w4, c->bias, c->norm, c->norm + mlp::kFeatures};
+}
+
+mlp::PackedMut packed_mut(const sphmp_corrector* c) {
+    return mlp::PackedMut{c->w1, c->w2, c->w3, c->w4, c->w2t, c->w3t, c->w4t, c->bias};
+}
+
+sphmp_status take_errors(sphmp_corrector* c) {
+    uint32_t bits = 0;
+    LCK(cudaMemcpyAsync(&bits, c->err, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    LCK(cudaMemsetAsync(c->err, 0, sizeof(bits), c->stream));
+    LCK(cudaStreamSynchronize(c->stream));
+    if (bits & mlp::kErrMmaTimeout) return lfail(SPHMP_ERR_TIMEOUT, "a tensor-core wait ran out");
+    return SPHMP_OK;
+}
+
+// forward with saves, output gradient, backward into c->grads
+sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t, int batch) {
+    using namespace mlp;
+    const cudaStream_t s = c->stream;
+    const int ld = c->max_batch;
+    const Saves S{c->z1, c->z2, c->z3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
+    LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
+    LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
+    float* g = c->grads;
+    // layer 4: dW4 = dY^T H3, db4, dH3 = dY W4
+    LCK(launch_gemm_tn(c->dyt, ld, c->h3t, ld, c->part, kOutPad, kHidden, batch, kSplitK, c->err, s));
+    LCK(launch_reduce_splits(c->part, kSplitK, kOutPad, kHidden, kOutputs, kHidden, g + kOffParamW4, s));
+    LCK(launch_row_sum(c->dyt, ld, kOutputs, batch, g + kOffParamB4, s));
+    LCK(launch_gemm_tn(c->dy, kOutPad, c->w4t, kOutPad, c->dh, batch, kHidden, kOutPad, 1, c->err, s));
+    LCK(launch_silu_back(c->dh, c->z3, batch, ld, c->dz, c->dzt, s));
+    // layer 3
+    LCK(launch_gemm_tn(c->dzt, ld, c->h2t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
+    LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW3, s));
+    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, g + kOffParamB3, s));
+    LCK(launch_gemm_tn(c->dz, kHidden, c->w3t, kHidden, c->dh, batch, kHidden, kHidden, 1, c->err, s));
+    LCK(launch_silu_back(c->dh, c->z2, batch, ld, c->dz, c->dzt, s));
+    // layer 2
+    LCK(launch_gemm_tn(c->dzt, ld, c->h1t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
+    LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW2, s));
+    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, g + kOffParamB2, s));
+    LCK(launch_gemm_tn(c->dz, kHidden, c->w2t, kHidden, c->dh, batch, kHidden, kHidden, 1, c->err, s));
+    LCK(launch_silu_back(c->dh, c->z1, batch, ld, c->dz, c->dzt, s));
+    // layer 1: dW1 = dZ1^T H0 (the first 48 of the 64 padded inputs)
+    LCK(launch_gemm_tn(c->dzt, ld, c->h0t, ld, c->part, kHidden, kInPad, batch, kSplitK, c->err, s));
+    LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kInPad, kHidden, kFeatures, g + kOffParamW1, s));
+    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, g + kOffParamB1, s));
+    return SPHMP_OK;
+}
+
+sphmp_status check_batch(const sphmp_corrector* c, const float* x, const float* t, int batch) {
+    if (!x || !t) return lfail(SPHMP_ERR_INVALID_ARG, "x and t must be device pointers");
+    if (batch <= 0 || batch % 128 != 0 || batch > c->max_batch)
+        return lfail(SPHMP_ERR_INVALID_ARG, "batch %d must be a positive multiple of 128 up to %d", batch, c->max_batch);
+    return SPHMP_OK;
+}
+
+}  // namespace
+
+// internal: used by the context's large step (sphmp_api.cu)
+namespace sphmp {
+cudaError_t corrector_forward_on(sphmp_corrector* c, const float* x, int n, float* y, uint32_t* err,
+                                 cudaStream_t s) {
+    return mlp::launch_forward(x, n, packed(c), mlp::Saves{}, y, err, c->num_sms, s);
+}
+const float* corrector_out_scale(const sphmp_corrector* c) { return c->norm + 2 * mlp::kFeatures; }
+int corrector_device(const sphmp_corrector* c) { return c->device; }
+}  // namespace sphmp
+
+extern "C" {
+
+sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corrector** out) {
+    using namespace mlp;
+    if (!out) return lfail(SPHMP_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (max_batch < 0 || max_batch % 128 != 0)
+        return lfail(SPHMP_ERR_INVALID_ARG, "max_batch %d must be a non-negative multiple of 128", max_batch);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return lfail(SPHMP_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    sphmp_corrector* c = new sphmp_corrector();
+    c->max_batch = max_batch;
+    c->stream = static_cast<cudaStream_t>(stream);
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    sphmp_status st = SPHMP_OK;
+    auto A = [&](auto** p, size_t n) {
+        if (st == SPHMP_OK) st = lalloc(c, p, n);
+    };
+    A(&c->params, kParams); A(&c->grads, kParams); A(&c->adam_m, kParams); A(&c->adam_v, kParams);
+    A(&c->w1, kHidden * kInPad); A(&c->w2, kHidden * kHidden); A(&c->w3, kHidden * kHidden);
+    A(&c->w4, kOutPad * kHidden); A(&c->w2t, kHidden * kHidden); A(&c->w3t, kHidden * kHidden);
+    A(&c->w4t, kHidden * kOutPad); A(&c->bias, 3 * kHidden + kOutPad); A(&c->norm, 2 * kFeatures + kOutputs);
+    A(&c->err, 1);
+    const size_t B = (size_t)max_batch;
+    if (B > 0) {
+        A(&c->z1, B * kHidden); A(&c->z2, B * kHidden); A(&c->z3, B * kHidden);
+        A(&c->y, B * 4); A(&c->dh, B * kHidden);
+        A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
+        A(&c->dz, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
+        A(&c->part, (size_t)kSplitK * kHidden * kHidden);
+        A(&c->loss_part, B / 256 + 1);
+        A(&c->loss, 1);
+    }
+    if (st != SPHMP_OK) {
+        sphmp_corrector_destroy(c);
+        return st;
+    }
+    // identity normalisation
+    std::vector<float> norm(2 * kFeatures + kOutputs, 1.f);
+    for (int i = 0; i < kFeatures; i++) norm[i] = 0.f;
+    if (cudaMemcpy(c->norm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        sphmp_corrector_destroy(c);
+        return lfail(SPHMP_ERR_CUDA, "normalisation upload failed");
+    }
+    *out = c;
+    return SPHMP_OK;
+}
+
+void sphmp_corrector_destroy(sphmp_corrector* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->allocs) cudaFree(p);
+    delete c;
+}
+
+sphmp_status sphmp_corrector_set_params(sphmp_corrector* c, const float* params) {
+    if (!c || !params) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
+    for (int i = 0; i < mlp::kParams; i++)
+        if (!isfinite(params[i])) return lfail(SPHMP_ERR_NOT_FINITE, "parameter %d is not finite", i);
+    LCK(cudaMemcpyAsync(c->params, params, sizeof(float) * mlp::kParams, cudaMemcpyHostToDevice, c->stream));
+    LCK(cudaMemsetAsync(c->adam_m, 0, sizeof(float) * mlp::kParams, c->stream));
+    LCK(cudaMemsetAsync(c->adam_v, 0, sizeof(float) * mlp::kParams, c->stream));
+    c->adam_step = 0;
+    LCK(mlp::launch_pack(c->params, packed_mut(c), c->stream));
+    LCK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_corrector_get_params(sphmp_corrector* c, float* params) {
+    if (!c || !params) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
+    LCK(cudaMemcpyAsync(params, c->params, sizeof(float) * mlp::kParams, cudaMemcpyDeviceToHost, c->stream));
+    LCK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_corrector_set_normalisation(sphmp_corrector* c, const float* feat_shift, const float* feat_scale,
+                                               const float* out_scale) {
+    using namespace mlp;
+    if (!c || !feat_shift || !feat_scale || !out_scale) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
+    std::vector<float> norm(2 * kFeatures + kOutputs);
+    for (int i = 0; i < kFeatures; i++) {
+        norm[i] = feat_shift[i];
+        norm[kFeatures + i] = feat_scale[i];
+    }
+    for (int i = 0; i < kOutputs; i++) norm[2 * kFeatures + i] = out_scale[i];
+    for (float v : norm)
+        if (!isfinite(v)) return lfail(SPHMP_ERR_NOT_FINITE, "normalisation not finite");
+    LCK(cudaMemcpyAsync(c->norm, norm.data(), sizeof(float) * norm.size(), cudaMemcpyHostToDevice, c->stream));
+    LCK(cudaStreamSynchronize(c->stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_corrector_forward(sphmp_corrector* c, const float* x, int32_t n, float* y) {
+    if (!c || !x || !y || n < 0) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
+    LCK(mlp::launch_forward(x, n, packed(c), mlp::Saves{}, y, c->err, c->num_sms, c->stream));
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_corrector_gradients(sphmp_corrector* c, const float* x, const float* t, int32_t batch,
+                                       float* grads, float* loss) {
+    if (!c || !grads) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
+    if (sphmp_status st = check_batch(c, x, t, batch)) return st;
+    if (sphmp_status st = enqueue_backward(c, x, t, batch)) return st;
+    LCK(cudaMemcpyAsync(grads, c->grads, sizeof(float) * mlp::kParams, cudaMemcpyDeviceToHost, c->stream));
+    if (loss) LCK(cudaMemcpyAsync(loss, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    return take_errors(c);
+}
+
+sphmp_status sphmp_corrector_train_step(sphmp_corrector* c, const float* x, const float* t, int32_t batch, float lr,
+                                        float* loss) {
+    if (!c) return lfail(SPHMP_ERR_INVALID_ARG, "corrector is NULL");
+    if (sphmp_status st = check_batch(c, x, t, batch)) return st;
+    if (!(lr > 0.f) || !isfinite(lr)) return lfail(SPHMP_ERR_INVALID_ARG, "lr must be > 0");
+    if (sphmp_status st = enqueue_backward(c, x, t, batch)) return st;
+    c->adam_step++;
+    LCK(mlp::launch_adam(c->params, c->grads, c->adam_m, c->adam_v, mlp::kParams, lr, 0.9f, 0.999f, 1e-8f,
+                         c->adam_step, c->stream));
+    LCK(mlp::launch_pack(c->params, packed_mut(c), c->stream));
+    if (loss) {
+        LCK(cudaMemcpyAsync(loss, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        return take_errors(c);
+    }
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_corrector_sync(sphmp_corrector* c) {
+    if (!c) return lfail(SPHMP_ERR_INVALID_ARG, "corrector is NULL");
+    return take_errors(c);
+}
+
+sphmp_status sphmp_gemm_bf16_tn(const void* a, int32_t lda, const void* b, int32_t ldb, float* d, int32_t m,
+                                int32_t n, int32_t k, int32_t splits, void* stream) {
+    if (!a || !b || !d) return lfail(SPHMP_ERR_INVALID_ARG, "null operand");
+    if (m <= 0 || n <= 0 || n > 128 || n % 16 != 0 || k < 0 || k % 8 != 0 || splits < 1 || lda % 8 != 0 ||
+        ldb % 8 != 0 || lda < k || ldb < k)
+        return lfail(SPHMP_ERR_INVALID_ARG, "unsupported GEMM shape m %d n %d k %d lda %d ldb %d splits %d", m, n, k,
+                     lda, ldb, splits);
+    uint32_t* err = nullptr;
+    LCK(cudaMalloc(&err, sizeof(uint32_t)));
+    LCK(cudaMemset(err, 0, sizeof(uint32_t)));
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = mlp::launch_gemm_tn(static_cast<const bf16*>(a), lda, static_cast<const bf16*>(b), ldb, d, m, n, k,
+                                        splits, err, s);
+    uint32_t bits = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, err, sizeof(bits), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(err);
+    if (e != cudaSuccess) return lfail(SPHMP_ERR_CUDA, "gemm: %s", cudaGetErrorString(e));
+    if (bits & mlp::kErrMmaTimeout) return lfail(SPHMP_ERR_TIMEOUT, "a tensor-core wait ran out");
+    return SPHMP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,562 @@
+// sphmp_mlp.cu — the learned large-step corrector's network on the tensor cores:
+// a per-particle MLP 48 -> 128 -> 128 -> 128 -> 4 with SiLU, bf16 weights and
+// activations, FP32 accumulation in TMEM (tcgen05.mma kind::f16), its backward
+// pass and Adam.
+//
+// * k_mlp_forward: all four layers of 128-particle tiles in one persistent
+//   kernel. The weights stay in shared memory; each layer is one chain of MMAs
+//   into TMEM, and its epilogue (bias, SiLU, bf16) writes the next layer's
+//   operand tile back into shared memory. With the training saves it also
+//   stores the pre-activations (FP32) and the bf16 activations transposed
+//   (feature-major), the operands of the weight-gradient GEMMs.
+// * k_gemm_tn: D = A B^T for K-major bf16 A [M][K] and B [N][K] (N <= 128),
+//   M in tiles of 128, K split over gridDim.y into FP32 partials (summed in a
+//   fixed order by k_reduce_splits), for the backward pass.
+// * elementwise kernels: the output gradient, the SiLU backward (with its
+//   transposed copy), bias gradients, Adam, and the packing of the FP32 master
+//   parameters into the padded bf16 operand layouts.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "sphmp_mlp.h"
+#include "sphmp_tc.cuh"
+
+namespace sphmp {
+namespace mlp {
+
+using bf16 = __nv_bfloat16;
+
+namespace {
+
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+
+__device__ __forceinline__ float silu_grad(float z) {
+    const float s = __fdividef(1.f, 1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// ---------------------------------------------------------------------------
+// Fused forward
+// ---------------------------------------------------------------------------
+
+constexpr int kFwdThreads = 256;  // 8 warps: lane quadrant (w % 4), column half (w / 4)
+constexpr int kTile = 128;
+// dynamic shared memory of the forward kernel
+constexpr int kOffW1 = 0;                                  // [128 rows][64] kc 64
+constexpr int kOffW2 = kOffW1 + kHidden * kInPad * 2;      // [128][128]
+constexpr int kOffW3 = kOffW2 + kHidden * kHidden * 2;     // [128][128]
+constexpr int kOffW4 = kOffW3 + kHidden * kHidden * 2;     // [16][128]
+constexpr int kOffAct = kOffW4 + kOutPad * kHidden * 2;    // [128][128] operand tile
+constexpr int kOffBias = kOffAct + kTile * kHidden * 2;    // 3 * 128 + 16 floats
+constexpr int kOffNorm = kOffBias + (3 * kHidden + kOutPad) * 4;  // shift[48], scale[48]
+constexpr int kFwdSmem = kOffNorm + 2 * kFeatures * 4;
+constexpr uint32_t kFwdTmemCols = 256;  // [0, 128): layers 1-3, [128, 144): layer 4
+
+__device__ __forceinline__ void stage_weights(uint8_t* dst, const bf16* src, int rows, int kc, int tid,
+                                              int nthreads) {
+    for (int q = tid; q < rows * (kc / 8); q += nthreads) {
+        const int r = q / (kc / 8), k = (q % (kc / 8)) * 8;
+        *reinterpret_cast<uint4*>(dst + tc::kmajor_offset(r, k, kc)) =
+            *reinterpret_cast<const uint4*>(src + (size_t)r * kc + k);
+    }
+}
+
+// one MMA chain: D[tmem_col ...] = act (K = kc) x W^T (N rows)
+__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t act, uint32_t w, int kc, int n, uint64_t* bar) {
+    const uint32_t idesc = tc::idesc_bf16_f32(kTile, n);
+    for (int ks = 0; ks < kc / 16; ks++)
+        tc::mma_bf16(tmem, tc::kmajor_desc(act, kc, ks), tc::kmajor_desc(w, kc, ks), idesc, ks > 0 ? 1u : 0u);
+    tc::mma_commit(bar);
+}
+
+// Every thread waits; the CTA agrees on the outcome (a barrier).
+__device__ __forceinline__ bool wait_all(uint64_t* bar, uint32_t& parity) {
+    const bool ok = tc::mbar_wait(bar, parity, tc::kWaitLimitNs);
+    parity ^= 1u;
+    const bool all = __syncthreads_and(ok) != 0;
+    tc::fence_after_sync();
+    return all;
+}
+
+// shared-memory writes of this thread done: order them before the next MMA
+__device__ __forceinline__ void handoff_to_mma() {
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+}
+
+// Epilogue of a hidden layer: bias + SiLU of this thread's 64 columns, the
+// bf16 activations into the operand tile (K = 128), and the training saves.
+__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lane, int half, const float* bias,
+                                                uint8_t* act, int row0, int n, float* z_save, bf16* ht_save,
+                                                int ldh) {
+    const int r = (warp & 3) * 32 + lane;
+    const int grow = row0 + r;
+    const bool live = grow < n;
+#pragma unroll 1
+    for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, c0), v);
+        float h[16];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const float z = v[i] + bias[c0 + i];
+            v[i] = z;
+            h[i] = silu(z);
+        }
+        uint4 lo, hi;
+        lo.x = pack2(h[0], h[1]); lo.y = pack2(h[2], h[3]); lo.z = pack2(h[4], h[5]); lo.w = pack2(h[6], h[7]);
+        hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
+        *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0, kHidden)) = lo;
+        *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0 + 8, kHidden)) = hi;
+        if (z_save && live) {
+            float4* zs = reinterpret_cast<float4*>(z_save + (size_t)grow * kHidden + c0);
+#pragma unroll
+            for (int i = 0; i < 4; i++) zs[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+        }
+        if (ht_save && live) {
+#pragma unroll
+            for (int i = 0; i < 16; i++) ht_save[(size_t)(c0 + i) * ldh + grow] = __float2bfloat16_rn(h[i]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __restrict__ x, int n,
+                                                                 const Packed W, const Saves S,
+                                                                 float* __restrict__ y, uint32_t* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, half = warp >> 2;
+    uint8_t* act = smem + kOffAct;
+    float* bias = reinterpret_cast<float*>(smem + kOffBias);
+    float* fshift = reinterpret_cast<float*>(smem + kOffNorm);
+    float* fscale = fshift + kFeatures;
+
+    stage_weights(smem + kOffW1, W.w1, kHidden, kInPad, tid, kFwdThreads);
+    stage_weights(smem + kOffW2, W.w2, kHidden, kHidden, tid, kFwdThreads);
+    stage_weights(smem + kOffW3, W.w3, kHidden, kHidden, tid, kFwdThreads);
+    stage_weights(smem + kOffW4, W.w4, kOutPad, kHidden, tid, kFwdThreads);
+    for (int i = tid; i < 3 * kHidden + kOutPad; i += kFwdThreads) bias[i] = W.bias[i];
+    for (int i = tid; i < kFeatures; i += kFwdThreads) {
+        fshift[i] = W.fshift[i];
+        fscale[i] = W.fscale[i];
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base, kFwdTmemCols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&bar, 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const uint32_t a_act = tc::smem_addr(act);
+    uint32_t parity = 0;
+    bool ok = true;
+    const int ntiles = (n + kTile - 1) / kTile;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int row0 = t * kTile;
+        // input tile: normalised features, bf16, K padded to 64 with zeros
+        {
+            const int r = tid >> 1, part = tid & 1;  // features [24 part, 24 part + 24)
+            const int grow = row0 + r;
+            float f[24];
+            if (grow < n) {
+                const float4* src = reinterpret_cast<const float4*>(x + (size_t)grow * kFeatures + part * 24);
+#pragma unroll
+                for (int i = 0; i < 6; i++) {
+                    const float4 q = src[i];
+                    f[4 * i] = q.x; f[4 * i + 1] = q.y; f[4 * i + 2] = q.z; f[4 * i + 3] = q.w;
+                }
+#pragma unroll
+                for (int i = 0; i < 24; i++) f[i] = (f[i] - fshift[part * 24 + i]) * fscale[part * 24 + i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 24; i++) f[i] = 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                uint4 q;
+                q.x = pack2(f[8 * c], f[8 * c + 1]); q.y = pack2(f[8 * c + 2], f[8 * c + 3]);
+                q.z = pack2(f[8 * c + 4], f[8 * c + 5]); q.w = pack2(f[8 * c + 6], f[8 * c + 7]);
+                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, part * 24 + 8 * c, kInPad)) = q;
+            }
+            if (part == 1) {
+                const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 48, kInPad)) = zero;
+                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 56, kInPad)) = zero;
+            }
+            if (S.h0t && grow < n) {
+#pragma unroll
+                for (int i = 0; i < 24; i++) S.h0t[(size_t)(part * 24 + i) * S.ldh + grow] = __float2bfloat16_rn(f[i]);
+            }
+        }
+        handoff_to_mma();
+        // layer 1
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW1), kInPad, kHidden, &bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        hidden_epilogue(tmem, warp, lane, half, bias, act, row0, n, S.z1, S.h1t, S.ldh);
+        handoff_to_mma();
+        // layer 2
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW2), kHidden, kHidden, &bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        hidden_epilogue(tmem, warp, lane, half, bias + kHidden, act, row0, n, S.z2, S.h2t, S.ldh);
+        handoff_to_mma();
+        // layer 3
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW3), kHidden, kHidden, &bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        hidden_epilogue(tmem, warp, lane, half, bias + 2 * kHidden, act, row0, n, S.z3, S.h3t, S.ldh);
+        handoff_to_mma();
+        // layer 4 (N = 16: outputs 0..3 and zero padding)
+        if (tid == 0) {
+            tc::fence_after_sync();
+            issue_layer(tmem + kHidden, a_act, tc::smem_addr(smem + kOffW4), kHidden, kOutPad, &bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        if (half == 0) {
+            float v[16];
+            tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, kHidden), v);
+            const int grow = row0 + (warp & 3) * 32 + lane;
+            const float* b4 = bias + 3 * kHidden;
+            if (grow < n)
+                reinterpret_cast<float4*>(y)[grow] = make_float4(v[0] + b4[0], v[1] + b4[1], v[2] + b4[2], v[3] + b4[3]);
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(err, kErrMmaTimeout);
+        tc::mbar_wait(&bar, parity ^ 1u, tc::kWaitLimitNs);  // the chain still in flight, bounded
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    }
+    if (warp == 0) tc::tmem_dealloc(tmem, kFwdTmemCols);
+}
+
+// ---------------------------------------------------------------------------
+// GEMM D = A B^T (K-major bf16 operands), split-K partials
+// ---------------------------------------------------------------------------
+
+constexpr int kGemmThreads = 128;
+constexpr int kKc = 64;
+// A tile + B tile (N <= 128): 32 KB, so at most 7 CTAs share an SM's shared
+// memory; with at most 128 TMEM columns each, a fifth CTA on an SM waits in
+// tcgen05.alloc until one of the first four has finished
+constexpr int kGemmSmem = kTile * kKc * 2 + 128 * kKc * 2;
+
+__global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict__ A, int lda,
+                                                          const bf16* __restrict__ B, int ldb, float* __restrict__ D,
+                                                          int M, int N, int K, int kper, uint32_t* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    uint8_t* sa = smem;
+    uint8_t* sb = smem + kTile * kKc * 2;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * kTile;
+    const int kb = blockIdx.y * kper, ke = min(K, kb + kper);
+    const uint32_t ncols = N <= 32 ? 32u : N <= 64 ? 64u : 128u;
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base, ncols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&bar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const uint32_t idesc = tc::idesc_bf16_f32(kTile, N);
+    uint32_t parity = 0;
+    bool ok = true;
+    int chunks = 0;
+    for (int k0 = kb; k0 < ke; k0 += kKc) {
+        for (int q = tid; q < kTile * (kKc / 8); q += kGemmThreads) {
+            const int r = q >> 3, k = (q & 7) * 8;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (m0 + r < M && k0 + k < ke) v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + k0 + k);
+            *reinterpret_cast<uint4*>(sa + tc::kmajor_offset(r, k, kKc)) = v;
+        }
+        for (int q = tid; q < N * (kKc / 8); q += kGemmThreads) {
+            const int r = q >> 3, k = (q & 7) * 8;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (k0 + k < ke) v = *reinterpret_cast<const uint4*>(B + (size_t)r * ldb + k0 + k);
+            *reinterpret_cast<uint4*>(sb + tc::kmajor_offset(r, k, kKc)) = v;
+        }
+        handoff_to_mma();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t a = tc::smem_addr(sa), b = tc::smem_addr(sb);
+            for (int ks = 0; ks < kKc / 16; ks++)
+                tc::mma_bf16(tmem, tc::kmajor_desc(a, kKc, ks), tc::kmajor_desc(b, kKc, ks), idesc,
+                             (chunks > 0 || ks > 0) ? 1u : 0u);
+            tc::mma_commit(&bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        chunks++;
+    }
+    const int r = warp * 32 + lane;
+    float* drow = D + ((size_t)blockIdx.y * M + (m0 + r)) * N;
+    if (ok) {
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, c0), v);
+            if (m0 + r < M) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) drow[c0 + i] = chunks ? v[i] : 0.f;
+            }
+        }
+    } else {
+        if (tid == 0) atomicOr(err, kErrMmaTimeout);
+        tc::mbar_wait(&bar, parity ^ 1u, tc::kWaitLimitNs);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// ---------------------------------------------------------------------------
+// Backward and optimiser helpers
+// ---------------------------------------------------------------------------
+
+// dY = 2 (y - t) / batch (the gradient of the mean over the batch of the
+// squared output error), bf16, row-major [batch][16] and transposed [16][ld];
+// per-block partial sums of the squared error.
+__global__ void k_out_grad(const float4* __restrict__ y, const float4* __restrict__ t, int batch, int ld,
+                           bf16* __restrict__ dy, bf16* __restrict__ dyt, float* __restrict__ loss_part) {
+    __shared__ float red[256 / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float se = 0.f;
+    if (i < batch) {
+        const float4 a = y[i], b = t[i];
+        const float d[4] = {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w};
+        const float s = 2.f / (float)batch;
+        uint4 lo, hi = make_uint4(0u, 0u, 0u, 0u);
+        lo.x = pack2(s * d[0], s * d[1]);
+        lo.y = pack2(s * d[2], s * d[3]);
+        lo.z = 0u;
+        lo.w = 0u;
+        reinterpret_cast<uint4*>(dy + (size_t)i * kOutPad)[0] = lo;
+        reinterpret_cast<uint4*>(dy + (size_t)i * kOutPad)[1] = hi;
+#pragma unroll
+        for (int o = 0; o < 4; o++) {
+            dyt[(size_t)o * ld + i] = __float2bfloat16_rn(s * d[o]);
+            se += d[o] * d[o];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) se += __shfl_xor_sync(0xffffffffu, se, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = se;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+        loss_part[blockIdx.x] = s;
+    }
+}
+
+// loss = sum of the partials / batch (one block, fixed order)
+__global__ void k_loss_sum(const float* __restrict__ part, int nparts, int batch, float* __restrict__ loss) {
+    __shared__ float red[256];
+    float s = 0.f;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += part[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *loss = red[0] / (float)batch;
+}
+
+// dZ = dH * SiLU'(Z), bf16, row-major [batch][128] and transposed [128][ld]
+// (32 x 32 tiles through shared memory so both stores are coalesced).
+__global__ void k_silu_back(const float* __restrict__ dh, const float* __restrict__ z, int batch, int ld,
+                            bf16* __restrict__ dz, bf16* __restrict__ dzt) {
+    __shared__ bf16 tile[32][34];
+    const int c = blockIdx.x * 32 + threadIdx.x;  // feature
+    for (int k = 0; k < 4; k++) {
+        const int r = blockIdx.y * 32 + threadIdx.y + 8 * k;  // row
+        bf16 v = __float2bfloat16_rn(0.f);
+        if (r < batch) {
+            const size_t o = (size_t)r * kHidden + c;
+            v = __float2bfloat16_rn(dh[o] * silu_grad(z[o]));
+            dz[o] = v;
+        }
+        tile[threadIdx.y + 8 * k][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; k++) {
+        const int cc = blockIdx.x * 32 + threadIdx.y + 8 * k;
+        const int r = blockIdx.y * 32 + threadIdx.x;
+        if (r < batch) dzt[(size_t)cc * ld + r] = tile[threadIdx.x][threadIdx.y + 8 * k];
+    }
+}
+
+// out[r * cols + c] = sum over the splits of part[s][r][c] (r < rows, c < cols)
+__global__ void k_reduce_splits(const float* __restrict__ part, int splits, int M, int N, int rows, int cols,
+                                float* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * cols) return;
+    const int r = i / cols, c = i % cols;
+    float s = 0.f;
+    for (int k = 0; k < splits; k++) s += part[((size_t)k * M + r) * N + c];
+    out[i] = s;
+}
+
+// out[r] = sum over the first `count` entries of row r of xt (one block per row)
+__global__ void k_row_sum(const bf16* __restrict__ xt, int ld, int count, float* __restrict__ out) {
+    __shared__ float red[256];
+    const bf16* row = xt + (size_t)blockIdx.x * ld;
+    float s = 0.f;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) s += __bfloat162float(row[i]);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, int count, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// FP32 master parameters -> padded bf16 operands (and their transposes) + biases
+__global__ void k_pack(const float* __restrict__ p, PackedMut W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float* w1 = p + kOffParamW1;
+    const float* w2 = p + kOffParamW2;
+    const float* w3 = p + kOffParamW3;
+    const float* w4 = p + kOffParamW4;
+    if (i < kHidden * kInPad) {  // w1 [128][64]
+        const int o = i / kInPad, k = i % kInPad;
+        W.w1[i] = __float2bfloat16_rn(k < kFeatures ? w1[o * kFeatures + k] : 0.f);
+    }
+    if (i < kHidden * kHidden) {  // w2, w3 and their transposes
+        const int o = i / kHidden, k = i % kHidden;
+        W.w2[i] = __float2bfloat16_rn(w2[i]);
+        W.w3[i] = __float2bfloat16_rn(w3[i]);
+        W.w2t[k * kHidden + o] = __float2bfloat16_rn(w2[i]);
+        W.w3t[k * kHidden + o] = __float2bfloat16_rn(w3[i]);
+    }
+    if (i < kOutPad * kHidden) {  // w4 [16][128], w4t [128][16]
+        const int o = i / kHidden, k = i % kHidden;
+        const float v = o < kOutputs ? w4[o * kHidden + k] : 0.f;
+        W.w4[i] = __float2bfloat16_rn(v);
+        W.w4t[k * kOutPad + o] = __float2bfloat16_rn(v);
+    }
+    if (i < 3 * kHidden + kOutPad) {
+        float b;
+        if (i < kHidden) b = p[kOffParamB1 + i];
+        else if (i < 2 * kHidden) b = p[kOffParamB2 + i - kHidden];
+        else if (i < 3 * kHidden) b = p[kOffParamB3 + i - 2 * kHidden];
+        else b = (i - 3 * kHidden) < kOutputs ? p[kOffParamB4 + i - 3 * kHidden] : 0.f;
+        W.bias[i] = b;
+    }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& S, float* y, uint32_t* err,
+                           int num_sms, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const int tiles = (n + kTile - 1) / kTile;
+    const int grid = tiles < num_sms ? tiles : num_sms;
+    k_mlp_forward<<<grid, kFwdThreads, kFwdSmem, s>>>(x, n, W, S, y, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_tn(const bf16* A, int lda, const bf16* B, int ldb, float* D, int M, int N, int K,
+                           int splits, uint32_t* err, cudaStream_t s) {
+    if (M <= 0 || N <= 0 || N > 128 || (N % 16) != 0 || K < 0 || (K % 8) != 0 || splits < 1 || (lda % 8) != 0 ||
+        (ldb % 8) != 0)
+        return cudaErrorInvalidValue;
+    int kper = (K + splits - 1) / splits;
+    kper = (kper + kKc - 1) / kKc * kKc;
+    if (kper == 0) kper = kKc;
+    dim3 grid((M + kTile - 1) / kTile, splits);
+    k_gemm_tn<<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, bf16* dy, bf16* dyt, float* loss_part,
+                            float* loss, cudaStream_t s) {
+    const int blocks = (batch + 255) / 256;
+    k_out_grad<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(y), reinterpret_cast<const float4*>(t), batch,
+                                      ld, dy, dyt, loss_part);
+    k_loss_sum<<<1, 256, 0, s>>>(loss_part, blocks, batch, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_silu_back(const float* dh, const float* z, int batch, int ld, bf16* dz, bf16* dzt, cudaStream_t s) {
+    dim3 grid(kHidden / 32, (batch + 31) / 32);
+    k_silu_back<<<grid, dim3(32, 8), 0, s>>>(dh, z, batch, ld, dz, dzt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
+                                 cudaStream_t s) {
+    k_reduce_splits<<<(rows * cols + 255) / 256, 256, 0, s>>>(part, splits, M, N, rows, cols, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_sum(const bf16* xt, int ld, int rows, int count, float* out, cudaStream_t s) {
+    k_row_sum<<<rows, 256, 0, s>>>(xt, ld, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int count, float lr, float b1, float b2,
+                        float eps, int step, cudaStream_t s) {
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    k_adam<<<(count + 255) / 256, 256, 0, s>>>(p, g, m, v, count, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s) {
+    k_pack<<<(kHidden * kHidden + 255) / 256, 256, 0, s>>>(p, W);
+    return cudaGetLastError();
+}
+
+}  // namespace mlp
+}  // namespace sphmp

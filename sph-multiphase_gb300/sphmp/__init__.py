@@ -89,6 +89,21 @@ def load():
         "sphmp_emit_disk": (st, [P(Params), P(abi.Emitter), C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_uint64,
                                  vp, vp, C.c_int32, P(C.c_int32)]),
         "sphmp_load_state": (st, [ctx, C.c_char_p]),
+        # the learned large-step corrector (include/sphmp_learned.h)
+        "sphmp_corrector_create": (st, [C.c_int32, vp, P(vp)]),
+        "sphmp_corrector_destroy": (None, [vp]),
+        "sphmp_corrector_set_params": (st, [vp, P(C.c_float)]),
+        "sphmp_corrector_get_params": (st, [vp, P(C.c_float)]),
+        "sphmp_corrector_set_normalisation": (st, [vp, P(C.c_float), P(C.c_float), P(C.c_float)]),
+        "sphmp_corrector_forward": (st, [vp, vp, C.c_int32, vp]),
+        "sphmp_corrector_gradients": (st, [vp, vp, vp, C.c_int32, P(C.c_float), P(C.c_float)]),
+        "sphmp_corrector_train_step": (st, [vp, vp, vp, C.c_int32, C.c_float, P(C.c_float)]),
+        "sphmp_corrector_sync": (st, [vp]),
+        "sphmp_gemm_bf16_tn": (st, [vp, C.c_int32, vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                    vp]),
+        "sphmp_step_large": (st, [ctx, vp, C.c_int32, C.c_int32]),
+        "sphmp_learned_features": (st, [ctx, vp, vp, vp, P(C.c_int32)]),
+        "sphmp_copy_state": (st, [ctx, ctx]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -348,6 +363,97 @@ class Context:
     def load_state(self, path):
         check(self._lib.sphmp_load_state(self._ptr, os.fsencode(path)))
 
+    # the learned large step (include/sphmp_learned.h)
+    def step_large(self, factor=8, nsteps=1, corrector=None):
+        """nsteps fused steps of factor x dt, each corrected by `corrector` (a Corrector) when given."""
+        cor = corrector._ptr if corrector is not None else None
+        check(self._lib.sphmp_step_large(self._ptr, cor, int(factor), int(nsteps)))
+
+    def learned_features(self, feat=None, ids=None, corr=None):
+        """Copy the last corrected step's per-row features / bornids / corrections into
+        device buffers (torch tensors or None); returns the row count."""
+        cnt = C.c_int32(0)
+        ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+        check(self._lib.sphmp_learned_features(self._ptr, ptr(feat), ptr(ids), ptr(corr), C.byref(cnt)))
+        return cnt.value
+
+    def copy_state_from(self, src):
+        """Replace this context's particles by those of `src` (on the device)."""
+        check(self._lib.sphmp_copy_state(self._ptr, src._ptr))
+
+
+class Corrector:
+    """The learned large-step corrector network (device parameters, Adam state,
+    training buffers for batches of up to max_batch rows). Device arrays are
+    passed as torch tensors (float32, contiguous, on the current device)."""
+
+    def __init__(self, max_batch=0, stream_ptr=0):
+        self._lib = load()
+        self._ptr = C.c_void_p()
+        check(self._lib.sphmp_corrector_create(int(max_batch), C.c_void_p(stream_ptr or 0), C.byref(self._ptr)))
+        self.max_batch = max_batch
+
+    def close(self):
+        if self._ptr:
+            self._lib.sphmp_corrector_destroy(self._ptr)
+            self._ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        a = np.ascontiguousarray(params, np.float32)
+        if a.size != abi.LC_PARAMS:
+            raise ValueError(f"need {abi.LC_PARAMS} parameters, got {a.size}")
+        check(self._lib.sphmp_corrector_set_params(self._ptr, a.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def get_params(self):
+        a = np.zeros(abi.LC_PARAMS, np.float32)
+        check(self._lib.sphmp_corrector_get_params(self._ptr, a.ctypes.data_as(C.POINTER(C.c_float))))
+        return a
+
+    def set_normalisation(self, feat_shift, feat_scale, out_scale):
+        fp = lambda v, n: np.ascontiguousarray(v, np.float32).reshape(n)
+        a, b, c = fp(feat_shift, abi.LC_FEATURES), fp(feat_scale, abi.LC_FEATURES), fp(out_scale, abi.LC_OUTPUTS)
+        P = C.POINTER(C.c_float)
+        check(self._lib.sphmp_corrector_set_normalisation(self._ptr, a.ctypes.data_as(P), b.ctypes.data_as(P),
+                                                          c.ctypes.data_as(P)))
+
+    def forward(self, x, y):
+        check(self._lib.sphmp_corrector_forward(self._ptr, C.c_void_p(x.data_ptr()), int(x.shape[0]),
+                                                C.c_void_p(y.data_ptr())))
+
+    def gradients(self, x, t):
+        """(flat gradient array, loss) of one batch, no update."""
+        g = np.zeros(abi.LC_PARAMS, np.float32)
+        loss = C.c_float(0.0)
+        check(self._lib.sphmp_corrector_gradients(self._ptr, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()),
+                                                  int(x.shape[0]), g.ctypes.data_as(C.POINTER(C.c_float)),
+                                                  C.byref(loss)))
+        return g, loss.value
+
+    def train_step(self, x, t, lr, want_loss=False):
+        loss = C.c_float(0.0)
+        check(self._lib.sphmp_corrector_train_step(self._ptr, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()),
+                                                   int(x.shape[0]), float(lr),
+                                                   C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def sync(self):
+        check(self._lib.sphmp_corrector_sync(self._ptr))
+
+
+def gemm_bf16_tn(a, b, d, splits=1, stream_ptr=0):
+    """d[s] = a @ b.T over split s's K range (torch bf16 a [m][k], b [n][k]; float32 d [splits][m][n])."""
+    m, k = a.shape
+    n = b.shape[0]
+    check(load().sphmp_gemm_bf16_tn(C.c_void_p(a.data_ptr()), int(a.stride(0)), C.c_void_p(b.data_ptr()),
+                                    int(b.stride(0)), C.c_void_p(d.data_ptr()), int(m), int(n), int(k), int(splits),
+                                    C.c_void_p(stream_ptr or 0)))
+
 
 # ---------------------------------------------------------------------------
 # particle data formats (host only)
@@ -397,6 +503,7 @@ def add_bi2_shape(p, disp, calc, count, pos, scale=0.005, offs=(0, 0, 0), vel=(0
     return n.value
 
 
-__all__ = ["abi", "Params", "DisplayPack", "CalcPack", "Context", "SphmpError", "load", "check", "last_error",
+__all__ = ["abi", "Params", "DisplayPack", "CalcPack", "Context", "Corrector", "gemm_bf16_tn", "SphmpError", "load",
+           "check", "last_error",
            "params_default", "setup_constants", "setup_grid", "boundary_spacing", "record_arrays",
            "add_fluid_volume", "add_wall", "add_open_box", "write_frame_text", "read_bi2", "add_bi2_shape", "emit_disk"]

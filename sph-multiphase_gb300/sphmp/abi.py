@@ -21,9 +21,10 @@ ERR_STATE = 7
 ERR_NO_DEVICE = 8
 ERR_BAD_MASS = 9
 ERR_GRID = 10
+ERR_TIMEOUT = 11
 STATUS_NAMES = {
     0: "OK", 1: "INVALID_ARG", 2: "CAPACITY", 3: "CUDA", 4: "UNSUPPORTED_TYPE", 5: "NOT_FINITE",
-    6: "CELL_OVERFLOW", 7: "STATE", 8: "NO_DEVICE", 9: "BAD_MASS", 10: "GRID",
+    6: "CELL_OVERFLOW", 7: "STATE", 8: "NO_DEVICE", 9: "BAD_MASS", 10: "GRID", 11: "TIMEOUT",
 }
 
 # sphmp_eos / sphmp_schedule
@@ -39,6 +40,12 @@ F_ALPHA, F_ALPHA_PRE, F_DRIFT, F_APREV, F_PMOD, F_TYPE, F_MASS, F_BORNID = range
 F_MGCELL, F_MIDSORT, F_MGNDX, F_MGRIDOFF, F_MGRIDCNT = range(16, 21)
 F_VELXCOR = 21
 F_COUNT = 22
+
+# the learned large-step corrector (include/sphmp_learned.h)
+LC_FEATURES = 48
+LC_HIDDEN = 128
+LC_OUTPUTS = 4
+LC_PARAMS = 39812
 
 _f3 = C.c_float * 3
 
@@ -138,7 +145,7 @@ def calc_dtype():
     ])
 
 
-# every symbol declared in include/sphmp.h and include/sphmp_legacy.h
+# every symbol declared in include/sphmp.h, include/sphmp_learned.h and include/sphmp_legacy.h
 EXPORTED_SYMBOLS = [
     "sphmp_params_default", "sphmp_setup_constants", "sphmp_setup_grid", "sphmp_add_fluid_volume",
     "sphmp_add_wall", "sphmp_add_open_box", "sphmp_boundary_spacing",
@@ -151,6 +158,11 @@ EXPORTED_SYMBOLS = [
     "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
     "sphmp_write_frame_text", "sphmp_read_bi2", "sphmp_add_bi2_shape", "sphmp_save_state", "sphmp_load_state",
     "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk", "sphmp_set_device_emitter",
+    # the learned large-step corrector (include/sphmp_learned.h)
+    "sphmp_corrector_create", "sphmp_corrector_destroy", "sphmp_corrector_set_params", "sphmp_corrector_get_params",
+    "sphmp_corrector_set_normalisation", "sphmp_corrector_forward", "sphmp_corrector_gradients",
+    "sphmp_corrector_train_step", "sphmp_corrector_sync", "sphmp_gemm_bf16_tn", "sphmp_step_large",
+    "sphmp_learned_features", "sphmp_copy_state",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "InitialSortCUDA", "SortGridCUDA", "CountingSortFullCUDA_", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",

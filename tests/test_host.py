@@ -24,7 +24,7 @@ def lib(built):
 
 def _declared_symbols():
     names = set()
-    for h in ("sphmp.h", "sphmp_legacy.h"):
+    for h in ("sphmp.h", "sphmp_legacy.h", "sphmp_learned.h"):
         src = open(os.path.join(REPO, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", src):
@@ -184,7 +184,7 @@ def test_param_carrier_prefix_layout():
         assert getattr(abi.Params, k).offset == v, k
 
 
-@pytest.mark.parametrize("header", ["sphmp.h", "sphmp_legacy.h"])
+@pytest.mark.parametrize("header", ["sphmp.h", "sphmp_legacy.h", "sphmp_learned.h"])
 @pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++11")])
 def test_headers_compile_as_c_and_cpp(header, lang, std):
     cc = "gcc" if lang == "c" else "g++"
