@@ -75,6 +75,36 @@ sphmp_status sphmp_learned_features(sphmp_ctx* ctx, float* feat_dev, int32_t* bo
    loading it into dst); both contexts on one device with the same phase count. */
 sphmp_status sphmp_copy_state(sphmp_ctx* dst, sphmp_ctx* src);
 
+/* Differences of b's state against a's over the fluid particles in the grid in
+   both, matched by bornid (bornids below the larger capacity): out[0] rms of
+   rho_b / rho_a - 1 over the stored densities, out[1] its largest magnitude,
+   out[2] rms volume-fraction difference (root of the mean over particles of the
+   sum over phases of the squared difference), out[3] rms |v_b - v_a| over rms
+   |v_a|, out[4] the particles compared. nout >= 5. */
+sphmp_status sphmp_compare_states(sphmp_ctx* a, sphmp_ctx* b, double* out, int32_t nout);
+
+typedef struct sphmp_rollout_stats {
+    int32_t large_steps;     /* large steps kept */
+    int32_t plain_steps;     /* plain steps run on the state (fallbacks, fallback windows, remainder) */
+    int32_t audits;          /* audited large steps */
+    int32_t fallbacks;       /* audits whose error exceeded the tolerance */
+    double density_err_max;  /* largest rms density error of an audit */
+    double alpha_err_max;    /* largest rms volume-fraction error of an audit */
+} sphmp_rollout_stats;
+
+/* Advance ctx by `steps` plain steps' worth of simulated time in large steps of
+   factor x dt, corrected by `cor` (NULL: uncorrected). The first and then every
+   audit_every-th large step is audited: `audit` (a second context with the same
+   parameters and capacity) runs `factor` plain steps from the same state, the
+   densities of both results are recomputed at their positions, and if the rms
+   density error or the rms volume-fraction error of the large step exceeds
+   `tol` (0.01 for 1 %), the plain result replaces it and the next
+   audit_every x factor steps run plain, after which the first large step is
+   audited again. Time that does not fill a large step runs plain.
+   Synchronises; stats may be NULL. */
+sphmp_status sphmp_rollout(sphmp_ctx* ctx, sphmp_ctx* audit, sphmp_corrector* cor, int32_t factor, int32_t steps,
+                           int32_t audit_every, double tol, sphmp_rollout_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,15 @@ def unpack(p):
     return out
 
 
+def _unpack64(p):
+    out, o = {}, 0
+    for name, shape in _SHAPES:
+        k = int(np.prod(shape))
+        out[name] = np.asarray(p[o:o + k], np.float64).reshape(shape)
+        o += k
+    return out
+
+
 def pack(d):
     return np.concatenate([np.asarray(d[name], np.float32).reshape(-1) for name, _ in _SHAPES])
 
@@ -75,39 +84,41 @@ def mlp_forward(params, shift, scale, X, rnd=None):
     """Network outputs y [n][4] and the intermediates the backward pass needs.
     `rnd` replaces the bf16 rounding (identity for a finite-difference check)."""
     bf16 = _bf16 if rnd is None else rnd
-    P = unpack(params)
-    x = bf16((np.asarray(X, np.float32) - np.float32(shift)) * np.float32(scale))
-    W = [bf16(P[f"W{i}"]).astype(np.float64) for i in range(1, 5)]
+    f32 = np.float32 if rnd is None else np.float64  # the exact mode keeps float64 throughout
+    P = unpack(params) if rnd is None else _unpack64(params)
+    x = bf16((np.asarray(X, f32) - f32(shift)) * f32(scale))
+    W = [np.asarray(bf16(P[f"W{i}"]), np.float64) for i in range(1, 5)]
     b = [P[f"b{i}"].astype(np.float64) for i in range(1, 5)]
     hs, zs = [x.astype(np.float64)], []
     h = hs[0]
     for i in range(3):
-        z = (h @ W[i].T + b[i]).astype(np.float32)
+        z = (h @ W[i].T + b[i]).astype(f32)
         zs.append(z)
-        h = bf16(silu(z)).astype(np.float64)
+        h = np.asarray(bf16(silu(z)), np.float64)
         hs.append(h)
-    y = (h @ W[3].T + b[3]).astype(np.float32)
+    y = (h @ W[3].T + b[3]).astype(f32)
     return y, {"h": hs, "z": zs, "W": W}
 
 
 def mlp_backward(params, shift, scale, X, T, rnd=None):
     """(flat gradients, loss) of loss = sum((y - t)^2) / batch."""
     bf16 = _bf16 if rnd is None else rnd
+    f32 = np.float32 if rnd is None else np.float64
     B = X.shape[0]
     y, c = mlp_forward(params, shift, scale, X, rnd)
-    d = (y - np.asarray(T, np.float32)).astype(np.float32)
+    d = (y - np.asarray(T, f32)).astype(f32)
     loss = float(np.sum(d.astype(np.float64) ** 2) / B)
-    dy = bf16(np.float32(2.0 / B) * d).astype(np.float64)
+    dy = bf16(f32(2.0 / B) * d).astype(np.float64)
     hs, zs, W = c["h"], c["z"], c["W"]
     g = {"W4": dy.T @ hs[3], "b4": dy.sum(0)}
     dz = dy
     for i in (3, 2, 1):  # layer i + 1 back to layer 1
         dh = dz @ W[i]  # W[i] is layer (i + 1)'s weight
-        dz = bf16((dh.astype(np.float32) * silu_grad(zs[i - 1])).astype(np.float32)).astype(np.float64)
+        dz = bf16((dh.astype(f32) * silu_grad(zs[i - 1])).astype(f32)).astype(np.float64)
         g[f"W{i}"] = dz.T @ hs[i - 1]
         g[f"b{i}"] = dz.sum(0)
     g["W1"] = g["W1"][:, :FEATURES]
-    return pack({k: np.asarray(v, np.float32) for k, v in g.items()}), loss
+    return np.concatenate([np.asarray(g[name], f32).reshape(-1) for name, _ in _SHAPES]), loss
 
 
 def adam(p, g, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):

@@ -63,6 +63,9 @@ struct sphmp_ctx {
     float* lcorr = nullptr;
     int lrows = 0;
     void* xstage = nullptr;  // sphmp_copy_state: fractions and (g - a) of the source
+    int32_t* cmap = nullptr; // sphmp_compare_states: bornid -> index
+    int cmap_size = 0;
+    double* cred = nullptr;  // sphmp_compare_states: 6 sums
 };
 
 namespace {
@@ -530,7 +533,7 @@ sphmp_status sphmp_destroy(sphmp_ctx* c) {
     }
     drop_graph(c);
     free_buffers(c);
-    void* lbufs[] = {c->lfeat, c->lids, c->ly, c->lcorr, c->xstage};
+    void* lbufs[] = {c->lfeat, c->lids, c->ly, c->lcorr, c->xstage, c->cmap, c->cred};
     for (void* q : lbufs) cudaFree(q);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
@@ -1156,6 +1159,93 @@ sphmp_status sphmp_copy_state(sphmp_ctx* dst, sphmp_ctx* src) {
         if (sphmp_status st = unpack_field_staged(dst, SPHMP_F_APREV, xg, n)) return st;
     }
     return SPHMP_OK;
+}
+
+sphmp_status sphmp_compare_states(sphmp_ctx* a, sphmp_ctx* b, double* out, int32_t nout) {
+    if (!a || !b || !out) return fail(SPHMP_ERR_INVALID_ARG, "bad arguments");
+    if (nout < 5) return fail(SPHMP_ERR_INVALID_ARG, "need 5 output slots");
+    if (a == b || a->device != b->device) return fail(SPHMP_ERR_INVALID_ARG, "need two contexts on one device");
+    if (sphmp_status st = refresh_n(a)) return st;
+    if (sphmp_status st = refresh_n(b)) return st;
+    const int msize = a->cap > b->cap ? a->cap : b->cap;
+    if (b->cmap_size < msize) {
+        cudaFree(b->cmap);
+        b->cmap = nullptr;
+        CK(cudaMalloc(&b->cmap, sizeof(int32_t) * (size_t)(msize > 0 ? msize : 1)));
+        b->cmap_size = msize;
+    }
+    if (!b->cred) CK(cudaMalloc(&b->cred, sizeof(double) * 6));
+    CK(cudaStreamSynchronize(a->stream));
+    launch_compare(dev_params(a), a->B, a->cur, dev_params(b), b->B, b->cur, b->cmap, msize, b->cred, b->stream);
+    CHECK_LAUNCH("compare states");
+    double r[6];
+    CK(cudaMemcpyAsync(r, b->cred, sizeof(r), cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    const double m = r[4] > 0 ? r[4] : 1.0;
+    out[0] = sqrt(r[0] / m);
+    out[1] = r[5];
+    out[2] = sqrt(r[1] / m);
+    out[3] = r[3] > 0 ? sqrt(r[2] / r[3]) : 0.0;
+    out[4] = r[4];
+    return SPHMP_OK;
+}
+
+// the stored densities recomputed at the current positions (sort + density pass)
+static sphmp_status recompute_density(sphmp_ctx* c) {
+    if (sphmp_status st = sphmp_get_particle_index(c)) return st;
+    if (sphmp_status st = sphmp_get_grid_list(c)) return st;
+    if (sphmp_status st = sphmp_rearrange_data(c)) return st;
+    return sphmp_compute_pressure(c);
+}
+
+sphmp_status sphmp_rollout(sphmp_ctx* c, sphmp_ctx* audit, sphmp_corrector* cor, int32_t factor, int32_t steps,
+                           int32_t audit_every, double tol, sphmp_rollout_stats* stats) {
+    if (!c || !audit || c == audit) return fail(SPHMP_ERR_INVALID_ARG, "need the context and a separate audit context");
+    if (factor < 1 || steps < 0 || audit_every < 1 || !(tol > 0.0))
+        return fail(SPHMP_ERR_INVALID_ARG, "factor >= 1, steps >= 0, audit_every >= 1 and tol > 0 required");
+    sphmp_rollout_stats S;
+    memset(&S, 0, sizeof(S));
+    int done = 0, plain_left = 0;
+    int since = audit_every - 1;  // the first large step is audited
+    while (done < steps) {
+        if (plain_left > 0 || steps - done < factor) {
+            const int k = plain_left > 0 ? (plain_left < steps - done ? plain_left : steps - done) : steps - done;
+            if (sphmp_status st = sphmp_step(c, k, SPHMP_SCHEDULE_FUSED, 1)) return st;
+            done += k;
+            S.plain_steps += k;
+            plain_left = plain_left > k ? plain_left - k : 0;
+            continue;
+        }
+        if (++since >= audit_every) {
+            since = 0;
+            S.audits++;
+            if (sphmp_status st = sphmp_copy_state(audit, c)) return st;
+            if (sphmp_status st = sphmp_step(audit, factor, SPHMP_SCHEDULE_FUSED, 0)) return st;
+            if (sphmp_status st = sphmp_step_large(c, cor, factor, 1)) return st;
+            if (sphmp_status st = recompute_density(c)) return st;
+            if (sphmp_status st = recompute_density(audit)) return st;
+            double e[5];
+            if (sphmp_status st = sphmp_compare_states(audit, c, e, 5)) return st;
+            if (e[0] > S.density_err_max) S.density_err_max = e[0];
+            if (e[2] > S.alpha_err_max) S.alpha_err_max = e[2];
+            if (!(e[0] <= tol && e[2] <= tol)) {  // NaN counts as a failure
+                S.fallbacks++;
+                if (sphmp_status st = sphmp_copy_state(c, audit)) return st;
+                S.plain_steps += factor;
+                plain_left = audit_every * factor;
+                since = audit_every - 1;  // the first large step after the plain window is audited
+            } else {
+                S.large_steps++;
+            }
+        } else {
+            if (sphmp_status st = sphmp_step_large(c, cor, factor, 1)) return st;
+            S.large_steps++;
+        }
+        done += factor;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    if (stats) *stats = S;
+    return take_device_errors(c, nullptr);
 }
 
 sphmp_status sphmp_conservation(sphmp_ctx* c, double* out, int32_t nout) {

@@ -150,7 +150,87 @@ __global__ void __launch_bounds__(256) k_apply_correction(const __grid_constant_
     corr[s] = make_float4(cx, cy, cz, cd);
 }
 
+// bornid -> internal index of the in-grid fluid particles of one state
+__global__ void k_id_map(const __grid_constant__ DevBuffers B, const float4* __restrict__ pos4,
+                         const float4* __restrict__ aprev4, int map_size, int32_t* __restrict__ map) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= active_n(B)) return;
+    if (!(pos4[s].w > 0.f) || B.mgcell[s] == kUndef) return;
+    const int32_t id = B.bornid[__float_as_uint(aprev4[s].w)];
+    if (id >= 0 && id < map_size) map[id] = s;
+}
+
+// Differences of state b against state a over the particles in-grid fluid in
+// both (matched by bornid): sums of (rho_b / rho_a - 1)^2, sum_k (alpha_b -
+// alpha_a)^2, |v_b - v_a|^2, |v_a|^2, the count, and max |rho_b / rho_a - 1|.
+__global__ void __launch_bounds__(256) k_compare(const __grid_constant__ DevBuffers Bb, const float4* __restrict__ pos_b,
+                                                 const float4* __restrict__ vel_b, const float4* __restrict__ alpha_b,
+                                                 const float4* __restrict__ aprev_b, const float2* __restrict__ dens_a,
+                                                 const float4* __restrict__ vel_a, const float4* __restrict__ alpha_a,
+                                                 const int32_t* __restrict__ map, int map_size, int nphase,
+                                                 double* __restrict__ out) {
+    __shared__ double sh[6][8];
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    const int n = active_n(Bb);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        if (!(pos_b[s].w > 0.f) || Bb.mgcell[s] == kUndef) continue;
+        const int32_t id = Bb.bornid[__float_as_uint(aprev_b[s].w)];
+        if (id < 0 || id >= map_size) continue;
+        const int32_t j = map[id];
+        if (j < 0) continue;
+        const double rel = (double)dens_a[j].x / (double)Bb.densp[s].x - 1.0;  // stored inverses
+        const float4 ab = alpha_b[s], aa = alpha_a[j];
+        double da = (double)(ab.x - aa.x) * (ab.x - aa.x);
+        if (nphase > 1) da += (double)(ab.y - aa.y) * (ab.y - aa.y);
+        if (nphase > 2) da += (double)(ab.z - aa.z) * (ab.z - aa.z);
+        const float4 vb = vel_b[s], va = vel_a[j];
+        acc[0] += rel * rel;
+        acc[1] += da;
+        acc[2] += (double)(vb.x - va.x) * (vb.x - va.x) + (double)(vb.y - va.y) * (vb.y - va.y) +
+                  (double)(vb.z - va.z) * (vb.z - va.z);
+        acc[3] += (double)va.x * va.x + (double)va.y * va.y + (double)va.z * va.z;
+        acc[4] += 1.0;
+        acc[5] = fmax(acc[5], fabs(rel));
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        double v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_xor_sync(0xffffffffu, v, o);
+            v = q == 5 ? fmax(v, u) : v + u;
+        }
+        if (lane == 0) sh[q][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 5; q++) {
+            double t = 0.0;
+            for (int k = 0; k < 8; k++) t += sh[q][k];
+            atomicAdd(&out[q], t);
+        }
+        double m = 0.0;
+        for (int k = 0; k < 8; k++) m = fmax(m, sh[5][k]);
+        atomicMax(reinterpret_cast<unsigned long long*>(&out[5]), (unsigned long long)__double_as_longlong(m));
+    }
+}
+
 }  // namespace
+
+void launch_compare(const DevParams& Pa, const DevBuffers& Ba, const int* cur_a, const DevParams& Pb,
+                    const DevBuffers& Bb, const int* cur_b, int32_t* map, int map_size, double* out, cudaStream_t s) {
+    cudaMemsetAsync(map, 0xFF, sizeof(int32_t) * (size_t)map_size, s);
+    cudaMemsetAsync(out, 0, sizeof(double) * 6, s);
+    if (Pa.n > 0)
+        k_id_map<<<(Pa.n + 255) / 256, 256, 0, s>>>(Ba, Ba.f4[POS][cur_a[POS]], Ba.f4[APREV][cur_a[APREV]], map_size,
+                                                    map);
+    if (Pb.n > 0)
+        k_compare<<<2 * 152, 256, 0, s>>>(Bb, Bb.f4[POS][cur_b[POS]], Bb.f4[VEL][cur_b[VEL]],
+                                          Bb.f4[ALPHA][cur_b[ALPHA]], Bb.f4[APREV][cur_b[APREV]], Ba.densp,
+                                          Ba.f4[VEL][cur_a[VEL]], Ba.f4[ALPHA][cur_a[ALPHA]], map, map_size,
+                                          Pb.nphase, out);
+}
 
 void launch_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids, float vs,
                      float dt_large, cudaStream_t s) {

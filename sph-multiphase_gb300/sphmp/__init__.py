@@ -104,6 +104,8 @@ def load():
         "sphmp_step_large": (st, [ctx, vp, C.c_int32, C.c_int32]),
         "sphmp_learned_features": (st, [ctx, vp, vp, vp, P(C.c_int32)]),
         "sphmp_copy_state": (st, [ctx, ctx]),
+        "sphmp_compare_states": (st, [ctx, ctx, P(C.c_double), C.c_int32]),
+        "sphmp_rollout": (st, [ctx, ctx, vp, C.c_int32, C.c_int32, C.c_int32, C.c_double, P(abi.RolloutStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -380,6 +382,21 @@ class Context:
     def copy_state_from(self, src):
         """Replace this context's particles by those of `src` (on the device)."""
         check(self._lib.sphmp_copy_state(self._ptr, src._ptr))
+
+    def compare_to(self, ref):
+        """Differences of this state against `ref`'s (sphmp_compare_states)."""
+        out = (C.c_double * 5)()
+        check(self._lib.sphmp_compare_states(ref._ptr, self._ptr, out, 5))
+        return {"density_rms": out[0], "density_max": out[1], "alpha_rms": out[2], "velocity_rms_rel": out[3],
+                "count": int(out[4])}
+
+    def rollout(self, audit, steps, factor=8, corrector=None, audit_every=16, tol=0.01):
+        """Advance by `steps` plain steps' worth of time in audited large steps (sphmp_rollout)."""
+        st = abi.RolloutStats()
+        cor = corrector._ptr if corrector is not None else None
+        check(self._lib.sphmp_rollout(self._ptr, audit._ptr, cor, int(factor), int(steps), int(audit_every),
+                                      float(tol), C.byref(st)))
+        return st.as_dict()
 
 
 class Corrector:

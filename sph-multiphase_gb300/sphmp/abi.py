@@ -162,7 +162,7 @@ EXPORTED_SYMBOLS = [
     "sphmp_corrector_create", "sphmp_corrector_destroy", "sphmp_corrector_set_params", "sphmp_corrector_get_params",
     "sphmp_corrector_set_normalisation", "sphmp_corrector_forward", "sphmp_corrector_gradients",
     "sphmp_corrector_train_step", "sphmp_corrector_sync", "sphmp_gemm_bf16_tn", "sphmp_step_large",
-    "sphmp_learned_features", "sphmp_copy_state",
+    "sphmp_learned_features", "sphmp_copy_state", "sphmp_compare_states", "sphmp_rollout",
     # reference entry-point names (include/sphmp_legacy.h)
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "InitialSortCUDA", "SortGridCUDA", "CountingSortFullCUDA_", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
@@ -180,6 +180,15 @@ class Bi2Info(C.Structure):
                 ("massbound", C.c_float), ("massfluid", C.c_float), ("time", C.c_float),
                 ("np", C.c_int32), ("nfixed", C.c_int32), ("nmoving", C.c_int32), ("nfloat", C.c_int32),
                 ("nfluidout", C.c_int32), ("nbound", C.c_int32), ("nfluid", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class RolloutStats(C.Structure):
+    """sphmp_rollout_stats (include/sphmp_learned.h)."""
+    _fields_ = [("large_steps", C.c_int32), ("plain_steps", C.c_int32), ("audits", C.c_int32),
+                ("fallbacks", C.c_int32), ("density_err_max", C.c_double), ("alpha_err_max", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -1,0 +1,337 @@
+"""The learned large-step corrector on the GPU (include/sphmp_learned.h) against
+its CPU oracle (oracle/learned.py):
+
+* the tcgen05 GEMM against float64 products of the same bf16 operands
+  (relative error below 1e-5: FP32 accumulation);
+* the fused forward pass, the backward pass and Adam against the oracle with
+  the same bf16 rounding points (outputs within 1e-3 of their largest
+  magnitude, gradients within 1e-3 relative per tensor: only the FP32
+  accumulation order and SiLU's exp differ);
+* the features against the oracle's restatement (relative 1e-4 per feature);
+* the correction applied exactly as stated, the device state copy equal to
+  saving and loading, the audit's fallback;
+* the trained network's gain: on a scene it was not trained on, a corrected
+  8 dt step misses 8 plain steps by less than the uncorrected one.
+"""
+import numpy as np
+import pytest
+import torch
+
+import sphmp
+from oracle import learned as OL
+from sphmp import abi, scenes
+from sphmp import learned as SL
+
+pytestmark = pytest.mark.gpu
+
+DEV = torch.device("cuda")
+
+
+def _bf16_tensor(rng, shape):
+    return torch.from_numpy(OL.bf16(rng.standard_normal(shape).astype(np.float32))).to(DEV).to(torch.bfloat16)
+
+
+@pytest.mark.parametrize("m,n,k,splits", [(128, 16, 16, 1), (300, 48, 200, 1), (256, 128, 1024, 4), (16, 128, 512, 3),
+                                          (1000, 64, 8, 2), (129, 32, 64, 7)])
+def test_gemm_matches_numpy(built, m, n, k, splits):
+    rng = np.random.default_rng(m + n + k)
+    a, b = _bf16_tensor(rng, (m, k)), _bf16_tensor(rng, (n, k))
+    d = torch.full((splits, m, n), float("nan"), dtype=torch.float32, device=DEV)
+    sphmp.gemm_bf16_tn(a, b, d, splits)
+    torch.cuda.synchronize()
+    got = d.sum(0).cpu().numpy().astype(np.float64)
+    ref = a.float().cpu().numpy().astype(np.float64) @ b.float().cpu().numpy().astype(np.float64).T
+    assert np.isfinite(got).all()
+    assert np.abs(got - ref).max() <= 1e-5 * max(np.abs(ref).max(), 1e-30)
+
+
+def test_gemm_rejects_unsupported_shapes(built):
+    a = torch.zeros((128, 64), dtype=torch.bfloat16, device=DEV)
+    d = torch.zeros((1, 128, 128), dtype=torch.float32, device=DEV)
+    for bad in [dict(n=24), dict(n=144), dict(k=12)]:
+        n, k = bad.get("n", 32), bad.get("k", 64)
+        b = torch.zeros((n, 64), dtype=torch.bfloat16, device=DEV)
+        with pytest.raises(sphmp.SphmpError) as e:
+            sphmp.check(sphmp.load().sphmp_gemm_bf16_tn(a.data_ptr(), 64, b.data_ptr(), 64, d.data_ptr(), 128, n, k,
+                                                        1, None))
+        assert e.value.status == abi.ERR_INVALID_ARG
+
+
+def _net(seed, batch=512):
+    rng = np.random.default_rng(seed)
+    p = OL.init_params(seed)
+    shift = (rng.standard_normal(48) * 0.1).astype(np.float32)
+    scale = (0.5 + rng.random(48)).astype(np.float32)
+    cor = sphmp.Corrector(max_batch=batch)
+    cor.set_params(p)
+    cor.set_normalisation(shift, scale, np.ones(4, np.float32))
+    return cor, p, shift, scale, rng
+
+
+@pytest.mark.parametrize("n", [1, 127, 1000, 20000])
+def test_forward_matches_oracle(built, n):
+    cor, p, shift, scale, rng = _net(3)
+    X = rng.standard_normal((n, 48)).astype(np.float32)
+    y = torch.full((n, 4), float("nan"), dtype=torch.float32, device=DEV)
+    cor.forward(torch.from_numpy(X).to(DEV), y)
+    cor.sync()
+    ref, _ = OL.mlp_forward(p, shift, scale, X)
+    got = y.cpu().numpy()
+    assert np.isfinite(got).all()
+    assert np.abs(got - ref).max() <= 1e-3 * np.abs(ref).max()
+    assert np.median(np.abs(got - ref)) <= 1e-5 * np.abs(ref).max()
+    cor.close()
+
+
+@pytest.mark.parametrize("batch", [128, 512])
+def test_gradients_match_oracle(built, batch):
+    cor, p, shift, scale, rng = _net(4, batch)
+    X = rng.standard_normal((batch, 48)).astype(np.float32)
+    T = rng.standard_normal((batch, 4)).astype(np.float32)
+    g, loss = cor.gradients(torch.from_numpy(X).to(DEV), torch.from_numpy(T).to(DEV))
+    gr, lr = OL.mlp_backward(p, shift, scale, X, T)
+    assert abs(loss - lr) <= 1e-5 * lr
+    G, R = OL.unpack(g), OL.unpack(gr)
+    for k in R:
+        assert np.linalg.norm(G[k] - R[k]) <= 1e-3 * np.linalg.norm(R[k]), k
+    cor.close()
+
+
+def test_bad_batches_are_rejected(built):
+    cor, p, shift, scale, rng = _net(5, 256)
+    x = torch.zeros((200, 48), dtype=torch.float32, device=DEV)
+    t = torch.zeros((200, 4), dtype=torch.float32, device=DEV)
+    with pytest.raises(sphmp.SphmpError):
+        cor.train_step(x, t, 1e-3)  # not a multiple of 128
+    x = torch.zeros((384, 48), dtype=torch.float32, device=DEV)
+    t = torch.zeros((384, 4), dtype=torch.float32, device=DEV)
+    with pytest.raises(sphmp.SphmpError):
+        cor.train_step(x, t, 1e-3)  # above max_batch
+    with pytest.raises(sphmp.SphmpError):
+        cor.set_params(np.full(abi.LC_PARAMS, np.nan, np.float32))
+    cor.close()
+
+
+def test_train_steps_are_adam(built):
+    cor, p, shift, scale, rng = _net(6, 256)
+    m = np.zeros(abi.LC_PARAMS)
+    v = np.zeros(abi.LC_PARAMS)
+    q = p.astype(np.float64)
+    for step in (1, 2, 3):
+        X = torch.from_numpy(rng.standard_normal((256, 48)).astype(np.float32)).to(DEV)
+        T = torch.from_numpy(rng.standard_normal((256, 4)).astype(np.float32)).to(DEV)
+        g, _ = cor.gradients(X, T)
+        cor.train_step(X, T, 1e-3)
+        q, m, v = OL.adam(q, g.astype(np.float64), m, v, step, 1e-3)
+        assert np.abs(cor.get_params() - q).max() <= 1e-6
+    cor.close()
+
+
+def test_training_fits_a_teacher_network(built):
+    """Targets from another network of the same shape: 400 Adam steps bring the
+    loss below a fifth of its start."""
+    rng = np.random.default_rng(7)
+    teacher = sphmp.Corrector(0)
+    teacher.set_params(OL.init_params(70) * 3)
+    X = torch.from_numpy(rng.standard_normal((65536, 48)).astype(np.float32)).to(DEV)
+    T = torch.empty((65536, 4), dtype=torch.float32, device=DEV)
+    teacher.forward(X, T)
+    teacher.sync()
+    T = (T - T.mean(0)) / T.std(0)
+    cor = sphmp.Corrector(4096)
+    cor.set_params(SL.init_params(71))
+    log = SL.train(cor, X, T.contiguous(), 400, 4096, 2e-3, seed=1, log_every=399)
+    assert log[-1][1] < 0.2 * log[0][1], log
+    cor.close()
+    teacher.close()
+
+
+# ---------------------------------------------------------------------------
+# the corrector inside the step
+# ---------------------------------------------------------------------------
+
+def _liquid_scene(n, seed):
+    """The 262,144-particle large-step scene's lattice, smaller, all liquid:
+    d = 0.005 m, h = 0.01 m, dt = 1e-4 s, linear EOS k = 3."""
+    sc = scenes.bubble_scene(seed=seed, n_particles=n, d=0.005, h=0.01, dt=1e-4)
+    sc.calc["restdens"][:sc.n_fluid] = sc.params.densArr[0]
+    sc.calc["mass"][:sc.n_fluid] = sc.params.massArr[0]
+    return sc
+
+
+def _run(sc, steps):
+    c = sphmp.Context(sc.params)
+    c.upload_aos(sc.disp[:sc.n], sc.calc[:sc.n])
+    c.before_first_step()
+    c.step(steps)
+    c.sync()
+    return c
+
+
+def test_copy_state_equals_save_and_load(built, tmp_path):
+    sc = _liquid_scene(4096, 11)
+    src = _run(sc, 40)
+    a, b = sphmp.Context(sc.params), sphmp.Context(sc.params)
+    a.copy_state_from(src)
+    src.save_state(str(tmp_path / "s.bin"))
+    b.load_state(str(tmp_path / "s.bin"))
+    for c in (a, b):
+        c.step(7)
+        c.sync()
+    da, ca = a.download_aos()
+    db, cb = b.download_aos()
+    assert a.n == b.n == src.n
+    assert da.tobytes() == db.tobytes() and ca.tobytes() == cb.tobytes()
+    assert np.array_equal(a.download_field(abi.F_ALPHA), b.download_field(abi.F_ALPHA))
+    same = a.compare_to(b)
+    assert same["density_rms"] == 0 and same["velocity_rms_rel"] == 0 and same["count"] > 0.9 * sc.n_fluid
+    for c in (src, a, b):
+        c.close()
+
+
+def test_features_match_oracle(built):
+    sc = _liquid_scene(4096, 12)
+    src = _run(sc, 60)
+    p = sc.params
+    ref = sphmp.Context(p)
+    ref.copy_state_from(src)
+    ref.sort()
+    ref.compute_pressure()
+    st = {k: ref.download_field(f) for k, f in (
+        ("pos", abi.F_POS), ("vel", abi.F_VEL), ("dens", abi.F_DENS), ("pres", abi.F_PRESSURE),
+        ("alpha", abi.F_ALPHA), ("rest", abi.F_RESTDENS), ("gma", abi.F_APREV), ("type", abi.F_TYPE),
+        ("mgcell", abi.F_MGCELL), ("bornid", abi.F_BORNID))}
+    F = OL.features(st["pos"], st["vel"], 1.0 / st["dens"], st["pres"], st["alpha"], st["rest"], st["gma"],
+                    st["type"] == abi.TYPE_FLUID, st["mgcell"] != abi.GRID_UNDEF, p.nphase, p.smoothradius,
+                    p.simscale, p.gravity, 8 * p.dt)
+    gpu = sphmp.Context(p)
+    gpu.copy_state_from(src)
+    zero = SL.zero_corrector()
+    gpu.step_large(8, 1, zero)
+    feat = torch.empty((gpu.n, 48), dtype=torch.float32, device=DEV)
+    ids = torch.empty(gpu.n, dtype=torch.int32, device=DEV)
+    rows = gpu.learned_features(feat, ids)
+    fg, ig = feat[:rows].cpu().numpy(), ids[:rows].cpu().numpy()
+    o = np.argsort(st["bornid"])
+    have = ig >= 0
+    assert have.sum() == ((st["type"] == 0) & (st["mgcell"] != abi.GRID_UNDEF)).sum()
+    Fo = F[o][np.searchsorted(st["bornid"][o], ig[have])]
+    scale = np.maximum(np.abs(Fo).max(0), 1e-6)
+    assert (np.abs(fg[have] - Fo) / scale).max() <= 1e-4
+    assert np.all(fg[~have] == 0)
+    for c in (src, ref, gpu):
+        c.close()
+    zero.close()
+
+
+def test_correction_is_applied_as_stated(built):
+    """A corrected large step = the uncorrected one, then v += c, veleval += c,
+    pos += c * dt_large / 2 (simulation units), stored 1/rho / (1 + c_rho)."""
+    sc = _liquid_scene(4096, 13)
+    src = _run(sc, 30)
+    p = sc.params
+    cor, *_ = _net(14, 0)
+    cor.set_normalisation(np.zeros(48, np.float32), np.full(48, 0.3, np.float32),
+                          np.array([1e-3, 2e-3, 1e-3, 1e-2], np.float32))
+    a, b = sphmp.Context(p), sphmp.Context(p)
+    a.copy_state_from(src)
+    b.copy_state_from(src)
+    zero = SL.zero_corrector()
+    a.step_large(8, 1, zero)
+    b.step_large(8, 1, cor)
+    corr = torch.empty((b.n, 4), dtype=torch.float32, device=DEV)
+    ids = torch.empty(b.n, dtype=torch.int32, device=DEV)
+    rows = b.learned_features(None, ids, corr)
+    ch, ih = corr[:rows].cpu().numpy(), ids[:rows].cpu().numpy()
+    assert np.abs(ch[ih >= 0]).max() > 0 and np.all(ch[ih < 0] == 0)
+
+    def by_id(c):
+        d = {k: c.download_field(f) for k, f in (("vel", abi.F_VEL), ("vev", abi.F_VELEVAL), ("pos", abi.F_POS),
+                                                  ("dens", abi.F_DENS), ("bornid", abi.F_BORNID))}
+        o = np.argsort(d["bornid"])
+        return {k: v[o] for k, v in d.items()}
+
+    A, B = by_id(a), by_id(b)
+    k = np.searchsorted(A["bornid"], ih[ih >= 0])
+    c = ch[ih >= 0]
+    f32 = np.float32
+    assert np.array_equal(B["vel"][k], (A["vel"][k] + c[:, :3]).astype(f32))
+    assert np.array_equal(B["vev"][k], (A["vev"][k] + c[:, :3]).astype(f32))
+    h = f32(0.5 * 8 * p.dt) / f32(p.simscale)
+    assert np.allclose(B["pos"][k], A["pos"][k] + c[:, :3] * h, rtol=0, atol=1e-7)
+    assert np.allclose(B["dens"][k], A["dens"][k] / (1 + c[:, 3]), rtol=2e-7)
+    for x in (src, a, b):
+        x.close()
+    cor.close()
+    zero.close()
+
+
+def test_rollout_audits_and_falls_back(built):
+    sc = _liquid_scene(4096, 15)
+    src = _run(sc, 30)
+    p = sc.params
+    ctx, aud = sphmp.Context(p), sphmp.Context(p)
+    # a generous tolerance: every large step is kept
+    ctx.copy_state_from(src)
+    st = ctx.rollout(aud, 8 * 10 + 3, factor=8, audit_every=4, tol=0.5)
+    assert st["large_steps"] == 10 and st["plain_steps"] == 3 and st["audits"] == 3 and st["fallbacks"] == 0
+    assert 0 < st["density_err_max"] < 0.5
+    # an impossible tolerance: every audited step falls back to the plain result,
+    # and the plain windows follow
+    ctx.copy_state_from(src)
+    st = ctx.rollout(aud, 8 * 10, factor=8, audit_every=2, tol=1e-12)
+    assert st["fallbacks"] == st["audits"] >= 1 and st["large_steps"] == 0 and st["plain_steps"] == 80
+    # the result is then the plain trajectory, up to the summation order of the copies
+    ref = sphmp.Context(p)
+    ref.copy_state_from(src)
+    ref.step(80)
+    for c in (ctx, ref):
+        c.sort()
+        c.compute_pressure()
+    d = ctx.compare_to(ref)
+    assert d["count"] > 0.9 * sc.n_fluid and d["density_rms"] < 1e-4 and d["velocity_rms_rel"] < 1e-3
+    for c in (src, ctx, aud, ref):
+        c.close()
+
+
+def test_trained_corrector_beats_the_uncorrected_large_step(built):
+    """Pairs from three all-liquid trajectories (seeds 5-7, 16 starts each);
+    on a fourth scene (seed 8) one corrected 8 dt step misses 8 plain steps by
+    less than the uncorrected one: velocity (densities recomputed at the end
+    positions) and the stored density of the result."""
+    Xs, Ts = [], []
+    for seed in (5, 6, 7):
+        sc = _liquid_scene(32768, seed)
+        c = _run(sc, 150)
+        large, plain = sphmp.Context(sc.params), sphmp.Context(sc.params)
+        X, T = SL.generate_pairs(c, large, plain, 8, starts=16, gap=10)
+        Xs.append(X)
+        Ts.append(T)
+        for x in (c, large, plain):
+            x.close()
+    X, T = torch.cat(Xs), np.concatenate(Ts)
+    shift, scale, osc = SL.normalisation(X, T)
+    cor = sphmp.Corrector(8192)
+    cor.set_params(SL.init_params(0))
+    cor.set_normalisation(shift, scale, osc)
+    log = SL.train(cor, X, torch.from_numpy(T / osc).to(DEV), 1500, 8192, 1e-3, seed=0, log_every=1499)
+    assert log[-1][1] < 0.3 * log[0][1], log
+    sc = _liquid_scene(32768, 8)
+    ev = _run(sc, 220)
+    large, plain = sphmp.Context(sc.params), sphmp.Context(sc.params)
+    v0, v1, s0, s1 = [], [], [], []
+    for _ in range(4):
+        v0.append(SL.step_errors(ev, large, plain, 8, None)["velocity_rms_rel"])
+        v1.append(SL.step_errors(ev, large, plain, 8, cor)["velocity_rms_rel"])
+        for c, out in ((None, s0), (cor, s1)):
+            large.copy_state_from(ev)
+            plain.copy_state_from(ev)
+            large.step_large(8, 1, c)
+            plain.step(8, abi.SCHEDULE_FUSED, use_graph=False)
+            out.append(large.compare_to(plain)["density_rms"])
+        ev.step(25)
+    assert np.mean(v1) < 0.8 * np.mean(v0), (v0, v1)
+    assert np.mean(s1) < 0.5 * np.mean(s0), (s0, s1)
+    for c in (ev, large, plain):
+        c.close()
+    cor.close()

@@ -1,0 +1,89 @@
+"""The CPU oracle of the learned corrector (oracle/learned.py) checked on its own:
+bf16 rounding, the parameter layout, the backward pass against finite
+differences, the features on a hand-computed pair. No GPU."""
+import numpy as np
+import pytest
+
+from oracle import learned as OL
+from sphmp import abi
+
+
+def test_parameter_layout_matches_the_header():
+    assert OL.PARAMS == abi.LC_PARAMS == 48 * 128 + 128 + 2 * (128 * 128 + 128) + 4 * 128 + 4
+    p = OL.init_params(1)
+    assert p.dtype == np.float32 and p.shape == (OL.PARAMS,)
+    d = OL.unpack(p)
+    assert d["W1"].shape == (128, 48) and d["W4"].shape == (4, 128) and d["b4"].shape == (4,)
+    assert np.array_equal(OL.pack(d), p)
+    assert np.abs(d["W1"]).max() <= 1 / np.sqrt(48) and np.abs(d["W2"]).max() <= 1 / np.sqrt(128)
+
+
+def test_bf16_rounds_to_nearest_even():
+    e = 2.0 ** -7  # bf16 spacing just above 1
+    x = np.array([1.0, 1 + e / 2, 1 + 1.5 * e, 1 + 0.75 * e, -3.0, 0.0, 1e-30, 65504.0], np.float32)
+    want = np.array([1.0, 1.0, 1 + 2 * e, 1 + e, -3.0, 0.0, None, None], object)
+    got = OL.bf16(x)
+    for g, w in zip(got[:6], want[:6]):
+        assert g == np.float32(w)
+    # every result has a zero low half
+    assert np.all(got.view(np.uint32) & 0xFFFF == 0)
+    assert abs(got[6] - 1e-30) / 1e-30 < 2 ** -8
+
+
+def test_backward_matches_finite_differences():
+    rng = np.random.default_rng(4)
+    p = OL.init_params(5).astype(np.float64)
+    X = rng.standard_normal((6, 48))
+    T = rng.standard_normal((6, 4))
+    ident = lambda a: np.asarray(a, np.float64)
+    shift, scale = np.zeros(48), np.ones(48)
+    g, loss = OL.mlp_backward(p, shift, scale, X, T, rnd=ident)
+
+    def L(q):
+        return OL.mlp_backward(q, shift, scale, X, T, rnd=ident)[1]
+
+    idx = rng.choice(OL.PARAMS, 60, replace=False)
+    idx = np.concatenate([idx, [OL.PARAMS - 1, OL.PARAMS - 5, 6144, 0]])  # b4, W4's last row, b1, W1
+    eps = 1e-3
+    for i in idx:
+        q = p.copy()
+        q[i] += eps
+        lp = L(q)
+        q[i] -= 2 * eps
+        lm = L(q)
+        fd = (lp - lm) / (2 * eps)
+        assert abs(fd - g[i]) <= 2e-3 * max(1e-2, abs(fd)), (i, fd, g[i])
+
+
+def test_adam_first_step_moves_each_parameter_by_lr():
+    p = np.zeros(5, np.float32)
+    g = np.array([1.0, -2.0, 0.5, 1e-3, -1e-6], np.float32)
+    q, m, v = OL.adam(p, g, np.zeros(5), np.zeros(5), 1, 1e-3)
+    # bias-corrected first step: m/c1 = g, v/c2 = g^2
+    assert np.allclose(q, -1e-3 * g / (np.abs(g) + 1e-8), rtol=1e-5)
+
+
+def test_features_of_a_pair():
+    h, ss = 0.02, 1.0
+    pos = np.array([[0.1, 0.1, 0.1], [0.1 + 0.01, 0.1, 0.1], [0.1, 0.1 + 0.015, 0.1]], np.float32)
+    vel = np.array([[0.0, 0.0, 0.0], [0.2, 0.0, 0.0], [0.0, 0.0, 0.0]], np.float32)
+    dens = np.array([1000.0, 1010.0, 1.0], np.float32)
+    pres = np.array([1.0, 3.0, 0.0], np.float32)
+    alpha = np.array([[1, 0, 0], [0.5, 0.5, 0], [0, 0, 0]], np.float32)
+    rest = np.array([1000.0, 1000.0, 1000.0], np.float32)
+    gma = np.zeros((3, 3), np.float32)
+    fluid = np.array([True, True, False])
+    F = OL.features(pos, vel, dens, pres, alpha, rest, gma, fluid, np.ones(3, bool), 2, h, ss, (0, -9.81, 0), 8e-4)
+    vs = np.sqrt(9.81 * h)
+    r = 0.01
+    w = (1 - (r / h) ** 2) ** 3
+    g = (1 - r / h) ** 2
+    f = F[0]
+    assert np.isclose(f[11], w) and np.isclose(f[12], w * (-0.01) / h)
+    assert np.isclose(f[15], w * 0.2 / vs)
+    assert np.isclose(f[18], w * 0.01) and np.isclose(f[20], -0.5 * w) and np.isclose(f[21], 0.5 * w)
+    assert np.isclose(f[29], -g) and np.isclose(f[32], g * (0.2 * -1) / vs)
+    assert np.isclose(f[39], 1 / 32) and np.isclose(f[44], 1 / 32)
+    rb = 0.015
+    assert np.isclose(f[40], (1 - (rb / h) ** 2) ** 3)
+    assert np.all(F[2] == 0)  # boundary particles carry no features
