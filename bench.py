@@ -523,6 +523,123 @@ def run_large_step(args):
     return 0
 
 
+def run_learned(args):
+    """The learned corrector's configurations: training throughput at a
+    65,536-particle minibatch, then the audited rollout on the 256 x 128 x 128
+    lattice against the plain pipeline over the same simulated time."""
+    import numpy as np
+    import torch
+
+    import sphmp
+    from sphmp import abi, scenes
+    from sphmp import learned as SL
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    factor, audit_every, tol = 8, 16, 0.01
+    sim_steps = args.learned_steps
+    flop_per_sample = 3 * 2 * (48 * 128 + 2 * 128 * 128 + 128 * 4)  # forward + backward (2x forward)
+
+    def fresh(sc, warm):
+        c = sphmp.Context(sc.params)
+        c.upload_aos(sc.disp[:sc.n], sc.calc[:sc.n])
+        c.before_first_step()
+        c.step(warm, abi.SCHEDULE_FUSED, use_graph=True)
+        c.sync()
+        return c
+
+    cases, training = {}, {}
+    for case in ("bubbles", "liquid"):
+        liquid = case == "liquid"
+        # training pairs: three 65,536-particle scenes of the same physics, 16 starts each
+        t0 = time.perf_counter()
+        Xs, Ts = [], []
+        for seed in (21, 22, 23):
+            sc = scenes.rollout_bubbles(seed=seed, lattice=(64, 32, 32), n_bubbles=4, liquid_only=liquid)
+            c = fresh(sc, 100)
+            large, plain = sphmp.Context(sc.params), sphmp.Context(sc.params)
+            X, T = SL.generate_pairs(c, large, plain, factor, starts=16, gap=10)
+            Xs.append(X)
+            Ts.append(np.nan_to_num(T, nan=0.0, posinf=0.0, neginf=0.0))
+            for x in (c, large, plain):
+                x.close()
+        X, T = torch.cat(Xs), np.concatenate(Ts)
+        X = torch.nan_to_num(X, nan=0.0, posinf=0.0, neginf=0.0)
+        t_pairs = time.perf_counter() - t0
+        shift, scale, osc = SL.normalisation(X, T)
+        cor = sphmp.Corrector(65536)
+        cor.set_params(SL.init_params(0))
+        cor.set_normalisation(shift, scale, osc)
+        Tn = torch.from_numpy(T / osc).to(dev)
+        SL.train(cor, X, Tn, 20, 65536, 1e-3, seed=1)  # warm-up
+        batches = [torch.randint(0, X.shape[0], (65536,), device=dev) for _ in range(4)]
+        xb = [X[i].contiguous() for i in batches]
+        tb = [Tn[i].contiguous() for i in batches]
+        nsteps = 400
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for k in range(nsteps):
+            cor.train_step(xb[k % 4], tb[k % 4], 1e-3)
+        e1.record()
+        torch.cuda.synchronize()
+        ms_train = e0.elapsed_time(e1) / nsteps
+        log = SL.train(cor, X, Tn, 1500, 65536, 1e-3, seed=2, log_every=1499)
+        training[case] = {"pairs": int(X.shape[0]), "pair_generation_s": round(t_pairs, 2), "batch": 65536,
+                          "ms_per_adam_step": ms_train, "samples_per_s": 65536 / (ms_train * 1e-3),
+                          "tflops": 65536 * flop_per_sample / (ms_train * 1e-3) / 1e12,
+                          "loss_first_last": [log[0][1], log[-1][1]]}
+        print(f"learned/{case}: trained on {X.shape[0]} pairs, {training[case]}", file=sys.stderr, flush=True)
+        # rollout on the full lattice
+        sc = scenes.rollout_bubbles(seed=9, liquid_only=liquid)
+        src = fresh(sc, 50)
+        res = {"fluid_particles": sc.n_fluid, "boundary_particles": sc.n_boundary}
+        for arm in ("plain", "learned"):
+            ctx = sphmp.Context(sc.params)
+            ctx.copy_state_from(src)
+            aud = sphmp.Context(sc.params) if arm == "learned" else None
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if arm == "plain":
+                ctx.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
+                ctx.sync()
+                st = None
+            else:
+                st = ctx.rollout(aud, sim_steps, factor=factor, corrector=cor, audit_every=audit_every, tol=tol)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            res[arm] = {"wall_s": wall, "sim_s_per_wall_s": sim_steps * sc.params.dt / wall}
+            print(f"learned/{case}/{arm}: {res[arm]} {st}", file=sys.stderr, flush=True)
+            if st:
+                res[arm]["stats"] = st
+            if arm == "plain":
+                ref = ctx
+            else:
+                for c in (ctx, ref):
+                    c.sort()
+                    c.compute_pressure()
+                res["learned_vs_plain_at_end"] = ctx.compare_to(ref)
+                ctx.close()
+                aud.close()
+                ref.close()
+        res["sim_s_per_wall_s_ratio"] = res["learned"]["sim_s_per_wall_s"] / res["plain"]["sim_s_per_wall_s"]
+        cases[case] = res
+        src.close()
+        cor.close()
+    line = {"metric": "learned vs plain sim-s/wall-s at <=1% density and volume-fraction error",
+            "value": cases["bubbles"]["sim_s_per_wall_s_ratio"], "unit": "x (sim-s/wall-s, learned over plain)",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 network (FP32 accumulate), f32 solver",
+            "data": "synthetic",
+            "config": {"workload": "rollout_256x128x128_2phase_256bubbles", "d": 0.005, "h": 0.01, "dt": 1e-4,
+                       "large_step": f"{factor} dt", "audit_every_large_steps": audit_every, "tolerance": tol,
+                       "simulated_s": sim_steps * 1e-4, "eos": "linear k=3",
+                       "training": "3 scenes of 64x32x32 with the same physics (4 bubbles each, or all liquid), "
+                                   "16 starts each, 1500 Adam steps at 65,536 per batch, lr 1e-3",
+                       "timing": "host clock around each arm (the rollout synchronises at its audits)"},
+            "cases": cases, "training": training}
+    print(json.dumps(line))
+    return 0
+
+
 def device_ref_scene(seed):
     """The benchmark lattice with the reference's only EOS (Tait) and liquid phases:
     the 1.2 kg/m^3 gas blobs become phase-0 liquid (Tait diverges next to them)."""
@@ -650,10 +767,13 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-every", type=int, default=100, help="steps between per-stage timing samples")
-    ap.add_argument("--workload", default="blobs", choices=["blobs", "batched", "large_step", "device_ref"],
+    ap.add_argument("--learned-steps", type=int, default=1280,
+                    help="simulated time of the learned workload's rollout, in plain steps of dt")
+    ap.add_argument("--workload", default="blobs", choices=["blobs", "batched", "large_step", "device_ref", "learned"],
                     help="blobs: the headline 2^20-particle scene; batched: 512 tiled bubble scenes; "
                          "large_step: one 8 dt step against 8 plain steps; device_ref: the Tait liquid lattice "
-                         "(with --impl reference: the reference's own GPU kernels)")
+                         "(with --impl reference: the reference's own GPU kernels); learned: corrector training "
+                         "and the audited rollout of the 256x128x128 bubble lattice against the plain pipeline")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -665,6 +785,8 @@ def main():
         return run_batched(args)
     if args.workload == "large_step":
         return run_large_step(args)
+    if args.workload == "learned":
+        return run_learned(args)
     return run_gpu(args)
 
 

@@ -266,6 +266,10 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(cudaMemset(B.color, 0, sizeof(float4) * N));
     CK(cudaMemset(B.bornid, 0, sizeof(int32_t) * N));
     CK(cudaMemset(B.mass_raw, 0, sizeof(float) * N));
+    // cudaMemset runs on the legacy default stream, which the context's
+    // non-blocking stream does not wait for: without this wait a first upload
+    // or state copy could be overwritten by a zero fill that runs after it
+    CK(cudaDeviceSynchronize());
     return SPHMP_OK;
 }
 

@@ -417,6 +417,8 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
         A(&c->loss_part, B / 256 + 1);
         A(&c->loss, 1);
     }
+    if (st == SPHMP_OK && cudaDeviceSynchronize() != cudaSuccess)  // the zero fills (legacy default stream)
+        st = lfail(SPHMP_ERR_CUDA, "zero fill of the corrector's buffers failed");
     if (st != SPHMP_OK) {
         sphmp_corrector_destroy(c);
         return st;

@@ -208,6 +208,36 @@ def bubble_scene(seed, n_particles, d=0.01, h=0.02, dt=2e-4, eos=abi.EOS_LINEAR,
     return _finish(p, disp, calc, count, n_fluid, f"bubbles_{nx}x{ny}x{nz}")
 
 
+def rollout_bubbles(seed=9, lattice=(256, 128, 128), d=0.005, h=0.01, dt=1e-4, n_bubbles=256, liquid_only=False,
+                    eos=abi.EOS_LINEAR, eos_k=3.0):
+    """The learned-corrector rollout scene: a lattice block (x, y, z sites at spacing d, +-0.05 d jitter) in
+    the low corner of an open box 4h longer in x and z and 1.25x taller than the block, two phases
+    (liquid 1000, gas 1.2 kg/m^3) with `n_bubbles` gas spheres of radius U(2h, 10h) centred uniformly in
+    the block; `liquid_only` keeps every particle liquid (same lattice, no bubbles)."""
+    rng = np.random.default_rng(seed)
+    ext = np.asarray(lattice, np.float64) * d
+    box = (float(ext[0] + 4 * h), float(ext[1] * 1.25), float(ext[2] + 4 * h))
+    bmin = (0.0, 0.0, 0.0)
+    p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=box, nphase=2, dens=(1000.0, 1.2), visc=(0.2, 0.2),
+                    eos=eos, eos_k=eos_k, multiphase=1)
+    nx, ny, nz = [int(b / d) + 8 for b in box]
+    cap = int(np.prod(lattice)) + 2 * (nx * nz + 2 * nx * ny + 2 * nz * ny) + 4096
+    disp, calc = record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, lattice, d, 0.05, seed)
+    n_fluid = count
+    if not liquid_only:
+        pos = disp["pos"][:count]
+        gas = np.zeros(count, bool)
+        centres = (rng.uniform(0.0, 1.0, size=(n_bubbles, 3)) * ext).astype(np.float32)
+        radii = rng.uniform(2 * h, 10 * h, size=n_bubbles).astype(np.float32)
+        for c, r in zip(centres, radii):
+            gas |= np.sum((pos - c) ** 2, axis=1) < r * r
+        _assign_phase(p, calc, np.nonzero(gas)[0], 1)
+    count = _walls(p, disp, calc, count, bmin, box, d)
+    name = ("liquid_" if liquid_only else "bubbles_") + "x".join(str(v) for v in lattice)
+    return _finish(p, disp, calc, count, n_fluid, name)
+
+
 def tile(scene_list, gap_cells=2):
     """Independent scenes in one domain, so that every pass covers all of them in one launch: each scene
     is moved into its own tile of a 3D arrangement (x fastest, then z, then y), tiles separated by

@@ -189,6 +189,22 @@ def test_copy_state_equals_save_and_load(built, tmp_path):
         c.close()
 
 
+def test_copy_into_fresh_full_size_contexts_keeps_every_field(built):
+    """Copies of a 4.5M-particle state into contexts created just before: the
+    creation's zero fill must be complete before the copy writes (it once ran on
+    another stream and overwrote copied masses)."""
+    sc = scenes.rollout_bubbles(seed=9, liquid_only=True)
+    src = _run(sc, 2)
+    want = src.download_aos()
+    for _ in range(2):
+        c = sphmp.Context(sc.params)
+        c.copy_state_from(src)
+        d, cc = c.download_aos()
+        assert d.tobytes() == want[0].tobytes() and cc.tobytes() == want[1].tobytes()
+        c.close()
+    src.close()
+
+
 def test_features_match_oracle(built):
     sc = _liquid_scene(4096, 12)
     src = _run(sc, 60)
