@@ -4,7 +4,8 @@
 // pass and Adam.
 //
 // * k_mlp_forward: all four layers of 128-particle tiles in one persistent
-//   kernel. The weights stay in shared memory; each layer is one chain of MMAs
+//   kernel, four tiles in flight per CTA. The weights stay in shared memory;
+//   each layer is one chain of MMAs
 //   into TMEM, and its epilogue (bias, SiLU, bf16) writes the next layer's
 //   operand tile back into shared memory. With the training saves it also
 //   stores the pre-activations (FP32) and the bf16 activations transposed
@@ -46,18 +47,27 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
 // Fused forward
 // ---------------------------------------------------------------------------
 
-constexpr int kFwdThreads = 256;  // 8 warps: lane quadrant (w % 4), column half (w / 4)
+constexpr int kGroups = 4;                     // tiles in flight per CTA
+constexpr int kGroupThreads = 128;             // 4 warps: one TMEM lane quadrant each
+constexpr int kFwdThreads = kGroups * kGroupThreads;
 constexpr int kTile = 128;
 // dynamic shared memory of the forward kernel
 constexpr int kOffW1 = 0;                                  // [128 rows][64] kc 64
 constexpr int kOffW2 = kOffW1 + kHidden * kInPad * 2;      // [128][128]
 constexpr int kOffW3 = kOffW2 + kHidden * kHidden * 2;     // [128][128]
 constexpr int kOffW4 = kOffW3 + kHidden * kHidden * 2;     // [16][128]
-constexpr int kOffAct = kOffW4 + kOutPad * kHidden * 2;    // [128][128] operand tile
-constexpr int kOffBias = kOffAct + kTile * kHidden * 2;    // 3 * 128 + 16 floats
+constexpr int kOffAct = kOffW4 + kOutPad * kHidden * 2;    // kGroups x [128][128] operand tiles
+constexpr int kActBytes = kTile * kHidden * 2;
+constexpr int kOffBias = kOffAct + kGroups * kActBytes;    // 3 * 128 + 16 floats
 constexpr int kOffNorm = kOffBias + (3 * kHidden + kOutPad) * 4;  // shift[48], scale[48]
 constexpr int kFwdSmem = kOffNorm + 2 * kFeatures * 4;
-constexpr uint32_t kFwdTmemCols = 256;  // [0, 128): layers 1-3, [128, 144): layer 4
+// TMEM: group g uses columns [128 g, 128 g + 128) for layers 1-3 and the first
+// 16 of them again for layer 4 (after layer 3's epilogue has read them)
+constexpr uint32_t kGroupTmemCols = 128;
+constexpr uint32_t kFwdTmemCols = kGroups * kGroupTmemCols;
+static_assert(kFwdTmemCols <= 512, "TMEM holds 512 columns");
+static_assert(kFwdSmem > 116 * 1024, "one CTA per SM: the TMEM allocation takes every column");
+static_assert(kFwdSmem <= 227 * 1024, "shared memory of one CTA");
 
 __device__ __forceinline__ void stage_weights(uint8_t* dst, const bf16* src, int rows, int kc, int tid,
                                               int nthreads) {
@@ -76,7 +86,7 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t act, uint32_
     tc::mma_commit(bar);
 }
 
-// Every thread waits; the CTA agrees on the outcome (a barrier).
+// Every thread of the CTA waits; the CTA agrees on the outcome (a barrier).
 __device__ __forceinline__ bool wait_all(uint64_t* bar, uint32_t& parity) {
     const bool ok = tc::mbar_wait(bar, parity, tc::kWaitLimitNs);
     parity ^= 1u;
@@ -92,16 +102,44 @@ __device__ __forceinline__ void handoff_to_mma() {
     __syncthreads();
 }
 
-// Epilogue of a hidden layer: bias + SiLU of this thread's 64 columns, the
-// bf16 activations into the operand tile (K = 128), and the training saves.
-__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lane, int half, const float* bias,
-                                                uint8_t* act, int row0, int n, float* z_save, bf16* ht_save,
-                                                int ldh) {
+// The same for the 128 threads of one tile group (named barrier 1 + g).
+__device__ __forceinline__ void group_sync(int g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(kGroupThreads) : "memory");
+}
+__device__ __forceinline__ bool group_all(int g, bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, %3, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + g), "r"(kGroupThreads)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ bool group_wait(uint64_t* bar, uint32_t& parity, int g) {
+    const bool ok = tc::mbar_wait(bar, parity, tc::kWaitLimitNs);
+    parity ^= 1u;
+    const bool all = group_all(g, ok);
+    tc::fence_after_sync();
+    return all;
+}
+__device__ __forceinline__ void group_handoff(int g) {
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    group_sync(g);
+}
+
+// Epilogue of a hidden layer for this thread's row (all 128 columns): bias +
+// SiLU, the bf16 activations into the operand tile (K = 128), the training saves.
+__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lane, const float* bias, uint8_t* act,
+                                                int row0, int n, float* z_save, bf16* ht_save, int ldh) {
     const int r = (warp & 3) * 32 + lane;
     const int grow = row0 + r;
     const bool live = grow < n;
 #pragma unroll 1
-    for (int c0 = half * 64; c0 < half * 64 + 64; c0 += 16) {
+    for (int c0 = 0; c0 < kHidden; c0 += 16) {
         float v[16];
         tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, c0), v);
         float h[16];
@@ -128,14 +166,18 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lan
     }
 }
 
+// kGroups independent tile pipelines per CTA (4 warps each), so that one
+// group's epilogue runs while the others' MMAs and loads are in flight; the
+// weights in shared memory are shared.
 __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __restrict__ x, int n,
                                                                  const Packed W, const Saves S,
                                                                  float* __restrict__ y, uint32_t* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bars[kGroups];
     __shared__ uint32_t tmem_base;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, half = warp >> 2;
-    uint8_t* act = smem + kOffAct;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = tid / kGroupThreads, gt = tid % kGroupThreads;
+    uint8_t* act = smem + kOffAct + g * kActBytes;
     float* bias = reinterpret_cast<float*>(smem + kOffBias);
     float* fshift = reinterpret_cast<float*>(smem + kOffNorm);
     float* fscale = fshift + kFeatures;
@@ -153,104 +195,98 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
         tc::tmem_alloc(&tmem_base, kFwdTmemCols);
         tc::tmem_relinquish();
     }
-    if (tid == 0) tc::mbar_init(&bar, 1);
+    if (tid == 0)
+        for (int k = 0; k < kGroups; k++) tc::mbar_init(&bars[k], 1);
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = tmem_base;
+    const uint32_t tmem = tmem_base + (uint32_t)g * kGroupTmemCols;
     const uint32_t a_act = tc::smem_addr(act);
+    uint64_t* bar = &bars[g];
     uint32_t parity = 0;
     bool ok = true;
     const int ntiles = (n + kTile - 1) / kTile;
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    for (int t = kGroups * blockIdx.x + g; t < ntiles && ok; t += kGroups * gridDim.x) {
         const int row0 = t * kTile;
         // input tile: normalised features, bf16, K padded to 64 with zeros
         {
-            const int r = tid >> 1, part = tid & 1;  // features [24 part, 24 part + 24)
+            const int r = gt;
             const int grow = row0 + r;
-            float f[24];
-            if (grow < n) {
-                const float4* src = reinterpret_cast<const float4*>(x + (size_t)grow * kFeatures + part * 24);
+            const bool live = grow < n;
+            const float4* src = reinterpret_cast<const float4*>(x + (size_t)(live ? grow : 0) * kFeatures);
+#pragma unroll 2
+            for (int c = 0; c < kFeatures / 8; c++) {  // 8 features at a time
+                float f[8];
+                const float4 a = live ? src[2 * c] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 b = live ? src[2 * c + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+                f[0] = a.x; f[1] = a.y; f[2] = a.z; f[3] = a.w; f[4] = b.x; f[5] = b.y; f[6] = b.z; f[7] = b.w;
 #pragma unroll
-                for (int i = 0; i < 6; i++) {
-                    const float4 q = src[i];
-                    f[4 * i] = q.x; f[4 * i + 1] = q.y; f[4 * i + 2] = q.z; f[4 * i + 3] = q.w;
-                }
-#pragma unroll
-                for (int i = 0; i < 24; i++) f[i] = (f[i] - fshift[part * 24 + i]) * fscale[part * 24 + i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < 24; i++) f[i] = 0.f;
-            }
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
+                for (int i = 0; i < 8; i++) f[i] = live ? (f[i] - fshift[8 * c + i]) * fscale[8 * c + i] : 0.f;
                 uint4 q;
-                q.x = pack2(f[8 * c], f[8 * c + 1]); q.y = pack2(f[8 * c + 2], f[8 * c + 3]);
-                q.z = pack2(f[8 * c + 4], f[8 * c + 5]); q.w = pack2(f[8 * c + 6], f[8 * c + 7]);
-                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, part * 24 + 8 * c, kInPad)) = q;
-            }
-            if (part == 1) {
-                const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
-                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 48, kInPad)) = zero;
-                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 56, kInPad)) = zero;
-            }
-            if (S.h0t && grow < n) {
+                q.x = pack2(f[0], f[1]); q.y = pack2(f[2], f[3]); q.z = pack2(f[4], f[5]); q.w = pack2(f[6], f[7]);
+                *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 8 * c, kInPad)) = q;
+                if (S.h0t && live) {
 #pragma unroll
-                for (int i = 0; i < 24; i++) S.h0t[(size_t)(part * 24 + i) * S.ldh + grow] = __float2bfloat16_rn(f[i]);
+                    for (int i = 0; i < 8; i++) S.h0t[(size_t)(8 * c + i) * S.ldh + grow] = __float2bfloat16_rn(f[i]);
+                }
             }
+            const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+            *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 48, kInPad)) = zero;
+            *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 56, kInPad)) = zero;
         }
-        handoff_to_mma();
+        group_handoff(g);
         // layer 1
-        if (tid == 0) {
+        if (gt == 0) {
             tc::fence_after_sync();
-            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW1), kInPad, kHidden, &bar);
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW1), kInPad, kHidden, bar);
         }
-        if (!(ok = wait_all(&bar, parity))) break;
-        hidden_epilogue(tmem, warp, lane, half, bias, act, row0, n, S.z1, S.h1t, S.ldh);
-        handoff_to_mma();
+        if (!(ok = group_wait(bar, parity, g))) break;
+        hidden_epilogue(tmem, warp, lane, bias, act, row0, n, S.z1, S.h1t, S.ldh);
+        group_handoff(g);
         // layer 2
-        if (tid == 0) {
+        if (gt == 0) {
             tc::fence_after_sync();
-            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW2), kHidden, kHidden, &bar);
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW2), kHidden, kHidden, bar);
         }
-        if (!(ok = wait_all(&bar, parity))) break;
-        hidden_epilogue(tmem, warp, lane, half, bias + kHidden, act, row0, n, S.z2, S.h2t, S.ldh);
-        handoff_to_mma();
+        if (!(ok = group_wait(bar, parity, g))) break;
+        hidden_epilogue(tmem, warp, lane, bias + kHidden, act, row0, n, S.z2, S.h2t, S.ldh);
+        group_handoff(g);
         // layer 3
-        if (tid == 0) {
+        if (gt == 0) {
             tc::fence_after_sync();
-            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW3), kHidden, kHidden, &bar);
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW3), kHidden, kHidden, bar);
         }
-        if (!(ok = wait_all(&bar, parity))) break;
-        hidden_epilogue(tmem, warp, lane, half, bias + 2 * kHidden, act, row0, n, S.z3, S.h3t, S.ldh);
-        handoff_to_mma();
+        if (!(ok = group_wait(bar, parity, g))) break;
+        hidden_epilogue(tmem, warp, lane, bias + 2 * kHidden, act, row0, n, S.z3, S.h3t, S.ldh);
+        group_handoff(g);
         // layer 4 (N = 16: outputs 0..3 and zero padding)
-        if (tid == 0) {
+        if (gt == 0) {
             tc::fence_after_sync();
-            issue_layer(tmem + kHidden, a_act, tc::smem_addr(smem + kOffW4), kHidden, kOutPad, &bar);
+            issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW4), kHidden, kOutPad, bar);
         }
-        if (!(ok = wait_all(&bar, parity))) break;
-        if (half == 0) {
+        if (!(ok = group_wait(bar, parity, g))) break;
+        {
             float v[16];
-            tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, kHidden), v);
-            const int grow = row0 + (warp & 3) * 32 + lane;
+            tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, 0), v);
+            const int grow = row0 + gt;
             const float* b4 = bias + 3 * kHidden;
             if (grow < n)
                 reinterpret_cast<float4*>(y)[grow] = make_float4(v[0] + b4[0], v[1] + b4[1], v[2] + b4[2], v[3] + b4[3]);
         }
+        // the accumulator reads above come before the next tile's first MMA
         tc::fence_before_sync();
-        __syncthreads();
+        group_sync(g);
         tc::fence_after_sync();
     }
     if (!ok) {
-        if (tid == 0) atomicOr(err, kErrMmaTimeout);
-        tc::mbar_wait(&bar, parity ^ 1u, tc::kWaitLimitNs);  // the chain still in flight, bounded
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
+        if (gt == 0) atomicOr(err, kErrMmaTimeout);
+        tc::mbar_wait(bar, parity ^ 1u, tc::kWaitLimitNs);  // the chain still in flight, bounded
     }
-    if (warp == 0) tc::tmem_dealloc(tmem, kFwdTmemCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem_base, kFwdTmemCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -502,7 +538,8 @@ cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& 
         attr_set = true;
     }
     const int tiles = (n + kTile - 1) / kTile;
-    const int grid = tiles < num_sms ? tiles : num_sms;
+    const int pairs = (tiles + kGroups - 1) / kGroups;
+    const int grid = pairs < num_sms ? pairs : num_sms;
     k_mlp_forward<<<grid, kFwdThreads, kFwdSmem, s>>>(x, n, W, S, y, err);
     return cudaGetLastError();
 }
