@@ -9,7 +9,9 @@ numpy, with the same rounding points:
   SiLU. Inputs (features - shift) * scale, weights, hidden activations and the
   backward's dY / dZ are rounded to bf16 (round to nearest even) where the GPU
   feeds them to the tensor cores; products are summed in float64 here (FP32 in
-  TMEM on the GPU), so the two agree to the accumulation rounding.
+  TMEM on the GPU), and SiLU is exact here (the GPU's forward pass computes it
+  as z/2 (1 + tanh(z/2)) with the hardware tanh), so the two agree to the
+  accumulation rounding and an occasional bf16 rounding step of an activation.
   Loss = sum over the batch and the 4 outputs of (y - t)^2, divided by the batch.
 * adam: one Adam step with bias correction (beta1 0.9, beta2 0.999, eps 1e-8).
 * features: the 48 per-particle features of include/sphmp_learned.h's large

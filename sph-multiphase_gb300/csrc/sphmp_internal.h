@@ -200,11 +200,12 @@ void launch_set_count(const DevBuffers& B, int n, cudaStream_t s);
 // device-side emission into the current buffers (one block)
 void launch_emit(const DevParams& P, const DevBuffers& B, const int* cur, const DevEmitter& E, cudaStream_t s);
 
-// learned large step (sphmp_learned.cu): the corrector's features of every
-// in-grid fluid particle after the density pass (feat [n][48], ids = bornid or
-// -1), and the correction of the step's result by the network outputs y [n][4]
-void launch_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids, float vs,
-                     float dt_large, cudaStream_t s);
+// learned large step: the force (+ drift) pass that also fills the corrector's
+// features of every particle (feat [n][48], ids = bornid, -1 without features;
+// sphmp_kernels.cu), and the correction of the step's result by the network
+// outputs y [n][4] (sphmp_learned.cu)
+void launch_force_drift_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids,
+                                 float vs, float dt_large, cudaStream_t s);
 void launch_apply_correction(const DevParams& P, const DevBuffers& B, const int* cur, const float* y,
                              const float* out_scale, const int32_t* ids, float dt_large, float* corr, cudaStream_t s);
 

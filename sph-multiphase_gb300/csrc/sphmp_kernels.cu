@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include "sphmp_device.cuh"
+#include "sphmp_features.cuh"
 #include "sphmp_emit.h"
 #include "sphmp_internal.h"
 
@@ -806,6 +807,55 @@ __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_consta
     force_drift_one<FORCE, DRIFT, NP>(P, B, pos4, vel4, alpha4, aprev4, vev4, s, pi);
 }
 
+// Force + drift of a corrected large step: the same pass, also filling the
+// corrector's features from the neighbours it gathers (alpha4 is gathered
+// even without drift). Features and ids cover every particle; 128 registers.
+template <bool DRIFT, int NP>
+__global__ void __launch_bounds__(kThreads, 2) k_force_drift_feat(const __grid_constant__ DevParams P,
+                                                                  const __grid_constant__ DevBuffers B,
+                                                                  const float4* __restrict__ pos4,
+                                                                  const float4* __restrict__ vel4,
+                                                                  const float4* __restrict__ alpha4,
+                                                                  const float4* __restrict__ aprev4,
+                                                                  const float4* __restrict__ vev4, float* feat,
+                                                                  int32_t* ids, float vs, float dt_large) {
+    const int s = blockIdx.x * kThreads + threadIdx.x;
+    if (s >= active_n(B)) return;
+    float* row = feat + (size_t)s * kLearnedFeatures;
+    if (B.mgcell[s] == kUndef) {
+        store_no_features(row, &ids[s]);
+        return;
+    }
+    const float4 pi = pos4[s];
+    if (pi.w < 0.f) {
+        B.accel4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (DRIFT) {
+            const float a0[3] = {0.f, 0.f, 0.f};
+            const float u0[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            write_nrec(B, s, pi, -1.f, make_float4(0.f, 0.f, 0.f, 0.f), a0, u0);
+        }
+        store_no_features(row, &ids[s]);
+        return;
+    }
+    const float4 vi = vel4[s], ai = alpha4[s], gi = aprev4[s];
+    const float2 di = B.densp[s];
+    ForceDrift<true, DRIFT, NP> acc;
+    acc.init(P, pi, vi, di, ai);
+    LearnedFeatures lf;
+    lf.init(P, pi, vi, ai, di, gi, vs, dt_large);
+    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        const float2 dpj = __ldg(&B.densp[j]);
+        const float4 vj = __ldg(&vel4[j]);
+        const float4 aj = __ldg(&alpha4[j]);
+        acc.pair(P, pj, dpj, vj, aj);
+        lf.pair(P, pj, dpj, vj, aj);
+    });
+    acc.finish(P, B, s, DRIFT ? gi : make_float4(0.f, 0.f, 0.f, 0.f), DRIFT ? vev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
+    lf.store(row);
+    ids[s] = B.bornid[__float_as_uint(gi.w)];
+}
+
 // Surface tension (reference SurfaceTension, fluid_system_kern.cu:569-625): all
 // 27 cells, squared distance compared with the radius K*h, added to accel.
 __global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_constant__ DevParams P,
@@ -1463,6 +1513,26 @@ void launch_force_drift(const DevParams& P, const DevBuffers& B, const int* cur,
     if (force && drift) fd_dispatch<true, true>(P, B, cur, s);
     else if (force) fd_dispatch<true, false>(P, B, cur, s);
     else fd_dispatch<false, true>(P, B, cur, s);
+}
+
+void launch_force_drift_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids,
+                                 float vs, float dt_large, cudaStream_t s) {
+    if (P.n <= 0) return;
+    const float4* pos = B.f4[POS][cur[POS]];
+    const float4* vel = B.f4[VEL][cur[VEL]];
+    const float4* al = B.f4[ALPHA][cur[ALPHA]];
+    const float4* ap = B.f4[APREV][cur[APREV]];
+    const float4* ve = B.f4[VEV][cur[VEV]];
+    const int g = blocks_for(P.n);
+    if (!P.multiphase) {
+        k_force_drift_feat<false, 0><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve, feat, ids, vs, dt_large);
+        return;
+    }
+    switch (P.nphase) {
+        case 1: k_force_drift_feat<true, 1><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve, feat, ids, vs, dt_large); break;
+        case 2: k_force_drift_feat<true, 2><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve, feat, ids, vs, dt_large); break;
+        default: k_force_drift_feat<true, 3><<<g, kThreads, 0, s>>>(P, B, pos, vel, al, ap, ve, feat, ids, vs, dt_large); break;
+    }
 }
 
 void launch_surface_tension(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {

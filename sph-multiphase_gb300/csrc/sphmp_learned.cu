@@ -1,7 +1,8 @@
-// sphmp_learned.cu — the learned large-step corrector: the per-particle feature
-// kernel, the correction kernel, and the network object (sphmp_corrector:
+// sphmp_learned.cu — the learned large-step corrector: the correction kernel,
+// the state comparison of the audit, and the network object (sphmp_corrector:
 // parameters, Adam state, training buffers) with its C ABI
-// (include/sphmp_learned.h). The network kernels are in sphmp_mlp.cu.
+// (include/sphmp_learned.h). The network kernels are in sphmp_mlp.cu; the
+// features are filled by the force pass of a corrected step (sphmp_features.cuh).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -26,100 +27,6 @@ using bf16 = __nv_bfloat16;
 
 namespace sphmp {
 namespace {
-
-using dev::for_slot_list;
-
-// Features of an in-grid fluid particle, from the state after the density pass
-// of a step (pos, vel, 1/rho and p, fractions and rest density, g - a of the
-// last advance) over its neighbours closer than h. With w = (1 - r^2/h^2)^3,
-// g = (1 - r/h)^2, x_ij = x_i - x_j (metres), u = unit x_ij, vs = sqrt(|g| h):
-//   0-2  v_i / vs                     3   rho_i / rho0_i - 1
-//   4    p_i / (rho0_i vs^2)          5-7 alpha_i
-//   8-10 (g - a)_i dt_large / vs      11  sum_fluid w
-//   12-14 sum_fluid w x_ij / h        15-17 sum_fluid w (v_j - v_i) / vs
-//   18   sum_fluid w (rho_j/rho0_j - rho_i/rho0_i)
-//   19   sum_fluid w (p_j - p_i) / (rho0_i vs^2)
-//   20-22 sum_fluid w (alpha_j - alpha_i)
-//   23-28 sum_fluid w x x^T / h^2 (xx, yy, zz, xy, xz, yz)
-//   29-31 sum_fluid g u               32  sum_fluid g (v_j - v_i).u / vs
-//   33-35 sum_fluid g ((v_j - v_i) x u) / vs
-//   36-38 sum_fluid g (p_i + p_j) u / (rho0_i vs^2)
-//   39   fluid neighbours / 32        40  sum_boundary w
-//   41-43 sum_boundary w x_ij / h     44  boundary neighbours / 32
-//   45-47 sum_fluid g (alpha_j0 - alpha_i0) u
-__global__ void __launch_bounds__(128) k_features(const __grid_constant__ DevParams P,
-                                                  const __grid_constant__ DevBuffers B,
-                                                  const float4* __restrict__ pos4, const float4* __restrict__ vel4,
-                                                  const float4* __restrict__ alpha4,
-                                                  const float4* __restrict__ aprev4, float vs, float dt_large,
-                                                  float* __restrict__ feat, int32_t* __restrict__ ids) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= active_n(B)) return;
-    const float4 pi = pos4[s];
-    float4* out = reinterpret_cast<float4*>(feat + (size_t)s * mlp::kFeatures);
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!(pi.w > 0.f) || B.mgcell[s] == kUndef) {
-        for (int i = 0; i < mlp::kFeatures / 4; i++) out[i] = zero;
-        ids[s] = -1;
-        return;
-    }
-    const float4 vi = vel4[s], ai = alpha4[s], gi = aprev4[s];
-    const float2 di = B.densp[s];
-    const float rhoi = 1.f / di.x, rho0 = ai.w;
-    const float ivs = 1.f / vs, ips = 1.f / (rho0 * vs * vs), ih = 1.f / P.h;
-    const float reli = rhoi / rho0;
-    float f[mlp::kFeatures];
-#pragma unroll
-    for (int k = 0; k < mlp::kFeatures; k++) f[k] = 0.f;
-    f[0] = vi.x * ivs; f[1] = vi.y * ivs; f[2] = vi.z * ivs;
-    f[3] = reli - 1.f;
-    f[4] = di.y * ips;
-    f[5] = ai.x; f[6] = P.nphase > 1 ? ai.y : 0.f; f[7] = P.nphase > 2 ? ai.z : 0.f;
-    f[8] = gi.x * dt_large * ivs; f[9] = gi.y * dt_large * ivs; f[10] = gi.z * dt_large * ivs;
-    for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
-        const float4 pj = __ldg(&pos4[j]);
-        const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
-        const float dsq = dx * dx + dy * dy + dz * dz;
-        if (!(dsq < P.r2 && dsq > 0.f)) return;
-        const float r = sqrtf(dsq);
-        const float q2 = dsq / P.r2, q = r * ih;
-        const float w = (1.f - q2) * (1.f - q2) * (1.f - q2);
-        const float g = (1.f - q) * (1.f - q);
-        const float ux = dx / r, uy = dy / r, uz = dz / r;
-        if (pj.w < 0.f) {  // boundary
-            f[40] += w;
-            f[41] += w * dx * ih; f[42] += w * dy * ih; f[43] += w * dz * ih;
-            f[44] += 1.f / 32.f;
-            return;
-        }
-        const float4 vj = __ldg(&vel4[j]), aj = __ldg(&alpha4[j]);
-        const float2 dj = __ldg(&B.densp[j]);
-        const float dvx = vj.x - vi.x, dvy = vj.y - vi.y, dvz = vj.z - vi.z;
-        f[11] += w;
-        f[12] += w * dx * ih; f[13] += w * dy * ih; f[14] += w * dz * ih;
-        f[15] += w * dvx * ivs; f[16] += w * dvy * ivs; f[17] += w * dvz * ivs;
-        f[18] += w * (1.f / (dj.x * aj.w) - reli);
-        f[19] += w * (dj.y - di.y) * ips;
-        f[20] += w * (aj.x - ai.x);
-        f[21] += w * (P.nphase > 1 ? aj.y - ai.y : 0.f);
-        f[22] += w * (P.nphase > 2 ? aj.z - ai.z : 0.f);
-        f[23] += w * dx * dx * ih * ih; f[24] += w * dy * dy * ih * ih; f[25] += w * dz * dz * ih * ih;
-        f[26] += w * dx * dy * ih * ih; f[27] += w * dx * dz * ih * ih; f[28] += w * dy * dz * ih * ih;
-        f[29] += g * ux; f[30] += g * uy; f[31] += g * uz;
-        f[32] += g * (dvx * ux + dvy * uy + dvz * uz) * ivs;
-        f[33] += g * (dvy * uz - dvz * uy) * ivs;
-        f[34] += g * (dvz * ux - dvx * uz) * ivs;
-        f[35] += g * (dvx * uy - dvy * ux) * ivs;
-        const float pp = g * (di.y + dj.y) * ips;
-        f[36] += pp * ux; f[37] += pp * uy; f[38] += pp * uz;
-        f[39] += 1.f / 32.f;
-        const float da = g * (aj.x - ai.x);
-        f[45] += da * ux; f[46] += da * uy; f[47] += da * uz;
-    });
-#pragma unroll
-    for (int i = 0; i < mlp::kFeatures / 4; i++) out[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
-    ids[s] = B.bornid[__float_as_uint(gi.w)];
-}
 
 // Apply the network's outputs (times out_scale) to the step's result.
 __global__ void __launch_bounds__(256) k_apply_correction(const __grid_constant__ DevParams P,
@@ -230,14 +137,6 @@ void launch_compare(const DevParams& Pa, const DevBuffers& Ba, const int* cur_a,
                                           Bb.f4[ALPHA][cur_b[ALPHA]], Bb.f4[APREV][cur_b[APREV]], Ba.densp,
                                           Ba.f4[VEL][cur_a[VEL]], Ba.f4[ALPHA][cur_a[ALPHA]], map, map_size,
                                           Pb.nphase, out);
-}
-
-void launch_features(const DevParams& P, const DevBuffers& B, const int* cur, float* feat, int32_t* ids, float vs,
-                     float dt_large, cudaStream_t s) {
-    if (P.n <= 0) return;
-    k_features<<<(P.n + 127) / 128, 128, 0, s>>>(P, B, B.f4[POS][cur[POS]], B.f4[VEL][cur[VEL]],
-                                                 B.f4[ALPHA][cur[ALPHA]], B.f4[APREV][cur[APREV]], vs, dt_large,
-                                                 feat, ids);
 }
 
 void launch_apply_correction(const DevParams& P, const DevBuffers& B, const int* cur, const float* y,

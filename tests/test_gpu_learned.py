@@ -4,9 +4,10 @@ its CPU oracle (oracle/learned.py):
 * the tcgen05 GEMM against float64 products of the same bf16 operands
   (relative error below 1e-5: FP32 accumulation);
 * the fused forward pass, the backward pass and Adam against the oracle with
-  the same bf16 rounding points (outputs within 1e-3 of their largest
-  magnitude, gradients within 1e-3 relative per tensor: only the FP32
-  accumulation order and SiLU's exp differ);
+  the same bf16 rounding points (outputs within 3e-3 of their largest
+  magnitude and a median error below 1e-5 of it, gradients within 1e-3
+  relative per tensor: only the FP32 accumulation order and the forward's
+  hardware tanh in SiLU differ);
 * the features against the oracle's restatement (relative 1e-4 per feature);
 * the correction applied exactly as stated, the device state copy equal to
   saving and loading, the audit's fallback;
@@ -78,7 +79,9 @@ def test_forward_matches_oracle(built, n):
     ref, _ = OL.mlp_forward(p, shift, scale, X)
     got = y.cpu().numpy()
     assert np.isfinite(got).all()
-    assert np.abs(got - ref).max() <= 1e-3 * np.abs(ref).max()
+    # the forward's SiLU uses the hardware tanh (relative error about 2^-11): now
+    # and then it moves a hidden activation across a bf16 rounding boundary
+    assert np.abs(got - ref).max() <= 3e-3 * np.abs(ref).max()
     assert np.median(np.abs(got - ref)) <= 1e-5 * np.abs(ref).max()
     cor.close()
 
