@@ -550,16 +550,21 @@ def run_learned(args):
     cases, training = {}, {}
     for case in ("bubbles", "liquid"):
         liquid = case == "liquid"
-        # training pairs: three 65,536-particle scenes of the same physics, 16 starts each
+        # training pairs: three scenes of the rollout's physics and depth (64 x 128 x 64 sites,
+        # 32 bubbles: the rollout lattice's bubble density), 16 starts spread over the rollout's
+        # time span, a quarter of each start's particles
         t0 = time.perf_counter()
         Xs, Ts = [], []
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(3)
         for seed in (21, 22, 23):
-            sc = scenes.rollout_bubbles(seed=seed, lattice=(64, 32, 32), n_bubbles=4, liquid_only=liquid)
-            c = fresh(sc, 100)
+            sc = scenes.rollout_bubbles(seed=seed, lattice=(64, 128, 64), n_bubbles=32, liquid_only=liquid)
+            c = fresh(sc, 50)
             large, plain = sphmp.Context(sc.params), sphmp.Context(sc.params)
-            X, T = SL.generate_pairs(c, large, plain, factor, starts=16, gap=10)
-            Xs.append(X)
-            Ts.append(np.nan_to_num(T, nan=0.0, posinf=0.0, neginf=0.0))
+            X, T = SL.generate_pairs(c, large, plain, factor, starts=16, gap=max(1, sim_steps // 16))
+            keep = torch.randperm(X.shape[0], device=dev, generator=gen)[: X.shape[0] // 4]
+            Xs.append(X[keep])
+            Ts.append(np.nan_to_num(T[keep.cpu().numpy()], nan=0.0, posinf=0.0, neginf=0.0))
             for x in (c, large, plain):
                 x.close()
         X, T = torch.cat(Xs), np.concatenate(Ts)
@@ -624,6 +629,35 @@ def run_learned(args):
                 ctx.close()
                 aud.close()
                 ref.close()
+        if liquid:
+            # two references for the end-of-run difference: the same audited rollout without the
+            # network, and the plain pipeline from the start state moved by one ulp in x (how far
+            # two faithful trajectories drift apart over the same time)
+            ref = sphmp.Context(sc.params)
+            ref.copy_state_from(src)
+            ref.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
+            ref.sort()
+            ref.compute_pressure()
+            for arm in ("uncorrected", "plain_one_ulp"):
+                ctx = sphmp.Context(sc.params)
+                ctx.copy_state_from(src)
+                if arm == "uncorrected":
+                    aud = sphmp.Context(sc.params)
+                    st = ctx.rollout(aud, sim_steps, factor=factor, corrector=None, audit_every=audit_every, tol=tol)
+                    aud.close()
+                    res[arm] = {"stats": st}
+                else:
+                    pos = ctx.download_field(abi.F_POS)
+                    pos[:, 0] = np.nextafter(pos[:, 0], np.float32(np.inf))
+                    ctx.upload_field(abi.F_POS, pos)
+                    ctx.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
+                    res[arm] = {}
+                ctx.sort()
+                ctx.compute_pressure()
+                res[arm]["vs_plain_at_end"] = ctx.compare_to(ref)
+                print(f"learned/{case}/{arm}: {res[arm]}", file=sys.stderr, flush=True)
+                ctx.close()
+            ref.close()
         res["sim_s_per_wall_s_ratio"] = res["learned"]["sim_s_per_wall_s"] / res["plain"]["sim_s_per_wall_s"]
         cases[case] = res
         src.close()
@@ -635,8 +669,9 @@ def run_learned(args):
             "config": {"workload": "rollout_256x128x128_2phase_256bubbles", "d": 0.005, "h": 0.01, "dt": 1e-4,
                        "large_step": f"{factor} dt", "audit_every_large_steps": audit_every, "tolerance": tol,
                        "simulated_s": sim_steps * 1e-4, "eos": "linear k=3",
-                       "training": "3 scenes of 64x32x32 with the same physics (4 bubbles each, or all liquid), "
-                                   "16 starts each, 1500 Adam steps at 65,536 per batch, lr 1e-3",
+                       "training": "3 scenes of 64x128x64 sites with the rollout's physics and depth (32 bubbles "
+                                   "each, or all liquid), 16 starts over the rollout's time span, a quarter of "
+                                   "each start's particles, 1500 Adam steps at 65,536 per batch, lr 1e-3",
                        "timing": "host clock around each arm (the rollout synchronises at its audits)"},
             "cases": cases, "training": training}
     print(json.dumps(line))

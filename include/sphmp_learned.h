@@ -6,9 +6,11 @@
  * The network: 48 neighbour-aggregated features -> 128 -> 128 -> 128 -> 4,
  * SiLU, bf16 weights and activations, FP32 accumulation on the tensor cores
  * (tcgen05), trained on the GPU with its own backward kernels and Adam. Its
- * outputs are a velocity correction (3, added to vel and veleval, with half of
- * it times the step added to the position) and a relative density correction
- * (the stored density of the step's result is multiplied by 1 + output).
+ * outputs are a correction of the particle's velocity over the step, applied to
+ * the position (3, m/s: the position moves by output x factor x dt; a step of
+ * 8 dt overshoots 8 steps of dt in position by 28 a dt^2 while its velocity
+ * agrees to second order) and a relative density correction (the stored
+ * density of the step's result is multiplied by 1 + output).
  *
  * The reference has no counterpart: this is a method on top of the reference's
  * step (the large step is the reference's own step with dt scaled).
@@ -80,7 +82,8 @@ sphmp_status sphmp_copy_state(sphmp_ctx* dst, sphmp_ctx* src);
    rho_b / rho_a - 1 over the stored densities, out[1] its largest magnitude,
    out[2] rms volume-fraction difference (root of the mean over particles of the
    sum over phases of the squared difference), out[3] rms |v_b - v_a| over rms
-   |v_a|, out[4] the particles compared. nout >= 5. */
+   |v_a|, out[4] the particles compared, out[5] (when nout >= 6) rms |x_b - x_a|
+   in metres. nout >= 5. */
 sphmp_status sphmp_compare_states(sphmp_ctx* a, sphmp_ctx* b, double* out, int32_t nout);
 
 typedef struct sphmp_rollout_stats {

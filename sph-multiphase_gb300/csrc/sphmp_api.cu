@@ -1179,19 +1179,20 @@ sphmp_status sphmp_compare_states(sphmp_ctx* a, sphmp_ctx* b, double* out, int32
         CK(cudaMalloc(&b->cmap, sizeof(int32_t) * (size_t)(msize > 0 ? msize : 1)));
         b->cmap_size = msize;
     }
-    if (!b->cred) CK(cudaMalloc(&b->cred, sizeof(double) * 6));
+    if (!b->cred) CK(cudaMalloc(&b->cred, sizeof(double) * 7));
     CK(cudaStreamSynchronize(a->stream));
     launch_compare(dev_params(a), a->B, a->cur, dev_params(b), b->B, b->cur, b->cmap, msize, b->cred, b->stream);
     CHECK_LAUNCH("compare states");
-    double r[6];
+    double r[7];
     CK(cudaMemcpyAsync(r, b->cred, sizeof(r), cudaMemcpyDeviceToHost, b->stream));
     CK(cudaStreamSynchronize(b->stream));
     const double m = r[4] > 0 ? r[4] : 1.0;
     out[0] = sqrt(r[0] / m);
-    out[1] = r[5];
+    out[1] = r[6];
     out[2] = sqrt(r[1] / m);
     out[3] = r[3] > 0 ? sqrt(r[2] / r[3]) : 0.0;
     out[4] = r[4];
+    if (nout > 5) out[5] = sqrt(r[5] / m);
     return SPHMP_OK;
 }
 

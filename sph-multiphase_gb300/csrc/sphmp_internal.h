@@ -210,7 +210,7 @@ void launch_apply_correction(const DevParams& P, const DevBuffers& B, const int*
                              const float* out_scale, const int32_t* ids, float dt_large, float* corr, cudaStream_t s);
 
 // differences of state b against state a (see sphmp_compare_states); map: scratch of map_size
-// entries (bornid -> index of a), out: 6 doubles (sums, then the maximum)
+// entries (bornid -> index of a), out: 7 doubles (6 sums, then the maximum)
 void launch_compare(const DevParams& Pa, const DevBuffers& Ba, const int* cur_a, const DevParams& Pb,
                     const DevBuffers& Bb, const int* cur_b, int32_t* map, int map_size, double* out, cudaStream_t s);
 

@@ -28,12 +28,18 @@ using bf16 = __nv_bfloat16;
 namespace sphmp {
 namespace {
 
-// Apply the network's outputs (times out_scale) to the step's result.
+constexpr float kOutClamp = 4.f;
+
+// Apply the network's outputs (times out_scale) to the step's result: outputs
+// 0-2 are a displacement rate c (m/s), the position moves by c * dt_large (the
+// large step's error is in its positions: a step of 8 dt overshoots 8 steps of
+// dt by 28 a dt^2 while its velocity agrees to second order); output 3 scales
+// the stored density of the result by 1 + output.
 __global__ void __launch_bounds__(256) k_apply_correction(const __grid_constant__ DevParams P,
                                                           const __grid_constant__ DevBuffers B, float4* pos4,
-                                                          float4* vel4, float4* vev4, const float4* __restrict__ y,
+                                                          const float4* __restrict__ y,
                                                           const float* __restrict__ out_scale,
-                                                          const int32_t* __restrict__ ids, float half_dt_over_ss,
+                                                          const int32_t* __restrict__ ids, float dt_over_ss,
                                                           float4* __restrict__ corr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= active_n(B)) return;
@@ -41,15 +47,15 @@ __global__ void __launch_bounds__(256) k_apply_correction(const __grid_constant_
         corr[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         return;
     }
+    // outputs beyond kOutClamp standard deviations of the training targets are
+    // extrapolation: clamped
     const float4 o = y[s];
-    const float cx = o.x * out_scale[0], cy = o.y * out_scale[1], cz = o.z * out_scale[2];
-    const float cd = fmaxf(o.w * out_scale[3], -0.5f);
-    float4 v = vel4[s], e = vev4[s], p = pos4[s];
-    v.x += cx; v.y += cy; v.z += cz;
-    e.x += cx; e.y += cy; e.z += cz;
-    p.x += cx * half_dt_over_ss; p.y += cy * half_dt_over_ss; p.z += cz * half_dt_over_ss;
-    vel4[s] = v;
-    vev4[s] = e;
+    const float ox = fminf(fmaxf(o.x, -kOutClamp), kOutClamp), oy = fminf(fmaxf(o.y, -kOutClamp), kOutClamp);
+    const float oz = fminf(fmaxf(o.z, -kOutClamp), kOutClamp), ow = fminf(fmaxf(o.w, -kOutClamp), kOutClamp);
+    const float cx = ox * out_scale[0], cy = oy * out_scale[1], cz = oz * out_scale[2];
+    const float cd = fmaxf(ow * out_scale[3], -0.5f);
+    float4 p = pos4[s];
+    p.x += cx * dt_over_ss; p.y += cy * dt_over_ss; p.z += cz * dt_over_ss;
     pos4[s] = p;
     float2 d = B.densp[s];
     d.x = d.x / (1.f + cd);
@@ -69,18 +75,23 @@ __global__ void k_id_map(const __grid_constant__ DevBuffers B, const float4* __r
 
 // Differences of state b against state a over the particles in-grid fluid in
 // both (matched by bornid): sums of (rho_b / rho_a - 1)^2, sum_k (alpha_b -
-// alpha_a)^2, |v_b - v_a|^2, |v_a|^2, the count, and max |rho_b / rho_a - 1|.
-__global__ void __launch_bounds__(256) k_compare(const __grid_constant__ DevBuffers Bb, const float4* __restrict__ pos_b,
+// alpha_a)^2, |v_b - v_a|^2, |v_a|^2, the count, |x_b - x_a|^2 (metres), and
+// max |rho_b / rho_a - 1|.
+constexpr int kCmpSums = 6;
+__global__ void __launch_bounds__(256) k_compare(const __grid_constant__ DevParams Pb,
+                                                 const __grid_constant__ DevBuffers Bb, const float4* __restrict__ pos_b,
                                                  const float4* __restrict__ vel_b, const float4* __restrict__ alpha_b,
                                                  const float4* __restrict__ aprev_b, const float2* __restrict__ dens_a,
-                                                 const float4* __restrict__ vel_a, const float4* __restrict__ alpha_a,
-                                                 const int32_t* __restrict__ map, int map_size, int nphase,
-                                                 double* __restrict__ out) {
-    __shared__ double sh[6][8];
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+                                                 const float4* __restrict__ pos_a, const float4* __restrict__ vel_a,
+                                                 const float4* __restrict__ alpha_a, const int32_t* __restrict__ map,
+                                                 int map_size, double* __restrict__ out) {
+    __shared__ double sh[kCmpSums + 1][8];
+    double acc[kCmpSums + 1] = {0, 0, 0, 0, 0, 0, 0};
     const int n = active_n(Bb);
+    const double ss = Pb.ss;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
-        if (!(pos_b[s].w > 0.f) || Bb.mgcell[s] == kUndef) continue;
+        const float4 pb = pos_b[s];
+        if (!(pb.w > 0.f) || Bb.mgcell[s] == kUndef) continue;
         const int32_t id = Bb.bornid[__float_as_uint(aprev_b[s].w)];
         if (id < 0 || id >= map_size) continue;
         const int32_t j = map[id];
@@ -88,38 +99,40 @@ __global__ void __launch_bounds__(256) k_compare(const __grid_constant__ DevBuff
         const double rel = (double)dens_a[j].x / (double)Bb.densp[s].x - 1.0;  // stored inverses
         const float4 ab = alpha_b[s], aa = alpha_a[j];
         double da = (double)(ab.x - aa.x) * (ab.x - aa.x);
-        if (nphase > 1) da += (double)(ab.y - aa.y) * (ab.y - aa.y);
-        if (nphase > 2) da += (double)(ab.z - aa.z) * (ab.z - aa.z);
-        const float4 vb = vel_b[s], va = vel_a[j];
+        if (Pb.nphase > 1) da += (double)(ab.y - aa.y) * (ab.y - aa.y);
+        if (Pb.nphase > 2) da += (double)(ab.z - aa.z) * (ab.z - aa.z);
+        const float4 vb = vel_b[s], va = vel_a[j], pa = pos_a[j];
+        const double dx = ((double)pb.x - pa.x) * ss, dy = ((double)pb.y - pa.y) * ss, dz = ((double)pb.z - pa.z) * ss;
         acc[0] += rel * rel;
         acc[1] += da;
         acc[2] += (double)(vb.x - va.x) * (vb.x - va.x) + (double)(vb.y - va.y) * (vb.y - va.y) +
                   (double)(vb.z - va.z) * (vb.z - va.z);
         acc[3] += (double)va.x * va.x + (double)va.y * va.y + (double)va.z * va.z;
         acc[4] += 1.0;
-        acc[5] = fmax(acc[5], fabs(rel));
+        acc[5] += dx * dx + dy * dy + dz * dz;
+        acc[6] = fmax(acc[6], fabs(rel));
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < 6; q++) {
+    for (int q = 0; q <= kCmpSums; q++) {
         double v = acc[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const double u = __shfl_xor_sync(0xffffffffu, v, o);
-            v = q == 5 ? fmax(v, u) : v + u;
+            v = q == kCmpSums ? fmax(v, u) : v + u;
         }
         if (lane == 0) sh[q][w] = v;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int q = 0; q < 5; q++) {
+        for (int q = 0; q < kCmpSums; q++) {
             double t = 0.0;
             for (int k = 0; k < 8; k++) t += sh[q][k];
             atomicAdd(&out[q], t);
         }
         double m = 0.0;
-        for (int k = 0; k < 8; k++) m = fmax(m, sh[5][k]);
-        atomicMax(reinterpret_cast<unsigned long long*>(&out[5]), (unsigned long long)__double_as_longlong(m));
+        for (int k = 0; k < 8; k++) m = fmax(m, sh[kCmpSums][k]);
+        atomicMax(reinterpret_cast<unsigned long long*>(&out[kCmpSums]), (unsigned long long)__double_as_longlong(m));
     }
 }
 
@@ -128,24 +141,24 @@ __global__ void __launch_bounds__(256) k_compare(const __grid_constant__ DevBuff
 void launch_compare(const DevParams& Pa, const DevBuffers& Ba, const int* cur_a, const DevParams& Pb,
                     const DevBuffers& Bb, const int* cur_b, int32_t* map, int map_size, double* out, cudaStream_t s) {
     cudaMemsetAsync(map, 0xFF, sizeof(int32_t) * (size_t)map_size, s);
-    cudaMemsetAsync(out, 0, sizeof(double) * 6, s);
+    cudaMemsetAsync(out, 0, sizeof(double) * (kCmpSums + 1), s);
     if (Pa.n > 0)
         k_id_map<<<(Pa.n + 255) / 256, 256, 0, s>>>(Ba, Ba.f4[POS][cur_a[POS]], Ba.f4[APREV][cur_a[APREV]], map_size,
                                                     map);
     if (Pb.n > 0)
-        k_compare<<<2 * 152, 256, 0, s>>>(Bb, Bb.f4[POS][cur_b[POS]], Bb.f4[VEL][cur_b[VEL]],
+        k_compare<<<2 * 152, 256, 0, s>>>(Pb, Bb, Bb.f4[POS][cur_b[POS]], Bb.f4[VEL][cur_b[VEL]],
                                           Bb.f4[ALPHA][cur_b[ALPHA]], Bb.f4[APREV][cur_b[APREV]], Ba.densp,
-                                          Ba.f4[VEL][cur_a[VEL]], Ba.f4[ALPHA][cur_a[ALPHA]], map, map_size,
-                                          Pb.nphase, out);
+                                          Ba.f4[POS][cur_a[POS]], Ba.f4[VEL][cur_a[VEL]], Ba.f4[ALPHA][cur_a[ALPHA]],
+                                          map, map_size, out);
 }
 
 void launch_apply_correction(const DevParams& P, const DevBuffers& B, const int* cur, const float* y,
                              const float* out_scale, const int32_t* ids, float dt_large, float* corr,
                              cudaStream_t s) {
     if (P.n <= 0) return;
-    k_apply_correction<<<(P.n + 255) / 256, 256, 0, s>>>(
-        P, B, B.f4[POS][cur[POS]], B.f4[VEL][cur[VEL]], B.f4[VEV][cur[VEV]], reinterpret_cast<const float4*>(y),
-        out_scale, ids, 0.5f * dt_large / P.ss, reinterpret_cast<float4*>(corr));
+    k_apply_correction<<<(P.n + 255) / 256, 256, 0, s>>>(P, B, B.f4[POS][cur[POS]], reinterpret_cast<const float4*>(y),
+                                                         out_scale, ids, dt_large / P.ss,
+                                                         reinterpret_cast<float4*>(corr));
 }
 
 }  // namespace sphmp

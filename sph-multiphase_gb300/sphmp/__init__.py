@@ -385,10 +385,10 @@ class Context:
 
     def compare_to(self, ref):
         """Differences of this state against `ref`'s (sphmp_compare_states)."""
-        out = (C.c_double * 5)()
-        check(self._lib.sphmp_compare_states(ref._ptr, self._ptr, out, 5))
+        out = (C.c_double * 6)()
+        check(self._lib.sphmp_compare_states(ref._ptr, self._ptr, out, 6))
         return {"density_rms": out[0], "density_max": out[1], "alpha_rms": out[2], "velocity_rms_rel": out[3],
-                "count": int(out[4])}
+                "count": int(out[4]), "position_rms_m": out[5]}
 
     def rollout(self, audit, steps, factor=8, corrector=None, audit_every=16, tol=0.01):
         """Advance by `steps` plain steps' worth of time in audited large steps (sphmp_rollout)."""

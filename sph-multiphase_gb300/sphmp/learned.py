@@ -5,8 +5,9 @@ for features and targets comes from torch. The pieces:
 
 * generate_pairs: from states along a plain trajectory, the features of a large
   step (factor x dt) and its targets: the plain solver's result after `factor`
-  steps minus the uncorrected large step's, per particle (matched by bornid):
-  velocity difference (3) and relative difference of the stored density.
+  steps against the uncorrected large step's, per particle (matched by bornid):
+  the position difference over the large step's length (3, m/s) and the
+  relative difference of the stored density.
 * normalisation: feature shift / scale and output scale from the training set.
 * train: Adam on random minibatches (the corrector's own tcgen05 kernels).
 * step_errors: what one large step (corrected or not) misses against `factor`
@@ -18,7 +19,7 @@ from . import Context, Corrector, abi
 
 
 def _by_bornid(ctx):
-    d = {k: ctx.download_field(f) for k, f in (("vel", abi.F_VEL), ("dens", abi.F_DENS), ("bornid", abi.F_BORNID),
+    d = {k: ctx.download_field(f) for k, f in (("pos", abi.F_POS), ("dens", abi.F_DENS), ("bornid", abi.F_BORNID),
                                                 ("type", abi.F_TYPE), ("mgcell", abi.F_MGCELL))}
     o = np.argsort(d["bornid"], kind="stable")
     return {k: v[o] for k, v in d.items()}
@@ -37,6 +38,8 @@ def generate_pairs(ctx, large, plain, factor, starts, gap):
     physical targets)."""
     import torch
     dev = torch.device("cuda", torch.cuda.current_device())
+    p = ctx.get_params()
+    to_rate = np.float32(p.simscale) / np.float32(factor * p.dt)  # simulation units -> m/s over the step
     zero = zero_corrector()
     xs, ts = [], []
     for _ in range(starts):
@@ -59,7 +62,7 @@ def generate_pairs(ctx, large, plain, factor, starts, gap):
              (a["mgcell"][pa] != abi.GRID_UNDEF) & (b["mgcell"][pb] != abi.GRID_UNDEF)
         pa, pb, keep = pa[ok], pb[ok], keep[ok]
         t = np.empty((len(keep), 4), np.float32)
-        t[:, :3] = a["vel"][pa] - b["vel"][pb]
+        t[:, :3] = (a["pos"][pa] - b["pos"][pb]) * to_rate
         t[:, 3] = b["dens"][pb] / a["dens"][pa] - 1.0  # stored inverses: rho_plain / rho_large - 1
         xs.append(feat[torch.from_numpy(keep).to(dev)])
         ts.append(t)
