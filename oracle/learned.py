@@ -3,7 +3,10 @@ tests/ and bench.py's checks use it; the library never does.
 
 The corrector has no counterpart in the reference (it is a method on top of the
 reference's step), so this module restates the library's own definitions in
-numpy, with the same rounding points:
+numpy, with the same rounding points. Parity unpinned by reference vectors
+(none can exist); the restatement is checked on its own instead: its backward
+pass against finite differences, its features against a hand-computed pair
+(tests/test_learned_oracle.py).
 
 * mlp_forward / mlp_backward: the network 48 -> 128 -> 128 -> 128 -> 4 with
   SiLU. Inputs (features - shift) * scale, weights, hidden activations and the
