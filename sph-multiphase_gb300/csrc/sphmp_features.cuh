@@ -33,7 +33,7 @@ constexpr int kLearnedFeatures = 48;
 struct LearnedFeatures {
     float f[kLearnedFeatures];
     float4 pi, vi, ai;
-    float pres_i, reli, ivs, ips, ih;
+    float pres_i, reli, ivs, ips, ih, ih2, ir2;
 
     // own features; pi, vi, ai, di, gi: this particle's pos4, vel4, alpha4,
     // (1/rho, p), aprev4
@@ -48,6 +48,8 @@ struct LearnedFeatures {
         ivs = 1.f / vs;
         ips = 1.f / (ai.w * vs * vs);
         ih = 1.f / P.h;
+        ih2 = ih * ih;
+        ir2 = 1.f / P.r2;
 #pragma unroll
         for (int k = 0; k < kLearnedFeatures; k++) f[k] = 0.f;
         f[0] = vi.x * ivs; f[1] = vi.y * ivs; f[2] = vi.z * ivs;
@@ -63,11 +65,11 @@ struct LearnedFeatures {
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
         const float dsq = dx * dx + dy * dy + dz * dz;
         if (!(dsq < P.r2 && dsq > 0.f)) return;
-        const float r = sqrtf(dsq);
-        const float q2 = dsq / P.r2, q = r * ih;
+        const float rinv = rsqrtf(dsq);
+        const float q2 = dsq * ir2, q = dsq * rinv * ih;
         const float w = (1.f - q2) * (1.f - q2) * (1.f - q2);
         const float g = (1.f - q) * (1.f - q);
-        const float ux = dx / r, uy = dy / r, uz = dz / r;
+        const float ux = dx * rinv, uy = dy * rinv, uz = dz * rinv;
         if (pj.w < 0.f) {  // boundary
             f[40] += w;
             f[41] += w * dx * ih; f[42] += w * dy * ih; f[43] += w * dz * ih;
@@ -78,13 +80,14 @@ struct LearnedFeatures {
         f[11] += w;
         f[12] += w * dx * ih; f[13] += w * dy * ih; f[14] += w * dz * ih;
         f[15] += w * dvx * ivs; f[16] += w * dvy * ivs; f[17] += w * dvz * ivs;
-        f[18] += w * (1.f / (dj.x * aj.w) - reli);
+        f[18] += w * (__fdividef(1.f, dj.x * aj.w) - reli);
         f[19] += w * (dj.y - pres_i) * ips;
         f[20] += w * (aj.x - ai.x);
         f[21] += w * (P.nphase > 1 ? aj.y - ai.y : 0.f);
         f[22] += w * (P.nphase > 2 ? aj.z - ai.z : 0.f);
-        f[23] += w * dx * dx * ih * ih; f[24] += w * dy * dy * ih * ih; f[25] += w * dz * dz * ih * ih;
-        f[26] += w * dx * dy * ih * ih; f[27] += w * dx * dz * ih * ih; f[28] += w * dy * dz * ih * ih;
+        const float wh2 = w * ih2;
+        f[23] += wh2 * dx * dx; f[24] += wh2 * dy * dy; f[25] += wh2 * dz * dz;
+        f[26] += wh2 * dx * dy; f[27] += wh2 * dx * dz; f[28] += wh2 * dy * dz;
         f[29] += g * ux; f[30] += g * uy; f[31] += g * uz;
         f[32] += g * (dvx * ux + dvy * uy + dvz * uz) * ivs;
         f[33] += g * (dvy * uz - dvz * uy) * ivs;
