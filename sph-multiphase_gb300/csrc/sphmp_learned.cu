@@ -187,6 +187,7 @@ struct sphmp_corrector {
     bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
     bf16 *dz = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
     float* part = nullptr;      // split-K partials
+    float* rpart = nullptr;     // row-sum partials
     float* loss_part = nullptr;
     float* loss = nullptr;
     std::vector<void*> allocs;
@@ -210,7 +211,13 @@ sphmp_status lfail(sphmp_status st, const char* fmt, ...) {
         if (e_ != cudaSuccess) return lfail(SPHMP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
-constexpr int kSplitK = 64;  // K chunks of the weight-gradient GEMMs (K = batch)
+// K splits of the weight-gradient GEMMs (K = the batch): 256 rows of the batch
+// per CTA, at most 256 CTAs, partials summed in a fixed order
+constexpr int kMaxSplitK = 256;
+int split_k(int batch) {
+    const int s = batch / 256;
+    return s < 1 ? 1 : (s > kMaxSplitK ? kMaxSplitK : s);
+}
 
 template <class T>
 sphmp_status lalloc(sphmp_corrector* c, T** p, size_t count) {
@@ -248,28 +255,29 @@ sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t
     LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
     LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
     float* g = c->grads;
+    const int kSplitK = split_k(batch);
     // layer 4: dW4 = dY^T H3, db4, dH3 = dY W4
     LCK(launch_gemm_tn(c->dyt, ld, c->h3t, ld, c->part, kOutPad, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kOutPad, kHidden, kOutputs, kHidden, g + kOffParamW4, s));
-    LCK(launch_row_sum(c->dyt, ld, kOutputs, batch, g + kOffParamB4, s));
+    LCK(launch_row_sum(c->dyt, ld, kOutputs, batch, c->rpart, g + kOffParamB4, s));
     LCK(launch_gemm_tn(c->dy, kOutPad, c->w4t, kOutPad, c->dh, batch, kHidden, kOutPad, 1, c->err, s));
     LCK(launch_silu_back(c->dh, c->z3, batch, ld, c->dz, c->dzt, s));
     // layer 3
     LCK(launch_gemm_tn(c->dzt, ld, c->h2t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW3, s));
-    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, g + kOffParamB3, s));
+    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB3, s));
     LCK(launch_gemm_tn(c->dz, kHidden, c->w3t, kHidden, c->dh, batch, kHidden, kHidden, 1, c->err, s));
     LCK(launch_silu_back(c->dh, c->z2, batch, ld, c->dz, c->dzt, s));
     // layer 2
     LCK(launch_gemm_tn(c->dzt, ld, c->h1t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW2, s));
-    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, g + kOffParamB2, s));
+    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB2, s));
     LCK(launch_gemm_tn(c->dz, kHidden, c->w2t, kHidden, c->dh, batch, kHidden, kHidden, 1, c->err, s));
     LCK(launch_silu_back(c->dh, c->z1, batch, ld, c->dz, c->dzt, s));
     // layer 1: dW1 = dZ1^T H0 (the first 48 of the 64 padded inputs)
     LCK(launch_gemm_tn(c->dzt, ld, c->h0t, ld, c->part, kHidden, kInPad, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kInPad, kHidden, kFeatures, g + kOffParamW1, s));
-    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, g + kOffParamB1, s));
+    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB1, s));
     return SPHMP_OK;
 }
 
@@ -325,7 +333,8 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
         A(&c->y, B * 4); A(&c->dh, B * kHidden);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
         A(&c->dz, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
-        A(&c->part, (size_t)kSplitK * kHidden * kHidden);
+        A(&c->part, (size_t)kMaxSplitK * kHidden * kHidden);
+        A(&c->rpart, (size_t)kRowSumMaxRows * 16);
         A(&c->loss_part, B / 256 + 1);
         A(&c->loss, 1);
     }

@@ -462,30 +462,68 @@ __global__ void k_silu_back(const float* __restrict__ dh, const float* __restric
     }
 }
 
-// out[r * cols + c] = sum over the splits of part[s][r][c] (r < rows, c < cols)
-__global__ void k_reduce_splits(const float* __restrict__ part, int splits, int M, int N, int rows, int cols,
-                                float* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= rows * cols) return;
-    const int r = i / cols, c = i % cols;
+// out[r * cols + c] = sum over the splits of part[s][r][c] (r < rows, c < cols):
+// 8 warps per block of 32 outputs, warp w sums every 8th split from w, then
+// warp 0 adds the eight partial sums in order (a fixed order for any launch).
+__global__ void __launch_bounds__(256) k_reduce_splits(const float* __restrict__ part, int splits, int M, int N,
+                                                       int rows, int cols, float* __restrict__ out) {
+    __shared__ float sh[8][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + lane;
     float s = 0.f;
-    for (int k = 0; k < splits; k++) s += part[((size_t)k * M + r) * N + c];
-    out[i] = s;
+    if (i < rows * cols) {
+        const int r = i / cols, c = i % cols;
+        for (int k = w; k < splits; k += 8) s += part[((size_t)k * M + r) * N + c];
+    }
+    sh[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && i < rows * cols) {
+        float t = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) t += sh[k][lane];
+        out[i] = t;
+    }
 }
 
-// out[r] = sum over the first `count` entries of row r of xt (one block per row)
-__global__ void k_row_sum(const bf16* __restrict__ xt, int ld, int count, float* __restrict__ out) {
+// out[r] = sum over the first `count` entries of row r of xt, in two fixed-order
+// passes: block (r, k) sums chunk k of row r (8 bf16 per 16-byte load), then
+// one thread per row sums the chunks.
+constexpr int kRowSplits = 16;
+__global__ void k_row_sum_part(const bf16* __restrict__ xt, int ld, int count, float* __restrict__ part) {
     __shared__ float red[256];
-    const bf16* row = xt + (size_t)blockIdx.x * ld;
+    const int r = blockIdx.x, k = blockIdx.y;
+    const int chunk = ((count + kRowSplits - 1) / kRowSplits + 7) / 8 * 8;
+    const int b = k * chunk, e = min(count, b + chunk);
+    const bf16* row = xt + (size_t)r * ld;
     float s = 0.f;
-    for (int i = threadIdx.x; i < count; i += blockDim.x) s += __bfloat162float(row[i]);
+    for (int i = b + 8 * (int)threadIdx.x; i < e; i += 8 * blockDim.x) {
+        if (i + 8 <= e) {
+            const uint4 q = *reinterpret_cast<const uint4*>(row + i);
+            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 f = __bfloat1622float2(h[j]);
+                s += f.x + f.y;
+            }
+        } else {
+            for (int j = i; j < e; j++) s += __bfloat162float(row[j]);
+        }
+    }
     red[threadIdx.x] = s;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
         if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+    if (threadIdx.x == 0) part[r * kRowSplits + k] = red[0];
+}
+
+__global__ void k_row_sum_final(const float* __restrict__ part, int rows, float* __restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    float s = 0.f;
+    for (int k = 0; k < kRowSplits; k++) s += part[r * kRowSplits + k];
+    out[r] = s;
 }
 
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
@@ -587,12 +625,14 @@ cudaError_t launch_silu_back(const float* dh, const float* z, int batch, int ld,
 
 cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
                                  cudaStream_t s) {
-    k_reduce_splits<<<(rows * cols + 255) / 256, 256, 0, s>>>(part, splits, M, N, rows, cols, out);
+    k_reduce_splits<<<(rows * cols + 31) / 32, 256, 0, s>>>(part, splits, M, N, rows, cols, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_row_sum(const bf16* xt, int ld, int rows, int count, float* out, cudaStream_t s) {
-    k_row_sum<<<rows, 256, 0, s>>>(xt, ld, count, out);
+cudaError_t launch_row_sum(const bf16* xt, int ld, int rows, int count, float* part, float* out, cudaStream_t s) {
+    if ((ld % 8) != 0 || rows > kRowSumMaxRows) return cudaErrorInvalidValue;
+    k_row_sum_part<<<dim3(rows, kRowSplits), 256, 0, s>>>(xt, ld, count, part);
+    k_row_sum_final<<<1, kRowSumMaxRows, 0, s>>>(part, rows, out);
     return cudaGetLastError();
 }
 

@@ -67,7 +67,11 @@ cudaError_t launch_silu_back(const float* dh, const float* z, int batch, int ld,
                              __nv_bfloat16* dzt, cudaStream_t s);
 cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
                                  cudaStream_t s);
-cudaError_t launch_row_sum(const __nv_bfloat16* xt, int ld, int rows, int count, float* out, cudaStream_t s);
+// out[r] = sum of the first count entries of row r (rows <= kRowSumMaxRows); part: scratch of
+// kRowSumMaxRows * 16 floats
+constexpr int kRowSumMaxRows = 128;
+cudaError_t launch_row_sum(const __nv_bfloat16* xt, int ld, int rows, int count, float* part, float* out,
+                           cudaStream_t s);
 cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int count, float lr, float b1, float b2,
                         float eps, int step, cudaStream_t s);
 cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s);

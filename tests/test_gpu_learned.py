@@ -149,6 +149,25 @@ def test_training_fits_a_teacher_network(built):
     teacher.close()
 
 
+def test_training_at_the_configured_batch(built):
+    """Adam steps on 65,536-row minibatches (the training configuration's batch)
+    of a teacher network's outputs: the loss falls."""
+    rng = np.random.default_rng(8)
+    teacher = sphmp.Corrector(0)
+    teacher.set_params(OL.init_params(80) * 3)
+    X = torch.from_numpy(rng.standard_normal((131072, 48)).astype(np.float32)).to(DEV)
+    T = torch.empty((131072, 4), dtype=torch.float32, device=DEV)
+    teacher.forward(X, T)
+    teacher.sync()
+    T = ((T - T.mean(0)) / T.std(0)).contiguous()
+    cor = sphmp.Corrector(65536)
+    cor.set_params(SL.init_params(81))
+    log = SL.train(cor, X, T, 60, 65536, 2e-3, seed=2, log_every=59)
+    assert log[-1][1] < 0.7 * log[0][1], log
+    cor.close()
+    teacher.close()
+
+
 # ---------------------------------------------------------------------------
 # the corrector inside the step
 # ---------------------------------------------------------------------------
