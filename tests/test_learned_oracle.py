@@ -1,6 +1,10 @@
 """The CPU oracle of the learned corrector (oracle/learned.py) checked on its own:
 bf16 rounding, the parameter layout, the backward pass against finite
-differences, the features on a hand-computed pair. No GPU."""
+differences, the features on a hand-computed pair; and the corrector's C ABI
+on a machine without a GPU (argument checks before any device use, loud
+failure instead of a fallback). No GPU."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -87,3 +91,29 @@ def test_features_of_a_pair():
     rb = 0.015
     assert np.isclose(f[40], (1 - (rb / h) ** 2) ** 3)
     assert np.all(F[2] == 0)  # boundary particles carry no features
+
+
+def _no_gpu():
+    import torch
+    return not torch.cuda.is_available()
+
+
+@pytest.mark.skipif(not _no_gpu(), reason="checks the behaviour without a GPU")
+def test_corrector_abi_without_a_device(built):
+    import sphmp
+    L = sphmp.load()
+    out = C.c_void_p()
+    # argument errors come first, then the missing device; nothing falls back to the CPU
+    assert L.sphmp_corrector_create(100, None, C.byref(out)) == abi.ERR_INVALID_ARG
+    assert L.sphmp_corrector_create(128, None, C.byref(out)) == abi.ERR_NO_DEVICE and not out.value
+    assert L.sphmp_corrector_create(128, None, None) == abi.ERR_INVALID_ARG
+    with pytest.raises(sphmp.SphmpError) as e:
+        sphmp.Corrector(128)
+    assert e.value.status == abi.ERR_NO_DEVICE
+    for m, n, k in [(128, 24, 64), (128, 144, 64), (128, 32, 12), (0, 32, 64)]:
+        assert L.sphmp_gemm_bf16_tn(C.c_void_p(16), 64, C.c_void_p(16), 64, C.c_void_p(16), m, n, k, 1,
+                                    None) == abi.ERR_INVALID_ARG
+    assert L.sphmp_step_large(None, None, 8, 1) == abi.ERR_INVALID_ARG
+    assert L.sphmp_copy_state(None, None) == abi.ERR_INVALID_ARG
+    assert L.sphmp_rollout(None, None, None, 8, 16, 16, 0.01, None) == abi.ERR_INVALID_ARG
+    assert L.sphmp_compare_states(None, None, None, 5) == abi.ERR_INVALID_ARG
