@@ -308,10 +308,10 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
 
 constexpr int kGemmThreads = 128;
 constexpr int kKc = 64;
-// A tile + B tile (N <= 128): 32 KB, so at most 7 CTAs share an SM's shared
-// memory; with at most 128 TMEM columns each, a fifth CTA on an SM waits in
-// tcgen05.alloc until one of the first four has finished
-constexpr int kGemmSmem = kTile * kKc * 2 + 128 * kKc * 2;
+// two stages of A tile + B tile (N <= 128): 64 KB, so at most 3 CTAs share an
+// SM, 384 of its 512 TMEM columns at 128 each
+constexpr int kStageBytes = kTile * kKc * 2 + 128 * kKc * 2;
+constexpr int kGemmSmem = 2 * kStageBytes;
 
 __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict__ A, int lda,
                                                           const bf16* __restrict__ B, int ldb, float* __restrict__ D,
@@ -319,8 +319,9 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tmem_base;
-    uint8_t* sa = smem;
-    uint8_t* sb = smem + kTile * kKc * 2;
+    // two stages of (A tile, B tile): chunk c + 1 loads while chunk c's MMAs run
+    auto stage_a = [&](int c) { return smem + (c & 1) * kStageBytes; };
+    auto stage_b = [&](int c) { return smem + (c & 1) * kStageBytes + kTile * kKc * 2; };
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m0 = blockIdx.x * kTile;
     const int kb = blockIdx.y * kper, ke = min(K, kb + kper);
@@ -335,31 +336,37 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
     const uint32_t idesc = tc::idesc_bf16_f32(kTile, N);
-    uint32_t parity = 0;
-    bool ok = true;
-    int chunks = 0;
-    for (int k0 = kb; k0 < ke; k0 += kKc) {
+    auto load_chunk = [&](int k0, uint8_t* a_s, uint8_t* b_s) {
         for (int q = tid; q < kTile * (kKc / 8); q += kGemmThreads) {
             const int r = q >> 3, k = (q & 7) * 8;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (m0 + r < M && k0 + k < ke) v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + k0 + k);
-            *reinterpret_cast<uint4*>(sa + tc::kmajor_offset(r, k, kKc)) = v;
+            *reinterpret_cast<uint4*>(a_s + tc::kmajor_offset(r, k, kKc)) = v;
         }
         for (int q = tid; q < N * (kKc / 8); q += kGemmThreads) {
             const int r = q >> 3, k = (q & 7) * 8;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
             if (k0 + k < ke) v = *reinterpret_cast<const uint4*>(B + (size_t)r * ldb + k0 + k);
-            *reinterpret_cast<uint4*>(sb + tc::kmajor_offset(r, k, kKc)) = v;
+            *reinterpret_cast<uint4*>(b_s + tc::kmajor_offset(r, k, kKc)) = v;
         }
-        handoff_to_mma();
+    };
+    uint32_t parity = 0;
+    bool ok = true;
+    const int nchunks = ke > kb ? (ke - kb + kKc - 1) / kKc : 0;
+    if (nchunks > 0) load_chunk(kb, stage_a(0), stage_b(0));
+    int chunks = 0;
+    for (int c = 0; c < nchunks; c++) {
+        handoff_to_mma();  // chunk c in shared memory for the tensor core
         if (tid == 0) {
             tc::fence_after_sync();
-            const uint32_t a = tc::smem_addr(sa), b = tc::smem_addr(sb);
+            const uint32_t a = tc::smem_addr(stage_a(c)), b = tc::smem_addr(stage_b(c));
             for (int ks = 0; ks < kKc / 16; ks++)
                 tc::mma_bf16(tmem, tc::kmajor_desc(a, kKc, ks), tc::kmajor_desc(b, kKc, ks), idesc,
-                             (chunks > 0 || ks > 0) ? 1u : 0u);
+                             (c > 0 || ks > 0) ? 1u : 0u);
             tc::mma_commit(&bar);
         }
+        // the other stage was last read by chunk c - 1's MMAs, complete since the last wait
+        if (c + 1 < nchunks) load_chunk(kb + (c + 1) * kKc, stage_a(c + 1), stage_b(c + 1));
         if (!(ok = wait_all(&bar, parity))) break;
         chunks++;
     }
@@ -603,6 +610,12 @@ cudaError_t launch_gemm_tn(const bf16* A, int lda, const bf16* B, int ldb, float
     int kper = (K + splits - 1) / splits;
     kper = (kper + kKc - 1) / kKc * kKc;
     if (kper == 0) kper = kKc;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
     dim3 grid((M + kTile - 1) / kTile, splits);
     k_gemm_tn<<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err);
     return cudaGetLastError();
