@@ -98,7 +98,8 @@ typedef struct sphmp_rollout_stats {
 /* Advance ctx by `steps` plain steps' worth of simulated time in large steps of
    factor x dt, corrected by `cor` (NULL: uncorrected). The first and then every
    audit_every-th large step is audited: `audit` (a second context with the same
-   parameters and capacity) runs `factor` plain steps from the same state, the
+   parameters and capacity, given the state by a device-side clone, so that it
+   continues exactly as ctx would) runs `factor` plain steps from it, the
    densities of both results are recomputed at their positions, and if the rms
    density error or the rms volume-fraction error of the large step exceeds
    `tol` (0.01 for 1 %), the plain result replaces it and the next

@@ -1196,6 +1196,71 @@ sphmp_status sphmp_compare_states(sphmp_ctx* a, sphmp_ctx* b, double* out, int32
     return SPHMP_OK;
 }
 
+// Device-side clone between contexts of the same capacity, grid and phase count
+// (the audit's copies): every array a step or a per-pass call reads, and the
+// host-side state, so that dst continues exactly as src would. Neighbour lists
+// are not copied (dst rebuilds them). Other contexts take sphmp_copy_state.
+static sphmp_status clone_state(sphmp_ctx* dst, sphmp_ctx* src) {
+    if (dst->cap != src->cap || dst->gcap != src->gcap || dst->prm.nphase != src->prm.nphase ||
+        dst->device != src->device || dst->prm.gridtotal != src->prm.gridtotal)
+        return sphmp_copy_state(dst, src);
+    if (sphmp_status st = refresh_n(src)) return st;
+    CK(cudaStreamSynchronize(src->stream));
+    CK(cudaStreamSynchronize(dst->stream));
+    const size_t N = (size_t)src->cap, G = (size_t)src->gcap;
+    const cudaStream_t s = dst->stream;
+    const DevBuffers& a = src->B;
+    DevBuffers& b = dst->B;
+    auto cp = [&](void* d, const void* x, size_t bytes) {
+        return cudaMemcpyAsync(d, x, bytes, cudaMemcpyDeviceToDevice, s);
+    };
+    for (int f = 0; f < kNumFloat4Fields; f++)
+        for (int k = 0; k < 2; k++) CK(cp(b.f4[f][k], a.f4[f][k], sizeof(float4) * N));
+    CK(cp(b.densp, a.densp, sizeof(float2) * N));
+    CK(cp(b.accel4, a.accel4, sizeof(float4) * N));
+    CK(cp(b.drift4, a.drift4, sizeof(float4) * 3 * N));
+    CK(cp(b.velxcor, a.velxcor, sizeof(float4) * N));
+    CK(cp(b.pmod, a.pmod, sizeof(float) * N));
+    CK(cp(b.mgcell, a.mgcell, sizeof(uint32_t) * N));
+    CK(cp(b.midsort, a.midsort, sizeof(uint32_t) * N));
+    CK(cp(b.mgndx, a.mgndx, sizeof(uint32_t) * N));
+    CK(cp(b.mgridoff, a.mgridoff, sizeof(int32_t) * G));
+    CK(cp(b.mgridcnt, a.mgridcnt, sizeof(int32_t) * G));
+    CK(cp(b.key, a.key, sizeof(uint32_t) * N));
+    CK(cp(b.octk, a.octk, sizeof(uint8_t) * N));
+    CK(cp(b.ccount, a.ccount, sizeof(uint32_t) * (G + 1)));
+    CK(cp(b.cstart, a.cstart, sizeof(uint32_t) * (G + 2)));
+    CK(cp(b.opos, a.opos, sizeof(uint32_t) * N));
+    CK(cp(b.oidx, a.oidx, sizeof(uint32_t) * N));
+    CK(cp(b.osrc, a.osrc, sizeof(uint32_t) * N));
+    CK(cp(b.oct_start, a.oct_start, sizeof(uint32_t) * 8 * G));
+    CK(cp(b.act, a.act, sizeof(uint32_t) * G));
+    CK(cp(b.act_n, a.act_n, sizeof(uint32_t)));
+    CK(cp(b.nact, a.nact, sizeof(int32_t)));
+    CK(cp(b.frame, a.frame, sizeof(int32_t)));
+    CK(cp(b.color, a.color, sizeof(float4) * N));
+    CK(cp(b.bornid, a.bornid, sizeof(int32_t) * N));
+    CK(cp(b.mass_raw, a.mass_raw, sizeof(float) * N));
+    CK(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), s));
+    CK(cudaStreamSynchronize(s));
+    dst->n = src->n;
+    dst->prm.num = src->prm.num;
+    memcpy(dst->cur, src->cur, sizeof(dst->cur));
+    dst->alpha_advanced = src->alpha_advanced;
+    dst->grid_valid = src->grid_valid;
+    dst->oct_valid = src->oct_valid;
+    dst->oct_built = src->oct_built;
+    dst->pos_sorted = src->pos_sorted;
+    dst->hash_n = src->hash_n;
+    dst->list_mode = src->list_mode;
+    dst->nbr_valid = false;
+    dst->n_stale = false;
+    dst->emit_on = src->emit_on;
+    dst->emitter = src->emitter;
+    drop_graph(dst);  // a captured graph holds the old buffer selectors
+    return SPHMP_OK;
+}
+
 // The stored densities recomputed at the current positions (sort, then the
 // density pass: after a sort it takes the bucket kernel, several times faster
 // than the cell search on the step's stale cell lists).
@@ -1227,7 +1292,7 @@ sphmp_status sphmp_rollout(sphmp_ctx* c, sphmp_ctx* audit, sphmp_corrector* cor,
         if (++since >= audit_every) {
             since = 0;
             S.audits++;
-            if (sphmp_status st = sphmp_copy_state(audit, c)) return st;
+            if (sphmp_status st = clone_state(audit, c)) return st;
             if (sphmp_status st = sphmp_step(audit, factor, SPHMP_SCHEDULE_FUSED, 0)) return st;
             if (sphmp_status st = sphmp_step_large(c, cor, factor, 1)) return st;
             if (sphmp_status st = recompute_density(c)) return st;
@@ -1238,7 +1303,7 @@ sphmp_status sphmp_rollout(sphmp_ctx* c, sphmp_ctx* audit, sphmp_corrector* cor,
             if (e[2] > S.alpha_err_max) S.alpha_err_max = e[2];
             if (!(e[0] <= tol && e[2] <= tol)) {  // NaN counts as a failure
                 S.fallbacks++;
-                if (sphmp_status st = sphmp_copy_state(c, audit)) return st;
+                if (sphmp_status st = clone_state(c, audit)) return st;
                 S.plain_steps += factor;
                 plain_left = audit_every * factor;
                 since = audit_every - 1;  // the first large step after the plain window is audited

@@ -318,7 +318,8 @@ def test_rollout_audits_and_falls_back(built):
     ctx.copy_state_from(src)
     st = ctx.rollout(aud, 8 * 10, factor=8, audit_every=2, tol=1e-12)
     assert st["fallbacks"] == st["audits"] >= 1 and st["large_steps"] == 0 and st["plain_steps"] == 80
-    # the result is then the plain trajectory, up to the summation order of the copies
+    # the audits clone the state on the device, so the result is the plain
+    # trajectory itself, bit for bit
     ref = sphmp.Context(p)
     ref.copy_state_from(src)
     ref.step(80)
@@ -326,7 +327,8 @@ def test_rollout_audits_and_falls_back(built):
         c.sort()
         c.compute_pressure()
     d = ctx.compare_to(ref)
-    assert d["count"] > 0.9 * sc.n_fluid and d["density_rms"] < 1e-4 and d["velocity_rms_rel"] < 1e-3
+    assert d["count"] > 0.9 * sc.n_fluid
+    assert d["density_rms"] == 0 and d["velocity_rms_rel"] == 0 and d["position_rms_m"] == 0
     for c in (src, ctx, aud, ref):
         c.close()
 
