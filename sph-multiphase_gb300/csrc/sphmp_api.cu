@@ -63,6 +63,10 @@ struct sphmp_ctx {
     float* lcorr = nullptr;
     int lrows = 0;
     void* xstage = nullptr;  // sphmp_copy_state: fractions and (g - a) of the source
+    // set by the rollout right after a sort and density pass of its own with no
+    // other call since; the next eager large step skips its sort and density
+    // pass, which would reproduce them bit for bit
+    bool sorted_dens_fresh = false;
     int32_t* cmap = nullptr; // sphmp_compare_states: bornid -> index
     int cmap_size = 0;
     double* cred = nullptr;  // sphmp_compare_states: 6 sums
@@ -368,36 +372,41 @@ struct LargeStep {
 // Queue one full step on the context stream (no host synchronisation). With
 // `L` (fused schedule only), the features are taken after the density pass and
 // the network's correction is applied to the step's result.
-sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr, const LargeStep* L = nullptr) {
+sphmp_status enqueue_step(sphmp_ctx* c, int schedule, StageTimer* T = nullptr, const LargeStep* L = nullptr,
+                          bool reuse_sorted = false) {
     const DevParams P = dev_params(c);
     const cudaStream_t s = c->stream;
     auto mark = [&](const char* nm) {
         if (T) T->mark(s, nm);
     };
     if (T) T->start(s);
-    if (c->emit_on) {
-        launch_emit(P, c->B, c->cur, c->emitter, s);
-        c->n_stale = true;
-        mark("emit");
+    const bool reuse = reuse_sorted && c->sorted_dens_fresh && !c->emit_on;
+    c->sorted_dens_fresh = false;
+    if (!reuse) {
+        if (c->emit_on) {
+            launch_emit(P, c->B, c->cur, c->emitter, s);
+            c->n_stale = true;
+            mark("emit");
+        }
+        launch_hash(P, c->B, c->cur, s);
+        mark("hash");
+        c->hash_n = c->emit_on ? -1 : c->n;  // with an emitter the count is only known on the device
+        launch_cell_starts(P, c->B, s);
+        mark("cell_starts");
+        launch_cell_order(P, c->B, c->cur, s);
+        mark("cell_order");
+        launch_rearrange(P, c->B, c->cur, false, s);
+        mark("rearrange");
+        swap_all(c);
+        c->alpha_advanced = false;
+        c->grid_valid = true;
+        c->oct_valid = true;
+        c->oct_built = false;
+        c->nbr_valid = false;
+        c->pos_sorted = true;
+        run_density(c, s);
+        mark("density");
     }
-    launch_hash(P, c->B, c->cur, s);
-    mark("hash");
-    c->hash_n = c->emit_on ? -1 : c->n;  // with an emitter the count is only known on the device
-    launch_cell_starts(P, c->B, s);
-    mark("cell_starts");
-    launch_cell_order(P, c->B, c->cur, s);
-    mark("cell_order");
-    launch_rearrange(P, c->B, c->cur, false, s);
-    mark("rearrange");
-    swap_all(c);
-    c->alpha_advanced = false;
-    c->grid_valid = true;
-    c->oct_valid = true;
-    c->oct_built = false;
-    c->nbr_valid = false;
-    c->pos_sorted = true;
-    run_density(c, s);
-    mark("density");
     const DevParams PL = dev_params(c);  // neighbour passes read the list
     if (schedule == SPHMP_SCHEDULE_FUSED) {
         if (L) {  // the force pass also fills the corrector's features
@@ -1116,7 +1125,8 @@ sphmp_status sphmp_step_large(sphmp_ctx* c, sphmp_corrector* cor, int32_t factor
     c->prm.dt = dt0 * (float)factor;
     const LargeStep L{cor, c->prm.dt};
     sphmp_status st = SPHMP_OK;
-    for (int t = 0; t < nsteps && !st; t++) st = enqueue_step(c, SPHMP_SCHEDULE_FUSED, nullptr, cor ? &L : nullptr);
+    for (int t = 0; t < nsteps && !st; t++)
+        st = enqueue_step(c, SPHMP_SCHEDULE_FUSED, nullptr, cor ? &L : nullptr, t == 0);
     c->prm.dt = dt0;
     return st;
 }
@@ -1276,6 +1286,10 @@ sphmp_status sphmp_rollout(sphmp_ctx* c, sphmp_ctx* audit, sphmp_corrector* cor,
     if (!c || !audit || c == audit) return fail(SPHMP_ERR_INVALID_ARG, "need the context and a separate audit context");
     if (factor < 1 || steps < 0 || audit_every < 1 || !(tol > 0.0))
         return fail(SPHMP_ERR_INVALID_ARG, "factor >= 1, steps >= 0, audit_every >= 1 and tol > 0 required");
+    struct ClearFresh {  // the skip never outlives the rollout, whichever way it returns
+        sphmp_ctx* c;
+        ~ClearFresh() { c->sorted_dens_fresh = false; }
+    } clear_fresh{c};
     sphmp_rollout_stats S;
     memset(&S, 0, sizeof(S));
     int done = 0, plain_left = 0;
@@ -1309,6 +1323,7 @@ sphmp_status sphmp_rollout(sphmp_ctx* c, sphmp_ctx* audit, sphmp_corrector* cor,
                 since = audit_every - 1;  // the first large step after the plain window is audited
             } else {
                 S.large_steps++;
+                c->sorted_dens_fresh = true;  // the next large step starts from this sort and density pass
             }
         } else {
             if (sphmp_status st = sphmp_step_large(c, cor, factor, 1)) return st;

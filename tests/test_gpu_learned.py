@@ -333,6 +333,35 @@ def test_rollout_audits_and_falls_back(built):
         c.close()
 
 
+def test_rollout_matches_the_same_steps_run_by_hand(built):
+    """A rollout that keeps every large step (one audit, generous tolerance) is
+    the sequence audited step, re-sort + density pass, further large steps run
+    through the public calls, bit for bit: after a passing audit the next large
+    step starts from the audit's sort and density pass instead of repeating them."""
+    sc = _liquid_scene(4096, 16)
+    src = _run(sc, 30)
+    p = sc.params
+    cor, *_ = _net(17, 0)
+    cor.set_params(SL.init_params(17))
+    a, aud, b = sphmp.Context(p), sphmp.Context(p), sphmp.Context(p)
+    a.copy_state_from(src)
+    b.copy_state_from(src)
+    st = a.rollout(aud, 8 * 5, factor=8, corrector=cor, audit_every=1000, tol=0.5)
+    assert st["large_steps"] == 5 and st["audits"] == 1 and st["fallbacks"] == 0
+    b.step_large(8, 1, cor)
+    b.sort()
+    b.compute_pressure()
+    b.step_large(8, 4, cor)
+    for c in (a, b):
+        c.sync()
+    da, ca = a.download_aos()
+    db, cb = b.download_aos()
+    assert da.tobytes() == db.tobytes() and ca.tobytes() == cb.tobytes()
+    for c in (src, a, aud, b):
+        c.close()
+    cor.close()
+
+
 def test_trained_corrector_beats_the_uncorrected_large_step(built):
     """Pairs from three all-liquid trajectories (seeds 5-7, 16 starts each);
     on a fourth scene (seed 8) one corrected 8 dt step misses 8 plain steps by
