@@ -60,7 +60,8 @@ sphmp_status sphmp_corrector_sync(sphmp_corrector* cor); /* waits; SPHMP_ERR_TIM
 
 /* D[s][m][n] = sum over the split's K range of A[m][k] B[n][k]: bf16 K-major
    operands (row strides lda, ldb elements, multiples of 8), FP32 out; n a multiple
-   of 16 up to 128, k a multiple of 8; splits >= 1 partial products. */
+   of 16 up to 128, k a multiple of 8; splits >= 1 partial products. A utility
+   (tests, callers' own networks): it allocates a status word and synchronises. */
 sphmp_status sphmp_gemm_bf16_tn(const void* a_dev, int32_t lda, const void* b_dev, int32_t ldb, float* d_dev,
                                 int32_t m, int32_t n, int32_t k, int32_t splits, void* stream);
 

@@ -589,12 +589,9 @@ __global__ void k_pack(const float* __restrict__ p, PackedMut W) {
 cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& S, float* y, uint32_t* err,
                            int num_sms, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    // per call (a host-side attribute of the current device): threads and devices stay independent
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
+    if (e != cudaSuccess) return e;
     const int tiles = (n + kTile - 1) / kTile;
     const int pairs = (tiles + kGroups - 1) / kGroups;
     const int grid = pairs < num_sms ? pairs : num_sms;
@@ -610,12 +607,8 @@ cudaError_t launch_gemm_tn(const bf16* A, int lda, const bf16* B, int ldb, float
     int kper = (K + splits - 1) / splits;
     kper = (kper + kKc - 1) / kKc * kKc;
     if (kper == 0) kper = kKc;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (e != cudaSuccess) return e;
     dim3 grid((M + kTile - 1) / kTile, splits);
     k_gemm_tn<<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err);
     return cudaGetLastError();
