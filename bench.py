@@ -50,8 +50,15 @@ timed as its wrappers run (a host synchronisation after every call) and
 stream-ordered. The reference arm needs oracle/_ref/sph_ref_kern.cubin (built
 where the reference checkout exists).
 
+--workload learned measures the learned large-step corrector: its training
+throughput (Adam steps at 65,536-row minibatches on pairs from three 64 x 128 x
+64 scenes of the rollout's physics) and the audited rollout (8 dt steps, a plain
+audit every 16, 1 % tolerance) of the 256 x 128 x 128 lattice (d = 0.005 m,
+h = 0.01 m, dt = 1e-4 s, linear EOS k = 3) against the plain pipeline over the
+same simulated time, with 256 gas bubbles (value) and all liquid; host clock.
+
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-       [--workload batched|large_step|device_ref]
+       [--workload batched|large_step|device_ref|learned]
 """
 import argparse
 import json
