@@ -34,6 +34,31 @@ def test_bf16_rounds_to_nearest_even():
     assert abs(got[6] - 1e-30) / 1e-30 < 2 ** -8
 
 
+def test_bf16_rounding_agrees_with_torch():
+    import torch
+    rng = np.random.default_rng(9)
+    x = np.concatenate([rng.standard_normal(100000).astype(np.float32) * 10.0 ** rng.integers(-20, 20, 100000),
+                        np.array([0.0, -0.0, 1.0, 3.0e38, -1e-39], np.float32)]).astype(np.float32)
+    ref = torch.from_numpy(x).to(torch.bfloat16).to(torch.float32).numpy()
+    assert np.array_equal(OL.bf16(x).view(np.uint32), ref.view(np.uint32))
+
+
+def test_normalisation_standardises_inputs_and_outputs():
+    import torch
+    from sphmp import learned as SL
+    rng = np.random.default_rng(10)
+    X = torch.from_numpy((rng.standard_normal((5000, 48)) * 3 + 2).astype(np.float32))
+    X[:, 7] = 0.0  # a constant feature (a phase that is absent): scale 1, not infinity
+    T = (rng.standard_normal((5000, 4)) * [1e-4, 2e-4, 3e-4, 1e-2]).astype(np.float32)
+    shift, scale, osc = SL.normalisation(X, T)
+    Z = (X.numpy() - shift) * scale
+    assert np.allclose(Z.mean(0), 0, atol=1e-4) and np.allclose(np.delete(Z.std(0), 7), 1, atol=1e-3)
+    assert scale[7] == 1 and np.all(np.isfinite(scale))
+    assert np.allclose(osc, T.std(0), rtol=1e-5)
+    p = SL.init_params(3)
+    assert p.shape == (abi.LC_PARAMS,) and np.abs(OL.unpack(p)["W4"]).max() <= 0.1 / np.sqrt(128)
+
+
 def test_backward_matches_finite_differences():
     rng = np.random.default_rng(4)
     p = OL.init_params(5).astype(np.float64)
