@@ -542,6 +542,7 @@ def run_learned(args):
     from sphmp import learned as SL
 
     dev = torch.device("cuda", torch.cuda.current_device())
+    torch.manual_seed(1)  # the timed Adam steps' minibatches: the same network in every run
     factor, audit_every, tol = 8, 16, 0.01
     sim_steps = args.learned_steps
     flop_per_sample = 3 * 2 * (48 * 128 + 2 * 128 * 128 + 128 * 4)  # forward + backward (2x forward)
