@@ -183,7 +183,7 @@ struct sphmp_corrector {
     float* norm = nullptr;      // fshift [48], fscale [48], out_scale [4]
     uint32_t* err = nullptr;
     // training buffers (max_batch rows)
-    float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *y = nullptr, *dh = nullptr;
+    float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *y = nullptr;
     bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
     bf16 *dz = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
     float* part = nullptr;      // split-K partials
@@ -260,20 +260,17 @@ sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t
     LCK(launch_gemm_tn(c->dyt, ld, c->h3t, ld, c->part, kOutPad, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kOutPad, kHidden, kOutputs, kHidden, g + kOffParamW4, s));
     LCK(launch_row_sum(c->dyt, ld, kOutputs, batch, c->rpart, g + kOffParamB4, s));
-    LCK(launch_gemm_tn(c->dy, kOutPad, c->w4t, kOutPad, c->dh, batch, kHidden, kOutPad, 1, c->err, s));
-    LCK(launch_silu_back(c->dh, c->z3, batch, ld, c->dz, c->dzt, s));
+    LCK(launch_gemm_silu_back(c->dy, kOutPad, c->w4t, kOutPad, batch, kOutPad, c->z3, c->dz, c->dzt, ld, c->err, s));
     // layer 3
     LCK(launch_gemm_tn(c->dzt, ld, c->h2t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW3, s));
     LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB3, s));
-    LCK(launch_gemm_tn(c->dz, kHidden, c->w3t, kHidden, c->dh, batch, kHidden, kHidden, 1, c->err, s));
-    LCK(launch_silu_back(c->dh, c->z2, batch, ld, c->dz, c->dzt, s));
+    LCK(launch_gemm_silu_back(c->dz, kHidden, c->w3t, kHidden, batch, kHidden, c->z2, c->dz, c->dzt, ld, c->err, s));
     // layer 2
     LCK(launch_gemm_tn(c->dzt, ld, c->h1t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW2, s));
     LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB2, s));
-    LCK(launch_gemm_tn(c->dz, kHidden, c->w2t, kHidden, c->dh, batch, kHidden, kHidden, 1, c->err, s));
-    LCK(launch_silu_back(c->dh, c->z1, batch, ld, c->dz, c->dzt, s));
+    LCK(launch_gemm_silu_back(c->dz, kHidden, c->w2t, kHidden, batch, kHidden, c->z1, c->dz, c->dzt, ld, c->err, s));
     // layer 1: dW1 = dZ1^T H0 (the first 48 of the 64 padded inputs)
     LCK(launch_gemm_tn(c->dzt, ld, c->h0t, ld, c->part, kHidden, kInPad, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kInPad, kHidden, kFeatures, g + kOffParamW1, s));
@@ -330,7 +327,7 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
     const size_t B = (size_t)max_batch;
     if (B > 0) {
         A(&c->z1, B * kHidden); A(&c->z2, B * kHidden); A(&c->z3, B * kHidden);
-        A(&c->y, B * 4); A(&c->dh, B * kHidden);
+        A(&c->y, B * 4);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
         A(&c->dz, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
         A(&c->part, (size_t)kMaxSplitK * kHidden * kHidden);

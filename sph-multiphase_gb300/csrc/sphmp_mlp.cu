@@ -13,9 +13,9 @@
 // * k_gemm_tn: D = A B^T for K-major bf16 A [M][K] and B [N][K] (N <= 128),
 //   M in tiles of 128, K split over gridDim.y into FP32 partials (summed in a
 //   fixed order by k_reduce_splits), for the backward pass.
-// * elementwise kernels: the output gradient, the SiLU backward (with its
-//   transposed copy), bias gradients, Adam, and the packing of the FP32 master
-//   parameters into the padded bf16 operand layouts.
+// * elementwise kernels: the output gradient, bias gradients, Adam, and the
+//   packing of the FP32 master parameters into the padded bf16 operand layouts
+//   (the SiLU backward runs in the epilogue of the dH GEMM).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -313,9 +313,21 @@ constexpr int kKc = 64;
 constexpr int kStageBytes = kTile * kKc * 2 + 128 * kKc * 2;
 constexpr int kGemmSmem = 2 * kStageBytes;
 
+// Epilogue of the SiLU-backward form (one K split, N = 128): dZ = D * SiLU'(Z)
+// straight from the accumulators, bf16, row-major [M][128] and transposed
+// [128][ldt] (D itself is not stored).
+struct SiluBack {
+    const float* z;
+    bf16* dz;
+    bf16* dzt;
+    int ldt;
+};
+
+template <bool SILU>
 __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict__ A, int lda,
                                                           const bf16* __restrict__ B, int ldb, float* __restrict__ D,
-                                                          int M, int N, int K, int kper, uint32_t* err) {
+                                                          int M, int N, int K, int kper, uint32_t* err,
+                                                          const SiluBack sb_out) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tmem_base;
@@ -371,14 +383,36 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
         chunks++;
     }
     const int r = warp * 32 + lane;
-    float* drow = D + ((size_t)blockIdx.y * M + (m0 + r)) * N;
+    float* drow = SILU ? nullptr : D + ((size_t)blockIdx.y * M + (m0 + r)) * N;
     if (ok) {
         for (int c0 = 0; c0 < N; c0 += 16) {
             float v[16];
             tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, c0), v);
             if (m0 + r < M) {
+                if (SILU) {
+                    const size_t row = (size_t)(m0 + r);
+                    const float4* zr = reinterpret_cast<const float4*>(sb_out.z + row * kHidden + c0);
+                    float h[16];
 #pragma unroll
-                for (int i = 0; i < 16; i++) drow[c0 + i] = chunks ? v[i] : 0.f;
+                    for (int q = 0; q < 4; q++) {
+                        const float4 zz = zr[q];
+                        const float zv[4] = {zz.x, zz.y, zz.z, zz.w};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) h[4 * q + j] = (chunks ? v[4 * q + j] : 0.f) * silu_grad(zv[j]);
+                    }
+                    uint4 lo, hi;
+                    lo.x = pack2(h[0], h[1]); lo.y = pack2(h[2], h[3]); lo.z = pack2(h[4], h[5]); lo.w = pack2(h[6], h[7]);
+                    hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
+                    uint4* dst = reinterpret_cast<uint4*>(sb_out.dz + row * kHidden + c0);
+                    dst[0] = lo;
+                    dst[1] = hi;
+#pragma unroll
+                    for (int i = 0; i < 16; i++)
+                        sb_out.dzt[(size_t)(c0 + i) * sb_out.ldt + row] = __float2bfloat16_rn(h[i]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 16; i++) drow[c0 + i] = chunks ? v[i] : 0.f;
+                }
             }
         }
     } else {
@@ -443,30 +477,6 @@ __global__ void k_loss_sum(const float* __restrict__ part, int nparts, int batch
         __syncthreads();
     }
     if (threadIdx.x == 0) *loss = red[0] / (float)batch;
-}
-
-// dZ = dH * SiLU'(Z), bf16, row-major [batch][128] and transposed [128][ld]
-// (32 x 32 tiles through shared memory so both stores are coalesced).
-__global__ void k_silu_back(const float* __restrict__ dh, const float* __restrict__ z, int batch, int ld,
-                            bf16* __restrict__ dz, bf16* __restrict__ dzt) {
-    __shared__ bf16 tile[32][34];
-    const int c = blockIdx.x * 32 + threadIdx.x;  // feature
-    for (int k = 0; k < 4; k++) {
-        const int r = blockIdx.y * 32 + threadIdx.y + 8 * k;  // row
-        bf16 v = __float2bfloat16_rn(0.f);
-        if (r < batch) {
-            const size_t o = (size_t)r * kHidden + c;
-            v = __float2bfloat16_rn(dh[o] * silu_grad(z[o]));
-            dz[o] = v;
-        }
-        tile[threadIdx.y + 8 * k][threadIdx.x] = v;
-    }
-    __syncthreads();
-    for (int k = 0; k < 4; k++) {
-        const int cc = blockIdx.x * 32 + threadIdx.y + 8 * k;
-        const int r = blockIdx.y * 32 + threadIdx.x;
-        if (r < batch) dzt[(size_t)cc * ld + r] = tile[threadIdx.x][threadIdx.y + 8 * k];
-    }
 }
 
 // out[r * cols + c] = sum over the splits of part[s][r][c] (r < rows, c < cols):
@@ -607,10 +617,24 @@ cudaError_t launch_gemm_tn(const bf16* A, int lda, const bf16* B, int ldb, float
     int kper = (K + splits - 1) / splits;
     kper = (kper + kKc - 1) / kKc * kKc;
     if (kper == 0) kper = kKc;
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
     if (e != cudaSuccess) return e;
     dim3 grid((M + kTile - 1) / kTile, splits);
-    k_gemm_tn<<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err);
+    k_gemm_tn<false><<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err, SiluBack{});
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_silu_back(const bf16* A, int lda, const bf16* B, int ldb, int M, int K, const float* z,
+                                  bf16* dz, bf16* dzt, int ldt, uint32_t* err, cudaStream_t s) {
+    if (M <= 0 || K < 0 || (K % 8) != 0 || (lda % 8) != 0 || (ldb % 8) != 0 || ldt < M)
+        return cudaErrorInvalidValue;
+    int kper = (K + kKc - 1) / kKc * kKc;
+    if (kper == 0) kper = kKc;
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((M + kTile - 1) / kTile, 1);
+    k_gemm_tn<true><<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, nullptr, M, kHidden, K, kper, err,
+                                                          SiluBack{z, dz, dzt, ldt});
     return cudaGetLastError();
 }
 
@@ -620,12 +644,6 @@ cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, b
     k_out_grad<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(y), reinterpret_cast<const float4*>(t), batch,
                                       ld, dy, dyt, loss_part);
     k_loss_sum<<<1, 256, 0, s>>>(loss_part, blocks, batch, loss);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_silu_back(const float* dh, const float* z, int batch, int ld, bf16* dz, bf16* dzt, cudaStream_t s) {
-    dim3 grid(kHidden / 32, (batch + 31) / 32);
-    k_silu_back<<<grid, dim3(32, 8), 0, s>>>(dh, z, batch, ld, dz, dzt);
     return cudaGetLastError();
 }
 

@@ -61,10 +61,13 @@ cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& 
 // D[split][M][N] = A[M][K] B[N][K]^T over the split's K range; N a multiple of 16, <= 128
 cudaError_t launch_gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* D, int M, int N,
                            int K, int splits, uint32_t* err, cudaStream_t s);
+// dZ = (A B^T) * SiLU'(Z) for N = 128 (the dH GEMM of a hidden layer with its SiLU backward in the
+// epilogue): bf16 dz [M][128] and dzt [128][ldt]
+cudaError_t launch_gemm_silu_back(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int K,
+                                  const float* z, __nv_bfloat16* dz, __nv_bfloat16* dzt, int ldt, uint32_t* err,
+                                  cudaStream_t s);
 cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, __nv_bfloat16* dy,
                             __nv_bfloat16* dyt, float* loss_part, float* loss, cudaStream_t s);
-cudaError_t launch_silu_back(const float* dh, const float* z, int batch, int ld, __nv_bfloat16* dz,
-                             __nv_bfloat16* dzt, cudaStream_t s);
 cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
                                  cudaStream_t s);
 // out[r] = sum of the first count entries of row r (rows <= kRowSumMaxRows); part: scratch of
