@@ -387,10 +387,15 @@ sphmp_status sphmp_get_grid_list(sphmp_ctx* ctx);
    gives. Its only scratch is a 4.2 MB static device array, so n is limited to
    SPHMP_NOALLOC_MAX_PARTICLES, gridtotal to SPHMP_NOALLOC_MAX_CELLS and one cell
    to 4096 particles (larger inputs return SPHMP_ERR_CAPACITY or
-   SPHMP_ERR_CELL_OVERFLOW). The first call on a device looks the scratch up
-   (cudaGetSymbolAddress) with that device current: make it before any stream
-   capture. Calls on one device share the scratch: calls that overlap in time
-   race and must be serialised. Returns after synchronising `stream`. */
+   SPHMP_ERR_CELL_OVERFLOW; a key that is neither a cell id below gridtotal nor
+   GRID_UNDEF returns SPHMP_ERR_INVALID_ARG). The first call in a CUDA context
+   (the device's primary context, or one the caller made current) looks the
+   scratch up with cudaGetSymbolAddress and keeps the address with the context's
+   id, so a call after cudaDeviceReset looks it up again. Every call copies an
+   error word to the host and synchronises `stream` before it returns, so no
+   call may be made while `stream` is being captured into a CUDA graph. Calls on
+   one device share the scratch: calls that overlap in time race and must be
+   serialised. */
 #define SPHMP_NOALLOC_MAX_PARTICLES 262144
 #define SPHMP_NOALLOC_MAX_CELLS 262144
 sphmp_status sphmp_sort_cells_noalloc(const uint32_t* cell, int32_t n, int32_t gridtotal,

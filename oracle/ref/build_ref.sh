@@ -11,7 +11,11 @@
 # The reference includes a few headers by Windows-style names with backslashes;
 # forwarding files with those literal names are generated into oracle/_ref/gen.
 set -e
-REF="${SPH_REFERENCE_ROOT:-/root/reference}/SPH_Solver"
+if [ -z "$SPH_REFERENCE_ROOT" ]; then
+    echo "build_ref.sh: set SPH_REFERENCE_ROOT to the reference checkout" >&2
+    exit 2
+fi
+REF="$SPH_REFERENCE_ROOT/SPH_Solver"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/../_ref"
 GEN="$OUT/gen"

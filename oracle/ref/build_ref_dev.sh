@@ -9,7 +9,11 @@
 # oracle/_ref/gen_dev). oracle/ref_gpu.py loads the module with the CUDA driver
 # API and runs the reference's launch sequence on the GPU ("device-ref").
 set -e
-REF="${SPH_REFERENCE_ROOT:-/root/reference}/SPH_Solver"
+if [ -z "$SPH_REFERENCE_ROOT" ]; then
+    echo "build_ref_dev.sh: set SPH_REFERENCE_ROOT to the reference checkout" >&2
+    exit 2
+fi
+REF="$SPH_REFERENCE_ROOT/SPH_Solver"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/../_ref"
 GEN="$OUT/gen_dev"

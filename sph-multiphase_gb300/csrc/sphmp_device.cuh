@@ -144,14 +144,16 @@ __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffe
 // Density + EOS (MfComputePressureCUDA)
 // ---------------------------------------------------------------------------
 
-// Tait (2.5 * rho0 * ((rho/rho0)^7 - 1), the 2.5 is a double literal in the
-// reference) or the linear extension, clamped at 0; rho == 0 reads as 1.
+// Tait (2.5 * rho0 * ((rho/rho0)^7 - 1)) or the linear extension, clamped at
+// 0; rho == 0 reads as 1. The reference's 2.5 is a double literal, so its two
+// products are taken in double (fluid_system_kern.cu:310) and rounded to float
+// once, as here.
 __device__ __forceinline__ float2 density_result(const DevParams& P, float wsum, float rho0) {
     float rho = wsum * P.kpoly6;
     if (rho == 0.f) rho = 1.f;
     float p;
     if (P.eos == SPHMP_EOS_LINEAR) p = P.eos_k * (rho - rho0);
-    else p = 2.5f * rho0 * (powf(rho / rho0, 7.0f) - 1.0f);
+    else p = (float)(2.5 * (double)rho0 * (double)(powf(rho / rho0, 7.0f) - 1.0f));
     if (p < 0.f) p = 0.f;
     return make_float2(1.f / rho, p);
 }

@@ -7,12 +7,19 @@
 // an FFI caller that wants no library-held allocations to outlive the call.
 // sphmp_sort_cells_noalloc serves them: its only scratch is the file-scope
 // static device array below, fixed at load time, whose address is looked up once
-// per device. It calls no cudaMalloc/cudaFree and no allocating library.
+// per CUDA context. It calls no cudaMalloc/cudaFree and no allocating library.
 //
 // Limits: n <= SPHMP_NOALLOC_MAX_PARTICLES, gridtotal <= SPHMP_NOALLOC_MAX_CELLS
 // and at most kNaMaxCellMembers particles in one cell; larger inputs are
 // rejected with an error before anything runs (cell occupancy: after the sort,
 // from a device flag).
+//
+// The scratch address is looked up once per CUDA context (the device's primary
+// context, or a context the caller made current), by the first call made in
+// that context, and kept with the context's unique id: after a
+// cudaDeviceReset the next call sees a new id and looks the address up again.
+// Every call copies the error word to the host and synchronises `stream`, so no
+// call can be made while the stream is being captured into a CUDA graph.
 //
 // Every call clears, on the stream, the scratch that has to start at zero (the
 // per-cell counters, the scatter cursors, the per-chunk out-of-grid counts and
@@ -20,6 +27,7 @@
 // initialisation. All calls on one device share the one scratch array, so calls
 // that overlap in time (two streams, two host threads) race on it and give wrong
 // results: serialise them on one stream or synchronise between them.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -41,7 +49,10 @@ constexpr uint32_t kNaErrKey = 1u;       // a key that is neither a cell id nor 
 constexpr uint32_t kNaErrCellSize = 2u;  // a cell above kNaMaxCellMembers
 
 // Scratch layout (32-bit words):
-//   count [G + 1]   particles per cell; entry G counts the out-of-grid keys
+//   count [G + 1]   particles per cell; entry G is cleared and never counted
+//                   into (out-of-grid keys are counted per chunk instead), so
+//                   that start[G] is the in-grid total, where the out-of-grid
+//                   tail begins
 //   start [G + 2]   exclusive prefix of count; start[G + 1] = n
 //   cursor[G + 1]   scatter cursors
 //   chunk [kNaChunks] out-of-grid keys per 256-key chunk, then its exclusive prefix
@@ -190,8 +201,63 @@ __global__ void k_na_order(const uint32_t* __restrict__ key, int G, NaScratch S,
     mgndx[s0 + r] = r;
 }
 
+// Scratch addresses by CUDA context: the context's unique id (cuCtxGetId, never
+// reused inside a process) and the address of g_na_scratch in it.
+struct NaEntry {
+    unsigned long long ctx_id;
+    uint32_t* ptr;
+};
+constexpr int kNaCacheSize = 64;
 std::mutex g_na_mutex;
-uint32_t* g_na_ptr[64] = {};
+NaEntry g_na_cache[kNaCacheSize] = {};
+int g_na_next = 0;
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Id of the context current on this thread; false if none is current. Called
+// with g_na_mutex held.
+bool current_ctx_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q2 != cudaDriverEntryPointSuccess)
+            return false;
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return g_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// The scratch address in the current context, looked up (cudaGetSymbolAddress,
+// which also makes the device's primary context current when none is) the first
+// time a context calls. Called with g_na_mutex held.
+cudaError_t scratch_address(uint32_t** out) {
+    unsigned long long id = 0;
+    if (current_ctx_id(&id)) {
+        for (const NaEntry& e : g_na_cache)
+            if (e.ptr && e.ctx_id == id) {
+                *out = e.ptr;
+                return cudaSuccess;
+            }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_na_scratch);
+    if (e != cudaSuccess) return e;
+    if (!current_ctx_id(&id)) return cudaErrorContextIsDestroyed;  // no context current after the lookup
+    g_na_cache[g_na_next] = NaEntry{id, static_cast<uint32_t*>(p)};
+    g_na_next = (g_na_next + 1) % kNaCacheSize;
+    *out = static_cast<uint32_t*>(p);
+    return cudaSuccess;
+}
 
 }  // namespace
 }  // namespace sphmp
@@ -210,19 +276,12 @@ extern "C" sphmp_status sphmp_sort_cells_noalloc(const uint32_t* cell, int32_t n
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return record_error(SPHMP_ERR_NO_DEVICE, cudaGetErrorString(e));
-    if (dev < 0 || dev >= 64) return record_error(SPHMP_ERR_NO_DEVICE, "sphmp_sort_cells_noalloc: device index >= 64");
     uint32_t* base = nullptr;
     {
-        // first call on this device: look up the scratch address with the device current
         std::lock_guard<std::mutex> lock(g_na_mutex);
-        if (!g_na_ptr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_na_scratch);
-            if (e != cudaSuccess) return record_error(SPHMP_ERR_CUDA, cudaGetErrorString(e));
-            g_na_ptr[dev] = static_cast<uint32_t*>(p);
-        }
-        base = g_na_ptr[dev];
+        e = scratch_address(&base);
     }
+    if (e != cudaSuccess) return record_error(SPHMP_ERR_CUDA, cudaGetErrorString(e));
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int G = gridtotal;
     const NaScratch S = carve(base, G);

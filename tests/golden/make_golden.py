@@ -7,7 +7,8 @@ parameters, the initial records and the output of every stage; tests replay
 the same stages through the oracle (bit-identical) and the CUDA library
 (within tolerance) on machines where the reference checkout does not exist.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root, with SPH_REFERENCE_ROOT naming the reference
+checkout:  SPH_REFERENCE_ROOT=<checkout> python tests/golden/make_golden.py
 """
 import json
 import os

@@ -85,3 +85,91 @@ def test_noalloc_matches_context_sort_twice(built, seed, shape, n_out):
         for name, t in outs.items():
             got = t.cpu().numpy().view(np.uint32 if name in ("midsort", "mgndx") else np.int32)
             assert np.array_equal(got, ref[name]), (call, name)
+
+
+def _noalloc_call(fn, keys, G, torch):
+    """One call on device copies of `keys`; returns the status and the four outputs."""
+    dev = torch.device("cuda:0")
+    n = len(keys)
+    d_keys = torch.from_numpy(keys.view(np.int32)).to(dev)
+    outs = {
+        "midsort": torch.full((max(n, 1),), -7, dtype=torch.int32, device=dev),
+        "mgndx": torch.full((max(n, 1),), -7, dtype=torch.int32, device=dev),
+        "gridoff": torch.full((G,), -3, dtype=torch.int32, device=dev),
+        "gridcnt": torch.full((G,), 77, dtype=torch.int32, device=dev),
+    }
+    torch.cuda.synchronize()
+    st = fn(d_keys.data_ptr(), n, G, outs["midsort"].data_ptr(), outs["mgndx"].data_ptr(),
+            outs["gridoff"].data_ptr(), outs["gridcnt"].data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+    got = {k: v.cpu().numpy()[:n if k in ("midsort", "mgndx") else G].view(
+        np.uint32 if k in ("midsort", "mgndx") else np.int32) for k, v in outs.items()}
+    return st, got
+
+
+def _stable_sort_reference(keys, G):
+    """GetGridListCUDA's outputs for `keys` from a stable sort (in-grid keys by cell,
+    then GRID_UNDEF keys, each group in index order)."""
+    order = np.argsort(keys.astype(np.uint64), kind="stable").astype(np.uint32)
+    sk = keys[order]
+    cnt = np.bincount(keys[keys != UNDEF].astype(np.int64), minlength=G).astype(np.int32)
+    off = np.zeros(G, np.int32)
+    off[1:] = np.cumsum(cnt)[:-1]
+    off[cnt == 0] = 0
+    ndx = np.full(len(keys), UNDEF, np.uint32)
+    ing = sk != UNDEF
+    starts = np.zeros(G + 1, np.int64)
+    starts[1:] = np.cumsum(cnt)
+    ndx[ing] = (np.arange(len(keys))[ing] - starts[sk[ing].astype(np.int64)]).astype(np.uint32)
+    return {"midsort": order, "mgndx": ndx, "gridoff": off, "gridcnt": cnt}
+
+
+@pytest.mark.gpu
+def test_noalloc_at_its_limits_matches_a_stable_sort(built):
+    """n = gridtotal = 262144 (the single-block scan runs 256 rounds, the serial
+    chunk prefix 1024 entries), random keys with a tenth GRID_UNDEF, twice."""
+    import torch
+    fn = _lib()
+    G = MAX_N
+    rng = np.random.default_rng(11)
+    keys = rng.integers(0, G, MAX_N).astype(np.uint32)
+    keys[rng.random(MAX_N) < 0.1] = UNDEF
+    ref = _stable_sort_reference(keys, G)
+    for call in range(2):
+        st, got = _noalloc_call(fn, keys, G, torch)
+        assert st == abi.OK, sphmp.last_error()
+        for name in ref:
+            assert np.array_equal(got[name], ref[name]), (call, name)
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_a_key_that_is_not_a_cell(built):
+    import torch
+    fn = _lib()
+    G = 1000
+    keys = np.arange(500, dtype=np.uint32) % G
+    keys[123] = G  # neither a cell id below gridtotal nor GRID_UNDEF
+    st, _ = _noalloc_call(fn, keys, G, torch)
+    assert st == abi.ERR_INVALID_ARG
+    assert "neither a cell id nor GRID_UNDEF" in sphmp.last_error()
+    # the next call with valid keys works and is exact
+    keys[123] = UNDEF
+    st, got = _noalloc_call(fn, keys, G, torch)
+    assert st == abi.OK, sphmp.last_error()
+    ref = _stable_sort_reference(keys, G)
+    for name in ref:
+        assert np.array_equal(got[name], ref[name]), name
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_a_cell_above_4096_members(built):
+    import torch
+    fn = _lib()
+    G = 100
+    rng = np.random.default_rng(12)
+    keys = rng.integers(0, G, 6000).astype(np.uint32)
+    keys[:4097] = 42
+    rng.shuffle(keys)
+    assert (keys == 42).sum() >= 4097
+    st, _ = _noalloc_call(fn, keys, G, torch)
+    assert st == abi.ERR_CELL_OVERFLOW
+    assert "4096" in sphmp.last_error()
