@@ -185,7 +185,9 @@ struct sphmp_corrector {
     // training buffers (max_batch rows)
     float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *y = nullptr;
     bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
-    bf16 *dz = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
+    // dz and dz2 alternate between layers: the SiLU-backward GEMM reads one as its
+    // A operand (declared __restrict__) and writes the other
+    bf16 *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
     float* part = nullptr;      // split-K partials
     float* rpart = nullptr;     // row-sum partials
     float* loss_part = nullptr;
@@ -265,12 +267,12 @@ sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t
     LCK(launch_gemm_tn(c->dzt, ld, c->h2t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW3, s));
     LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB3, s));
-    LCK(launch_gemm_silu_back(c->dz, kHidden, c->w3t, kHidden, batch, kHidden, c->z2, c->dz, c->dzt, ld, c->err, s));
+    LCK(launch_gemm_silu_back(c->dz, kHidden, c->w3t, kHidden, batch, kHidden, c->z2, c->dz2, c->dzt, ld, c->err, s));
     // layer 2
     LCK(launch_gemm_tn(c->dzt, ld, c->h1t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW2, s));
     LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB2, s));
-    LCK(launch_gemm_silu_back(c->dz, kHidden, c->w2t, kHidden, batch, kHidden, c->z1, c->dz, c->dzt, ld, c->err, s));
+    LCK(launch_gemm_silu_back(c->dz2, kHidden, c->w2t, kHidden, batch, kHidden, c->z1, c->dz, c->dzt, ld, c->err, s));
     // layer 1: dW1 = dZ1^T H0 (the first 48 of the 64 padded inputs)
     LCK(launch_gemm_tn(c->dzt, ld, c->h0t, ld, c->part, kHidden, kInPad, batch, kSplitK, c->err, s));
     LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kInPad, kHidden, kFeatures, g + kOffParamW1, s));
@@ -329,7 +331,7 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
         A(&c->z1, B * kHidden); A(&c->z2, B * kHidden); A(&c->z3, B * kHidden);
         A(&c->y, B * 4);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
-        A(&c->dz, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
+        A(&c->dz, B * kHidden); A(&c->dz2, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
         A(&c->part, (size_t)kMaxSplitK * kHidden * kHidden);
         A(&c->rpart, (size_t)kRowSumMaxRows * 16);
         A(&c->loss_part, B / 256 + 1);
