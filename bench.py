@@ -145,6 +145,60 @@ def _traffic(stage):
         return None
 
 
+def _ncu_counts(stage):
+    """Warp instructions per launch of `stage` (smsp__inst_executed.sum, summed over the
+    stage's kernels) from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(REPO, "profiles", "ncu_counts.json")) as f:
+            d = json.load(f)
+        v = d.get("inst_per_launch", {}).get(stage)
+        return None if v is None else float(v)
+    except Exception:
+        return None
+
+
+SM_COUNT = 152
+SCHEDULERS_PER_SM = 4
+
+
+def roofline_line(dom, stages, samples, units, algo, achieved, peak, peak_kind, step_bytes, clocks):
+    """The roofline object: the dominant stage against the measured HBM bandwidth, its DRAM
+    traffic, and its issue-slot utilisation (warp instructions per launch from ncu over the
+    scheduler slots of the timed launch at the sampled SM clock); `bound` names the limit
+    the two fractions point to."""
+    frac = achieved / peak
+    traffic = _traffic(dom)
+    step_dram = None
+    try:
+        with open(os.path.join(REPO, "profiles", "ncu_traffic.json")) as f:
+            d = json.load(f)
+        step_dram = sum(float(v) for k, v in d.items() if not k.startswith("_"))
+    except Exception:
+        pass
+    issue = None
+    inst = _ncu_counts(dom)
+    mhz = clocks.get("sm_mhz") or 2070
+    if inst is not None:
+        slots = stages[dom] * 1e-3 * SM_COUNT * SCHEDULERS_PER_SM * mhz * 1e6
+        issue = {"inst_per_launch": inst, "achieved_inst_per_s": inst / (stages[dom] * 1e-3),
+                 "peak_inst_per_s": SM_COUNT * SCHEDULERS_PER_SM * mhz * 1e6, "frac": inst / slots,
+                 "how": "smsp__inst_executed.sum per launch (profiles/ncu_counts.json) over 152 SMs x 4 "
+                        "schedulers x the median SM clock sampled during the timed steps"}
+    if frac >= 0.5:
+        bound = "hbm"
+    elif issue is not None and issue["frac"] >= 0.5:
+        bound = "issue"
+    else:
+        bound = "latency"
+    return {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": frac,
+            "peak_source": peak_kind, "denominator": "measured HBM copy bandwidth (MEASURED_PEAKS.json)",
+            "traffic": traffic, "algorithmic_bytes_per_launch": algo, "launch_ms": stages[dom],
+            "launch_ms_from": f"mean of {samples} eager steps spread over the timed steps (CUDA events)",
+            "issue": issue, "step_algorithmic_bytes": step_bytes, "step_dram_bytes": step_dram,
+            "step_dram_from": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, summed over the "
+                              "stages (profiles/ncu_traffic.json)"}
+
+
 class ClockSampler:
     """nvidia-smi SM clocks / throttle reasons sampled every 200 ms while running."""
 
@@ -197,14 +251,29 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
 
 
-def build_scene(seed):
+def build_scene(seed, gen=None):
+    """The benchmark scene; `gen` = the scene generators (default: the library's; the reference
+    arm passes the oracle's restatement, which builds the same records byte for byte without
+    loading the CUDA library)."""
     from sphmp import abi, scenes
-    return scenes.blobs_3phase(seed=seed, eos=abi.EOS_LINEAR, eos_k=3.0)
+    return scenes.blobs_3phase(seed=seed, eos=abi.EOS_LINEAR, eos_k=3.0, gen=gen or scenes.LIBRARY)
+
+
+def scene_config(scene):
+    """The workload description both arms print in `config` (identical for the same scene)."""
+    p = scene.params
+    return {"workload": scene.name, "fluid_particles": scene.n_fluid, "boundary_particles": scene.n_boundary,
+            "phases": int(p.nphase), "h": 0.01, "d": 0.005, "box": [1.28, 0.64, 0.64], "dt": 1e-4,
+            "eos": "linear k=3", "schedule": SCHEDULE_NAME, "seed": None}
+
+
+SCHEDULE_NAME = "fused (3 neighbour passes)"
 
 
 def cpu_sample(scene, steps, budget_s, threads=None, warmup=1):
-    """Time the CPU oracle on the bench scene after `warmup` untimed steps (their own budget of
-    budget_s); returns (particle-steps/s, steps done, seconds, threads, warm-up steps done)."""
+    """Time the CPU oracle on the bench scene (the fused schedule, as the GPU arm) after `warmup`
+    untimed steps (their own budget of budget_s); returns (particle-steps/s, steps done, seconds,
+    threads, warm-up steps done)."""
     from oracle import oracle as O
     from sphmp import abi
     O.build()
@@ -221,14 +290,14 @@ def cpu_sample(scene, steps, budget_s, threads=None, warmup=1):
     warm = 0
     tw = time.perf_counter()
     while warm < max(1, warmup):  # page-in, thread pool
-        O.step(p, s, abi.SCHEDULE_REFERENCE, 1)
+        O.step(p, s, abi.SCHEDULE_FUSED, 1)
         warm += 1
         if time.perf_counter() - tw > budget_s:
             break
     done = 0
     t0 = time.perf_counter()
     while done < steps:
-        O.step(p, s, abi.SCHEDULE_REFERENCE, 1)
+        O.step(p, s, abi.SCHEDULE_FUSED, 1)
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
@@ -236,25 +305,38 @@ def cpu_sample(scene, steps, budget_s, threads=None, warmup=1):
     return scene.n_fluid * done / dt, done, dt, nthr, warm
 
 
+def _repo_libraries():
+    """Shared libraries of this repository mapped into this process (Linux /proc/self/maps)."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so") and REPO in ln}
+        return sorted(os.path.relpath(p, REPO) for p in paths)
+    except OSError:
+        return None
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    scene = build_scene(args.seed)
+    from oracle import oracle as O
+    scene = build_scene(args.seed, gen=O.Generators)   # the oracle's generators: no CUDA library here
     # warm-up steps are part of the sample's own warm-up; the timed part is bounded
     value, done, dt, nthr, warm = cpu_sample(scene, max(1, args.steps), budget_s=args.cpu_budget,
                                              warmup=args.warmup)
+    cfg = scene_config(scene)
+    cfg["seed"] = args.seed
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": done, "warmup": warm, "ms_per_step": 1000.0 * dt / max(done, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": scene.name, "fluid_particles": scene.n_fluid,
-                   "boundary_particles": scene.n_boundary, "schedule": "reference call order",
-                   "eos": "linear k=3"},
+        "config": cfg,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthr, "kind": "port",
-                         "sample": f"{done} full steps of the {scene.n_fluid}-fluid-particle scene "
-                                   f"(capped at {args.cpu_budget:.0f} s; requested {args.steps})"},
+                         "sample": f"{done} fused steps of the {scene.n_fluid}-fluid-particle scene on the oracle "
+                                   f"(capped at {args.cpu_budget:.0f} s; requested {args.steps}); scene built by "
+                                   f"the oracle's generators, no CUDA library loaded"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "repo_libraries_loaded": _repo_libraries(),
     }
     print(json.dumps(line))
     return 0
@@ -309,7 +391,8 @@ def run_gpu(args):
     ctx.before_first_step()
     ctx.step(args.warmup, abi.SCHEDULE_FUSED, use_graph=True)
     stages = {}
-    every = max(1, min(args.profile_every, args.steps))
+    # at least five samples spread over the timed steps, at most one every --profile-every steps
+    every = max(1, min(args.profile_every, args.steps // 5))
     samples = 0
     done = 0
     while done < args.steps:
@@ -326,10 +409,6 @@ def run_gpu(args):
     algo = ALGO_BYTES[dom] * units
     achieved = algo / (stages[dom] * 1e-3) / 1e9
     peak, peak_kind = _peaks()
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": _traffic(dom),
-                "algorithmic_bytes_per_launch": algo, "launch_ms": stages[dom],
-                "launch_ms_from": f"mean of {samples} eager steps spread over the timed trajectory"}
     step_bytes = sum(ALGO_BYTES.get(k, 0) for k in stages) * units
     ctx.close()
 
@@ -364,25 +443,27 @@ def run_gpu(args):
 
     value = ws * n_fluid * args.steps / (ms * 1e-3)
     e2e_value = ws * n_fluid * e2e_steps / e2e_s
+    clocks = clk.summary()
+    cfg = scene_config(scene)
+    cfg["seed"] = args.seed
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": scene.name, "fluid_particles": n_fluid, "boundary_particles": scene.n_boundary,
-                   "phases": 3, "h": 0.01, "d": 0.005, "box": [1.28, 0.64, 0.64], "dt": 1e-4,
-                   "eos": "linear k=3", "schedule": "fused (3 neighbour passes)", "graph": True,
-                   "l2": "working set ~0.5 GB > 129 MB L2 (no flush needed)",
-                   "in_grid_after": n_in, "parallelism": f"replicas x{ws}",
-                   "stage_ms": {k: round(v, 4) for k, v in stages.items()},
-                   "step_algorithmic_bytes": step_bytes,
-                   "mass_fp64": cons["mass"], "alpha_sum_err": cons["alpha_sum_err"]},
-        "roofline": roofline,
+        "config": cfg,
+        "run": {"graph": True, "l2": "working set ~0.5 GB > 129 MB L2 (no flush needed)",
+                "parallelism": f"replicas x{ws}", "in_grid_after": n_in,
+                "stage_ms": {k: round(v, 4) for k, v in stages.items()},
+                "stage_ms_from": f"mean of {samples} eager steps spread over the timed steps",
+                "mass_fp64": cons["mass"], "alpha_sum_err": cons["alpha_sum_err"]},
+        "roofline": roofline_line(dom, stages, samples, units, algo, achieved, peak, peak_kind, step_bytes,
+                                  clocks),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": scene.n * 256 / e2e_steps,
                 "d2h_bytes_per_step": scene.n * 32,
                 "how": f"one TransferToCUDA upload + sort, then {e2e_steps} x (step + display download "
                        f"to pinned host memory, each copy overlapping the next step), host clock"},
         "gpu_launches": KERNELS_PER_FUSED_STEP * args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
         v, done, dt, nthr, _ = cpu_sample(scene, args.cpu_steps, budget_s=args.cpu_budget)

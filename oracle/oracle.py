@@ -152,6 +152,13 @@ def lib():
                 fn.argtypes = [C.POINTER(abi.Params), C.POINTER(S)]
             fn = getattr(L, "orc_step" + sfx)
             fn.argtypes = [C.POINTER(abi.Params), C.POINTER(S), C.c_int, C.c_int]
+        L.orc_params_default.argtypes = [C.POINTER(abi.Params)]
+        L.orc_params_default.restype = None
+        f3 = C.POINTER(C.c_float)
+        L.orc_add_fluid_volume.argtypes = [C.POINTER(abi.Params), f3, f3, C.c_float, f3, C.c_int32, C.c_float,
+                                           C.c_uint64, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]
+        L.orc_add_open_box.argtypes = [C.POINTER(abi.Params), f3, f3, C.c_float, C.c_void_p, C.c_void_p, C.c_int32,
+                                       C.POINTER(C.c_int32)]
         L.orc_setup_constants.argtypes = [C.POINTER(abi.Params)]
         L.orc_setup_grid.argtypes = [C.POINTER(abi.Params)]
         L.orc_set_num_threads.argtypes = [C.c_int]
@@ -197,6 +204,55 @@ def setup_constants(params):
 
 def setup_grid(params):
     lib().orc_setup_grid(C.byref(params))
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+class Generators:
+    """The scene-generation functions of sphmp.scenes (parameter defaults, kernel
+    constants, grid, fluid lattice, open box) from the oracle's restatement, so that a
+    CPU-only run (the benchmark's reference arm) builds its scene without loading the
+    CUDA library. tests/test_host.py checks the records equal the library's."""
+
+    @staticmethod
+    def params_default():
+        p = abi.Params()
+        lib().orc_params_default(C.byref(p))
+        return p
+
+    @staticmethod
+    def setup_constants(p):
+        if lib().orc_setup_constants(C.byref(p)) != 0:
+            raise ValueError("smoothing radius must be positive")
+        return p
+
+    @staticmethod
+    def setup_grid(p):
+        lib().orc_setup_grid(C.byref(p))
+        return p
+
+    @staticmethod
+    def record_arrays(cap):
+        return np.zeros(cap, abi.display_dtype()), np.zeros(cap, abi.calc_dtype())
+
+    @staticmethod
+    def add_fluid_volume(p, disp, calc, count, vmin, vmax, spacing, phase=0, jitter=0.0, seed=0, offs=(0, 0, 0)):
+        n = C.c_int32(count)
+        if lib().orc_add_fluid_volume(C.byref(p), _f3(vmin), _f3(vmax), float(spacing), _f3(offs), int(phase),
+                                      float(jitter), int(seed), disp.ctypes.data, calc.ctypes.data, len(disp),
+                                      C.byref(n)) != 0:
+            raise ValueError("record arrays too small")
+        return n.value
+
+    @staticmethod
+    def add_open_box(p, disp, calc, count, vmin, vmax, thickness):
+        n = C.c_int32(count)
+        if lib().orc_add_open_box(C.byref(p), _f3(vmin), _f3(vmax), float(thickness), disp.ctypes.data,
+                                  calc.ctypes.data, len(disp), C.byref(n)) != 0:
+            raise ValueError("record arrays too small")
+        return n.value
 
 
 def set_threads(n):

@@ -82,6 +82,142 @@ int orc_setup_grid(sphmp_params* p) {
     return 0;
 }
 
+/* ---- scene generation, so that a CPU-only run builds its inputs without the
+   CUDA library (the benchmark's reference arm); tests check the records equal
+   the library's generators byte for byte ---- */
+
+/* Parameter defaults: the reference's ParamCarrier values where it has them,
+   and the drift-flux constants the library chose where the reference reads
+   them from a scene file that no longer exists (relax 1e-5, diffusion 1e-3,
+   cont = cont1 = cont2 = 1, pintstiff 0.03, project-U factors 1). */
+void orc_params_default(sphmp_params* p) {
+    memset(p, 0, sizeof(*p));
+    p->gravity[1] = -9.8f;
+    p->simscale = 1.0f;
+    p->dt = 1e-4f;
+    p->smoothradius = 0.01f;
+    p->viscosity = 0.2f;
+    p->restdensity = 1000.0f;
+    p->mass = 1.25e-4f;
+    for (int k = 0; k < SPHMP_MAX_PHASES; k++) {
+        p->massArr[k] = p->mass;
+        p->densArr[k] = p->restdensity;
+        p->viscArr[k] = p->viscosity;
+    }
+    p->bmass = 1.25e-4f;
+    p->bRestdensity = 1000.0f;
+    p->bvisc = 100.0f;
+    p->nphase = 1;
+    p->eos = SPHMP_EOS_TAIT;
+    p->eos_stiffness = 3.0f;
+    p->mf_relax = 1.0e-5f;
+    p->mf_diffusion = 1.0e-3f;
+    p->mf_cont = 1.0f;
+    p->mf_cont1 = 1.0f;
+    p->mf_cont2 = 1.0f;
+    p->mf_pintstiff = 0.03f;
+    p->mf_omega = 1.0f;
+    p->mf_visc_factor = 1.0f;
+}
+
+/* The seeded lattice jitter: splitmix64 (Steele, Lea and Flood, "Fast splittable
+   pseudorandom number generators", OOPSLA 2014) over the counter, stream seed
+   * 0x100000001B3 + i, top 24 bits as a float in [0, 1). */
+static uint64_t orc_splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+static float orc_uniform01(uint64_t seed, uint64_t i) {
+    return (float)(orc_splitmix64(seed * 0x100000001B3ull + i) >> 40) * (1.0f / 16777216.0f);
+}
+
+/* AddParticle (SPH_Solver/fluids/fluid_system.cpp:702-717): a fresh record. */
+static void orc_init_record(sphmp_display_pack* d, sphmp_calc_pack* c, int32_t n) {
+    memset(d, 0, sizeof(*d));
+    memset(c, 0, sizeof(*c));
+    c->bornid = n;
+    c->deformGrad[0] = c->deformGrad[4] = c->deformGrad[8] = 1.0f;
+}
+
+/* FluidSystem::AddFluidVolume (SPH_Solver/fluids/fluid_system.cpp:719-762): the
+   lattice walked y, z, x (loop bounds compared against the float counts), each
+   component jittered by U(-jitter/2, jitter/2) from the seeded stream in place of
+   rand(). Returns 0, or -1 when `cap` records are not enough. */
+int orc_add_fluid_volume(const sphmp_params* p, const float vmin[3], const float vmax[3], float spacing,
+                         const float offs[3], int32_t phase, float jitter, uint64_t seed,
+                         sphmp_display_pack* disp, sphmp_calc_pack* calc, int32_t cap, int32_t* count) {
+    const float cnts[3] = {(vmax[0] - vmin[0]) / spacing, (vmax[1] - vmin[1]) / spacing,
+                           (vmax[2] - vmin[2]) / spacing};
+    uint64_t ctr = 0;
+    for (int y = 0; y < cnts[1]; y++)
+        for (int z = 0; z < cnts[2]; z++)
+            for (int x = 0; x < cnts[0]; x++) {
+                const int32_t n = *count;
+                if (n >= cap) return -1;
+                float r3[3];
+                for (int a = 0; a < 3; a++) r3[a] = orc_uniform01(seed, ctr++) * jitter - jitter * 0.5f;
+                sphmp_display_pack* d = disp + n;
+                sphmp_calc_pack* c = calc + n;
+                orc_init_record(d, c, n);
+                const float xyz[3] = {(float)x, (float)y, (float)z};
+                for (int a = 0; a < 3; a++) d->pos[a] = xyz[a] * spacing + vmin[a] + r3[a] + offs[a];
+                d->color[0] = 0.2f; d->color[1] = 0.5f; d->color[2] = 0.8f; d->color[3] = 0.5f;
+                d->type = SPHMP_TYPE_FLUID;
+                c->restdens = p->densArr[phase];
+                c->mass = p->massArr[phase];
+                c->visc = p->viscArr[phase];
+                *count = n + 1;
+            }
+    return 0;
+}
+
+/* SetupAddWall (SPH_Solver/fluids/AddShape.cpp:306-353) at the boundary spacing
+   of CalcBoundarySpacing (:265-271): layers at y = min.y, min.y + s, ... (float
+   accumulation, inclusive of max.y), each an x-z lattice of ceil(dx/s) * ceil(dz/s). */
+int orc_add_wall(const sphmp_params* p, const float vmin[3], const float vmax[3], sphmp_display_pack* disp,
+                 sphmp_calc_pack* calc, int32_t cap, int32_t* count) {
+    const float spacing = powf((p->bmass / p->bRestdensity), 1 / 3.0f) / p->simscale;
+    const int cntx = (int)ceilf((vmax[0] - vmin[0]) / spacing);
+    const int cntz = (int)ceilf((vmax[2] - vmin[2]) / spacing);
+    const int cnt = cntx * cntz;
+    for (float y = vmin[1]; y <= vmax[1]; y += spacing)
+        for (int xz = 0; xz < cnt; xz++) {
+            const int32_t n = *count;
+            if (n >= cap) return -1;
+            sphmp_display_pack* d = disp + n;
+            sphmp_calc_pack* c = calc + n;
+            orc_init_record(d, c, n);
+            d->pos[0] = vmin[0] + (xz % cntx) * spacing;
+            d->pos[1] = y;
+            d->pos[2] = vmin[2] + (xz / cntx) * spacing;
+            d->color[0] = 1.0f; d->color[1] = 1.0f; d->color[2] = 1.0f; d->color[3] = d->pos[2] > 0 ? 0.0f : 0.2f;
+            d->type = SPHMP_TYPE_BOUNDARY;
+            c->mass = p->bmass;
+            c->restdens = p->bRestdensity;
+            c->visc = p->bvisc;
+            *count = n + 1;
+        }
+    return 0;
+}
+
+/* SetupAddOpenBox (SPH_Solver/fluids/AddShape.cpp:355-366): the ground and four walls. */
+int orc_add_open_box(const sphmp_params* p, const float mn[3], const float mx[3], float t, sphmp_display_pack* disp,
+                     sphmp_calc_pack* calc, int32_t cap, int32_t* count) {
+    const float walls[5][2][3] = {
+        {{mn[0], mn[1] - t, mn[2]}, {mx[0], mn[1], mx[2]}},
+        {{mn[0] - t, mn[1], mn[2] - t}, {mx[0] + t, mx[1], mn[2]}},
+        {{mn[0] - t, mn[1], mx[2]}, {mx[0] + t, mx[1], mx[2] + t}},
+        {{mn[0] - t, mn[1], mn[2]}, {mn[0], mx[1], mx[2]}},
+        {{mx[0], mn[1], mn[2]}, {mx[0] + t, mx[1], mx[2]}},
+    };
+    for (int w = 0; w < 5; w++)
+        if (orc_add_wall(p, walls[w][0], walls[w][1], disp, calc, cap, count)) return -1;
+    return 0;
+}
+
 void orc_set_num_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);

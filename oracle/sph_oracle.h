@@ -80,6 +80,20 @@ ORC_DECLARE(_f64, orc_state_f64)
 int orc_setup_constants(sphmp_params* p);
 int orc_setup_grid(sphmp_params* p);
 
+/* Scene generation restated from the reference's AddFluidVolume, SetupAddWall and
+   SetupAddOpenBox (fluid_system.cpp:719-762, AddShape.cpp:265-366) with the
+   library's seeded jitter stream, and the library's parameter defaults: a CPU
+   run builds the same records as the CUDA library's generators without loading
+   it. The generators return 0, or -1 when `cap` records are not enough. */
+void orc_params_default(sphmp_params* p);
+int orc_add_fluid_volume(const sphmp_params* p, const float vmin[3], const float vmax[3], float spacing,
+                         const float offs[3], int32_t phase, float jitter, uint64_t seed,
+                         sphmp_display_pack* disp, sphmp_calc_pack* calc, int32_t cap, int32_t* count);
+int orc_add_wall(const sphmp_params* p, const float vmin[3], const float vmax[3], sphmp_display_pack* disp,
+                 sphmp_calc_pack* calc, int32_t cap, int32_t* count);
+int orc_add_open_box(const sphmp_params* p, const float mn[3], const float mx[3], float t, sphmp_display_pack* disp,
+                     sphmp_calc_pack* calc, int32_t cap, int32_t* count);
+
 void orc_set_num_threads(int n);
 int orc_get_num_threads(void);
 

@@ -14,14 +14,21 @@ densities of the workloads this library is measured on:
 Particles are generated with the library's own reference-equivalent generators
 (sphmp_add_fluid_volume / sphmp_add_open_box) and the phase of each liquid
 particle is then set from the blob layout. Boundary walls are two lattice
-layers at the fluid spacing.
+layers at the fluid spacing. The builders that take ``gen`` accept another set of
+generator functions with the same signatures (the CPU oracle's, for runs that must
+not load the CUDA library).
 """
 from dataclasses import dataclass
+from types import SimpleNamespace
 
 import numpy as np
 
 from . import abi
 from . import add_fluid_volume, add_open_box, params_default, record_arrays, setup_constants, setup_grid
+
+# the library's generators (the default of every builder's `gen`)
+LIBRARY = SimpleNamespace(params_default=params_default, setup_constants=setup_constants, setup_grid=setup_grid,
+                          record_arrays=record_arrays, add_fluid_volume=add_fluid_volume, add_open_box=add_open_box)
 
 
 @dataclass
@@ -39,10 +46,10 @@ class Scene:
 
 
 def make_params(*, h, d, dt, box_min, box_max, nphase, dens, visc, simscale=1.0, gravity=(0.0, -9.81, 0.0),
-                eos=abi.EOS_LINEAR, eos_k=3.0, multiphase=1, headroom=None, bvisc=100.0, wall_layers=2):
+                eos=abi.EOS_LINEAR, eos_k=3.0, multiphase=1, headroom=None, bvisc=100.0, wall_layers=2, gen=LIBRARY):
     """Parameters for a box [box_min, box_max] (sim units) with `wall_layers` boundary layers at spacing d.
     Masses are rest density times (d * simscale)^3, the physical volume of a lattice site."""
-    p = params_default()
+    p = gen.params_default()
     p.smoothradius = h
     p.simscale = simscale
     p.dt = dt
@@ -63,7 +70,7 @@ def make_params(*, h, d, dt, box_min, box_max, nphase, dens, visc, simscale=1.0,
     p.bRestdensity = 1000.0
     p.bmass = np.float32(1000.0) * np.float32(d * simscale) ** 3
     p.bvisc = bvisc
-    setup_constants(p)
+    gen.setup_constants(p)
     # grid: walls (thickness t) plus two cells of padding; extra headroom above the box
     t = (wall_layers - 0.5) * d
     pad = t + 2.0 * p.cellsize / simscale
@@ -71,18 +78,18 @@ def make_params(*, h, d, dt, box_min, box_max, nphase, dens, visc, simscale=1.0,
     for a in range(3):
         p.volmin[a] = box_min[a] - pad
         p.volmax[a] = box_max[a] + pad + (hr if a == 1 else 0.0)
-    setup_grid(p)
+    gen.setup_grid(p)
     return p
 
 
-def _block(p, disp, calc, count, corner, counts, d, jitter, seed, phase=0):
+def _block(p, disp, calc, count, corner, counts, d, jitter, seed, phase=0, gen=LIBRARY):
     vmin = [corner[a] + 0.5 * d for a in range(3)]
     vmax = [vmin[a] + (counts[a] - 0.5) * d for a in range(3)]
-    return add_fluid_volume(p, disp, calc, count, vmin, vmax, d, phase=phase, jitter=jitter * d, seed=seed)
+    return gen.add_fluid_volume(p, disp, calc, count, vmin, vmax, d, phase=phase, jitter=jitter * d, seed=seed)
 
 
-def _walls(p, disp, calc, count, box_min, box_max, d, layers=2):
-    return add_open_box(p, disp, calc, count, box_min, box_max, (layers - 0.5) * d)
+def _walls(p, disp, calc, count, box_min, box_max, d, layers=2, gen=LIBRARY):
+    return gen.add_open_box(p, disp, calc, count, box_min, box_max, (layers - 0.5) * d)
 
 
 def _assign_phase(p, calc, sel, phase):
@@ -100,37 +107,38 @@ def _finish(p, disp, calc, count, n_fluid, name):
 
 
 def dam_break_2phase(seed=1, n_side=32, d=0.01, h=0.02, box=0.64, dt=2e-4, eos=abi.EOS_LINEAR, eos_k=3.0,
-                     gas_center=(0.16, 0.10, 0.16), gas_radius=0.06, multiphase=1, walls=True):
+                     gas_center=(0.16, 0.10, 0.16), gas_radius=0.06, multiphase=1, walls=True, gen=LIBRARY):
     """32^3 liquid block with a gas sphere in a `box`-metre open box (liquid 1000, gas 1.2 kg/m^3)."""
     bmin, bmax = (0.0, 0.0, 0.0), (box, box, box)
     p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=2, dens=(1000.0, 1.2), visc=(0.2, 0.2),
-                    eos=eos, eos_k=eos_k, multiphase=multiphase)
+                    eos=eos, eos_k=eos_k, multiphase=multiphase, gen=gen)
     cap = n_side ** 3 + (int(6 * (box / d + 4) ** 2 * 2.2) if walls else 0)
-    disp, calc = record_arrays(cap)
-    count = _block(p, disp, calc, 0, bmin, (n_side,) * 3, d, 0.1, seed)
+    disp, calc = gen.record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, (n_side,) * 3, d, 0.1, seed, gen=gen)
     n_fluid = count
     pos = disp["pos"][:count]
     gas = np.sum((pos - np.asarray(gas_center, np.float32)) ** 2, axis=1) < gas_radius ** 2
     _assign_phase(p, calc, np.nonzero(gas)[0], 1)
     if walls:
-        count = _walls(p, disp, calc, count, bmin, bmax, d)
+        count = _walls(p, disp, calc, count, bmin, bmax, d, gen=gen)
     return _finish(p, disp, calc, count, n_fluid, f"dam_break_2phase_{n_side}")
 
 
 def blobs_3phase(seed=2, lattice=(128, 64, 128), d=0.005, h=0.01, box=(1.28, 0.64, 0.64), dt=1e-4,
-                 eos=abi.EOS_LINEAR, eos_k=3.0, n_blobs=64, rmin=0.02, rmax=0.08, multiphase=1, walls=True):
+                 eos=abi.EOS_LINEAR, eos_k=3.0, n_blobs=64, rmin=0.02, rmax=0.08, multiphase=1, walls=True,
+                 gen=LIBRARY):
     """A lattice block in the low-x corner of the box; phases 0/1/2 (1000/800/1.2 kg/m^3) from
     random blobs (the last blob containing a particle wins, phase 0 elsewhere)."""
     bmin, bmax = (0.0, 0.0, 0.0), tuple(box)
     p = make_params(h=h, d=d, dt=dt, box_min=bmin, box_max=bmax, nphase=3, dens=(1000.0, 800.0, 1.2),
-                    visc=(0.2, 0.2, 0.2), eos=eos, eos_k=eos_k, multiphase=multiphase)
+                    visc=(0.2, 0.2, 0.2), eos=eos, eos_k=eos_k, multiphase=multiphase, gen=gen)
     wall_est = 0
     if walls:
         nx, ny, nz = [int(b / d) + 8 for b in box]
         wall_est = 2 * (nx * nz + 2 * nx * ny + 2 * nz * ny) + 4096
     cap = int(np.prod(lattice)) + wall_est
-    disp, calc = record_arrays(cap)
-    count = _block(p, disp, calc, 0, bmin, lattice, d, 0.1, seed)
+    disp, calc = gen.record_arrays(cap)
+    count = _block(p, disp, calc, 0, bmin, lattice, d, 0.1, seed, gen=gen)
     n_fluid = count
     rng = np.random.default_rng(seed)
     ext = np.asarray(lattice, np.float32) * np.float32(d)
@@ -145,7 +153,7 @@ def blobs_3phase(seed=2, lattice=(128, 64, 128), d=0.005, h=0.01, box=(1.28, 0.6
     for k in range(3):
         _assign_phase(p, calc, np.nonzero(phase == k)[0], k)
     if walls:
-        count = _walls(p, disp, calc, count, bmin, bmax, d)
+        count = _walls(p, disp, calc, count, bmin, bmax, d, gen=gen)
     name = "blobs_3phase_" + "x".join(str(v) for v in lattice)
     return _finish(p, disp, calc, count, n_fluid, name)
 

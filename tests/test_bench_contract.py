@@ -27,3 +27,10 @@ def test_reference_arm_prints_contract_line(built):
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["fluid_particles"] == 1048576
+    # the same workload description as the GPU arm, and no CUDA library in the process
+    for k in ("workload", "phases", "h", "d", "dt", "box", "eos", "schedule", "seed"):
+        assert k in d["config"], k
+    assert d["config"]["schedule"].startswith("fused")
+    libs = d["repo_libraries_loaded"]
+    assert libs is not None and any("liboracle" in x for x in libs), libs
+    assert not any("libsphmp" in x for x in libs), libs

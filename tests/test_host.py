@@ -209,3 +209,19 @@ def test_cpp_host_links_and_fails_loudly_without_a_device(lib, tmp_path):
     assert r.returncode == 3, (r.returncode, r.stderr)
     assert "CUDA ERROR: FluidSetupCUDA" in r.stderr and "no CUDA device" in r.stderr
 
+
+
+@pytest.mark.parametrize("build", ["dam_break", "blobs"])
+def test_oracle_generators_build_the_library_scenes(lib, build):
+    """The oracle's restated generators (used where the CUDA library must not be
+    loaded: the benchmark's reference arm) give the library's records byte for byte."""
+    from oracle import oracle as O
+    if build == "dam_break":
+        make = lambda gen: scenes.dam_break_2phase(seed=5, n_side=20, gen=gen)  # noqa: E731
+    else:
+        make = lambda gen: scenes.blobs_3phase(seed=6, lattice=(40, 16, 24), gen=gen)  # noqa: E731
+    a, b = make(scenes.LIBRARY), make(O.Generators)
+    assert bytes(a.params) == bytes(b.params)
+    assert a.n == b.n and a.n_fluid == b.n_fluid
+    assert a.disp.tobytes() == b.disp.tobytes()
+    assert a.calc.tobytes() == b.calc.tobytes()
