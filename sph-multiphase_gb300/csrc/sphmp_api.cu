@@ -185,7 +185,7 @@ void free_buffers(sphmp_ctx* c) {
         for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.velxcor, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
                     B.key, B.octk, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
-                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
+                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.wq, B.wq_n, B.hq, B.hq_n, B.hctr, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
                     B.act, B.act_n, B.nact, B.frame, c->stage};
     for (void* q : ptrs) cudaFree(q);
     memset(&c->B, 0, sizeof(c->B));
@@ -234,6 +234,13 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.nmask, (size_t)kMaskWords * N));
     CK(dalloc(&B.btab, 8 * G * kTabStride));
     CK(dalloc(&B.dctr, 1));
+    CK(dalloc(&B.wq, N / kBucketWindow + 16));
+    CK(dalloc(&B.wq_n, 1));
+    CK(cudaMemset(B.wq_n, 0, sizeof(uint32_t)));
+    CK(dalloc(&B.hq, N));
+    CK(dalloc(&B.hq_n, 1));
+    CK(dalloc(&B.hctr, 2));
+    CK(cudaMemset(B.hq_n, 0, sizeof(uint32_t)));
     CK(dalloc(&B.nrec, (size_t)kNrecFloat4 * N));
     CK(dalloc(&B.opos, N));
     CK(dalloc(&B.oidx, N));

@@ -85,8 +85,8 @@ __device__ __forceinline__ void cell_coords(const DevParams& P, uint32_t cell, i
 // grid's interior, so every cell visited exists. Cells along x are adjacent in
 // the sorted order, so each (y, z) row of cells is one contiguous slot range.
 template <class F>
-__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart,
-                                               uint32_t cell, float x, float y, float z, F&& f) {
+__device__ __forceinline__ void for_candidate_rows(const DevParams& P, const uint32_t* __restrict__ cstart,
+                                                   uint32_t cell, float x, float y, float z, F&& f) {
     const float t[3] = {grid_t(x, P.gmin[0], P.fac[0]), grid_t(y, P.gmin[1], P.fac[1]),
                         grid_t(z, P.gmin[2], P.fac[2])};
     int g[3];
@@ -104,11 +104,18 @@ __device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_
     for (int yy = lo[1]; yy <= hi[1]; yy++) {
         for (int zz = lo[2]; zz <= hi[2]; zz++) {
             const int base = (yy * P.rz + zz) * P.rx;
-            const uint32_t j0 = __ldg(&cstart[base + lo[0]]);
-            const uint32_t j1 = __ldg(&cstart[base + hi[0] + 1]);
-            for (uint32_t j = j0; j < j1; j++) f(j);
+            f(__ldg(&cstart[base + lo[0]]), __ldg(&cstart[base + hi[0] + 1]));
         }
     }
+}
+
+// The candidates one by one (see for_candidate_rows: each row is the slot range [j0, j1)).
+template <class F>
+__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart,
+                                               uint32_t cell, float x, float y, float z, F&& f) {
+    for_candidate_rows(P, cstart, cell, x, y, z, [&](uint32_t j0, uint32_t j1) {
+        for (uint32_t j = j0; j < j1; j++) f(j);
+    });
 }
 
 // Rows of the column-major neighbour lists are streamed from DRAM (the lists
@@ -118,13 +125,45 @@ constexpr uint32_t kListPrefetch = 8;
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
+// The candidates marked in mask words wd0, wd0 + step, ... of particle s's
+// bucket mask list (bucket `bid`, whose range table in btab maps sequence
+// position e to index e + delta of the range holding e).
+template <class F>
+__device__ __forceinline__ void for_mask_words(const DevParams& P, const DevBuffers& B, int s, uint32_t bid,
+                                               uint32_t wd0, uint32_t step, F&& f) {
+    const uint32_t* __restrict__ tab = B.btab + (size_t)bid * kTabStride;
+    const uint32_t nw = (__ldg(&tab[18]) + 31u) >> 5;
+    const size_t cap = (size_t)P.cap;
+    int r = 0;
+    uint32_t end = __ldg(&tab[1]), delta = __ldg(&tab[20]);
+    for (uint32_t wd = wd0; wd < nw; wd += step) {
+        uint32_t m = __ldg(&B.nmask[(size_t)wd * cap + s]);
+        while (m != 0u) {
+            const uint32_t e = (wd << 5) + (uint32_t)(__ffs(m) - 1);
+            m &= m - 1u;
+            while (e >= end) {  // ends at tab[18] = the sequence length > e
+                r++;
+                end = __ldg(&tab[r + 1]);
+                delta = __ldg(&tab[20 + r]);
+            }
+            f(e + delta);
+        }
+    }
+}
+
 // Visit the neighbours of particle s from the index list of the density pass
-// when it is valid and did not overflow, otherwise by the cell search.
+// when it is valid and did not overflow, from the bucket mask list when the
+// index list overflowed, otherwise by the cell search.
 template <class F>
 __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffers& B, int s, float x, float y,
                                               float z, F&& f) {
     if (P.list_mode != 0) {
-        const uint32_t cnt = B.nbr_cnt[s];
+        const uint32_t raw = B.nbr_cnt[s];
+        if (raw & kMaskList) {
+            for_mask_words(P, B, s, raw & ~kMaskList, 0u, 1u, f);
+            return;
+        }
+        const uint32_t cnt = raw & ~kHeavyFlag;  // kRescan stays above kMaxNbr
         if (cnt <= (uint32_t)kMaxNbr) {
             const uint32_t* __restrict__ col = B.nbr + s;
             const size_t cap = (size_t)P.cap;
@@ -138,6 +177,58 @@ __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffe
         }
     }
     for_candidates(P, B.cstart, B.mgcell[s], x, y, z, f);
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Heavy particles: in the force and alpha passes every warp first takes heavy
+// particles from hq (one particle per warp, its neighbours shared out over the
+// lanes) while any are left, then its own 32 particles without the heavy ones.
+// In a squeezed cluster all 32 particles of a warp can have hundreds of
+// neighbours; walked by their own threads they would hold that warp for
+// hundreds of dependent list steps while the rest of the GPU idles.
+__device__ __forceinline__ bool is_heavy(const DevParams& P, uint32_t raw) {
+    return P.list_mode != 0 && (raw & (kHeavyFlag | kMaskList)) != 0u;
+}
+
+// The next queue entry for the calling warp (every lane calls), or n when the
+// queue of n entries is used up; the atomic is skipped once the counter has
+// passed n, so that the warps arriving after the queue is empty do not all
+// serialise on it.
+__device__ __forceinline__ uint32_t next_item(uint32_t* ctr, uint32_t n, unsigned lane) {
+    uint32_t v = n;
+    if (lane == 0 && *(volatile uint32_t*)ctr < n) v = min(atomicAdd(ctr, 1u), n);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// The neighbours of particle s shared out over the 32 lanes of the warp (every
+// lane calls with the same s): list entries k = lane, lane + 32, ..., or each
+// row of the cell search likewise. The caller reduces the lanes' partial sums.
+template <class F>
+__device__ __forceinline__ void warp_for_slot_list(const DevParams& P, const DevBuffers& B, int s, float x, float y,
+                                                   float z, F&& f) {
+    const unsigned lane = lane_id();
+    if (P.list_mode != 0) {
+        const uint32_t raw = B.nbr_cnt[s];
+        if (raw & kMaskList) {  // one mask word (32 candidates) per lane at a time
+            for_mask_words(P, B, s, raw & ~kMaskList, lane, 32u, f);
+            return;
+        }
+        const uint32_t cnt = raw & ~kHeavyFlag;
+        if (cnt <= (uint32_t)kMaxNbr) {
+            const uint32_t* __restrict__ col = B.nbr + s;
+            const size_t cap = (size_t)P.cap;
+            for (uint32_t k = lane; k < cnt; k += 32) f(__ldg(col + (size_t)k * cap));
+            return;
+        }
+    }
+    for_candidate_rows(P, B.cstart, B.mgcell[s], x, y, z, [&](uint32_t j0, uint32_t j1) {
+        for (uint32_t j = j0 + lane; j < j1; j += 32) f(j);
+    });
 }
 
 // ---------------------------------------------------------------------------
@@ -258,6 +349,22 @@ struct ForceDrift {
                 pij = pij * P.bvisc * P.h / 2.f / rho0;
                 pij = g1 * rho0 * V * pij;
                 fx += dx * pij; fy += dy * pij; fz += dz * pij;
+            }
+        }
+    }
+
+    // Sum the lanes' partial sums (warp-cooperative particles); every lane gets the totals.
+    __device__ __forceinline__ void warp_reduce() {
+        if (FORCE) {
+            fx = warp_sum_f(fx);
+            fy = warp_sum_f(fy);
+            fz = warp_sum_f(fz);
+        }
+        if (DRIFT) {
+#pragma unroll
+            for (int k = 0; k < NP; k++) {
+                dv[k].x = warp_sum_f(dv[k].x); dv[k].y = warp_sum_f(dv[k].y); dv[k].z = warp_sum_f(dv[k].z);
+                ag[k].x = warp_sum_f(ag[k].x); ag[k].y = warp_sum_f(ag[k].y); ag[k].z = warp_sum_f(ag[k].z);
             }
         }
     }
@@ -437,6 +544,15 @@ struct AlphaChange {
             const float vy = ja[k] * uj[k].y + ia[k] * um[k].y;
             const float vz = ja[k] * uj[k].z + ia[k] * um[k].z;
             acc[k].add(-(cm * (vx * dx + vy * dy + vz * dz)));
+        }
+    }
+
+    // Sum the lanes' compensated partial sums (warp-cooperative particles).
+    __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            acc[k].s = warp_sum_f(acc[k].s - acc[k].c);
+            acc[k].c = 0.f;
         }
     }
 

@@ -46,8 +46,14 @@ constexpr int kNrecFloat4 = 5;        // float4 per neighbour record of the alph
 // h-subcells around it as 18 index ranges), one word per 32 candidates.
 constexpr int kMaskWords = 64;        // mask words per particle (more candidates: the passes rescan)
 constexpr int kTabStride = 40;        // per bucket: [0..18] range ends in the sequence, [20..37] index - sequence
+constexpr uint32_t kBucketWindow = 32;  // members of a bucket taken by one warp of the density pass
 constexpr uint32_t kMaskList = 0x80000000u;  // nbr_cnt flag: bucket mask list, low bits = bucket (cell * 8 + octant)
 constexpr uint32_t kRescan = 0x7fffffffu;    // nbr_cnt value: no list, search the cells
+// Heavy particles (long lists, overflowed lists, cell searches) are queued in hq by
+// the list expansion and taken by whole warps in the force and alpha passes; an
+// index list of a heavy particle carries this flag over its length.
+constexpr uint32_t kHeavyFlag = 0x40000000u;
+constexpr uint32_t kHeavyList = 128;         // index lists longer than this are heavy
 
 // Error bits accumulated in the device error word (1 << sphmp_status).
 constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
@@ -120,6 +126,12 @@ struct DevBuffers {
     uint32_t* nmask;    // [kMaskWords * cap] bucket mask lists, column-major: word k of particle s at k * cap + s
     uint32_t* btab;     // [8 * G * kTabStride] candidate ranges of each bucket with a mask list
     uint32_t* dctr;     // [1] work counter of the bucket density kernel
+    uint2* wq;          // [cap / kBucketWindow + 16] member windows after the first of large buckets:
+                        // x = bucket (cell * 8 + octant), y = first member (internal index)
+    uint32_t* wq_n;     // [1] entries in wq (cleared by the scan, filled by the cell sort)
+    uint32_t* hq;       // [cap] heavy particles (internal index), filled by the list expansion
+    uint32_t* hq_n;     // [1] entries in hq (cleared by the scan)
+    uint32_t* hctr;     // [2] work counters over hq of the force and the alpha pass
     float4* nrec;       // [kNrecFloat4 * cap] neighbour records of the alpha pass (written by force + drift)
     // Internal order: inside every 2h cell, members grouped by the h-subcell
     // (octant) they occupy, octant index (oy * 2 + oz) * 2 + ox.

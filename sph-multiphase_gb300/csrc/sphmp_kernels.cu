@@ -162,6 +162,8 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_top(const __grid_constant__
         B.cstart[P.G + 1] = (uint32_t)active_n(B);
         B.big[0] = 0u;
         *B.act_n = 0u;
+        *B.wq_n = 0u;
+        *B.hq_n = 0u;
     }
 }
 
@@ -275,6 +277,15 @@ __device__ __forceinline__ void emit_octant(const DevBuffers& B, uint32_t c, uin
         for (uint32_t b = oct + 1; b < 8; b++) B.oct_start[(size_t)c * 8 + b] = start + cnt;
 }
 
+// Queue the member windows after the first of bucket (c, b) = members [m0, m1)
+// for the density pass (one warp per window of kBucketWindow members).
+__device__ __forceinline__ void push_windows(const DevBuffers& B, uint32_t c, uint32_t b, uint32_t m0, uint32_t m1) {
+    if (m1 <= m0 + kBucketWindow) return;
+    const uint32_t nw = (m1 - m0 - 1) / kBucketWindow;  // <= (m1 - m0) / kBucketWindow: wq never overflows
+    const uint32_t base = atomicAdd(B.wq_n, nw);
+    for (uint32_t i = 0; i < nw; i++) B.wq[base + i] = make_uint2(c * 8u + b, m0 + (i + 1) * kBucketWindow);
+}
+
 template <int E>
 __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuffers& B, const float4* __restrict__ pos_in,
                                                uint32_t* wsm, uint32_t c, uint32_t start, uint32_t cnt) {
@@ -314,6 +325,12 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
             const uint32_t pre = q < cnt ? wsm[k & 255u] : 0u;
             emit_octant(B, c, start, cnt, q, q < cnt ? k : (8u << 8), prev_oct, 8, pre);
         }
+    }
+    __syncwarp();  // the bucket starts written above are visible to the whole warp
+    if (lane < 8 && cnt > kBucketWindow) {
+        const uint32_t b0 = B.oct_start[(size_t)c * 8 + lane];
+        const uint32_t b1 = lane == 7 ? start + cnt : B.oct_start[(size_t)c * 8 + lane + 1];
+        push_windows(B, c, lane, b0, b1);
     }
     __syncwarp();
 }
@@ -385,6 +402,12 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
             const uint32_t prev_oct = q == 0 ? 0xFFFFFFFFu : (pk >> 13);
             const uint32_t pre = q < cnt ? B.midsort[start + (k & 0x1FFFu)] : 0u;
             emit_octant(B, c, start, cnt, q, k, prev_oct, 13, pre);
+        }
+        __syncthreads();
+        if (threadIdx.x < 8) {
+            const uint32_t b0 = B.oct_start[(size_t)c * 8 + threadIdx.x];
+            const uint32_t b1 = threadIdx.x == 7 ? start + cnt : B.oct_start[(size_t)c * 8 + threadIdx.x + 1];
+            push_windows(B, c, threadIdx.x, b0, b1);
         }
         __syncthreads();
     }
@@ -480,16 +503,19 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // to below 1e-7 of a typical term). The 27 subcells form 18 contiguous index
 // ranges (per (y, z) row: the x-neighbour bucket in the adjacent cell and the
 // two buckets of the same cell); their concatenation is the bucket's candidate
-// sequence, recorded in btab. The warp takes the candidates in blocks of
-// 32 * kBucketChunks held in registers, one per lane and chunk; for each block
-// it walks the bucket's members, every lane testing its candidates against the
-// member. The neighbour list of a member is the ballot of those tests, one
-// mask word per 32 candidates. The density terms are non-negative; each lane
-// sums at most kBucketChunks of them per block, the lanes are summed pairwise
-// and the blocks with Kahan compensation, so the relative rounding error of a
-// member's sum stays below (kBucketChunks + 6) * 2^-24. Warps take buckets from
-// a shared counter (bucket costs differ by orders of magnitude). Buckets with
-// more than kBucketMaxMembers members are taken in windows of that many.
+// sequence, recorded in btab. A warp takes one window of up to kBucketWindow
+// members of a bucket (one member per lane, broadcast by shuffles) and the
+// bucket's candidates in blocks of 32 * kBucketChunks held in registers, one
+// per lane and chunk; for each block it walks the window's members, every lane
+// testing its candidates against the member. The neighbour list of a member is
+// the ballot of those tests, one mask word per 32 candidates, without the
+// member itself. The density terms are non-negative; each lane sums at most
+// kBucketChunks of them per block, the lanes are summed pairwise and the blocks
+// with Kahan compensation (in the member's lane), so the relative rounding
+// error of a member's sum stays below (kBucketChunks + 6) * 2^-24. Warps take
+// work items from a shared counter (their costs differ by orders of magnitude):
+// the first window of every bucket, then the further windows of large buckets,
+// which the cell sort queued in wq, so that no bucket serialises on one warp.
 // The candidate sequence of bucket (c, q): the 27 h-subcells around it as 18
 // contiguous index ranges, two per (y, z) subcell row (the x-neighbour bucket in
 // the adjacent cell, and both x buckets of the bucket's own cell column). Lane i
@@ -551,13 +577,6 @@ __device__ __forceinline__ uint32_t seq_index(const uint32_t* rstart, const uint
 }
 
 constexpr int kBucketChunks = 8;
-constexpr int kBucketMaxMembers = 128;
-
-__device__ __forceinline__ float warp_sum_f(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 __device__ __forceinline__ uint32_t next_bucket(uint32_t* ctr, unsigned lane) {
     uint32_t v = 0;
@@ -572,108 +591,118 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
                                                                 const float4* __restrict__ alpha4) {
     constexpr int kWarps = kThreads / 32;
     __shared__ uint32_t tab[kWarps][2][20];                 // range starts and sequence offsets
-    __shared__ float2 msum[kWarps][kBucketMaxMembers];      // member sums (Kahan s, c) over blocks
     const unsigned lane = lane_id();
     const int w = threadIdx.x >> 5;
     uint32_t* rstart = tab[w][0];
     uint32_t* roff = tab[w][1];
     const uint32_t nb = *B.act_n * 8u;
+    const uint32_t nitems = nb + *B.wq_n;  // the first window of every bucket, then the queued windows
     const size_t cap = (size_t)P.cap;
     const float r2 = P.r2, r2list = P.r2list, ss = P.ss;
     const float kFar = __int_as_float(0x7f800000);  // +inf: never within range
-    for (uint32_t b = next_bucket(B.dctr, lane); b < nb; b = next_bucket(B.dctr, lane)) {
-        const uint32_t c = __ldg(&B.act[b >> 3]), q = b & 7u;
-        const uint32_t m0 = __ldg(&B.oct_start[(size_t)c * 8 + q]);
-        const uint32_t m1 = q == 7 ? __ldg(&B.cstart[c + 1]) : __ldg(&B.oct_start[(size_t)c * 8 + q + 1]);
-        if (m0 >= m1) continue;
-        // boundary members carry their volume and need no list
-        bool fluid = false;
-        for (uint32_t i = m0 + lane; i < m1; i += 32) {
-            const float wv = __ldg(&pos4[i]).w;
-            if (wv < 0.f) {
-                B.densp[i] = make_float2(-wv, 0.f);
-                B.nbr_cnt[i] = 0;
+    for (uint32_t it = next_bucket(B.dctr, lane); it < nitems; it = next_bucket(B.dctr, lane)) {
+        uint32_t c, q, w0;
+        if (it < nb) {
+            c = __ldg(&B.act[it >> 3]);
+            q = it & 7u;
+            w0 = __ldg(&B.oct_start[(size_t)c * 8 + q]);
+        } else {
+            const uint2 e = B.wq[it - nb];
+            c = e.x >> 3;
+            q = e.x & 7u;
+            w0 = e.y;
+        }
+        const uint32_t bid = c * 8u + q;
+        const uint32_t m0 = __ldg(&B.oct_start[(size_t)bid]);
+        const uint32_t m1 = q == 7 ? __ldg(&B.cstart[c + 1]) : __ldg(&B.oct_start[(size_t)bid + 1]);
+        if (w0 >= m1) continue;
+        const uint32_t w1 = min(m1, w0 + kBucketWindow);
+        // the window's members, one per lane; boundary members carry their volume and need no list
+        const uint32_t tl = w0 + lane;
+        float4 pm = make_float4(kFar, kFar, kFar, -1.f);
+        float rm = 0.f;
+        if (tl < w1) {
+            pm = __ldg(&pos4[tl]);
+            if (pm.w < 0.f) {
+                B.densp[tl] = make_float2(-pm.w, 0.f);
+                B.nbr_cnt[tl] = 0;
             } else {
-                fluid = true;
+                rm = __ldg(&alpha4[tl]).w;
             }
         }
-        if (!__any_sync(0xffffffffu, fluid)) continue;
+        const uint32_t fluid = __ballot_sync(0xffffffffu, tl < w1 && pm.w >= 0.f);
+        if (!fluid) continue;
         uint32_t st, off;
         const uint32_t T = bucket_ranges(P, B, c, q, lane, rstart, roff, st, off);
-        const uint32_t bid = c * 8u + q;
         const bool masked = T <= 32u * kMaskWords;
-        uint32_t* __restrict__ bt = B.btab + (size_t)bid * kTabStride;
-        if (masked && lane < 18) {
-            bt[lane] = off;
-            bt[20 + lane] = st - off;
+        if (masked && w0 == m0) {  // the bucket's range table, once per bucket
+            uint32_t* __restrict__ bt = B.btab + (size_t)bid * kTabStride;
+            if (lane < 18) {
+                bt[lane] = off;
+                bt[20 + lane] = st - off;
+            }
+            if (lane == 18) bt[18] = T;
         }
-        if (masked && lane == 18) bt[18] = T;
         const uint32_t lst = masked ? (kMaskList | bid) : kRescan;
-        // the members in windows of kBucketMaxMembers (more than one only in squeezed regions)
-        for (uint32_t w0 = m0; w0 < m1; w0 += (uint32_t)kBucketMaxMembers) {
-            const uint32_t w1 = min(m1, w0 + (uint32_t)kBucketMaxMembers);
-            int r = 0;
-            for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
-                float4 cj[kBucketChunks];  // w: fluid mass (0 for boundary)
-                float vb[kBucketChunks];   // boundary volume (0 for fluid)
+        // sequence position of member t = t + self_base: the bucket lies in the range of its own
+        // cell column on its own subcell row (range 8 + part, part = 1 for the low x half)
+        const int rs = 8 + ((q & 1u) == 0u ? 1 : 0);
+        const uint32_t self_base = __shfl_sync(0xffffffffu, off, rs) - __shfl_sync(0xffffffffu, st, rs);
+        Kahan msum;  // lane i: member w0 + i, summed over the candidate blocks
+        int r = 0;
+        for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
+            float4 cj[kBucketChunks];  // w: fluid mass (0 for boundary)
+            float vb[kBucketChunks];   // boundary volume (0 for fluid)
+#pragma unroll
+            for (int ch = 0; ch < kBucketChunks; ch++) {
+                const uint32_t e = base + lane + 32u * ch;
+                cj[ch] = make_float4(kFar, kFar, kFar, 0.f);
+                vb[ch] = 0.f;
+                if (e < T) {
+                    cj[ch] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
+                    vb[ch] = fmaxf(-cj[ch].w, 0.f);
+                    cj[ch].w = fmaxf(cj[ch].w, 0.f);
+                }
+            }
+            const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
+            const uint32_t word0 = base >> 5;
+            for (uint32_t fm = fluid; fm != 0u; fm &= fm - 1u) {
+                const int i = __ffs(fm) - 1;
+                const float px = __shfl_sync(0xffffffffu, pm.x, i);
+                const float py = __shfl_sync(0xffffffffu, pm.y, i);
+                const float pz = __shfl_sync(0xffffffffu, pm.z, i);
+                const float rho0 = __shfl_sync(0xffffffffu, rm, i);
+                const uint32_t t = w0 + (uint32_t)i;
+                float acc = 0.f;
+                uint32_t mine = 0;  // lane k keeps the mask word of chunk k
 #pragma unroll
                 for (int ch = 0; ch < kBucketChunks; ch++) {
-                    const uint32_t e = base + lane + 32u * ch;
-                    cj[ch] = make_float4(kFar, kFar, kFar, 0.f);
-                    vb[ch] = 0.f;
-                    if (e < T) {
-                        cj[ch] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
-                        vb[ch] = fmaxf(-cj[ch].w, 0.f);
-                        cj[ch].w = fmaxf(cj[ch].w, 0.f);
+                    if (ch < nch) {
+                        float dx = px - cj[ch].x, dy = py - cj[ch].y, dz = pz - cj[ch].z;
+                        if (!SS1) {
+                            dx *= ss;
+                            dy *= ss;
+                            dz *= ss;
+                        }
+                        const float dsq = dx * dx + dy * dy + dz * dz;
+                        const float cc = fmaxf(r2 - dsq, 0.f);  // 0 outside h (and for the padding lanes)
+                        acc = fmaf(cc * cc * cc, fmaf(rho0, vb[ch], cj[ch].w), acc);
+                        // coincident particles stay in the list (every consumer skips r == 0);
+                        // the member itself is cleared below
+                        const uint32_t bal = __ballot_sync(0xffffffffu, dsq < r2list);
+                        mine = lane == (unsigned)ch ? bal : mine;
                     }
                 }
-                const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
-                const uint32_t word0 = base >> 5;
-                const bool first = base == 0;
-                for (uint32_t t = w0; t < w1; t++) {
-                    const float4 pt = __ldg(&pos4[t]);
-                    if (pt.w < 0.f) continue;
-                    const float rho0 = __ldg(&alpha4[t]).w;
-                    float acc = 0.f;
-                    uint32_t mine = 0;  // lane k keeps the mask word of chunk k
-#pragma unroll
-                    for (int ch = 0; ch < kBucketChunks; ch++) {
-                        if (ch < nch) {
-                            float dx = pt.x - cj[ch].x, dy = pt.y - cj[ch].y, dz = pt.z - cj[ch].z;
-                            if (!SS1) {
-                                dx *= ss;
-                                dy *= ss;
-                                dz *= ss;
-                            }
-                            const float dsq = dx * dx + dy * dy + dz * dz;
-                            const float cc = fmaxf(r2 - dsq, 0.f);  // 0 outside h (and for the padding lanes)
-                            acc = fmaf(cc * cc * cc, fmaf(rho0, vb[ch], cj[ch].w), acc);
-                            const uint32_t bal = __ballot_sync(0xffffffffu, dsq > 0.f && dsq < r2list);
-                            mine = lane == (unsigned)ch ? bal : mine;
-                        }
-                    }
-                    if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
-                    const float part = warp_sum_f(acc);
-                    if (lane == 0) {
-                        Kahan tot;
-                        if (!first) {
-                            const float2 prev = msum[w][t - w0];
-                            tot.s = prev.x;
-                            tot.c = prev.y;
-                        }
-                        tot.add(part);
-                        msum[w][t - w0] = make_float2(tot.s, tot.c);
-                    }
-                }
-                __syncwarp();
+                const uint32_t es = t + self_base - base;  // the member's own bit, if in this block
+                if (es < 32u * kBucketChunks && lane == (es >> 5)) mine &= ~(1u << (es & 31u));
+                if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
+                const float part = warp_sum_f(acc);
+                if (lane == (unsigned)i) msum.add(part);
             }
-            for (uint32_t i = lane; i < w1 - w0; i += 32) {
-                const uint32_t t = w0 + i;
-                if (__ldg(&pos4[t]).w < 0.f) continue;
-                B.nbr_cnt[t] = lst;
-                B.densp[t] = density_result(P, msum[w][i].x, __ldg(&alpha4[t]).w);
-            }
-            __syncwarp();
+        }
+        if (tl < w1 && pm.w >= 0.f) {
+            B.nbr_cnt[tl] = lst;
+            B.densp[tl] = density_result(P, msum.s, rm);
         }
     }
 }
@@ -682,8 +711,11 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
 // candidate e of its bucket's sequence, whose index is e plus the offset of the
 // sequence range holding e (btab). One thread per in-grid particle; the lanes
 // of a warp emit their n-th entries together so that every row of the
-// column-major list is written by one coalesced store. Lists longer than
-// kMaxNbr leave the particle to the cell search.
+// column-major list is written by one coalesced store. A particle with more
+// than kMaxNbr neighbours keeps its mask list (nbr_cnt = kMaskList | bucket),
+// which the passes decode directly. Particles with more than kHeavyList
+// neighbours (their lists flagged kHeavyFlag), with mask lists or left to the
+// cell search are queued in hq for the force and alpha passes.
 __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant__ DevParams P,
                                                            const __grid_constant__ DevBuffers B) {
     const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
@@ -696,7 +728,9 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
     // hits of this particle, then of the warp's busiest lane (the loop bound)
     uint32_t cnt = 0;
     for (uint32_t wd = 0; wd < nw; wd++) cnt += __popc(__ldg(mw + (size_t)wd * cap));
-    uint32_t rounds = min(cnt, (uint32_t)kMaxNbr);
+    const bool over = cnt > (uint32_t)kMaxNbr;  // keeps its mask list: nothing to write
+    if (over) cnt = 0;
+    uint32_t rounds = cnt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
     uint32_t* __restrict__ col = B.nbr + t;
@@ -719,7 +753,16 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
             col[(size_t)n * cap] = e + delta;
         }
     }
-    if (mine) B.nbr_cnt[t] = cnt <= (uint32_t)kMaxNbr ? cnt : kRescan;
+    const bool heavy = (mine && (over || cnt > kHeavyList)) || lst == kRescan;
+    if (mine && !over) B.nbr_cnt[t] = heavy ? (cnt | kHeavyFlag) : cnt;
+    const uint32_t hb = __ballot_sync(0xffffffffu, heavy);
+    if (hb) {
+        const unsigned lane = lane_id();
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(B.hq_n, (uint32_t)__popc(hb));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (heavy) B.hq[base + __popc(hb & lanemask_lt())] = t;
+    }
 }
 
 __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ DevParams P,
@@ -782,8 +825,34 @@ __device__ __forceinline__ void force_drift_one(const DevParams& P, const DevBuf
                FORCE && DRIFT ? vev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
 }
 
-// Force + drift, one thread per particle. With both, it also writes every
-// in-grid particle's neighbour record for the fused alpha pass.
+// Force + drift of heavy particle s by the whole warp (every lane calls with
+// the same s): the lanes share its neighbours out, their partial sums are
+// added, lane 0 stores.
+template <bool FORCE, bool DRIFT, int NP>
+__device__ __forceinline__ void force_drift_warp(const DevParams& P, const DevBuffers& B,
+                                                 const float4* __restrict__ pos4, const float4* __restrict__ vel4,
+                                                 const float4* __restrict__ alpha4, const float4* __restrict__ aprev4,
+                                                 const float4* __restrict__ vev4, int s) {
+    const float4 pi = pos4[s];
+    ForceDrift<FORCE, DRIFT, NP> acc;
+    acc.init(P, pi, vel4[s], B.densp[s], alpha4[s]);
+    warp_for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4 pj = __ldg(&pos4[j]);
+        const float2 dpj = __ldg(&B.densp[j]);
+        const float4 vj = FORCE ? __ldg(&vel4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 aj = DRIFT ? __ldg(&alpha4[j]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        acc.pair(P, pj, dpj, vj, aj);
+    });
+    acc.warp_reduce();
+    if (lane_id() == 0)
+        acc.finish(P, B, s, DRIFT ? aprev4[s] : make_float4(0.f, 0.f, 0.f, 0.f),
+                   FORCE && DRIFT ? vev4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
+}
+
+// Force + drift, one thread per particle; every warp first takes heavy
+// particles from the queue (whole warp per particle) while any are left. With
+// both, it also writes every in-grid particle's neighbour record for the fused
+// alpha pass.
 template <bool FORCE, bool DRIFT, int NP>
 __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_constant__ DevParams P,
                                                              const __grid_constant__ DevBuffers B,
@@ -792,6 +861,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_consta
                                                              const float4* __restrict__ alpha4,
                                                              const float4* __restrict__ aprev4,
                                                              const float4* __restrict__ vev4) {
+    if (P.list_mode != 0) {
+        const unsigned lane = lane_id();
+        const uint32_t nh = *B.hq_n;
+        for (uint32_t h = next_item(&B.hctr[0], nh, lane); h < nh; h = next_item(&B.hctr[0], nh, lane))
+            force_drift_warp<FORCE, DRIFT, NP>(P, B, pos4, vel4, alpha4, aprev4, vev4, (int)B.hq[h]);
+    }
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= active_n(B) || B.mgcell[s] == kUndef) return;
     const float4 pi = pos4[s];
@@ -804,6 +879,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_force_drift(const __grid_consta
         }
         return;
     }
+    if (is_heavy(P, B.nbr_cnt[s])) return;  // taken from the queue
     force_drift_one<FORCE, DRIFT, NP>(P, B, pos4, vel4, alpha4, aprev4, vev4, s, pi);
 }
 
@@ -1066,12 +1142,44 @@ __device__ __forceinline__ void alpha_change_nrec(const DevParams& P, const DevB
     acc.result(P, out);
 }
 
+// Alpha change of heavy particle s by the whole warp (every lane calls with the
+// same s and gets the result).
+template <int NP>
+__device__ __forceinline__ void alpha_change_nrec_warp(const DevParams& P, const DevBuffers& B, const F4Set& S, int s,
+                                                       float (&out)[3]) {
+    const float4 pi = S.in[POS][s], vei = S.in[VEV][s], ai = S.in[ALPHA][s];
+    float3 um[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        const float4 u = B.drift4[(size_t)k * P.cap + s];
+        um[k] = make_float3(u.x, u.y, u.z);
+    }
+    AlphaChange<NP> acc;
+    acc.init(pi, vei, ai, um);
+    warp_for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
+        const float4* __restrict__ r = B.nrec + (size_t)j * kNrecFloat4;
+        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+        const float4 r4 = NP > 2 ? __ldg(r + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 uj[NP];
+        uj[0] = make_float4(r2.z, r2.w, r3.x, 0.f);
+        if (NP > 1) uj[NP > 1 ? 1 : 0] = make_float4(r3.y, r3.z, r3.w, 0.f);
+        if (NP > 2) uj[NP > 2 ? 2 : 0] = make_float4(r4.x, r4.y, r4.z, 0.f);
+        acc.pair(P, r0, r0.w, make_float4(r1.x, r1.y, r1.z, 0.f), make_float4(r1.w, r2.x, r2.y, 0.f), uj);
+    });
+    acc.warp_reduce();
+    acc.result(P, out);
+}
+
+// Alpha + correction + advance of one slot whose alpha sum (in-grid fluid
+// particles) is `anew`; writes the five float4 fields to the other buffer.
 template <int NP, bool MP>
-__device__ __forceinline__ void pass_c_one(const DevParams& P, const DevBuffers& B, const F4Set& S, int s) {
-    float4 p = S.in[POS][s], v = S.in[VEL][s], ve = S.in[VEV][s], al = S.in[ALPHA][s], ap = S.in[APREV][s];
-    const float4 pi = p, vei = ve, ai = al;
-    pass_c_slot<NP, MP>(P, B, s, B.mgcell[s] == kUndef, p, v, ve, al, ap, [&](float (&a)[3]) {
-        alpha_change_nrec<NP>(P, B, s, pi, vei, ai, a);
+__device__ __forceinline__ void pass_c_finish(const DevParams& P, const DevBuffers& B, const F4Set& S, int s,
+                                              bool undef, float4 p, float4 ve, float4 al, const float (&anew)[3]) {
+    float4 v = S.in[VEL][s], ap = S.in[APREV][s];
+    pass_c_slot<NP, MP>(P, B, s, undef, p, v, ve, al, ap, [&](float (&a)[3]) {
+        a[0] = anew[0];
+        a[1] = anew[1];
+        a[2] = anew[2];
     });
     S.out[POS][s] = p;
     S.out[VEL][s] = v;
@@ -1081,14 +1189,33 @@ __device__ __forceinline__ void pass_c_one(const DevParams& P, const DevBuffers&
 }
 
 // Fused alpha advance + correction + advance, one thread per particle: reads the
-// cur buffers, writes every float4 field of every particle into the other buffer.
+// cur buffers, writes every float4 field of every particle into the other
+// buffer. Every warp first takes heavy particles from the queue (whole warp per
+// alpha sum, lane 0 finishes the particle) while any are left.
 template <int NP, bool MP>
 __global__ void __launch_bounds__(kThreads, 4) k_pass_c(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
+    if (MP && P.list_mode != 0) {
+        const unsigned lane = lane_id();
+        const uint32_t nh = *B.hq_n;
+        for (uint32_t h = next_item(&B.hctr[1], nh, lane); h < nh; h = next_item(&B.hctr[1], nh, lane)) {
+            const int sh = (int)B.hq[h];
+            float a[3];
+            alpha_change_nrec_warp<NP>(P, B, S, sh, a);
+            if (lane == 0) pass_c_finish<NP, MP>(P, B, S, sh, false, S.in[POS][sh], S.in[VEV][sh], S.in[ALPHA][sh], a);
+        }
+    }
     const int s = blockIdx.x * kThreads + threadIdx.x;
     if (s >= active_n(B)) return;
-    pass_c_one<NP, MP>(P, B, S, s);
+    const float4 p = S.in[POS][s], ve = S.in[VEV][s], al = S.in[ALPHA][s];
+    const bool undef = B.mgcell[s] == kUndef;
+    // the alpha sum is needed for in-grid fluid particles (pass_c_slot)
+    const bool walk = MP && !undef && !(p.w < 0.f);
+    if (walk && is_heavy(P, B.nbr_cnt[s])) return;  // taken from the queue
+    float anew[3] = {al.x, al.y, al.z};
+    if (walk) alpha_change_nrec<NP>(P, B, s, p, ve, al, anew);
+    pass_c_finish<NP, MP>(P, B, S, s, undef, p, ve, al, anew);
 }
 
 // ---------------------------------------------------------------------------
@@ -1490,6 +1617,7 @@ void launch_density_oct(const DevParams& P, const DevBuffers& B, const int* cur,
 
 template <bool F, bool D>
 static void fd_dispatch(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {
+    cudaMemsetAsync(&B.hctr[0], 0, sizeof(uint32_t), s);  // the heavy-particle queue's work counter
     const float4* pos = B.f4[POS][cur[POS]];
     const float4* vel = B.f4[VEL][cur[VEL]];
     const float4* al = B.f4[ALPHA][cur[ALPHA]];
@@ -1594,6 +1722,7 @@ void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cuda
     if (P.n <= 0) return;
     const F4Set S = make_set(B, cur, true);
     const int g = blocks_for(P.n);
+    cudaMemsetAsync(&B.hctr[1], 0, sizeof(uint32_t), s);  // the heavy-particle queue's work counter
     if (!P.multiphase) {
         k_pass_c<1, false><<<g, kThreads, 0, s>>>(P, B, S);
         return;
