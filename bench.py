@@ -26,6 +26,11 @@ timed on the host clock.
 CPU oracle (a statement-by-statement restatement of the reference kernels,
 bit-identical to them) on the same scene, all host threads, the same metric.
 
+--workload dam_break measures the 32^3 two-phase dam break (32,768 fluid
+particles, d = 0.01 m, h = 0.02 m, 0.64 m box, gas sphere, linear EOS k = 3,
+dt = 2e-4 s) on the GPU (captured graph, CUDA events) with the CPU oracle on the
+same scene beside it; with --impl reference, the CPU oracle alone.
+
 --workload batched measures the batched configuration instead (not the headline
 line): 512 independent two-phase bubble scenes, particle counts log-uniform in
 [4096, 65536], 1-4 gas bubbles of radius 3h-8h each, h = 0.02 m, tiled into one
@@ -58,7 +63,7 @@ h = 0.01 m, dt = 1e-4 s, linear EOS k = 3) against the plain pipeline over the
 same simulated time, with 256 gas bubbles (value) and all liquid; host clock.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-       [--workload batched|large_step|device_ref|learned]
+       [--workload dam_break|batched|large_step|device_ref|learned]
 """
 import argparse
 import json
@@ -78,9 +83,9 @@ UNIT = "particle-steps/s"
 # neighbour re-reads assumed to hit L2 / shared memory)
 ALGO_BYTES = {"hash": 24, "cell_starts": 0, "cell_order": 16, "rearrange": 128, "density": 24,
               "force_drift": 136, "alpha_correct_advance": 168, "advance": 168}
-# hash, 3 scan, scatter, cell sort, big-cell sort, rearrange, index update, bucket density,
+# hash, 3 scan, scatter, cell sort, big-cell sort, rearrange (with the slot map), bucket density,
 # list expansion, force + drift, alpha + correction + advance
-KERNELS_PER_FUSED_STEP = 13
+KERNELS_PER_FUSED_STEP = 12
 
 
 def _dist():
@@ -354,6 +359,7 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev_index = torch.cuda.current_device()
     scene = build_scene(args.seed + rank)
+    scene.params.cell_order = abi.CELL_ORDER_MORTON if args.cell_order == "morton" else abi.CELL_ORDER_LINEAR
     n_fluid = scene.n_fluid
 
     ctx = sphmp.Context(scene.params)
@@ -446,6 +452,8 @@ def run_gpu(args):
     clocks = clk.summary()
     cfg = scene_config(scene)
     cfg["seed"] = args.seed
+    if args.cell_order != "linear":
+        cfg["cell_order"] = args.cell_order
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -502,6 +510,10 @@ def run_batched(args):
     ctx.before_first_step()
     ctx.step(args.warmup, abi.SCHEDULE_FUSED, use_graph=True)
     ctx.sync()
+    # the launch-shape autotuner on the warmed state (timed trials in a scratch context); the
+    # hand-swept default is its first trial
+    tuning = ctx.autotune(trial_steps=args.tune_steps, allow_reorder=args.cell_order == "morton") \
+        if args.tune_steps > 0 else None
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     rep.barrier()
@@ -524,7 +536,8 @@ def run_batched(args):
                    "fluid_particles": scene.n_fluid, "boundary_particles": scene.n_boundary, "h": 0.02,
                    "d": 0.01, "dt": 2e-4, "eos": "linear k=3", "schedule": "fused, one launch per pass for all "
                    "scenes (spatial tiling)", "graph": True, "stage_ms_after": {k: round(v, 4) for k, v in
-                                                                                  stages.items()}},
+                                                                                  stages.items()},
+                   "autotune": tuning},
         "gpu_launches": KERNELS_PER_FUSED_STEP * args.steps,
         "clocks": clk.summary(),
     }
@@ -882,6 +895,92 @@ def run_device_ref_reference(args):
     return 0
 
 
+def dam_break_scene(seed, gen=None):
+    """The 32^3 two-phase dam break (32,768 fluid particles, d = 0.01 m, h = 0.02 m, 0.64 m
+    box, gas sphere r = 0.06 m, linear EOS k = 3, dt = 2e-4 s)."""
+    from sphmp import scenes
+    return scenes.dam_break_2phase(seed=seed, n_side=32, gen=gen or scenes.LIBRARY)
+
+
+def dam_break_config(sc, seed):
+    return {"workload": sc.name, "fluid_particles": sc.n_fluid, "boundary_particles": sc.n_boundary, "phases": 2,
+            "h": 0.02, "d": 0.01, "box": [0.64, 0.64, 0.64], "dt": 2e-4, "eos": "linear k=3",
+            "schedule": SCHEDULE_NAME, "seed": seed}
+
+
+def run_dam_break(args):
+    """The dam break on the GPU (captured-graph steps, CUDA events on the launch stream) and the
+    CPU oracle on the same scene (a bounded sample of the same steps)."""
+    import torch
+
+    import sphmp
+    from sphmp import abi
+
+    rep = Replicas()
+    torch.cuda.set_device(rep.local)
+    sc = dam_break_scene(args.seed + rep.rank)
+    stream = torch.cuda.Stream()
+    ctx = sphmp.Context(sc.params)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_aos(sc.disp, sc.calc)
+    ctx.before_first_step()
+    ctx.step(args.warmup, abi.SCHEDULE_FUSED, use_graph=True)
+    ctx.sync()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    rep.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ev0.record(stream)
+        ctx.step(args.steps, abi.SCHEDULE_FUSED, use_graph=True)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    rep.barrier()
+    ms = rep.max(ev0.elapsed_time(ev1))
+    ctx.close()
+    line = {
+        "metric": "particle-steps/s, 32^3 two-phase dam break (1 GB300)",
+        "value": rep.ws * sc.n_fluid * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": rep.ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dam_break_config(sc, args.seed + rep.rank),
+        "run": {"graph": True, "l2": "working set ~20 MB, inside the 129 MB L2 (state resident, no flush)"},
+        "gpu_launches": KERNELS_PER_FUSED_STEP * args.steps, "clocks": clk.summary(),
+    }
+    if rep.rank == 0 and not args.no_cpu_baseline:
+        v, done, dt, nthr, _ = cpu_sample(sc, args.cpu_steps_dam, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthr, "kind": "port",
+                                "sample": f"{done} fused steps of the same scene on the CPU oracle "
+                                          f"({dt:.1f} s, {nthr} threads)"}
+    if rep.rank == 0:
+        print(json.dumps(line))
+    rep.close()
+    return 0
+
+
+def run_dam_break_reference(args):
+    """--impl reference --workload dam_break: the CPU oracle alone on the dam break."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    sc = dam_break_scene(args.seed, gen=O.Generators)
+    value, done, dt, nthr, warm = cpu_sample(sc, max(1, args.steps), budget_s=args.cpu_budget, warmup=args.warmup)
+    line = {
+        "metric": "particle-steps/s, 32^3 two-phase dam break (1 GB300)", "value": value, "unit": UNIT,
+        "impl": "reference", "n_gpus": args.gpus, "steps": done, "warmup": warm,
+        "ms_per_step": 1000.0 * dt / max(done, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": dam_break_config(sc, args.seed),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthr, "kind": "port",
+                         "sample": f"{done} fused steps of the dam break on the oracle (capped at "
+                                   f"{args.cpu_budget:.0f} s; requested {args.steps})"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "repo_libraries_loaded": _repo_libraries(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -896,8 +995,16 @@ def main():
     ap.add_argument("--profile-every", type=int, default=100, help="steps between per-stage timing samples")
     ap.add_argument("--learned-steps", type=int, default=1280,
                     help="simulated time of the learned workload's rollout, in plain steps of dt")
-    ap.add_argument("--workload", default="blobs", choices=["blobs", "batched", "large_step", "device_ref", "learned"],
-                    help="blobs: the headline 2^20-particle scene; batched: 512 tiled bubble scenes; "
+    ap.add_argument("--cell-order", default="linear", choices=["linear", "morton"],
+                    help="order of the cells in the sorted arrays (blobs workload): the reference's linear key "
+                         "order (bit-exact sort, the default) or Z-order")
+    ap.add_argument("--tune-steps", type=int, default=10,
+                    help="batched workload: fused steps per autotuner trial (0: no autotuning)")
+    ap.add_argument("--cpu-steps-dam", type=int, default=200, help="CPU-oracle sample of the dam-break workload")
+    ap.add_argument("--workload", default="blobs",
+                    choices=["blobs", "dam_break", "batched", "large_step", "device_ref", "learned"],
+                    help="blobs: the headline 2^20-particle scene; dam_break: the 32^3 two-phase dam break "
+                         "(GPU and CPU oracle); batched: 512 tiled bubble scenes; "
                          "large_step: one 8 dt step against 8 plain steps; device_ref: the Tait liquid lattice "
                          "(with --impl reference: the reference's own GPU kernels); learned: corrector training "
                          "and the audited rollout of the 256x128x128 bubble lattice against the plain pipeline")
@@ -906,6 +1013,8 @@ def main():
         args.warmup = 3
     if args.workload == "device_ref":
         return run_device_ref_reference(args) if args.impl == "reference" else run_device_ref_library(args)
+    if args.workload == "dam_break":
+        return run_dam_break_reference(args) if args.impl == "reference" else run_dam_break(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":

@@ -83,6 +83,20 @@ typedef enum sphmp_schedule {
  * extensions for the multiphase kernels (whose constants lived in the removed
  * legacy `FluidParams simData`) and for this implementation.
  */
+/* Order of the cells in the sorted particle arrays. LINEAR is the reference's
+   key order, (gy * rz + gz) * rx + gx (fluid_system_kern.cu:55), and is the only
+   order whose midsort / mgridoff are bit-identical to GetGridListCUDA's. MORTON
+   sorts the same cells by the Z-order (bit-interleaved) code of (gx, gy, gz):
+   every cell holds the same particles in the same order as in LINEAR mode
+   (mgcell per particle, mgridcnt and mgndx are unchanged), only the sequence of
+   the cells in the sorted arrays differs, so that neighbouring cells sit close
+   in memory along all three axes. Caller-supplied sort arrays (uploads of
+   SPHMP_F_MIDSORT / SPHMP_F_MGRIDCNT) are refused in MORTON mode. */
+typedef enum sphmp_cell_order {
+    SPHMP_CELL_ORDER_LINEAR = 0,
+    SPHMP_CELL_ORDER_MORTON = 1
+} sphmp_cell_order;
+
 typedef struct sphmp_params {
     /* environment */
     float acclimit;
@@ -163,7 +177,9 @@ typedef struct sphmp_params {
     float mf_pintstiff;          /* simData.pintstiff (pressure-correction stiffness) */
     float mf_omega;              /* simData.omega: boundary pressure factor of the project-U force */
     float mf_visc_factor;        /* simData.visc_factor: boundary viscosity factor of the project-U force */
-    int32_t reserved[3];
+    int32_t cell_order;          /* sphmp_cell_order: order of the cells in the sorted arrays */
+    int32_t bucket_window;       /* members of one h-subcell per work item of the density pass, 8..32 (0: 32) */
+    int32_t heavy_list;          /* neighbour lists longer than this are walked by a whole warp, 32..256 (0: 128) */
 } sphmp_params;
 
 /* Byte-compatible copies of the reference records (SPH_Solver/common_header.h:112-137). */
@@ -427,6 +443,65 @@ sphmp_status sphmp_compute_force(sphmp_ctx* ctx);
 sphmp_status sphmp_compute_force_projectu(sphmp_ctx* ctx);
 /* MfAdvanceCUDA (fluid_system_host.cu:385-394). */
 sphmp_status sphmp_advance(sphmp_ctx* ctx);
+
+/* ---- the IISPH step (implicit incompressible SPH, RunIISPH,
+   fluid_system.cpp:567-588; kernels fluid_system_kern.cu:637-1115) ----
+   The reference's kernels as written: the cubic spline of support 2h and its
+   gradient, the advection acceleration from the boundary's artificial
+   viscosity within 2h plus gravity, every other gradient sum over fluid
+   neighbours within h, relaxed Jacobi with omega = 0.1 starting from half the
+   stored pressure. After sphmp_iisph_density, SPHMP_F_DENS reads the density
+   itself (the reference stores it there), not its inverse. Each needs the cell
+   lists of the current sort. */
+/* ComputeDensityIISPH_CUDA (fluid_system_host.cu:505-508). */
+sphmp_status sphmp_iisph_density(sphmp_ctx* ctx);
+/* PredictAdvection (fluid_system_host.cu:515-524): ComputeDii then ComputeAii. */
+sphmp_status sphmp_iisph_predict_advection(sphmp_ctx* ctx);
+/* One pass of PressureSolve's loop (fluid_system_host.cu:529-540): Pressure_DP,
+   Pressure_Iter (accel and pressure of the iterate), press_l = press_l1. With
+   `residue`: residue[0] = the reference's quantity (the residues summed over
+   every slot, boundary particles 0, divided by the slot count), residue[1] = the
+   mean |residue| over in-grid fluid particles (kg/m^3). Synchronises the
+   context stream. */
+sphmp_status sphmp_iisph_pressure_iteration(sphmp_ctx* ctx, double* residue);
+/* PressureSolve with a stopping rule of this library's own (the reference's
+   loop never ends): iterate until residue[1] <= tol after at least min_iter
+   iterations, or max_iter iterations; `iters` and `residue` (2 doubles) receive
+   the count and the last residues. */
+sphmp_status sphmp_iisph_pressure_solve(sphmp_ctx* ctx, float tol, int32_t min_iter, int32_t max_iter,
+                                        int32_t* iters, double* residue);
+/* Integration (IntegrateIISPH, fluid_system_host.cu:552-556): vel = veleval +
+   accel dt, pos += vel dt / simscale. */
+sphmp_status sphmp_iisph_integrate(sphmp_ctx* ctx);
+/* ---- launch-shape autotuner; no counterpart in the reference (which runs one
+   scene at a fixed 384-thread launch geometry, fluid_system_host.cu:70-76) ---- */
+typedef struct sphmp_tuning {
+    int32_t cell_order;     /* chosen sphmp_cell_order */
+    int32_t bucket_window;  /* chosen members per density work item */
+    int32_t heavy_list;     /* chosen heavy-list threshold */
+    int32_t trials;         /* configurations timed */
+    float ms_per_step;      /* fused step of the chosen configuration */
+    float ms_before;        /* fused step of the configuration the context had */
+} sphmp_tuning;
+/* Times the fused step of the context's current state in a scratch context of
+   the same capacity for each candidate configuration (members per density work
+   item 16 or 32, heavy-list threshold 64, 128 or 256, and with allow_reorder the
+   Morton cell order beside the linear one): a device copy of the state, one
+   captured-graph step to warm, then trial_steps graph steps timed with CUDA
+   events on the scratch stream. The fastest configuration is written into the
+   context's parameters (its graph is re-captured at the next step); the
+   context's own state does not move. The window and threshold change no result
+   beyond the summation order of the heavy particles; the Morton order changes the
+   order of the sorted arrays (not bit-exact with the reference's sort), hence
+   the opt-in. Allocates the scratch context for the duration of the call. */
+sphmp_status sphmp_autotune(sphmp_ctx* ctx, int32_t trial_steps, int32_t allow_reorder, sphmp_tuning* out);
+
+/* nsteps IISPH steps: the sort, density, PredictAdvection, the pressure solve
+   (tol, at least 2 and at most max_iter iterations) and the integration the
+   reference comments out; iters[k] (if given) = the iterations of step k,
+   residue (2 doubles, if given) = the last step's final residues. */
+sphmp_status sphmp_step_iisph(sphmp_ctx* ctx, int32_t nsteps, float tol, int32_t max_iter, int32_t* iters,
+                              double* residue);
 
 /* nsteps full steps (sort ... advance) in the given sphmp_schedule. Steps run
    from a captured CUDA graph when `use_graph` is 1 (one step per graph for the

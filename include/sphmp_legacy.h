@@ -64,6 +64,18 @@ void ComputeForceCUDA_ProjectU(void);
 void MfAdvanceCUDA(void);
 /* ComputeBoundaryDensity (fluid_system_host.cu:510-513) */
 void ComputeBoundaryDensity(void);
+/* The IISPH step of RunIISPH (fluid_system.cpp:567-588):
+   ComputeDensityIISPH_CUDA (fluid_system_host.cu:505-508), PredictAdvection
+   (:515-524), PressureSolve (:526-550) and Integration (:552-556). The
+   reference's PressureSolve loop never ends (its break is commented out); this
+   one stops once the mean |density residue| over in-grid fluid particles is at
+   most 0.1 kg/m^3 after at least 2 iterations, or after 100 iterations (the
+   sphmp_iisph_pressure_solve entry point takes its own limits), and prints no
+   per-iteration line. */
+void ComputeDensityIISPH_CUDA(void);
+void PredictAdvection(void);
+void PressureSolve(void);
+void Integration(void);
 /* computeNumBlocks (fluid_system_host.cu:70-76): launch geometry helper. */
 void computeNumBlocks(int numPnts, int maxThreads, int* numBlocks, int* numThreads);
 

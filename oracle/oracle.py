@@ -77,6 +77,8 @@ def _state_struct(R):
         ("alpha", P(R)), ("alpha_pre", P(R)), ("drift", P(R)), ("aprev", P(R)), ("pmod", P(R)),
         ("mgcell", P(C.c_uint32)), ("midsort", P(C.c_uint32)), ("mgndx", P(C.c_uint32)),
         ("mgridoff", P(C.c_int32)), ("mgridcnt", P(C.c_int32)), ("velxcor", P(R)),
+        ("dii", P(R)), ("aii", P(R)), ("rho_adv", P(R)), ("press_l", P(R)), ("press_l1", P(R)),
+        ("dijpj", P(R)), ("residue", P(R)),
     ]})
 
 
@@ -86,7 +88,8 @@ StateF64 = _state_struct(C.c_double)
 # per-particle real-valued fields and their trailing shapes
 REAL_FIELDS = {"pos": (3,), "vel": (3,), "veleval": (3,), "pressure": (), "dens": (), "restdens": (),
                "mass": (), "visc": (), "accel": (3,), "alpha": (3,), "alpha_pre": (3,), "drift": (3, 3),
-               "aprev": (3,), "pmod": (), "velxcor": (3,)}
+               "aprev": (3,), "pmod": (), "velxcor": (3,), "dii": (3,), "aii": (), "rho_adv": (),
+               "press_l": (), "press_l1": (), "dijpj": (3,), "residue": ()}
 INT_FIELDS = {"type": np.int32, "bornid": np.int32, "mgcell": np.uint32, "midsort": np.uint32,
               "mgndx": np.uint32}
 GRID_FIELDS = ("mgridoff", "mgridcnt")
@@ -138,7 +141,8 @@ _REF = None
 _FUNCS = ["orc_get_particle_index", "orc_get_grid_list", "orc_rearrange_data",
           "orc_compute_boundary_volume", "orc_compute_pressure", "orc_compute_force",
           "orc_surface_tension", "orc_advance", "orc_compute_drift_vel", "orc_compute_alpha_advance",
-          "orc_compute_correction", "orc_compute_force_projectu", "orc_before_first_step"]
+          "orc_compute_correction", "orc_compute_force_projectu", "orc_before_first_step",
+          "orc_iisph_density", "orc_iisph_predict", "orc_iisph_iteration", "orc_iisph_integrate"]
 
 
 def lib():
@@ -152,6 +156,7 @@ def lib():
                 fn.argtypes = [C.POINTER(abi.Params), C.POINTER(S)]
             fn = getattr(L, "orc_step" + sfx)
             fn.argtypes = [C.POINTER(abi.Params), C.POINTER(S), C.c_int, C.c_int]
+            getattr(L, "orc_iisph_iteration" + sfx).restype = C.c_double
         L.orc_params_default.argtypes = [C.POINTER(abi.Params)]
         L.orc_params_default.restype = None
         f3 = C.POINTER(C.c_float)
@@ -178,8 +183,10 @@ def ref_lib():
         for f in ["ref_get_particle_index", "ref_get_grid_list", "ref_rearrange_data",
                   "ref_compute_boundary_volume", "ref_compute_pressure", "ref_compute_force",
                   "ref_surface_tension", "ref_advance", "ref_compute_drift_vel",
-                  "ref_compute_alpha_advance", "ref_compute_correction", "ref_compute_force_projectu"]:
+                  "ref_compute_alpha_advance", "ref_compute_correction", "ref_compute_force_projectu",
+                  "ref_iisph_density", "ref_iisph_predict", "ref_iisph_iteration", "ref_iisph_integrate"]:
             getattr(L, f).argtypes = [C.POINTER(abi.Params), C.POINTER(StateF32)]
+        L.ref_iisph_iteration.restype = C.c_double
         L.ref_set_num_threads.argtypes = [C.c_int]
         _REF = L
     return _REF

@@ -37,6 +37,8 @@ static void ensure(int n, int g) {
     if (n > cap_n) {
         free(fbuf.displayBuffer); free(fbuf.calcBuffer); free(fbuf.msortbuf);
         free(fbuf.mgcell); free(fbuf.mgndx); free(fbuf.midsort); free(fbuf.MFidTable);
+        free(fbuf.dii); free(fbuf.aii); free(fbuf.rho_adv); free(fbuf.press_l); free(fbuf.press_l1);
+        free(fbuf.dijpj); free(fbuf.densityResidue);
         fbuf.displayBuffer = (displayPack*)calloc(n, sizeof(displayPack));
         fbuf.calcBuffer = (calculationPack*)calloc(n, sizeof(calculationPack));
         fbuf.msortbuf = (char*)calloc(n, sizeof(displayPack) + sizeof(calculationPack));
@@ -44,6 +46,13 @@ static void ensure(int n, int g) {
         fbuf.mgndx = (uint*)calloc(n, sizeof(uint));
         fbuf.midsort = (uint*)calloc(n, sizeof(uint));
         fbuf.MFidTable = (int*)calloc(n, sizeof(int));
+        fbuf.dii = (cfloat3*)calloc(n, sizeof(cfloat3));
+        fbuf.aii = (float*)calloc(n, sizeof(float));
+        fbuf.rho_adv = (float*)calloc(n, sizeof(float));
+        fbuf.press_l = (float*)calloc(n, sizeof(float));
+        fbuf.press_l1 = (float*)calloc(n, sizeof(float));
+        fbuf.dijpj = (cfloat3*)calloc(n, sizeof(cfloat3));
+        fbuf.densityResidue = (float*)calloc(n, sizeof(float));
         cap_n = n;
     }
     if (g > cap_g) {
@@ -73,6 +82,13 @@ static void load(const sphmp_params* p, const orc_state_f32* s) {
         c.visc = s->visc[i];
         c.bornid = s->bornid[i];
         c.accel.Set(s->accel[3 * i], s->accel[3 * i + 1], s->accel[3 * i + 2]);
+        fbuf.dii[i].Set(s->dii[3 * i], s->dii[3 * i + 1], s->dii[3 * i + 2]);
+        fbuf.dijpj[i].Set(s->dijpj[3 * i], s->dijpj[3 * i + 1], s->dijpj[3 * i + 2]);
+        fbuf.aii[i] = s->aii[i];
+        fbuf.rho_adv[i] = s->rho_adv[i];
+        fbuf.press_l[i] = s->press_l[i];
+        fbuf.press_l1[i] = s->press_l1[i];
+        fbuf.densityResidue[i] = s->residue[i];
     }
     memcpy(fbuf.mgcell, s->mgcell, sizeof(uint) * s->n);
     memcpy(fbuf.midsort, s->midsort, sizeof(uint) * s->n);
@@ -98,6 +114,14 @@ static void store(const sphmp_params* p, orc_state_f32* s) {
         s->visc[i] = c.visc;
         s->bornid[i] = c.bornid;
         s->accel[3 * i] = c.accel.x; s->accel[3 * i + 1] = c.accel.y; s->accel[3 * i + 2] = c.accel.z;
+        s->dii[3 * i] = fbuf.dii[i].x; s->dii[3 * i + 1] = fbuf.dii[i].y; s->dii[3 * i + 2] = fbuf.dii[i].z;
+        s->dijpj[3 * i] = fbuf.dijpj[i].x; s->dijpj[3 * i + 1] = fbuf.dijpj[i].y;
+        s->dijpj[3 * i + 2] = fbuf.dijpj[i].z;
+        s->aii[i] = fbuf.aii[i];
+        s->rho_adv[i] = fbuf.rho_adv[i];
+        s->press_l[i] = fbuf.press_l[i];
+        s->press_l1[i] = fbuf.press_l1[i];
+        s->residue[i] = fbuf.densityResidue[i];
     }
     memcpy(s->mgcell, fbuf.mgcell, sizeof(uint) * s->n);
     memcpy(s->midsort, fbuf.midsort, sizeof(uint) * s->n);
@@ -187,6 +211,42 @@ void ref_surface_tension(const sphmp_params* p, orc_state_f32* s) {
 void ref_advance(const sphmp_params* p, orc_state_f32* s) {
     load(p, s);
     launch(AdvanceParticles, s->n);
+    store(p, s);
+}
+
+/* ComputeDensityIISPH_CUDA, fluid_system_host.cu:505-508 */
+void ref_iisph_density(const sphmp_params* p, orc_state_f32* s) {
+    load(p, s);
+    launch(ComputeDensityIISPH, s->n);
+    store(p, s);
+}
+
+/* PredictAdvection, fluid_system_host.cu:515-524 */
+void ref_iisph_predict(const sphmp_params* p, orc_state_f32* s) {
+    load(p, s);
+    launch(ComputeDii, s->n);
+    launch(ComputeAii, s->n);
+    store(p, s);
+}
+
+/* One pass of PressureSolve's loop, fluid_system_host.cu:529-540: Pressure_DP,
+   Pressure_Iter, press_l = press_l1, and the mean of densityResidue (thrust::reduce
+   over pnum, divided by pnum). */
+double ref_iisph_iteration(const sphmp_params* p, orc_state_f32* s) {
+    load(p, s);
+    launch(Pressure_DP, s->n);
+    launch(Pressure_Iter, s->n);
+    memcpy(fbuf.press_l, fbuf.press_l1, sizeof(float) * s->n);
+    double sum = 0;
+    for (int i = 0; i < s->n; i++) sum += fbuf.densityResidue[i];
+    store(p, s);
+    return s->n > 0 ? sum / s->n : 0.0;
+}
+
+/* Integration (IntegrateIISPH), fluid_system_host.cu:553-556 */
+void ref_iisph_integrate(const sphmp_params* p, orc_state_f32* s) {
+    load(p, s);
+    launch(IntegrateIISPH, s->n);
     store(p, s);
 }
 

@@ -894,6 +894,270 @@ void FN(orc_compute_force_projectu)(const sphmp_params* p, ST* s) {
 /* ------------------------------------------------------------------------- */
 
 /* FluidSystem::BeforeFirstStep (fluid_system.cpp:62-70): sort, then boundary volumes. */
+/* ------------------------------------------------------------------------- */
+/* IISPH (fluid_system_kern.cu:637-1115, the launches of fluid_system_host.cu:504-557) */
+/* ------------------------------------------------------------------------- */
+
+/* kern (:637-645): the cubic spline of support 2h, kspline = 1/(pi h^3). */
+static inline R FN(iikern)(const sphmp_params* p, const R d[3]) {
+    R q = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) / (R)p->smoothradius;
+    if (q > 2) return (R)0;
+    else if (q > 1) return (R)0.25f * RPOW(2 - q, (R)3.0f) * (R)p->kspline;
+    else return (1 - (R)1.5f * q * q + (R)0.75f * RPOW(q, (R)3.0f)) * (R)p->kspline;
+}
+
+/* nablakern (:647-671): its gradient, r * fac. */
+static inline void FN(iinabla)(const sphmp_params* p, const R d[3], R out[3]) {
+    R rmod = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    R q = rmod / (R)p->smoothradius;
+    R fac = 0;
+    if (q > 2) {
+        out[0] = out[1] = out[2] = 0;
+        return;
+    } else if (q > 1) {
+        fac = (R)0.75f * (2 - q) * (2 - q) * (-1) / (R)p->smoothradius / rmod * (R)p->kspline;
+    } else {
+        fac = (-3 * q + (R)2.25f * q * q) / (R)p->smoothradius / rmod * (R)p->kspline;
+    }
+    out[0] = d[0] * fac;
+    out[1] = d[1] * fac;
+    out[2] = d[2] * fac;
+}
+
+/* the reference's 27-cell loop around particle i's cell (gc + neighborid[c]),
+   skipping empty cells, with the cell's slot range [cfirst, clast) */
+#define II_CELLS(i, ...)                                                    \
+    for (int c = 0; c < p->neighbornum; c++) {                              \
+        uint32_t cell = s->mgcell[i] + (uint32_t)p->neighborid[c];          \
+        if (s->mgridcnt[cell] == 0) continue;                               \
+        int cfirst = s->mgridoff[cell];                                     \
+        int clast = cfirst + s->mgridcnt[cell];                             \
+        __VA_ARGS__                                                         \
+    }
+
+/* ComputeDensityIISPH + contributeIIDensity (:1067-1115): the density itself
+   (not its inverse) over every candidate of the 27 cells, with m_j = mass_j for
+   fluid and restdens_i * V_j for boundary neighbours. */
+void FN(orc_iisph_density)(const sphmp_params* p, ST* s) {
+    const R ss = (R)p->simscale;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == SPHMP_TYPE_BOUNDARY) continue;
+        if (s->mgcell[i] == UNDEF) continue;
+        R sum = (R)0.0;
+        R massj = 0;
+        II_CELLS(i, {
+            for (int j = cfirst; j < clast; j++) {
+                if (s->type[j] == 0) massj = s->mass[j];
+                else if (s->type[j] == 1) massj = s->restdens[i] * s->dens[j];
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                sum += FN(iikern)(p, d) * massj;
+            }
+        })
+        s->dens[i] = sum;
+    }
+}
+
+/* PredictAdvection (:516-524): ComputeDii (:673-799) then ComputeAii (:801-908).
+   ComputeDii: the advection acceleration (boundary artificial viscosity within
+   2h, per cell, plus gravity) gives veleval = vel + a_adv dt; dii = -sum over
+   fluid j within h of nabla W_ij m_j, / rho_i / rho_i * dt * dt.
+   ComputeAii: rho_adv = rho_i + dt sum_j m_j (veleval_i - veleval_j).nabla W_ij,
+   press_l = 0.5 p_i (0.5 a double literal), aii = sum_j m_j (dii - dji).nabla W_ij
+   with dji = nabla W_ij m_i / rho_i / rho_i dt dt. */
+void FN(orc_iisph_predict)(const sphmp_params* p, ST* s) {
+    const R ss = (R)p->simscale;
+    const R h = (R)p->smoothradius;
+    const R h2 = h * h;
+    const R dt = (R)p->dt;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == SPHMP_TYPE_BOUNDARY) continue;
+        if (s->mgcell[i] == UNDEF) continue;
+        R acc[3] = {0, 0, 0};
+        II_CELLS(i, {
+            R accel[3] = {0, 0, 0};
+            for (int j = cfirst; j < clast; j++) {
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                R dist = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (!(dist < 2 * h && dist > 0)) continue;
+                R nw[3];
+                FN(iinabla)(p, d, nw);
+                if (s->type[j] == 1) {
+                    R vij[3];
+                    for (int a = 0; a < 3; a++) vij[a] = s->vel[3 * i + a] - s->vel[3 * j + a];
+                    R pi_ij = d[0] * vij[0] + d[1] * vij[1] + d[2] * vij[2];
+                    if (pi_ij < 0) {
+                        pi_ij = (R)(pi_ij / (dist * dist + h2 * 0.01));
+                        pi_ij = pi_ij * (R)p->bvisc * (R)p->smoothradius / 2 / s->restdens[i];
+                        pi_ij = s->restdens[i] * s->dens[j] * pi_ij;
+                        for (int a = 0; a < 3; a++) accel[a] += nw[a] * pi_ij;
+                    }
+                }
+            }
+            for (int a = 0; a < 3; a++) acc[a] = acc[a] + accel[a];
+        })
+        for (int a = 0; a < 3; a++) acc[a] += (R)p->gravity[a];
+        for (int a = 0; a < 3; a++) s->veleval[3 * i + a] = s->vel[3 * i + a] + acc[a] * dt;
+        R dii[3] = {0, 0, 0};
+        II_CELLS(i, {
+            for (int j = cfirst; j < clast; j++) {
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                R dist = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (!(dist < h && dist > 0)) continue;
+                R nw[3];
+                FN(iinabla)(p, d, nw);
+                if (s->type[j] != SPHMP_TYPE_BOUNDARY)
+                    for (int a = 0; a < 3; a++) dii[a] = dii[a] - nw[a] * s->mass[j];
+            }
+        })
+        for (int a = 0; a < 3; a++) s->dii[3 * i + a] = dii[a] / s->dens[i] / s->dens[i] * dt * dt;
+    }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == SPHMP_TYPE_BOUNDARY) continue;
+        if (s->mgcell[i] == UNDEF) continue;
+        R denschange = 0;
+        II_CELLS(i, {
+            R sum = 0;
+            for (int j = cfirst; j < clast; j++) {
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                R dist = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (!(dist < h && dist > 0)) continue;
+                R vij[3];
+                for (int a = 0; a < 3; a++) vij[a] = s->veleval[3 * i + a] - s->veleval[3 * j + a];
+                R nw[3];
+                FN(iinabla)(p, d, nw);
+                if (s->type[j] != SPHMP_TYPE_BOUNDARY)
+                    sum += (vij[0] * nw[0] + vij[1] * nw[1] + vij[2] * nw[2]) * s->mass[j] * dt;
+            }
+            denschange += sum;
+        })
+        s->rho_adv[i] = s->dens[i] + denschange;
+        s->press_l[i] = (R)(0.5 * (double)s->pressure[i]);
+        R aii = 0;
+        II_CELLS(i, {
+            R sum = 0;
+            for (int j = cfirst; j < clast; j++) {
+                if (s->type[j] == SPHMP_TYPE_BOUNDARY) continue;
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                R dist = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (!(dist < h && dist > 0)) continue;
+                R nw[3];
+                FN(iinabla)(p, d, nw);
+                R dtmp[3];
+                for (int a = 0; a < 3; a++) {
+                    R dji = nw[a] * s->mass[i] / s->dens[i] / s->dens[i] * dt * dt;
+                    dtmp[a] = s->dii[3 * i + a] - dji;
+                }
+                sum += (dtmp[0] * nw[0] + dtmp[1] * nw[1] + dtmp[2] * nw[2]) * s->mass[j];
+            }
+            aii += sum;
+        })
+        s->aii[i] = aii;
+    }
+}
+
+/* One relaxed-Jacobi iteration of PressureSolve (:526-549): Pressure_DP (:910-958)
+   dijpj = -dt dt sum over fluid j within h of nabla W_ij p_j m_j / rho_j / rho_j;
+   Pressure_Iter (:960-1050) with omega 0.1: p_l1 = (1 - omega) p_l + omega / aii
+   (rho0 - rho_adv - sum_j m_j (dijpj_i - djj p_j - (dijpj_j - dji p_i)).nabla W_ij)
+   (p_l1 = p_l where |aii| < 1e-5), the density residue, accel = (dii p_l +
+   dijpj) / dt / dt and pressure = p_l1; then p_l = p_l1 (the device copy).
+   Returns the reference's criterion quantity: the residues summed over all slots
+   (boundary particles 0) divided by the slot count. */
+double FN(orc_iisph_iteration)(const sphmp_params* p, ST* s) {
+    const R ss = (R)p->simscale;
+    const R h = (R)p->smoothradius;
+    const R dt = (R)p->dt;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == SPHMP_TYPE_BOUNDARY) continue;
+        if (s->mgcell[i] == UNDEF) continue;
+        R dp[3] = {0, 0, 0};
+        II_CELLS(i, {
+            for (int j = cfirst; j < clast; j++) {
+                if (s->type[j] == SPHMP_TYPE_BOUNDARY) continue;
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                R dist = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (!(dist < h && dist > 0)) continue;
+                R nw[3];
+                FN(iinabla)(p, d, nw);
+                for (int a = 0; a < 3; a++)
+                    dp[a] = dp[a] + nw[a] * s->press_l[j] * s->mass[j] / s->dens[j] / s->dens[j] * (-1);
+            }
+        })
+        for (int a = 0; a < 3; a++) s->dijpj[3 * i + a] = dp[a] * dt * dt;
+    }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == SPHMP_TYPE_BOUNDARY) {
+            s->residue[i] = 0;
+            continue;
+        }
+        if (s->mgcell[i] == UNDEF) continue;
+        R updateterm = 0;
+        II_CELLS(i, {
+            for (int j = cfirst; j < clast; j++) {
+                R d[3];
+                dist_sq(s, i, j, ss, d);
+                R dist = RSQRT(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                if (!(dist < h && dist > 0)) continue;
+                R nw[3];
+                FN(iinabla)(p, d, nw);
+                if (s->type[j] != SPHMP_TYPE_BOUNDARY) {
+                    R tmp[3];
+                    for (int a = 0; a < 3; a++) {
+                        R dji = nw[a] * s->mass[i] / s->dens[i] / s->dens[i] * dt * dt;
+                        R djkpk = s->dijpj[3 * j + a] - dji * s->press_l[i];
+                        tmp[a] = s->dijpj[3 * i + a] - s->dii[3 * j + a] * s->press_l[j] - djkpk;
+                    }
+                    updateterm += s->mass[j] * (tmp[0] * nw[0] + tmp[1] * nw[1] + tmp[2] * nw[2]);
+                }
+            }
+        })
+        const R omega = (R)0.1f;
+        R aii = s->aii[i];
+        if ((aii < 0 ? -aii : aii) < (R)0.00001f)
+            s->press_l1[i] = s->press_l[i];
+        else
+            s->press_l1[i] = (1 - omega) * s->press_l[i] + omega / aii * (s->restdens[i] - s->rho_adv[i] - updateterm);
+        s->residue[i] = -s->restdens[i] + (s->rho_adv[i] + updateterm + aii * s->press_l[i]);
+        for (int a = 0; a < 3; a++) {
+            R force = s->dii[3 * i + a] * s->press_l[i] + s->dijpj[3 * i + a];
+            s->accel[3 * i + a] = force / dt / dt;
+        }
+        s->pressure[i] = s->press_l1[i];
+    }
+    double sum = 0;
+    for (int i = 0; i < s->n; i++) {
+        s->press_l[i] = s->press_l1[i];
+        sum += (double)s->residue[i];
+    }
+    return s->n > 0 ? sum / s->n : 0.0;
+}
+
+/* IntegrateIISPH (:1052-1065): vel = veleval + accel dt; pos += vel dt / simscale. */
+void FN(orc_iisph_integrate)(const sphmp_params* p, ST* s) {
+    const R dt = (R)p->dt;
+    const R ss = (R)p->simscale;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < s->n; i++) {
+        if (s->type[i] == SPHMP_TYPE_BOUNDARY) continue;
+        if (s->mgcell[i] == UNDEF) continue;
+        for (int a = 0; a < 3; a++) {
+            s->vel[3 * i + a] = s->veleval[3 * i + a] + s->accel[3 * i + a] * dt;
+            s->pos[3 * i + a] += s->vel[3 * i + a] * dt / ss;
+        }
+    }
+}
+
 int FN(orc_before_first_step)(const sphmp_params* p, ST* s) {
     FN(orc_get_particle_index)(p, s);
     FN(orc_get_grid_list)(p, s);

@@ -51,7 +51,14 @@ extern "C" {
     uint32_t* mgndx;    /* [n] */                                                 \
     int32_t* mgridoff;  /* [gridtotal] */                                         \
     int32_t* mgridcnt;  /* [gridtotal] */                                         \
-    R* velxcor;         /* [3n] mf_velxcor (project-U force) */
+    R* velxcor;         /* [3n] mf_velxcor (project-U force) */                   \
+    R* dii;             /* [3n] IISPH d_ii */                                     \
+    R* aii;             /* [n]  IISPH a_ii */                                     \
+    R* rho_adv;         /* [n]  IISPH predicted density */                        \
+    R* press_l;         /* [n]  IISPH pressure iterate */                         \
+    R* press_l1;        /* [n]  IISPH next iterate */                             \
+    R* dijpj;           /* [3n] IISPH sum_j d_ij p_j */                           \
+    R* residue;         /* [n]  IISPH density residue */
 
 typedef struct orc_state_f32 { ORC_STATE_FIELDS(float) } orc_state_f32;
 typedef struct orc_state_f64 { ORC_STATE_FIELDS(double) } orc_state_f64;
@@ -70,7 +77,11 @@ typedef struct orc_state_f64 { ORC_STATE_FIELDS(double) } orc_state_f64;
     void orc_compute_correction##SFX(const sphmp_params* p, ST* s);                  \
     void orc_compute_force_projectu##SFX(const sphmp_params* p, ST* s);              \
     int orc_step##SFX(const sphmp_params* p, ST* s, int schedule, int nsteps);       \
-    int orc_before_first_step##SFX(const sphmp_params* p, ST* s);
+    int orc_before_first_step##SFX(const sphmp_params* p, ST* s);                 \
+    void orc_iisph_density##SFX(const sphmp_params* p, ST* s);                     \
+    void orc_iisph_predict##SFX(const sphmp_params* p, ST* s);                     \
+    double orc_iisph_iteration##SFX(const sphmp_params* p, ST* s);                 \
+    void orc_iisph_integrate##SFX(const sphmp_params* p, ST* s);
 
 ORC_DECLARE(_f32, orc_state_f32)
 ORC_DECLARE(_f64, orc_state_f64)

@@ -7,8 +7,11 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "sphmp.h"
 #include "sphmp_emit.h"
@@ -22,6 +25,7 @@ struct sphmp_ctx {
     sphmp_params prm;
     int cap = 0;         // particle capacity
     int gcap = 0;        // grid cells allocated
+    int corder_res[3] = {0, 0, 0};  // grid the Z-order cell permutation (B.corder) was built for
     int n = 0;           // active slots
     int cur[kNumFloat4Fields] = {0, 0, 0, 0, 0};
     bool alpha_advanced = false;  // alpha4[cur] = advanced fractions, alpha4[cur^1] = start of step
@@ -102,6 +106,17 @@ sphmp_status cuda_fail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, what);          \
     } while (0)
 
+// Z-order (Morton) code of a cell: the bits of gx, gz and gy interleaved, x lowest.
+uint64_t morton_code(uint32_t gx, uint32_t gy, uint32_t gz) {
+    uint64_t m = 0;
+    for (int b = 0; b < 21; b++) {
+        m |= (uint64_t)((gx >> b) & 1u) << (3 * b);
+        m |= (uint64_t)((gz >> b) & 1u) << (3 * b + 1);
+        m |= (uint64_t)((gy >> b) & 1u) << (3 * b + 2);
+    }
+    return m;
+}
+
 sphmp_status validate_params(const sphmp_params* p) {
     if (!p) return fail(SPHMP_ERR_INVALID_ARG, "params is NULL");
     if (p->maxNum <= 0) return fail(SPHMP_ERR_INVALID_ARG, "maxNum must be > 0 (got %d)", p->maxNum);
@@ -120,6 +135,12 @@ sphmp_status validate_params(const sphmp_params* p) {
     if (g != p->gridtotal) return fail(SPHMP_ERR_GRID, "gridtotal %d != product of gridres %lld", p->gridtotal, g);
     if (g > (1ll << 31) - 16) return fail(SPHMP_ERR_GRID, "grid too large (%lld cells)", g);
     if (p->eos != SPHMP_EOS_TAIT && p->eos != SPHMP_EOS_LINEAR) return fail(SPHMP_ERR_INVALID_ARG, "unknown eos %d", p->eos);
+    if (p->cell_order != SPHMP_CELL_ORDER_LINEAR && p->cell_order != SPHMP_CELL_ORDER_MORTON)
+        return fail(SPHMP_ERR_INVALID_ARG, "unknown cell order %d", p->cell_order);
+    if (p->bucket_window != 0 && (p->bucket_window < (int)kBucketWindowMin || p->bucket_window > (int)kBucketWindow))
+        return fail(SPHMP_ERR_INVALID_ARG, "bucket_window must be 0 or 8..32 (got %d)", p->bucket_window);
+    if (p->heavy_list != 0 && (p->heavy_list < 32 || p->heavy_list > kMaxNbr))
+        return fail(SPHMP_ERR_INVALID_ARG, "heavy_list must be 0 or 32..256 (got %d)", p->heavy_list);
     return SPHMP_OK;
 }
 
@@ -147,6 +168,7 @@ DevParams dev_params(const sphmp_ctx* c) {
     P.narrow = c->pos_sorted ? 1 : 0;
     P.dt = p.dt;
     P.kpoly6 = p.kpoly6;
+    P.kspline = p.kspline;
     P.kspikydiff = p.kspikydiff;
     P.bvisc = p.bvisc;
     P.nphase = p.nphase;
@@ -169,6 +191,9 @@ DevParams dev_params(const sphmp_ctx* c) {
     P.st_K = p.surfaceTensionK;
     P.st_C = p.surfaceTensionFluidC;
     for (int k = 0; k < 27; k++) P.neighborid[k] = p.neighborid[k];
+    P.morton = p.cell_order == SPHMP_CELL_ORDER_MORTON;
+    P.bwin = p.bucket_window > 0 ? p.bucket_window : (int)kBucketWindow;
+    P.heavy = p.heavy_list > 0 ? (uint32_t)p.heavy_list : kHeavyList;
     return P;
 }
 
@@ -184,8 +209,8 @@ void free_buffers(sphmp_ctx* c) {
     for (int f = 0; f < kNumFloat4Fields; f++)
         for (int b = 0; b < 2; b++) cudaFree(B.f4[f][b]);
     void* ptrs[] = {B.densp, B.accel4, B.drift4, B.velxcor, B.pmod, B.mgcell, B.midsort, B.mgndx, B.mgridoff, B.mgridcnt,
-                    B.key, B.octk, B.arank, B.sidx, B.ccount, B.cstart, B.bsum, B.uchunk, B.big, B.color, B.bornid,
-                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.wq, B.wq_n, B.hq, B.hq_n, B.hctr, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
+                    B.key, B.octk, B.arank, B.sidx, B.ccount, B.cstart, B.cend, B.corder, B.bsum, B.uchunk, B.big, B.color, B.bornid,
+                    B.mass_raw, B.err, B.red, B.vtmp, B.nbr, B.nbr_cnt, B.nmask, B.btab, B.dctr, B.wq, B.wq_n, B.hq, B.hq_n, B.hctr, B.iis_dii, B.iis_dijpj, B.iis_aii, B.iis_rho_adv, B.iis_pl, B.iis_pl1, B.iis_res, B.nrec, B.opos, B.oidx, B.osrc, B.oct_start,
                     B.act, B.act_n, B.nact, B.frame, c->stage};
     for (void* q : ptrs) cudaFree(q);
     memset(&c->B, 0, sizeof(c->B));
@@ -219,6 +244,8 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.sidx, N));
     CK(dalloc(&B.ccount, G + 1));
     CK(dalloc(&B.cstart, G + 2));
+    CK(dalloc(&B.cend, G));
+    CK(dalloc(&B.corder, G));
     const size_t per = (size_t)kScanBlock * kScanItems;
     CK(dalloc(&B.bsum, (G + per - 1) / per + 1));
     CK(dalloc(&B.uchunk, N / kHashBlock + 2));
@@ -234,13 +261,24 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(dalloc(&B.nmask, (size_t)kMaskWords * N));
     CK(dalloc(&B.btab, 8 * G * kTabStride));
     CK(dalloc(&B.dctr, 1));
-    CK(dalloc(&B.wq, N / kBucketWindow + 16));
+    CK(dalloc(&B.wq, N / kBucketWindowMin + 16));
     CK(dalloc(&B.wq_n, 1));
     CK(cudaMemset(B.wq_n, 0, sizeof(uint32_t)));
     CK(dalloc(&B.hq, N));
     CK(dalloc(&B.hq_n, 1));
     CK(dalloc(&B.hctr, 2));
     CK(cudaMemset(B.hq_n, 0, sizeof(uint32_t)));
+    CK(dalloc(&B.iis_dii, N));
+    CK(dalloc(&B.iis_dijpj, N));
+    CK(dalloc(&B.iis_aii, N));
+    CK(dalloc(&B.iis_rho_adv, N));
+    CK(dalloc(&B.iis_pl, N));
+    CK(dalloc(&B.iis_pl1, N));
+    CK(dalloc(&B.iis_res, N));
+    CK(cudaMemset(B.iis_dii, 0, sizeof(float4) * N));
+    CK(cudaMemset(B.iis_dijpj, 0, sizeof(float4) * N));
+    CK(cudaMemset(B.iis_pl, 0, sizeof(float) * N));
+    CK(cudaMemset(B.iis_res, 0, sizeof(float) * N));
     CK(dalloc(&B.nrec, (size_t)kNrecFloat4 * N));
     CK(dalloc(&B.opos, N));
     CK(dalloc(&B.oidx, N));
@@ -506,6 +544,28 @@ const char* sphmp_last_error(void) { return g_err.c_str(); }
 
 const char* sphmp_version(void) { return "sphmp 0.1 sm_103a"; }
 
+// The cells in Z-order for the Morton cell order (uploaded once per grid shape).
+sphmp_status ensure_cell_order(sphmp_ctx* c) {
+    const sphmp_params& p = c->prm;
+    if (p.cell_order != SPHMP_CELL_ORDER_MORTON) return SPHMP_OK;
+    if (memcmp(c->corder_res, p.gridres, sizeof(c->corder_res)) == 0) return SPHMP_OK;
+    const uint32_t rx = (uint32_t)p.gridres[0], ry = (uint32_t)p.gridres[1], rz = (uint32_t)p.gridres[2];
+    std::vector<std::pair<uint64_t, uint32_t>> key((size_t)p.gridtotal);
+    for (uint32_t y = 0; y < ry; y++)
+        for (uint32_t z = 0; z < rz; z++)
+            for (uint32_t x = 0; x < rx; x++) {
+                const uint32_t cell = (y * rz + z) * rx + x;
+                key[cell] = {morton_code(x, y, z), cell};
+            }
+    std::sort(key.begin(), key.end());
+    std::vector<uint32_t> order(key.size());
+    for (size_t i = 0; i < key.size(); i++) order[i] = key[i].second;
+    CK(cudaMemcpyAsync(c->B.corder, order.data(), sizeof(uint32_t) * order.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    memcpy(c->corder_res, p.gridres, sizeof(c->corder_res));
+    return SPHMP_OK;
+}
+
 sphmp_status sphmp_create(const sphmp_params* p, sphmp_ctx** out) {
     if (!out) return fail(SPHMP_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
@@ -536,6 +596,11 @@ sphmp_status sphmp_create(const sphmp_params* p, sphmp_ctx** out) {
         return st;
     }
     launch_set_count(c->B, c->n, c->stream);
+    st = ensure_cell_order(c);
+    if (st) {
+        sphmp_destroy(c);
+        return st;
+    }
     *out = c;
     return SPHMP_OK;
 }
@@ -572,11 +637,13 @@ sphmp_status sphmp_set_params(sphmp_ctx* c, const sphmp_params* p) {
                               memcmp(p->gridIdfac, c->prm.gridIdfac, sizeof(p->gridIdfac)) != 0;
     // neighbour lists and the octant buckets hold for the radius they were built with
     const bool radius_changed = p->smoothradius != c->prm.smoothradius || p->simscale != c->prm.simscale;
+    const bool order_changed = p->cell_order != c->prm.cell_order;
     c->prm = *p;
     c->prm.maxNum = c->cap;
     c->prm.num = c->n;
-    if (grid_changed) c->grid_valid = false;
-    if (grid_changed || radius_changed) {
+    if (sphmp_status st = ensure_cell_order(c)) return st;
+    if (grid_changed || order_changed) c->grid_valid = false;
+    if (grid_changed || radius_changed || order_changed) {
         c->nbr_valid = false;
         c->oct_valid = false;
     }
@@ -827,6 +894,8 @@ sphmp_status sphmp_upload_field(sphmp_ctx* c, int32_t field, const void* host, i
         return fail(SPHMP_ERR_INVALID_ARG, "field %d is download-only (upload it with sphmp_upload_aos)", field);
     size_t count = 0;
     if (void* arr = sort_array(c, field, &count)) {
+        if (c->prm.cell_order != SPHMP_CELL_ORDER_LINEAR)
+            return fail(SPHMP_ERR_STATE, "sort arrays can be uploaded only in the linear cell order");
         if (n < 0 || (size_t)n > count) return fail(SPHMP_ERR_CAPACITY, "n %d exceeds %zu entries", n, count);
         if (sphmp_status st = check_sort_upload(c, field, host, n)) return st;
         CK(cudaMemcpyAsync(arr, host, sizeof(uint32_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
@@ -1022,6 +1091,171 @@ sphmp_status sphmp_advance(sphmp_ctx* c) {
     c->nbr_valid = false;
     c->oct_valid = false;
     c->pos_sorted = false;
+    return SPHMP_OK;
+}
+
+// ---- launch-shape autotuner ----
+
+static sphmp_status clone_state(sphmp_ctx* dst, sphmp_ctx* src);
+
+sphmp_status sphmp_autotune(sphmp_ctx* c, int32_t trial_steps, int32_t allow_reorder, sphmp_tuning* out) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!out || trial_steps < 1) return fail(SPHMP_ERR_INVALID_ARG, "need an output and trial_steps >= 1");
+    if (c->emit_on) return fail(SPHMP_ERR_STATE, "autotune a context without a device emitter");
+    if (sphmp_status st = refresh_n(c)) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    sphmp_params base = c->prm;
+    base.num = c->n;
+    base.maxNum = c->cap;
+    base.gridtotal = c->prm.gridtotal;
+    sphmp_ctx* t = nullptr;
+    if (sphmp_status st = sphmp_create(&base, &t)) return st;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    sphmp_status st = SPHMP_OK;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        st = fail(SPHMP_ERR_CUDA, "cudaEventCreate failed");
+    struct Cand {
+        int order, window, heavy;
+    };
+    std::vector<Cand> cands;
+    const int orders[2] = {SPHMP_CELL_ORDER_LINEAR, SPHMP_CELL_ORDER_MORTON};
+    for (int o = 0; o < (allow_reorder ? 2 : 1); o++)
+        for (int w : {16, 32})
+            for (int h : {64, 128, 256}) cands.push_back({orders[o], w, h});
+    // the context's own configuration first: its time is ms_before
+    const Cand cur = {c->prm.cell_order, c->prm.bucket_window ? c->prm.bucket_window : (int)kBucketWindow,
+                      c->prm.heavy_list ? c->prm.heavy_list : (int)kHeavyList};
+    cands.insert(cands.begin(), cur);
+    float best = 0.f;
+    Cand pick = cur;
+    int trials = 0;
+    for (size_t k = 0; k < cands.size() && st == SPHMP_OK; k++) {
+        sphmp_params q = base;
+        q.cell_order = cands[k].order;
+        q.bucket_window = cands[k].window;
+        q.heavy_list = cands[k].heavy;
+        if ((st = sphmp_set_params(t, &q))) break;
+        if ((st = clone_state(t, c))) break;
+        if ((st = sphmp_step(t, 1, SPHMP_SCHEDULE_FUSED, 1))) break;  // captures the graph
+        if ((st = clone_state(t, c))) break;
+        if ((st = sphmp_step(t, 1, SPHMP_SCHEDULE_FUSED, 1))) break;  // a warm replay from the same state
+        if ((st = clone_state(t, c))) break;
+        cudaEventRecord(e0, t->stream);
+        if ((st = sphmp_step(t, trial_steps, SPHMP_SCHEDULE_FUSED, 1))) break;
+        cudaEventRecord(e1, t->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            st = fail(SPHMP_ERR_CUDA, "autotune timing failed");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)trial_steps;
+        trials++;
+        if (k == 0) out->ms_before = ms;
+        if (k == 0 || ms < best) {
+            best = ms;
+            pick = cands[k];
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    sphmp_destroy(t);
+    if (st) return st;
+    sphmp_params chosen = c->prm;
+    chosen.cell_order = pick.order;
+    chosen.bucket_window = pick.window;
+    chosen.heavy_list = pick.heavy;
+    if (sphmp_status s2 = sphmp_set_params(c, &chosen)) return s2;
+    out->cell_order = pick.order;
+    out->bucket_window = pick.window;
+    out->heavy_list = pick.heavy;
+    out->trials = trials;
+    out->ms_per_step = best;
+    return SPHMP_OK;
+}
+
+// ---- IISPH (fluid_system_host.cu:504-557, kernels in sphmp_iisph.cu) ----
+
+sphmp_status sphmp_iisph_density(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    launch_iisph_density(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("ComputeDensityIISPH");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_iisph_predict_advection(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    launch_iisph_predict(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("PredictAdvection");
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_iisph_pressure_iteration(sphmp_ctx* c, double* residue) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    if (sphmp_status st = refresh_n(c)) return st;
+    launch_iisph_iteration(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("Pressure_DP / Pressure_Iter");
+    double red[3];
+    CK(cudaMemcpyAsync(red, c->B.red + 8, sizeof(red), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (residue) {
+        residue[0] = c->n > 0 ? red[0] / c->n : 0.0;      // the reference's quantity: sum / pnum
+        residue[1] = red[2] > 0 ? red[1] / red[2] : 0.0;  // mean |residue| over in-grid fluid particles
+    }
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_iisph_pressure_solve(sphmp_ctx* c, float tol, int32_t min_iter, int32_t max_iter,
+                                        int32_t* iters, double* residue) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (!(tol >= 0.f) || min_iter < 0 || max_iter < 1 || min_iter > max_iter)
+        return fail(SPHMP_ERR_INVALID_ARG, "need tol >= 0 and 0 <= min_iter <= max_iter, max_iter >= 1");
+    double r[2] = {0.0, 0.0};
+    int it = 0;
+    while (it < max_iter) {
+        if (sphmp_status st = sphmp_iisph_pressure_iteration(c, r)) return st;
+        it++;
+        if (it >= min_iter && r[1] <= (double)tol) break;
+    }
+    if (iters) *iters = it;
+    if (residue) {
+        residue[0] = r[0];
+        residue[1] = r[1];
+    }
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_iisph_integrate(sphmp_ctx* c) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (sphmp_status st = need_grid(c)) return st;
+    launch_iisph_integrate(dev_params(c), c->B, c->cur, c->stream);
+    CHECK_LAUNCH("IntegrateIISPH");
+    c->nbr_valid = false;
+    c->oct_valid = false;
+    c->pos_sorted = false;
+    return SPHMP_OK;
+}
+
+sphmp_status sphmp_step_iisph(sphmp_ctx* c, int32_t nsteps, float tol, int32_t max_iter, int32_t* iters,
+                              double* residue) {
+    if (sphmp_status st = need_ctx(c)) return st;
+    if (nsteps < 0) return fail(SPHMP_ERR_INVALID_ARG, "nsteps < 0");
+    for (int k = 0; k < nsteps; k++) {
+        // RunIISPH (fluid_system.cpp:567-588) with its Integration call, which the reference comments out
+        if (sphmp_status st = sphmp_get_particle_index(c)) return st;
+        if (sphmp_status st = sphmp_get_grid_list(c)) return st;
+        if (sphmp_status st = sphmp_rearrange_data(c)) return st;
+        if (sphmp_status st = sphmp_iisph_density(c)) return st;
+        if (sphmp_status st = sphmp_iisph_predict_advection(c)) return st;
+        int32_t it = 0;
+        if (sphmp_status st = sphmp_iisph_pressure_solve(c, tol, 2, max_iter, &it, residue)) return st;
+        if (iters) iters[k] = it;
+        if (sphmp_status st = sphmp_iisph_integrate(c)) return st;
+    }
+    CK(cudaStreamSynchronize(c->stream));
     return SPHMP_OK;
 }
 
@@ -1247,6 +1481,7 @@ static sphmp_status clone_state(sphmp_ctx* dst, sphmp_ctx* src) {
     CK(cp(b.octk, a.octk, sizeof(uint8_t) * N));
     CK(cp(b.ccount, a.ccount, sizeof(uint32_t) * (G + 1)));
     CK(cp(b.cstart, a.cstart, sizeof(uint32_t) * (G + 2)));
+    CK(cp(b.cend, a.cend, sizeof(uint32_t) * G));
     CK(cp(b.opos, a.opos, sizeof(uint32_t) * N));
     CK(cp(b.oidx, a.oidx, sizeof(uint32_t) * N));
     CK(cp(b.osrc, a.osrc, sizeof(uint32_t) * N));
@@ -1382,6 +1617,15 @@ static void legacy_run(const char* call, sphmp_status (*fn)(sphmp_ctx*)) {
     legacy_report(call, st);
 }
 
+// PressureSolve's stopping rule for the reference-named call (the reference's own
+// loop has its break commented out and never returns): mean |density residue|
+// over in-grid fluid particles at most 0.1 kg/m^3 after at least 2 iterations,
+// the residue threshold and minimum of the reference's commented criterion
+// (fluid_system_host.cu:543-546), and at most 100 iterations.
+static sphmp_status legacy_pressure_solve(sphmp_ctx* c) {
+    return sphmp_iisph_pressure_solve(c, 0.1f, 2, 100, nullptr, nullptr);
+}
+
 sphmp_ctx* sphmp_legacy_context(void) { return g_legacy; }
 
 void cudaInit(int, char**) {
@@ -1439,6 +1683,10 @@ void MfComputeForceCUDA(void) { legacy_run("MfComputeForceCUDA", sphmp_compute_f
 void ComputeForceCUDA_ProjectU(void) { legacy_run("MfComputeForceCUDA", sphmp_compute_force_projectu); }
 void MfAdvanceCUDA(void) { legacy_run("MfAdvanceCUDA", sphmp_advance); }
 void ComputeBoundaryDensity(void) { legacy_run("ComputeBoundaryDensity", sphmp_compute_boundary_density); }
+void ComputeDensityIISPH_CUDA(void) { legacy_run("ComputeDensityIISPH_CUDA", sphmp_iisph_density); }
+void PredictAdvection(void) { legacy_run("PredictAdvection", sphmp_iisph_predict_advection); }
+void PressureSolve(void) { legacy_run("PressureSolve", legacy_pressure_solve); }
+void Integration(void) { legacy_run("Integration", sphmp_iisph_integrate); }
 
 void computeNumBlocks(int numPnts, int maxThreads, int* numBlocks, int* numThreads) {
     int t = numPnts < maxThreads ? numPnts : maxThreads;

@@ -82,11 +82,13 @@ __device__ __forceinline__ void cell_coords(const DevParams& P, uint32_t cell, i
 // (R = h in cell units plus a margin), which hold every particle within h of
 // it; after the particles have moved (a pass called without a new sort) the
 // whole block is scanned, as the reference does. The stored cell lies in the
-// grid's interior, so every cell visited exists. Cells along x are adjacent in
-// the sorted order, so each (y, z) row of cells is one contiguous slot range.
+// grid's interior, so every cell visited exists. In the linear cell order the
+// cells along x are adjacent in the sorted arrays, so each (y, z) row of cells
+// is one contiguous slot range; in the Morton order each cell is its own range.
 template <class F>
-__device__ __forceinline__ void for_candidate_rows(const DevParams& P, const uint32_t* __restrict__ cstart,
-                                                   uint32_t cell, float x, float y, float z, F&& f) {
+__device__ __forceinline__ void for_candidate_rows(const DevParams& P, const DevBuffers& B, uint32_t cell, float x,
+                                                   float y, float z, F&& f) {
+    const uint32_t* __restrict__ cstart = B.cstart;
     const float t[3] = {grid_t(x, P.gmin[0], P.fac[0]), grid_t(y, P.gmin[1], P.fac[1]),
                         grid_t(z, P.gmin[2], P.fac[2])};
     int g[3];
@@ -104,16 +106,20 @@ __device__ __forceinline__ void for_candidate_rows(const DevParams& P, const uin
     for (int yy = lo[1]; yy <= hi[1]; yy++) {
         for (int zz = lo[2]; zz <= hi[2]; zz++) {
             const int base = (yy * P.rz + zz) * P.rx;
-            f(__ldg(&cstart[base + lo[0]]), __ldg(&cstart[base + hi[0] + 1]));
+            if (P.morton) {
+                for (int xx = lo[0]; xx <= hi[0]; xx++) f(__ldg(&cstart[base + xx]), __ldg(&B.cend[base + xx]));
+            } else {
+                f(__ldg(&cstart[base + lo[0]]), __ldg(&cstart[base + hi[0] + 1]));
+            }
         }
     }
 }
 
 // The candidates one by one (see for_candidate_rows: each row is the slot range [j0, j1)).
 template <class F>
-__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ cstart,
-                                               uint32_t cell, float x, float y, float z, F&& f) {
-    for_candidate_rows(P, cstart, cell, x, y, z, [&](uint32_t j0, uint32_t j1) {
+__device__ __forceinline__ void for_candidates(const DevParams& P, const DevBuffers& B, uint32_t cell, float x,
+                                               float y, float z, F&& f) {
+    for_candidate_rows(P, B, cell, x, y, z, [&](uint32_t j0, uint32_t j1) {
         for (uint32_t j = j0; j < j1; j++) f(j);
     });
 }
@@ -176,7 +182,7 @@ __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffe
             return;
         }
     }
-    for_candidates(P, B.cstart, B.mgcell[s], x, y, z, f);
+    for_candidates(P, B, B.mgcell[s], x, y, z, f);
 }
 
 __device__ __forceinline__ float warp_sum_f(float v) {
@@ -226,7 +232,7 @@ __device__ __forceinline__ void warp_for_slot_list(const DevParams& P, const Dev
             return;
         }
     }
-    for_candidate_rows(P, B.cstart, B.mgcell[s], x, y, z, [&](uint32_t j0, uint32_t j1) {
+    for_candidate_rows(P, B, B.mgcell[s], x, y, z, [&](uint32_t j0, uint32_t j1) {
         for (uint32_t j = j0 + lane; j < j1; j += 32) f(j);
     });
 }

@@ -46,14 +46,15 @@ constexpr int kNrecFloat4 = 5;        // float4 per neighbour record of the alph
 // h-subcells around it as 18 index ranges), one word per 32 candidates.
 constexpr int kMaskWords = 64;        // mask words per particle (more candidates: the passes rescan)
 constexpr int kTabStride = 40;        // per bucket: [0..18] range ends in the sequence, [20..37] index - sequence
-constexpr uint32_t kBucketWindow = 32;  // members of a bucket taken by one warp of the density pass
+constexpr uint32_t kBucketWindow = 32;  // largest member window of one density work item (one member per lane)
+constexpr uint32_t kBucketWindowMin = 8;
 constexpr uint32_t kMaskList = 0x80000000u;  // nbr_cnt flag: bucket mask list, low bits = bucket (cell * 8 + octant)
 constexpr uint32_t kRescan = 0x7fffffffu;    // nbr_cnt value: no list, search the cells
 // Heavy particles (long lists, overflowed lists, cell searches) are queued in hq by
 // the list expansion and taken by whole warps in the force and alpha passes; an
 // index list of a heavy particle carries this flag over its length.
 constexpr uint32_t kHeavyFlag = 0x40000000u;
-constexpr uint32_t kHeavyList = 128;         // index lists longer than this are heavy
+constexpr uint32_t kHeavyList = 128;         // default: index lists longer than this are heavy
 
 // Error bits accumulated in the device error word (1 << sphmp_status).
 constexpr uint32_t kErrCellOverflow = 1u << SPHMP_ERR_CELL_OVERFLOW;
@@ -80,6 +81,7 @@ struct DevParams {
                      // search may skip the cells beyond h of the current position)
     float dt;
     float kpoly6, kspikydiff;
+    float kspline;   // 1 / (pi h^3), the cubic spline of the IISPH step
     float bvisc;
     float grav[3];
     int nphase;
@@ -92,6 +94,9 @@ struct DevParams {
     int st_on;
     float st_K, st_C;
     int neighborid[27];
+    int morton;      // 1: cells in Z-order in the sorted arrays (corder), 0: the reference's linear order
+    int bwin;        // members per work item of the bucket density pass (8..32)
+    uint32_t heavy;  // index lists longer than this are heavy (queued in hq)
 };
 
 struct DevBuffers {
@@ -111,7 +116,10 @@ struct DevBuffers {
     uint32_t* arank;    // [cap] rank inside the bin (atomic order; exact for out-of-grid)
     uint32_t* sidx;     // [cap] scatter target (pre-sort slots grouped by cell)
     uint32_t* ccount;   // [G + 1] histogram, bin G = out-of-grid
-    uint32_t* cstart;   // [G + 2] exclusive scan of ccount; cstart[G] = in-grid count, cstart[G+1] = n
+    uint32_t* cstart;   // [G + 2] exclusive scan of ccount in the cell order; cstart[G] = in-grid count,
+                        // cstart[G+1] = n
+    uint32_t* cend;     // [G] end of each cell's range (cstart[c + 1] in the linear order only)
+    uint32_t* corder;   // [G] cells in Z-order (the scan order of the Morton mode)
     uint32_t* bsum;     // [nblocks] scan block sums
     uint32_t* uchunk;   // [cap / kHashBlock + 1] out-of-grid count per hash chunk, scanned in place
     uint32_t* big;      // [cap / (kWarpSortMax+1) + 2]: big[0] = count, then big cell ids
@@ -126,12 +134,21 @@ struct DevBuffers {
     uint32_t* nmask;    // [kMaskWords * cap] bucket mask lists, column-major: word k of particle s at k * cap + s
     uint32_t* btab;     // [8 * G * kTabStride] candidate ranges of each bucket with a mask list
     uint32_t* dctr;     // [1] work counter of the bucket density kernel
-    uint2* wq;          // [cap / kBucketWindow + 16] member windows after the first of large buckets:
+    uint2* wq;          // [cap / kBucketWindowMin + 16] member windows after the first of large buckets:
                         // x = bucket (cell * 8 + octant), y = first member (internal index)
     uint32_t* wq_n;     // [1] entries in wq (cleared by the scan, filled by the cell sort)
     uint32_t* hq;       // [cap] heavy particles (internal index), filled by the list expansion
     uint32_t* hq_n;     // [1] entries in hq (cleared by the scan)
     uint32_t* hctr;     // [2] work counters over hq of the force and the alpha pass
+    // IISPH step (sphmp_iisph.cu): d_ii, sum_j d_ij p_j (float4, w unused), a_ii, the
+    // predicted density, the pressure iterates p_l and p_l+1, the density residue
+    float4* iis_dii;
+    float4* iis_dijpj;
+    float* iis_aii;
+    float* iis_rho_adv;
+    float* iis_pl;
+    float* iis_pl1;
+    float* iis_res;
     float4* nrec;       // [kNrecFloat4 * cap] neighbour records of the alpha pass (written by force + drift)
     // Internal order: inside every 2h cell, members grouped by the h-subcell
     // (octant) they occupy, octant index (oy * 2 + oz) * 2 + ox.
@@ -207,6 +224,13 @@ void launch_advance(const DevParams& P, const DevBuffers& B, const int* cur, cud
 // fused alpha + correction + advance: reads cur, writes cur^1 for all five float4 fields
 void launch_pass_c(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 void launch_conservation(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+// IISPH step (sphmp_iisph.cu): density (densp.x = rho), PredictAdvection (veleval,
+// d_ii, rho_adv, p_l = p / 2, a_ii), one pressure iteration (dijpj, p_l1, residue,
+// accel, pressure, then p_l = p_l1; FP64 residue sums in red[8..10]), integration
+void launch_iisph_density(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_iisph_predict(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_iisph_iteration(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
+void launch_iisph_integrate(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s);
 // set the device counter of active slots
 void launch_set_count(const DevBuffers& B, int n, cudaStream_t s);
 // device-side emission into the current buffers (one block)

@@ -123,12 +123,23 @@ __device__ __forceinline__ void load4(const uint32_t* in, int len, int idx, uint
     }
 }
 
+// Counts of the cells at scan positions idx .. idx + 3: cell = position in the
+// linear order, corder[position] in the Morton order.
+__device__ __forceinline__ void load4_cells(const DevParams& P, const DevBuffers& B, int idx, uint32_t v[4]) {
+    if (!P.morton) {
+        load4(B.ccount, P.G, idx, v);
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = idx + k < P.G ? B.ccount[B.corder[idx + k]] : 0u;
+}
+
 // Phase A: block sums of the cell histogram.
 __global__ void __launch_bounds__(kScanBlock) k_scan_reduce(const __grid_constant__ DevParams P,
                                                             const __grid_constant__ DevBuffers B) {
     const int idx = (blockIdx.x * kScanBlock + threadIdx.x) * kScanItems;
     uint32_t v[4];
-    load4(B.ccount, P.G, idx, v);
+    load4_cells(P, B, idx, v);
     uint32_t total;
     block_excl_scan(v[0] + v[1] + v[2] + v[3], &total);
     if (threadIdx.x == 0) B.bsum[blockIdx.x] = total;
@@ -173,14 +184,15 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_apply(const __grid_constant
                                                            const __grid_constant__ DevBuffers B) {
     const int idx = (blockIdx.x * kScanBlock + threadIdx.x) * kScanItems;
     uint32_t v[4];
-    load4(B.ccount, P.G, idx, v);
+    load4_cells(P, B, idx, v);
     uint32_t total;
     uint32_t run = B.bsum[blockIdx.x] + block_excl_scan(v[0] + v[1] + v[2] + v[3], &total);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        const int c = idx + k;
-        if (c < P.G) {
+        if (idx + k < P.G) {
+            const int c = P.morton ? (int)B.corder[idx + k] : idx + k;
             B.cstart[c] = run;
+            B.cend[c] = run + v[k];
             B.mgridoff[c] = v[k] ? (int32_t)run : 0;
             B.mgridcnt[c] = (int32_t)v[k];
             if (v[k]) B.act[atomicAdd(B.act_n, 1u)] = (uint32_t)c;
@@ -278,12 +290,14 @@ __device__ __forceinline__ void emit_octant(const DevBuffers& B, uint32_t c, uin
 }
 
 // Queue the member windows after the first of bucket (c, b) = members [m0, m1)
-// for the density pass (one warp per window of kBucketWindow members).
-__device__ __forceinline__ void push_windows(const DevBuffers& B, uint32_t c, uint32_t b, uint32_t m0, uint32_t m1) {
-    if (m1 <= m0 + kBucketWindow) return;
-    const uint32_t nw = (m1 - m0 - 1) / kBucketWindow;  // <= (m1 - m0) / kBucketWindow: wq never overflows
+// for the density pass (one warp per window of P.bwin members).
+__device__ __forceinline__ void push_windows(const DevParams& P, const DevBuffers& B, uint32_t c, uint32_t b,
+                                             uint32_t m0, uint32_t m1) {
+    const uint32_t W = (uint32_t)P.bwin;
+    if (m1 <= m0 + W) return;
+    const uint32_t nw = (m1 - m0 - 1) / W;  // <= (m1 - m0) / kBucketWindowMin: wq never overflows
     const uint32_t base = atomicAdd(B.wq_n, nw);
-    for (uint32_t i = 0; i < nw; i++) B.wq[base + i] = make_uint2(c * 8u + b, m0 + (i + 1) * kBucketWindow);
+    for (uint32_t i = 0; i < nw; i++) B.wq[base + i] = make_uint2(c * 8u + b, m0 + (i + 1) * W);
 }
 
 template <int E>
@@ -327,10 +341,10 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
         }
     }
     __syncwarp();  // the bucket starts written above are visible to the whole warp
-    if (lane < 8 && cnt > kBucketWindow) {
+    if (lane < 8 && cnt > (uint32_t)P.bwin) {
         const uint32_t b0 = B.oct_start[(size_t)c * 8 + lane];
         const uint32_t b1 = lane == 7 ? start + cnt : B.oct_start[(size_t)c * 8 + lane + 1];
-        push_windows(B, c, lane, b0, b1);
+        push_windows(P, B, c, lane, b0, b1);
     }
     __syncwarp();
 }
@@ -346,7 +360,7 @@ __global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ 
     for (uint32_t a = (blockIdx.x * kThreads + threadIdx.x) >> 5; a < nact; a += (uint32_t)nwarps) {
         const uint32_t c = B.act[a];
         const uint32_t start = B.cstart[c];
-        const uint32_t cnt = B.cstart[c + 1] - start;
+        const uint32_t cnt = B.cend[c] - start;
         if (cnt == 0 || cnt > (uint32_t)kWarpSortMax) continue;
         if (cnt <= 32) warp_sort_cell<1>(P, B, pos_in, wsm, c, start, cnt);
         else if (cnt <= 64) warp_sort_cell<2>(P, B, pos_in, wsm, c, start, cnt);
@@ -380,7 +394,7 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
     for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
         const uint32_t c = B.big[1 + b];
         const uint32_t start = B.cstart[c];
-        const uint32_t cnt = B.cstart[c + 1] - start;
+        const uint32_t cnt = B.cend[c] - start;
         uint32_t M = 1;
         while (M < cnt) M <<= 1;
         for (uint32_t k = threadIdx.x; k < M; k += blockDim.x) sm[k] = k < cnt ? B.sidx[start + k] : 0xFFFFFFFFu;
@@ -407,7 +421,7 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
         if (threadIdx.x < 8) {
             const uint32_t b0 = B.oct_start[(size_t)c * 8 + threadIdx.x];
             const uint32_t b1 = threadIdx.x == 7 ? start + cnt : B.oct_start[(size_t)c * 8 + threadIdx.x + 1];
-            push_windows(B, c, threadIdx.x, b0, b1);
+            push_windows(P, B, c, threadIdx.x, b0, b1);
         }
         __syncthreads();
     }
@@ -422,24 +436,20 @@ __global__ void __launch_bounds__(1024) k_big_cell_sort(const __grid_constant__ 
 // (the reference gathers every slot: its `int cell != GRID_UNDEF` test at
 // fluid_system_kern.cu:104-108 compares against a 64-bit literal on LP64 hosts
 // and is always true there; out-of-grid particles are parked at (-1000)^3 by the
-// advance). The slot -> index map is updated last.
+// advance), and the slot -> index map follows (no kernel reads opos between the
+// cell order, which reads the old map, and this one).
 __global__ void __launch_bounds__(kThreads) k_rearrange(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
                                                         const __grid_constant__ F4Set S) {
     const int o = blockIdx.x * kThreads + threadIdx.x;
-    if (o >= active_n(B)) return;
+    const int n = active_n(B);
+    if (o >= n) return;
     uint32_t src = B.osrc[o];
-    if (src >= (uint32_t)active_n(B)) src = o;  // only after a cell-overflow error (flagged by the scan)
+    if (src >= (uint32_t)n) src = o;  // only after a cell-overflow error (flagged by the scan)
 #pragma unroll
     for (int f = 0; f < kNumFloat4Fields; f++) S.out[f][o] = S.in[f][src];
-}
-
-__global__ void __launch_bounds__(kThreads) k_update_opos(const __grid_constant__ DevParams P,
-                                                          const __grid_constant__ DevBuffers B) {
-    const int o = blockIdx.x * kThreads + threadIdx.x;
-    if (o >= active_n(B)) return;
     const uint32_t slot = B.oidx[o];
-    if (slot < (uint32_t)active_n(B)) B.opos[slot] = (uint32_t)o;
+    if (slot < (uint32_t)n) B.opos[slot] = (uint32_t)o;
 }
 
 // New internal order = the sorted slot order (midsort given, no octant order).
@@ -464,7 +474,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume(const __grid_const
     const float4 pi = pos4[s];
     if (!(pi.w < 0.f)) return;
     Kahan sum;
-    for_candidates(P, B.cstart, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
+    for_candidates(P, B, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         if (!(pj.w < 0.f)) return;
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
@@ -503,7 +513,7 @@ __global__ void __launch_bounds__(kThreads) k_boundary_volume_store(const __grid
 // to below 1e-7 of a typical term). The 27 subcells form 18 contiguous index
 // ranges (per (y, z) row: the x-neighbour bucket in the adjacent cell and the
 // two buckets of the same cell); their concatenation is the bucket's candidate
-// sequence, recorded in btab. A warp takes one window of up to kBucketWindow
+// sequence, recorded in btab. A warp takes one window of up to P.bwin (<= 32)
 // members of a bucket (one member per lane, broadcast by shuffles) and the
 // bucket's candidates in blocks of 32 * kBucketChunks held in registers, one
 // per lane and chunk; for each block it walks the window's members, every lane
@@ -545,7 +555,7 @@ __device__ __forceinline__ uint32_t bucket_ranges(const DevParams& P, const DevB
             xhi = 1;
         }
         const uint32_t cc = (uint32_t)(((sy >> 1) * P.rz + (sz >> 1)) * P.rx + ccx);
-        const uint32_t cs = __ldg(&B.cstart[cc]), ce = __ldg(&B.cstart[cc + 1]);
+        const uint32_t cs = __ldg(&B.cstart[cc]), ce = __ldg(&B.cend[cc]);
         if (cs < ce) {
             st = __ldg(&B.oct_start[(size_t)cc * 8 + oyz + xlo]);
             const uint32_t en = (oyz + xhi == 7) ? ce : __ldg(&B.oct_start[(size_t)cc * 8 + oyz + xhi + 1]);
@@ -614,9 +624,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
         }
         const uint32_t bid = c * 8u + q;
         const uint32_t m0 = __ldg(&B.oct_start[(size_t)bid]);
-        const uint32_t m1 = q == 7 ? __ldg(&B.cstart[c + 1]) : __ldg(&B.oct_start[(size_t)bid + 1]);
+        const uint32_t m1 = q == 7 ? __ldg(&B.cend[c]) : __ldg(&B.oct_start[(size_t)bid + 1]);
         if (w0 >= m1) continue;
-        const uint32_t w1 = min(m1, w0 + kBucketWindow);
+        const uint32_t w1 = min(m1, w0 + (uint32_t)P.bwin);
         // the window's members, one per lane; boundary members carry their volume and need no list
         const uint32_t tl = w0 + lane;
         float4 pm = make_float4(kFar, kFar, kFar, -1.f);
@@ -650,19 +660,26 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
         const uint32_t self_base = __shfl_sync(0xffffffffu, off, rs) - __shfl_sync(0xffffffffu, st, rs);
         Kahan msum;  // lane i: member w0 + i, summed over the candidate blocks
         int r = 0;
+        const float2 R2 = make_float2(r2, r2), NEG1 = make_float2(-1.f, -1.f);
         for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
-            float4 cj[kBucketChunks];  // w: fluid mass (0 for boundary)
-            float vb[kBucketChunks];   // boundary volume (0 for fluid)
+            // chunks 2p and 2p + 1 side by side in float2 pairs (packed FP32 arithmetic):
+            // negated coordinates, fluid mass (0 for boundary), boundary volume (0 for fluid)
+            float2 NX[kBucketChunks / 2], NY[kBucketChunks / 2], NZ[kBucketChunks / 2];
+            float2 CW[kBucketChunks / 2], CV[kBucketChunks / 2];
 #pragma unroll
-            for (int ch = 0; ch < kBucketChunks; ch++) {
-                const uint32_t e = base + lane + 32u * ch;
-                cj[ch] = make_float4(kFar, kFar, kFar, 0.f);
-                vb[ch] = 0.f;
-                if (e < T) {
-                    cj[ch] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
-                    vb[ch] = fmaxf(-cj[ch].w, 0.f);
-                    cj[ch].w = fmaxf(cj[ch].w, 0.f);
+            for (int pr = 0; pr < kBucketChunks / 2; pr++) {
+                float4 c2[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const uint32_t e = base + lane + 32u * (2 * pr + h);
+                    c2[h] = make_float4(kFar, kFar, kFar, 0.f);
+                    if (e < T) c2[h] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
                 }
+                NX[pr] = make_float2(-c2[0].x, -c2[1].x);
+                NY[pr] = make_float2(-c2[0].y, -c2[1].y);
+                NZ[pr] = make_float2(-c2[0].z, -c2[1].z);
+                CW[pr] = make_float2(fmaxf(c2[0].w, 0.f), fmaxf(c2[1].w, 0.f));
+                CV[pr] = make_float2(fmaxf(-c2[0].w, 0.f), fmaxf(-c2[1].w, 0.f));
             }
             const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
             const uint32_t word0 = base >> 5;
@@ -672,31 +689,41 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
                 const float py = __shfl_sync(0xffffffffu, pm.y, i);
                 const float pz = __shfl_sync(0xffffffffu, pm.z, i);
                 const float rho0 = __shfl_sync(0xffffffffu, rm, i);
+                const float2 PX = make_float2(px, px), PY = make_float2(py, py), PZ = make_float2(pz, pz);
+                const float2 RHO = make_float2(rho0, rho0);
                 const uint32_t t = w0 + (uint32_t)i;
-                float acc = 0.f;
+                float2 acc = make_float2(0.f, 0.f);
                 uint32_t mine = 0;  // lane k keeps the mask word of chunk k
 #pragma unroll
-                for (int ch = 0; ch < kBucketChunks; ch++) {
-                    if (ch < nch) {
-                        float dx = px - cj[ch].x, dy = py - cj[ch].y, dz = pz - cj[ch].z;
+                for (int pr = 0; pr < kBucketChunks / 2; pr++) {
+                    if (2 * pr < nch) {
+                        float2 dx = __fadd2_rn(PX, NX[pr]), dy = __fadd2_rn(PY, NY[pr]), dz = __fadd2_rn(PZ, NZ[pr]);
                         if (!SS1) {
-                            dx *= ss;
-                            dy *= ss;
-                            dz *= ss;
+                            const float2 SS = make_float2(ss, ss);
+                            dx = __fmul2_rn(dx, SS);
+                            dy = __fmul2_rn(dy, SS);
+                            dz = __fmul2_rn(dz, SS);
                         }
-                        const float dsq = dx * dx + dy * dy + dz * dz;
-                        const float cc = fmaxf(r2 - dsq, 0.f);  // 0 outside h (and for the padding lanes)
-                        acc = fmaf(cc * cc * cc, fmaf(rho0, vb[ch], cj[ch].w), acc);
+                        float2 dsq = __fmul2_rn(dx, dx);
+                        dsq = __ffma2_rn(dy, dy, dsq);
+                        dsq = __ffma2_rn(dz, dz, dsq);
+                        float2 cc = __ffma2_rn(dsq, NEG1, R2);  // r2 - dsq, rounded once
+                        cc.x = fmaxf(cc.x, 0.f);                // 0 outside h (and for the padding lanes)
+                        cc.y = fmaxf(cc.y, 0.f);
+                        const float2 c3 = __fmul2_rn(__fmul2_rn(cc, cc), cc);
+                        acc = __ffma2_rn(c3, __ffma2_rn(RHO, CV[pr], CW[pr]), acc);
                         // coincident particles stay in the list (every consumer skips r == 0);
                         // the member itself is cleared below
-                        const uint32_t bal = __ballot_sync(0xffffffffu, dsq < r2list);
-                        mine = lane == (unsigned)ch ? bal : mine;
+                        const uint32_t b0 = __ballot_sync(0xffffffffu, dsq.x < r2list);
+                        const uint32_t b1 = __ballot_sync(0xffffffffu, dsq.y < r2list);
+                        mine = lane == (unsigned)(2 * pr) ? b0 : mine;
+                        mine = lane == (unsigned)(2 * pr + 1) ? b1 : mine;
                     }
                 }
                 const uint32_t es = t + self_base - base;  // the member's own bit, if in this block
                 if (es < 32u * kBucketChunks && lane == (es >> 5)) mine &= ~(1u << (es & 31u));
                 if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
-                const float part = warp_sum_f(acc);
+                const float part = warp_sum_f(acc.x + acc.y);
                 if (lane == (unsigned)i) msum.add(part);
             }
         }
@@ -713,7 +740,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
 // of a warp emit their n-th entries together so that every row of the
 // column-major list is written by one coalesced store. A particle with more
 // than kMaxNbr neighbours keeps its mask list (nbr_cnt = kMaskList | bucket),
-// which the passes decode directly. Particles with more than kHeavyList
+// which the passes decode directly. Particles with more than P.heavy
 // neighbours (their lists flagged kHeavyFlag), with mask lists or left to the
 // cell search are queued in hq for the force and alpha passes.
 __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant__ DevParams P,
@@ -753,7 +780,7 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
             col[(size_t)n * cap] = e + delta;
         }
     }
-    const bool heavy = (mine && (over || cnt > kHeavyList)) || lst == kRescan;
+    const bool heavy = (mine && (over || cnt > P.heavy)) || lst == kRescan;
     if (mine && !over) B.nbr_cnt[t] = heavy ? (cnt | kHeavyFlag) : cnt;
     const uint32_t hb = __ballot_sync(0xffffffffu, heavy);
     if (hb) {
@@ -781,7 +808,7 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
     Kahan sum;
     uint32_t cnt = 0;
     uint32_t* __restrict__ col = B.nbr + s;
-    for_candidates(P, B.cstart, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
+    for_candidates(P, B, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
         const float dsq = dx * dx + dy * dy + dz * dz;
@@ -946,7 +973,7 @@ __global__ void __launch_bounds__(kThreads) k_surface_tension(const __grid_const
     float rx = 0.f, ry = 0.f, rz = 0.f;
     for (int c = 0; c < 27; c++) {
         const uint32_t cell = gc + (uint32_t)P.neighborid[c];
-        const uint32_t j0 = B.cstart[cell], j1 = B.cstart[cell + 1];
+        const uint32_t j0 = B.cstart[cell], j1 = B.cend[cell];
         for (uint32_t j = j0; j < j1; j++) {
             const float4 pj = __ldg(&pos4[j]);
             const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
@@ -1589,7 +1616,6 @@ void launch_rearrange(const DevParams& P, const DevBuffers& B, const int* cur, b
     if (P.n <= 0) return;
     if (slot_order) k_slot_order<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
     k_rearrange<<<blocks_for(P.n), kThreads, 0, s>>>(P, B, make_set(B, cur, true));
-    k_update_opos<<<blocks_for(P.n), kThreads, 0, s>>>(P, B);
 }
 
 void launch_boundary_volume(const DevParams& P, const DevBuffers& B, const int* cur, cudaStream_t s) {

@@ -70,6 +70,13 @@ def load():
         "sphmp_compute_force": (st, [ctx]),
         "sphmp_compute_force_projectu": (st, [ctx]),
         "sphmp_advance": (st, [ctx]),
+        "sphmp_iisph_density": (st, [ctx]),
+        "sphmp_iisph_predict_advection": (st, [ctx]),
+        "sphmp_iisph_pressure_iteration": (st, [ctx, P(C.c_double)]),
+        "sphmp_iisph_pressure_solve": (st, [ctx, C.c_float, C.c_int32, C.c_int32, P(C.c_int32), P(C.c_double)]),
+        "sphmp_iisph_integrate": (st, [ctx]),
+        "sphmp_step_iisph": (st, [ctx, C.c_int32, C.c_float, C.c_int32, P(C.c_int32), P(C.c_double)]),
+        "sphmp_autotune": (st, [ctx, C.c_int32, C.c_int32, P(abi.Tuning)]),
         "sphmp_step": (st, [ctx, C.c_int32, C.c_int32, C.c_int32]),
         "sphmp_conservation": (st, [ctx, P(C.c_double), C.c_int32]),
         "sphmp_step_profile": (C.c_int32, [ctx, C.c_int32, P(C.c_float), C.c_char_p, C.c_int32]),
@@ -308,6 +315,42 @@ class Context:
 
     def advance(self):
         check(self._lib.sphmp_advance(self._ptr))
+
+    def autotune(self, trial_steps=10, allow_reorder=False):
+        """Pick the fastest launch configuration for the current state (sphmp_autotune)."""
+        t = abi.Tuning()
+        check(self._lib.sphmp_autotune(self._ptr, int(trial_steps), int(bool(allow_reorder)), C.byref(t)))
+        return t.as_dict()
+
+    # ---- IISPH step ----
+    def iisph_density(self):
+        check(self._lib.sphmp_iisph_density(self._ptr))
+
+    def iisph_predict_advection(self):
+        check(self._lib.sphmp_iisph_predict_advection(self._ptr))
+
+    def iisph_pressure_iteration(self):
+        """One pressure iteration; returns (the reference's mean residue over all slots,
+        mean |residue| over in-grid fluid particles)."""
+        r = (C.c_double * 2)()
+        check(self._lib.sphmp_iisph_pressure_iteration(self._ptr, r))
+        return r[0], r[1]
+
+    def iisph_pressure_solve(self, tol=0.1, min_iter=2, max_iter=100):
+        it = C.c_int32(0)
+        r = (C.c_double * 2)()
+        check(self._lib.sphmp_iisph_pressure_solve(self._ptr, float(tol), int(min_iter), int(max_iter),
+                                                   C.byref(it), r))
+        return it.value, (r[0], r[1])
+
+    def iisph_integrate(self):
+        check(self._lib.sphmp_iisph_integrate(self._ptr))
+
+    def step_iisph(self, nsteps=1, tol=0.1, max_iter=100):
+        its = (C.c_int32 * max(int(nsteps), 1))()
+        r = (C.c_double * 2)()
+        check(self._lib.sphmp_step_iisph(self._ptr, int(nsteps), float(tol), int(max_iter), its, r))
+        return list(its)[:int(nsteps)], (r[0], r[1])
 
     def set_device_emitter(self, position, direction, speed, radius, spacing, layers=2, phase=0, interval=22,
                            jitter=1.0, seed=0):

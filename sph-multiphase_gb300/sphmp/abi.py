@@ -33,6 +33,8 @@ EOS_LINEAR = 1
 SCHEDULE_REFERENCE = 0
 SCHEDULE_FUSED = 1
 SCHEDULE_PROJECTU = 2
+CELL_ORDER_LINEAR = 0
+CELL_ORDER_MORTON = 1
 
 # sphmp_field
 F_POS, F_VEL, F_VELEVAL, F_PRESSURE, F_DENS, F_RESTDENS, F_VISC, F_ACCEL = range(8)
@@ -78,7 +80,8 @@ class Params(C.Structure):
         ("eos", C.c_int32), ("eos_stiffness", C.c_float), ("mf_relax", C.c_float),
         ("mf_diffusion", C.c_float), ("mf_cont", C.c_float), ("mf_cont1", C.c_float),
         ("mf_cont2", C.c_float), ("mf_pintstiff", C.c_float), ("mf_omega", C.c_float),
-        ("mf_visc_factor", C.c_float), ("reserved", C.c_int32 * 3),
+        ("mf_visc_factor", C.c_float), ("cell_order", C.c_int32), ("bucket_window", C.c_int32),
+        ("heavy_list", C.c_int32),
     ]
 
     def copy(self):
@@ -155,6 +158,8 @@ EXPORTED_SYMBOLS = [
     "sphmp_rearrange_data", "sphmp_compute_boundary_density", "sphmp_compute_pressure",
     "sphmp_compute_drift_vel", "sphmp_compute_alpha_advance", "sphmp_compute_correction",
     "sphmp_compute_force", "sphmp_compute_force_projectu", "sphmp_advance", "sphmp_step", "sphmp_conservation",
+    "sphmp_iisph_density", "sphmp_iisph_predict_advection", "sphmp_iisph_pressure_iteration",
+    "sphmp_iisph_pressure_solve", "sphmp_iisph_integrate", "sphmp_step_iisph", "sphmp_autotune",
     "sphmp_device_errors", "sphmp_last_error", "sphmp_version", "sphmp_sort_cells_noalloc",
     "sphmp_write_frame_text", "sphmp_read_bi2", "sphmp_add_bi2_shape", "sphmp_save_state", "sphmp_load_state",
     "sphmp_download_display_async", "sphmp_download_wait", "sphmp_emit_disk", "sphmp_set_device_emitter",
@@ -167,7 +172,7 @@ EXPORTED_SYMBOLS = [
     "cudaInit", "cudaExit", "FluidClearCUDA", "FluidSetupCUDA", "GetParticleIndexCUDA",
     "GetGridListCUDA", "RearrageDataCUDA", "InitialSortCUDA", "SortGridCUDA", "CountingSortFullCUDA_", "MfComputePressureCUDA", "MfComputeDriftVelCUDA",
     "MfComputeAlphaAdvanceCUDA", "MfComputeCorrectionCUDA", "MfComputeForceCUDA", "ComputeForceCUDA_ProjectU",
-    "MfAdvanceCUDA",
+    "MfAdvanceCUDA", "ComputeDensityIISPH_CUDA", "PredictAdvection", "PressureSolve", "Integration",
     "ComputeBoundaryDensity", "computeNumBlocks", "sphmp_legacy_context", "TransferToCUDA",
     "TransferFromCUDA", "EmitUpdateCUDA",
 ]
@@ -180,6 +185,15 @@ class Bi2Info(C.Structure):
                 ("massbound", C.c_float), ("massfluid", C.c_float), ("time", C.c_float),
                 ("np", C.c_int32), ("nfixed", C.c_int32), ("nmoving", C.c_int32), ("nfloat", C.c_int32),
                 ("nfluidout", C.c_int32), ("nbound", C.c_int32), ("nfluid", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    """sphmp_tuning (include/sphmp.h): the autotuner's choice and its step times."""
+    _fields_ = [("cell_order", C.c_int32), ("bucket_window", C.c_int32), ("heavy_list", C.c_int32),
+                ("trials", C.c_int32), ("ms_per_step", C.c_float), ("ms_before", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -20,7 +20,8 @@ OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libsphmp.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["sphmp_kernels.cu", "sphmp_api.cu", "sphmp_noalloc.cu", "sphmp_mlp.cu", "sphmp_learned.cu"]
+CUDA_SOURCES = ["sphmp_kernels.cu", "sphmp_api.cu", "sphmp_iisph.cu", "sphmp_noalloc.cu", "sphmp_mlp.cu",
+                "sphmp_learned.cu"]
 HOST_SOURCES = ["sphmp_host.cpp", "sphmp_io.cpp"]
 
 

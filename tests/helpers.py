@@ -66,6 +66,25 @@ def field_err(got, ref, floor=0.0):
     return float(np.max(np.abs(got - ref))) / scale
 
 
+def rel_err_quantile(got, ref, q=99.9, floor_frac=1e-3):
+    """The q-th percentile over elements of |got - ref| / max(|ref|, floor_frac * max|ref|):
+    a per-element relative error beside the max-norm of field_err (the floor keeps
+    elements near zero from reading as large relative errors)."""
+    got = np.asarray(got, np.float64).ravel()
+    ref = np.asarray(ref, np.float64).ravel()
+    if ref.size == 0:
+        return 0.0
+    den = np.maximum(np.abs(ref), floor_frac * max(float(np.max(np.abs(ref))), 1e-300))
+    return float(np.percentile(np.abs(got - ref) / den, q))
+
+
+def rms_err(got, ref):
+    """sqrt(mean (got - ref)^2) / sqrt(mean ref^2)."""
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return float(np.sqrt(np.mean((got - ref) ** 2)) / max(np.sqrt(np.mean(ref ** 2)), 1e-300))
+
+
 def bits_equal(a, b):
     a = np.ascontiguousarray(a)
     b = np.ascontiguousarray(b)

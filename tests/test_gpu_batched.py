@@ -88,3 +88,48 @@ def test_tiled_scenes_match_solo_runs():
         for k in ("vel", "dens", "accel"):
             assert field_err(gb[k][ob][f], g1[k][o1][f]) < tol, (i, k)
         assert field_err(gb["alpha"][ob][f][:, :2], g1["alpha"][o1][f][:, :2], floor=1.0) < tol
+
+
+@pytest.mark.slow
+def test_512_scenes_match_solo_runs():
+    """The batched configuration at its size: 512 two-phase bubble scenes,
+    particle counts log-uniform in [4096, 65536] (20.2 M particles, 11.2 M fluid),
+    tiled into one domain and run three fused steps in one launch per pass; every
+    scene against the same scene run alone (tolerance as above, from the largest
+    tiled coordinate, about 9 m here)."""
+    rng = np.random.default_rng(7)
+    counts = np.floor(np.exp(rng.uniform(np.log(4096), np.log(65536), 512))).astype(int)
+    solo = [scenes.bubble_scene(seed=7 * 100003 + i, n_particles=int(c)) for i, c in enumerate(counts)]
+    big, layout = scenes.tile(solo)
+    assert len(layout) == 512 and big.n_fluid > 10_000_000
+    tol = RTOL + 20 * np.finfo(np.float32).eps * float(np.abs(big.disp["pos"]).max()) / 0.01
+    steps = 3
+    ctx = sphmp.Context(big.params)
+    ctx.upload_aos(big.disp, big.calc)
+    ctx.before_first_step()
+    ctx.step(steps, abi.SCHEDULE_FUSED, use_graph=True)
+    ctx.sync()
+    assert ctx.device_errors() == 0
+    gb = _state(ctx)
+    ctx.close()
+    order = np.argsort(gb["bornid"])
+    worst = 0.0
+    for i, sc in enumerate(solo):
+        first, count, off = layout[i]
+        c1 = sphmp.Context(sc.params)
+        c1.upload_aos(sc.disp, sc.calc)
+        c1.before_first_step()
+        c1.step(steps, abi.SCHEDULE_FUSED, use_graph=False)
+        c1.sync()
+        g1 = _state(c1)
+        c1.close()
+        o1 = np.argsort(g1["bornid"])
+        ob = order[first:first + count]
+        assert np.array_equal(gb["bornid"][ob] - first, g1["bornid"][o1]), i
+        f = g1["type"][o1] == 0
+        errs = [field_err(gb["pos"][ob][f] - off, g1["pos"][o1][f])]
+        errs += [field_err(gb[k][ob][f], g1[k][o1][f]) for k in ("vel", "dens", "accel")]
+        errs.append(field_err(gb["alpha"][ob][f][:, :2], g1["alpha"][o1][f][:, :2], floor=1.0))
+        worst = max(worst, max(errs))
+        assert max(errs) < tol, (i, errs, tol)
+    print(f"512 scenes: largest difference to the solo runs {worst:.2e} (tolerance {tol:.2e})")

@@ -5,7 +5,11 @@ from 64 seeded blobs (rest densities 1000 / 800 / 1.2), linear EOS k = 3.
 * One fused step: the cell ids, offsets, counts, rank in cell and permutation
   are bit-identical to the FP32 oracle on all 1.3 M slots, and density,
   acceleration, positions, velocities and volume fractions agree within
-  RTOL = 1e-5 (max |gpu - oracle| / max |oracle| over in-grid fluid slots).
+  RTOL = 1e-5 (max |gpu - oracle| / max |oracle| over in-grid fluid slots);
+  per element, the 99.9th percentile of |gpu - oracle| / |oracle| stays below
+  1e-3 (elements below 1e-3 of the field's largest value measured against that
+  floor; the force sums cancel large terms, so the acceleration's per-element
+  error is about 1.4e-4 where the density's is 3.3e-7).
 * Ten fused steps against the FP64 oracle: per field, the GPU's error is at most
   four times the error of the FP32 oracle (the reference's own float
   arithmetic) against the same FP64 run, or 1e-6 where that is smaller.
@@ -19,13 +23,14 @@ import os
 import numpy as np
 import pytest
 
-from helpers import bits_equal, device_ctx, download_state, field_err, in_grid_fluid, oracle_state
+from helpers import bits_equal, device_ctx, download_state, field_err, in_grid_fluid, oracle_state, rel_err_quantile
 from oracle import oracle as O
 from sphmp import abi, scenes
 
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
 
 RTOL = 1e-5
+Q999 = 1e-3
 
 
 @pytest.fixture(scope="module")
@@ -57,9 +62,12 @@ def test_one_step_sort_bit_exact_fields_within_tolerance(built, scene):
         assert bits_equal(g[k], getattr(s, k)), k
     f = in_grid_fluid(s)
     assert f.sum() > 1_000_000
-    for k in ("dens", "accel", "pos", "vel", "veleval"):
-        assert field_err(g[k][f], getattr(s, k)[f]) < RTOL, k
-    assert field_err(g["alpha"][f], s.alpha[f], floor=1.0) < RTOL
+    for k in ("dens", "accel", "pos", "vel", "veleval", "alpha"):
+        e = field_err(g[k][f], getattr(s, k)[f], floor=1.0 if k == "alpha" else 0.0)
+        q = rel_err_quantile(g[k][f], getattr(s, k)[f])
+        print(f"{k}: max-norm {e:.2e}, p99.9 per element {q:.2e}")
+        assert e < RTOL, (k, e)
+        assert q < Q999, (k, q)
 
 
 def _by_bornid(bornid, arr):
