@@ -256,12 +256,17 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
 
 
-def build_scene(seed, gen=None):
+LATTICE = (128, 64, 128)
+
+
+def build_scene(seed, gen=None, lattice=LATTICE):
     """The benchmark scene; `gen` = the scene generators (default: the library's; the reference
     arm passes the oracle's restatement, which builds the same records byte for byte without
-    loading the CUDA library)."""
+    loading the CUDA library). A smaller `lattice` keeps the scene's physics and box (profiling
+    captures that must stay small)."""
     from sphmp import abi, scenes
-    return scenes.blobs_3phase(seed=seed, eos=abi.EOS_LINEAR, eos_k=3.0, gen=gen or scenes.LIBRARY)
+    return scenes.blobs_3phase(seed=seed, lattice=tuple(lattice), eos=abi.EOS_LINEAR, eos_k=3.0,
+                               gen=gen or scenes.LIBRARY)
 
 
 def scene_config(scene):
@@ -325,7 +330,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     from oracle import oracle as O
-    scene = build_scene(args.seed, gen=O.Generators)   # the oracle's generators: no CUDA library here
+    scene = build_scene(args.seed, gen=O.Generators, lattice=args.lattice)  # the oracle's generators: no CUDA
     # warm-up steps are part of the sample's own warm-up; the timed part is bounded
     value, done, dt, nthr, warm = cpu_sample(scene, max(1, args.steps), budget_s=args.cpu_budget,
                                              warmup=args.warmup)
@@ -358,7 +363,7 @@ def run_gpu(args):
     ws, rank, local = rep.ws, rep.rank, rep.local
     torch.cuda.set_device(local)
     dev_index = torch.cuda.current_device()
-    scene = build_scene(args.seed + rank)
+    scene = build_scene(args.seed + rank, lattice=args.lattice)
     scene.params.cell_order = abi.CELL_ORDER_MORTON if args.cell_order == "morton" else abi.CELL_ORDER_LINEAR
     n_fluid = scene.n_fluid
 
@@ -731,35 +736,35 @@ def run_learned(args):
                 ctx.close()
                 aud.close()
                 ref.close()
-        if liquid:
-            # two references for the end-of-run difference: the same audited rollout without the
-            # network, and the plain pipeline from the start state moved by one ulp in x (how far
-            # two faithful trajectories drift apart over the same time)
-            ref = sphmp.Context(sc.params)
-            ref.copy_state_from(src)
-            ref.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
-            ref.sort()
-            ref.compute_pressure()
-            for arm in ("uncorrected", "plain_one_ulp"):
-                ctx = sphmp.Context(sc.params)
-                ctx.copy_state_from(src)
-                if arm == "uncorrected":
-                    aud = sphmp.Context(sc.params)
-                    st = ctx.rollout(aud, sim_steps, factor=factor, corrector=None, audit_every=audit_every, tol=tol)
-                    aud.close()
-                    res[arm] = {"stats": st}
-                else:
-                    pos = ctx.download_field(abi.F_POS)
-                    pos[:, 0] = np.nextafter(pos[:, 0], np.float32(np.inf))
-                    ctx.upload_field(abi.F_POS, pos)
-                    ctx.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
-                    res[arm] = {}
-                ctx.sort()
-                ctx.compute_pressure()
-                res[arm]["vs_plain_at_end"] = ctx.compare_to(ref)
-                print(f"learned/{case}/{arm}: {res[arm]}", file=sys.stderr, flush=True)
-                ctx.close()
-            ref.close()
+        # references for the end-of-run difference: the plain pipeline from the start state moved
+        # by one ulp in x (how far two faithful trajectories drift apart over the same time: the
+        # floor under any method's error against the plain run) and, all liquid, the same audited
+        # rollout without the network
+        ref = sphmp.Context(sc.params)
+        ref.copy_state_from(src)
+        ref.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
+        ref.sort()
+        ref.compute_pressure()
+        for arm in (("uncorrected", "plain_one_ulp") if liquid else ("plain_one_ulp",)):
+            ctx = sphmp.Context(sc.params)
+            ctx.copy_state_from(src)
+            if arm == "uncorrected":
+                aud = sphmp.Context(sc.params)
+                st = ctx.rollout(aud, sim_steps, factor=factor, corrector=None, audit_every=audit_every, tol=tol)
+                aud.close()
+                res[arm] = {"stats": st}
+            else:
+                pos = ctx.download_field(abi.F_POS)
+                pos[:, 0] = np.nextafter(pos[:, 0], np.float32(np.inf))
+                ctx.upload_field(abi.F_POS, pos)
+                ctx.step(sim_steps, abi.SCHEDULE_FUSED, use_graph=True)
+                res[arm] = {}
+            ctx.sort()
+            ctx.compute_pressure()
+            res[arm]["vs_plain_at_end"] = ctx.compare_to(ref)
+            print(f"learned/{case}/{arm}: {res[arm]}", file=sys.stderr, flush=True)
+            ctx.close()
+        ref.close()
         res["sim_s_per_wall_s_ratio"] = res["learned"]["sim_s_per_wall_s"] / res["plain"]["sim_s_per_wall_s"]
         cases[case] = res
         src.close()
@@ -995,6 +1000,9 @@ def main():
     ap.add_argument("--profile-every", type=int, default=100, help="steps between per-stage timing samples")
     ap.add_argument("--learned-steps", type=int, default=1280,
                     help="simulated time of the learned workload's rollout, in plain steps of dt")
+    ap.add_argument("--lattice", default="128,64,128", type=lambda v: tuple(int(x) for x in v.split(",")),
+                    help="blobs workload: fluid lattice x,y,z (the headline scene is 128,64,128; smaller ones are "
+                         "for small profiling captures)")
     ap.add_argument("--cell-order", default="linear", choices=["linear", "morton"],
                     help="order of the cells in the sorted arrays (blobs workload): the reference's linear key "
                          "order (bit-exact sort, the default) or Z-order")
