@@ -275,7 +275,8 @@ __device__ __forceinline__ void warp_bitonic(uint32_t (&v)[E]) {
 // held at sorted position q (cellstart + q is its internal index): the member's
 // previous internal index (osrc), its slot (oidx) and the bucket starts.
 __device__ __forceinline__ void emit_octant(const DevBuffers& B, uint32_t c, uint32_t start, uint32_t cnt, uint32_t q,
-                                            uint32_t key, uint32_t prev_oct, int shift, uint32_t pre_slot) {
+                                            uint32_t key, uint32_t prev_oct, int shift, uint32_t pre_slot,
+                                            uint32_t* bst = nullptr) {
     const uint32_t oct = key >> shift;
     const uint32_t idx = key & ((1u << shift) - 1u);
     if (q < cnt) {
@@ -284,9 +285,15 @@ __device__ __forceinline__ void emit_octant(const DevBuffers& B, uint32_t c, uin
     }
     // bucket starts: every bucket in (prev_oct, oct] begins at q (8 marks past the end)
     const uint32_t hi = q < cnt ? oct : 8u;
-    for (uint32_t b = prev_oct + 1; b <= hi && b < 8; b++) B.oct_start[(size_t)c * 8 + b] = start + q;
+    for (uint32_t b = prev_oct + 1; b <= hi && b < 8; b++) {
+        B.oct_start[(size_t)c * 8 + b] = start + q;
+        if (bst) bst[b] = start + q;
+    }
     if (q == cnt - 1)
-        for (uint32_t b = oct + 1; b < 8; b++) B.oct_start[(size_t)c * 8 + b] = start + cnt;
+        for (uint32_t b = oct + 1; b < 8; b++) {
+            B.oct_start[(size_t)c * 8 + b] = start + cnt;
+            if (bst) bst[b] = start + cnt;
+        }
 }
 
 // Queue the member windows after the first of bucket (c, b) = members [m0, m1)
@@ -302,7 +309,7 @@ __device__ __forceinline__ void push_windows(const DevParams& P, const DevBuffer
 
 template <int E>
 __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuffers& B, const float4* __restrict__ pos_in,
-                                               uint32_t* wsm, uint32_t c, uint32_t start, uint32_t cnt) {
+                                               uint32_t* wsm, uint32_t* bst, uint32_t c, uint32_t start, uint32_t cnt) {
     uint32_t v[E];
     const unsigned lane = lane_id();
 #pragma unroll
@@ -337,13 +344,13 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
         if (q <= cnt) {
             const uint32_t k = key[r];
             const uint32_t pre = q < cnt ? wsm[k & 255u] : 0u;
-            emit_octant(B, c, start, cnt, q, q < cnt ? k : (8u << 8), prev_oct, 8, pre);
+            emit_octant(B, c, start, cnt, q, q < cnt ? k : (8u << 8), prev_oct, 8, pre, bst);
         }
     }
-    __syncwarp();  // the bucket starts written above are visible to the whole warp
+    __syncwarp();  // the bucket starts in bst are visible to the whole warp
     if (lane < 8 && cnt > (uint32_t)P.bwin) {
-        const uint32_t b0 = B.oct_start[(size_t)c * 8 + lane];
-        const uint32_t b1 = lane == 7 ? start + cnt : B.oct_start[(size_t)c * 8 + lane + 1];
+        const uint32_t b0 = bst[lane];
+        const uint32_t b1 = lane == 7 ? start + cnt : bst[lane + 1];
         push_windows(P, B, c, lane, b0, b1);
     }
     __syncwarp();
@@ -354,7 +361,9 @@ __global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ 
                                                         const __grid_constant__ DevBuffers B,
                                                         const float4* __restrict__ pos_in) {
     __shared__ uint32_t sm[kThreads / 32][kWarpSortMax];
+    __shared__ uint32_t bs[kThreads / 32][8];  // the bucket starts of the warp's current cell
     uint32_t* wsm = sm[threadIdx.x >> 5];
+    uint32_t* bst = bs[threadIdx.x >> 5];
     const int nwarps = (gridDim.x * kThreads) >> 5;
     const uint32_t nact = *B.act_n;  // the occupied cells, listed by the scan
     for (uint32_t a = (blockIdx.x * kThreads + threadIdx.x) >> 5; a < nact; a += (uint32_t)nwarps) {
@@ -362,10 +371,10 @@ __global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ 
         const uint32_t start = B.cstart[c];
         const uint32_t cnt = B.cend[c] - start;
         if (cnt == 0 || cnt > (uint32_t)kWarpSortMax) continue;
-        if (cnt <= 32) warp_sort_cell<1>(P, B, pos_in, wsm, c, start, cnt);
-        else if (cnt <= 64) warp_sort_cell<2>(P, B, pos_in, wsm, c, start, cnt);
-        else if (cnt <= 128) warp_sort_cell<4>(P, B, pos_in, wsm, c, start, cnt);
-        else warp_sort_cell<8>(P, B, pos_in, wsm, c, start, cnt);
+        if (cnt <= 32) warp_sort_cell<1>(P, B, pos_in, wsm, bst, c, start, cnt);
+        else if (cnt <= 64) warp_sort_cell<2>(P, B, pos_in, wsm, bst, c, start, cnt);
+        else if (cnt <= 128) warp_sort_cell<4>(P, B, pos_in, wsm, bst, c, start, cnt);
+        else warp_sort_cell<8>(P, B, pos_in, wsm, bst, c, start, cnt);
     }
 }
 
