@@ -124,10 +124,19 @@ __device__ __forceinline__ void for_candidates(const DevParams& P, const DevBuff
     });
 }
 
-// Rows of the column-major neighbour lists are streamed from DRAM (the lists
-// outgrow L2); the walk asks L2 for the row kListPrefetch entries ahead, so the
-// index load of a row rarely waits on DRAM.
-constexpr uint32_t kListPrefetch = 8;
+// Neighbour index lists: entry k of particle s at ((k / 4) * cap + s) * 4 + k % 4,
+// i.e. groups of four consecutive entries per particle with the groups
+// column-major: a warp reads one group row (entries 4g .. 4g + 3 of its 32
+// particles) as one coalesced 512-byte load, and a walk holds the next three
+// indices in registers before it needs them.
+__device__ __forceinline__ size_t nbr_at(size_t cap, uint32_t s, uint32_t k) {
+    return ((size_t)(k >> 2) * cap + (size_t)s) * 4u + (k & 3u);
+}
+
+// Group rows of the lists are streamed from DRAM (the lists outgrow L2); the
+// walk asks L2 for the row kListPrefetch groups ahead, so the load of a group
+// rarely waits on DRAM.
+constexpr uint32_t kListPrefetch = 2;
 
 __device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
@@ -171,13 +180,18 @@ __device__ __forceinline__ void for_slot_list(const DevParams& P, const DevBuffe
         }
         const uint32_t cnt = raw & ~kHeavyFlag;  // kRescan stays above kMaxNbr
         if (cnt <= (uint32_t)kMaxNbr) {
-            const uint32_t* __restrict__ col = B.nbr + s;
+            const uint4* __restrict__ grp = reinterpret_cast<const uint4*>(B.nbr) + s;
             const size_t cap = (size_t)P.cap;
-            for (uint32_t k = 0; k < kListPrefetch && k < cnt; k++) prefetch_l2(col + (size_t)k * cap);
-#pragma unroll 2
-            for (uint32_t k = 0; k < cnt; k++) {
-                if (k + kListPrefetch < cnt) prefetch_l2(col + (size_t)(k + kListPrefetch) * cap);
-                f(__ldg(col + (size_t)k * cap));
+            const uint32_t ng = (cnt + 3u) >> 2;
+            for (uint32_t g = 0; g < kListPrefetch && g < ng; g++) prefetch_l2(grp + (size_t)g * cap);
+            for (uint32_t g = 0; g < ng; g++) {
+                if (g + kListPrefetch < ng) prefetch_l2(grp + (size_t)(g + kListPrefetch) * cap);
+                const uint4 q = __ldg(grp + (size_t)g * cap);
+                const uint32_t k = g << 2;
+                f(q.x);
+                if (k + 1u < cnt) f(q.y);
+                if (k + 2u < cnt) f(q.z);
+                if (k + 3u < cnt) f(q.w);
             }
             return;
         }
@@ -226,9 +240,8 @@ __device__ __forceinline__ void warp_for_slot_list(const DevParams& P, const Dev
         }
         const uint32_t cnt = raw & ~kHeavyFlag;
         if (cnt <= (uint32_t)kMaxNbr) {
-            const uint32_t* __restrict__ col = B.nbr + s;
             const size_t cap = (size_t)P.cap;
-            for (uint32_t k = lane; k < cnt; k += 32) f(__ldg(col + (size_t)k * cap));
+            for (uint32_t k = lane; k < cnt; k += 32) f(__ldg(B.nbr + nbr_at(cap, (uint32_t)s, k)));
             return;
         }
     }

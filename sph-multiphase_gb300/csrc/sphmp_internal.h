@@ -129,7 +129,7 @@ struct DevBuffers {
     uint32_t* err;      // device error word
     double* red;        // [16] FP64 reduction results
     float* vtmp;        // [cap] scratch (boundary volumes)
-    uint32_t* nbr;      // [kMaxNbr * cap] neighbour indices, column-major: entry k of particle s at k * cap + s
+    uint32_t* nbr;      // [kMaxNbr * cap] neighbour indices, groups of 4 column-major: entry k of s at ((k / 4) * cap + s) * 4 + k % 4
     uint32_t* nbr_cnt;  // [cap] list of particle s: kMaskList | bucket, index count (<= kMaxNbr) or kRescan
     uint32_t* nmask;    // [kMaskWords * cap] bucket mask lists, column-major: word k of particle s at k * cap + s
     uint32_t* btab;     // [8 * G * kTabStride] candidate ranges of each bucket with a mask list

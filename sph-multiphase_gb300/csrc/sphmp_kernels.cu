@@ -746,8 +746,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
 // Index lists from the bucket mask lists: bit e of a member's mask stands for
 // candidate e of its bucket's sequence, whose index is e plus the offset of the
 // sequence range holding e (btab). One thread per in-grid particle; the lanes
-// of a warp emit their n-th entries together so that every row of the
-// column-major list is written by one coalesced store. A particle with more
+// of a warp emit their n-th entries together and store each group of four as
+// one 16-byte word, so that every group row of the lists is written by one
+// coalesced store. A particle with more
 // than kMaxNbr neighbours keeps its mask list (nbr_cnt = kMaskList | bucket),
 // which the passes decode directly. Particles with more than P.heavy
 // neighbours (their lists flagged kHeavyFlag), with mask lists or left to the
@@ -769,24 +770,41 @@ __global__ void __launch_bounds__(kThreads) k_expand_lists(const __grid_constant
     uint32_t rounds = cnt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
-    uint32_t* __restrict__ col = B.nbr + t;
-    uint32_t r = 0, end = 0, delta = 0;
+    uint4* __restrict__ grp = reinterpret_cast<uint4*>(B.nbr) + t;
+    uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;  // the list group being filled
+    // the next mask word and the next range of the table are loaded one ahead, so
+    // that the lockstep rounds wait on neither (only on a run of empty words or ranges)
+    int r = 0;
+    uint32_t end = 0, delta = 0, endn = 0, deltan = 0;
     if (mine) {
         end = __ldg(&tab[1]);
         delta = __ldg(&tab[20]);
+        endn = __ldg(&tab[2]);
+        deltan = __ldg(&tab[21]);
     }
-    uint32_t wd = 0, m = nw > 0 ? __ldg(mw) : 0u;
+    uint32_t wd = 0, m = nw > 0u ? __ldg(mw) : 0u, mn = nw > 1u ? __ldg(mw + cap) : 0u;
     for (uint32_t n = 0; n < rounds; n++) {
         if (n < cnt) {
-            while (m == 0u) m = __ldg(mw + (size_t)(++wd) * cap);
+            while (m == 0u) {
+                m = mn;
+                ++wd;
+                mn = wd + 1u < nw ? __ldg(mw + (size_t)(wd + 1u) * cap) : 0u;
+            }
             const uint32_t e = (wd << 5) + (uint32_t)(__ffs(m) - 1);
             m &= m - 1u;
-            while (e >= end) {  // ends at tab[18] = the sequence length > e
+            while (e >= end) {  // ends at tab[18] = the sequence length > e; reads stay below tab[39]
                 r++;
-                end = __ldg(&tab[r + 1]);
-                delta = __ldg(&tab[20 + r]);
+                end = endn;
+                delta = deltan;
+                endn = __ldg(&tab[r + 2]);
+                deltan = __ldg(&tab[21 + r]);
             }
-            col[(size_t)n * cap] = e + delta;
+            const uint32_t v = e + delta, u = n & 3u;
+            q0 = u == 0u ? v : q0;
+            q1 = u == 1u ? v : q1;
+            q2 = u == 2u ? v : q2;
+            q3 = u == 3u ? v : q3;
+            if (u == 3u || n + 1u == cnt) grp[(size_t)(n >> 2) * cap] = make_uint4(q0, q1, q2, q3);
         }
     }
     const bool heavy = (mine && (over || cnt > P.heavy)) || lst == kRescan;
@@ -816,7 +834,6 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
     const float rho0 = alpha4[s].w;
     Kahan sum;
     uint32_t cnt = 0;
-    uint32_t* __restrict__ col = B.nbr + s;
     for_candidates(P, B, B.mgcell[s], pi.x, pi.y, pi.z, [&](uint32_t j) {
         const float4 pj = __ldg(&pos4[j]);
         const float dx = (pi.x - pj.x) * P.ss, dy = (pi.y - pj.y) * P.ss, dz = (pi.z - pj.z) * P.ss;
@@ -827,7 +844,7 @@ __global__ void __launch_bounds__(kThreads) k_density(const __grid_constant__ De
             sum.add(c * c * c * m);
         }
         if (dsq > 0.f && dsq < P.r2list) {
-            if (cnt < (uint32_t)kMaxNbr) col[(size_t)cnt * P.cap] = j;
+            if (cnt < (uint32_t)kMaxNbr) B.nbr[nbr_at((size_t)P.cap, (uint32_t)s, cnt)] = j;
             cnt++;
         }
     });
