@@ -58,4 +58,4 @@ def test_single_rank_is_a_no_op(monkeypatch):
 def test_each_rank_builds_its_own_replica_scene():
     """Ranks seed their scene with seed + rank: replicas are independent simulations."""
     src = open(os.path.join(REPO, "bench.py")).read()
-    assert "build_scene(args.seed + rank)" in src
+    assert "build_scene(args.seed + rank," in src or "build_scene(args.seed + rank)" in src
