@@ -272,14 +272,13 @@ __device__ __forceinline__ float2 density_result(const DevParams& P, float wsum,
 // Force + drift velocity (MfComputeForceCUDA, MfComputeDriftVelCUDA)
 // ---------------------------------------------------------------------------
 
-// Accumulates the force (contributeForce_new) and / or the drift-velocity terms
-// (contributeDriftVel) of one in-grid fluid particle over its neighbours.
-// `pair` takes the neighbour's pos4, (1/rho, p), vel4 and alpha4.
 // Neighbour record of particle s for the alpha pass, 80 contiguous bytes:
 //   {x, y, z, md}, {veleval xyz, alpha_0}, {alpha_1, alpha_2, u_0x, u_0y},
 //   {u_0z, u_1xyz}, {u_2xyz, 0}
 // with md = mass * (1/rho) for fluid particles and -1 for boundary particles
-// (which exchange no volume fraction), u_k the drift velocities.
+// (which exchange no volume fraction), u_k the drift velocities. (A 96-byte
+// record read with three 32-byte loads measured slower: 0.314 against
+// 0.295 ms per alpha pass, from the larger records missing L2.)
 __device__ __forceinline__ void write_nrec(const DevBuffers& B, int s, const float4 p, float md, const float4 ve,
                                            const float (&a)[3], const float (&u)[9]) {
     float4* r = B.nrec + (size_t)s * kNrecFloat4;
@@ -290,6 +289,20 @@ __device__ __forceinline__ void write_nrec(const DevBuffers& B, int s, const flo
     r[4] = make_float4(u[6], u[7], u[8], 0.f);
 }
 
+// The five float4 of neighbour j's record (the fifth only with three phases).
+template <int NP>
+__device__ __forceinline__ void read_nrec(const DevBuffers& B, uint32_t j, float4 (&q)[5]) {
+    const float4* __restrict__ r = B.nrec + (size_t)j * kNrecFloat4;
+    q[0] = __ldg(r);
+    q[1] = __ldg(r + 1);
+    q[2] = __ldg(r + 2);
+    q[3] = __ldg(r + 3);
+    q[4] = NP > 2 ? __ldg(r + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Accumulates the force (contributeForce_new) and / or the drift-velocity terms
+// (contributeDriftVel) of one in-grid fluid particle over its neighbours.
+// `pair` takes the neighbour's pos4, (1/rho, p), vel4 and alpha4.
 template <bool FORCE, bool DRIFT, int NP>
 struct ForceDrift {
     static constexpr int K = NP > 0 ? NP : 1;
@@ -299,7 +312,7 @@ struct ForceDrift {
     float mc[K];
     float relax_coef, invdens;
     float fx, fy, fz;
-    float3 dv[K], ag[K];
+    float3 dv[K], ag[K];  // dv: the pressure-gradient sums of phase k until finish() forms the drift term
 
     __device__ __forceinline__ void init(const DevParams& P, float4 pi_, float4 vi_, float2 dpi, float4 ai) {
         pi = pi_;
@@ -341,21 +354,15 @@ struct ForceDrift {
             }
             if (DRIFT) {
                 const float ja[3] = {aj.x, aj.y, aj.z};
-                float3 pg[K];
-                float3 psum = make_float3(0.f, 0.f, 0.f);
+                // the pressure-gradient terms summed per phase; the mass-weighted
+                // phase average is subtracted once per particle (finish): the sum
+                // over pairs of (pg_k - sum_k' mc_k' pg_k') is linear in pg
 #pragma unroll
                 for (int k = 0; k < NP; k++) {
                     const float pm = g * (-ia[k] * ipress + ja[k] * dpj.y);
-                    pg[k] = make_float3(pm * dx, pm * dy, pm * dz);
-                    psum.x += pg[k].x * mc[k]; psum.y += pg[k].y * mc[k]; psum.z += pg[k].z * mc[k];
+                    dv[k].x += pm * dx; dv[k].y += pm * dy; dv[k].z += pm * dz;
                     const float ga = (ja[k] - ia[k]) * g;
                     ag[k].x += ga * dx; ag[k].y += ga * dy; ag[k].z += ga * dz;
-                }
-#pragma unroll
-                for (int k = 0; k < NP; k++) {
-                    dv[k].x -= relax_coef * (pg[k].x - psum.x);
-                    dv[k].y -= relax_coef * (pg[k].y - psum.y);
-                    dv[k].z -= relax_coef * (pg[k].z - psum.z);
                 }
             }
         } else if (FORCE) {  // boundary neighbour, volume V_j = -w
@@ -401,6 +408,19 @@ struct ForceDrift {
             float3 out[K], st[K];
             float dsum = 0.f;
             float3 ssum = make_float3(0.f, 0.f, 0.f);
+            {  // dv_k = -relax (sum pg_k - sum_k' mc_k' sum pg_k')
+                float3 psum = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    psum.x += dv[k].x * mc[k]; psum.y += dv[k].y * mc[k]; psum.z += dv[k].z * mc[k];
+                }
+#pragma unroll
+                for (int k = 0; k < NP; k++) {
+                    dv[k].x = -(relax_coef * (dv[k].x - psum.x));
+                    dv[k].y = -(relax_coef * (dv[k].y - psum.y));
+                    dv[k].z = -(relax_coef * (dv[k].z - psum.z));
+                }
+            }
 #pragma unroll
             for (int k = 0; k < NP; k++) {
                 out[k] = make_float3(cc * dv[k].x, cc * dv[k].y, cc * dv[k].z);
@@ -526,23 +546,52 @@ struct ProjectU {
 // Volume-fraction advance (MfComputeAlphaAdvanceCUDA)
 // ---------------------------------------------------------------------------
 
+#ifndef SPHMP_ALPHA_SUMS
+#define SPHMP_ALPHA_SUMS 0
+#endif
+
 // Alpha change of one in-grid fluid particle (contributeAlphaChange), Kahan-
 // compensated per phase. `pair` takes the neighbour's pos4, md = mass * (1/rho)
 // (zero for boundary neighbours, which exchange no volume fraction), veleval,
 // alpha4 and drift velocities.
+//
+// Per pair and phase k the reference adds
+//   -(0.5 cm (a_jk + a_ik) dot1) - cm (a_jk u_jk + a_ik u_ik) . d
+// with cm the kernel-gradient factor times md and dot1 = (v_j - v_i) . d. The
+// terms in a_ik are the particle's own fraction times the sums S_dot = sum cm
+// dot1 and S_d = sum cm d, which are taken once for all phases; the neighbour
+// terms -cm a_jk (0.5 dot1 + u_jk . d) are summed per phase (Kahan), and
+// result() adds -a_ik (0.5 S_dot + u_ik . S_d) to each phase's compensated sum.
 template <int NP>
 struct AlphaChange {
     float4 pi, vei;
     float ia[3];
     float3 um[NP];
     Kahan acc[NP];
+    const float4* udrift;  // the particle's own drift velocity of phase k at udrift[k * ustride]
+    size_t ustride;
+#if SPHMP_ALPHA_SUMS
+    float sdot = 0.f, sdx = 0.f, sdy = 0.f, sdz = 0.f;
+#endif
 
-    __device__ __forceinline__ void init(const float4 pi_, const float4 vei_, const float4 ai, const float3* um_) {
+    __device__ __forceinline__ void load_own_drift() {
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const float4 u = udrift[(size_t)k * ustride];
+            um[k] = make_float3(u.x, u.y, u.z);
+        }
+    }
+
+    // u is the particle's drift velocity of phase 0 (phase k at u[k * stride]);
+    // with the factored sums it is read after the neighbour walk.
+    __device__ __forceinline__ void init(const float4 pi_, const float4 vei_, const float4 ai, const float4* u,
+                                         size_t stride) {
         pi = pi_;
         vei = vei_;
         ia[0] = ai.x; ia[1] = ai.y; ia[2] = ai.z;
-#pragma unroll
-        for (int k = 0; k < NP; k++) um[k] = um_[k];
+        udrift = u;
+        ustride = stride;
+        if (!SPHMP_ALPHA_SUMS) load_own_drift();
     }
 
     __device__ __forceinline__ void pair(const DevParams& P, const float4 pj, const float md, const float4 vej,
@@ -556,6 +605,18 @@ struct AlphaChange {
         const float cm = P.kspikydiff * c * c * rinv * md;
         const float dot1 = (vej.x - vei.x) * dx + (vej.y - vei.y) * dy + (vej.z - vei.z) * dz;
         const float ja[3] = {aj.x, aj.y, aj.z};
+#if SPHMP_ALPHA_SUMS
+        sdot += cm * dot1;
+        sdx += cm * dx;
+        sdy += cm * dy;
+        sdz += cm * dz;
+        const float hd = 0.5f * dot1;
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            const float ud = uj[k].x * dx + uj[k].y * dy + uj[k].z * dz;
+            acc[k].add(-(cm * (ja[k] * (hd + ud))));
+        }
+#else
 #pragma unroll
         for (int k = 0; k < NP; k++) {
             acc[k].add(-(0.5f * cm * (ja[k] + ia[k]) * dot1));
@@ -564,6 +625,7 @@ struct AlphaChange {
             const float vz = ja[k] * uj[k].z + ia[k] * um[k].z;
             acc[k].add(-(cm * (vx * dx + vy * dy + vz * dz)));
         }
+#endif
     }
 
     // Sum the lanes' compensated partial sums (warp-cooperative particles).
@@ -573,12 +635,23 @@ struct AlphaChange {
             acc[k].s = warp_sum_f(acc[k].s - acc[k].c);
             acc[k].c = 0.f;
         }
+#if SPHMP_ALPHA_SUMS
+        sdot = warp_sum_f(sdot);
+        sdx = warp_sum_f(sdx);
+        sdy = warp_sum_f(sdy);
+        sdz = warp_sum_f(sdz);
+#endif
     }
 
     // dalpha * dt clamped at -0.99, added to the start-of-step fraction.
-    __device__ __forceinline__ void result(const DevParams& P, float (&out)[3]) const {
+    __device__ __forceinline__ void result(const DevParams& P, float (&out)[3]) {
+        if (SPHMP_ALPHA_SUMS) load_own_drift();
 #pragma unroll
         for (int k = 0; k < NP; k++) {
+#if SPHMP_ALPHA_SUMS
+            const float own = 0.5f * sdot + (um[k].x * sdx + um[k].y * sdy + um[k].z * sdz);
+            acc[k].add(-(ia[k] * own));
+#endif
             float ch = acc[k].s * P.dt;
             // `ch < -0.99` in double is exactly `ch <= -0.99f` in float
             if (ch <= -0.99f) ch = -0.99f;

@@ -596,6 +596,9 @@ __device__ __forceinline__ uint32_t seq_index(const uint32_t* rstart, const uint
 }
 
 constexpr int kBucketChunks = 8;
+#ifndef SPHMP_ODD_TAIL
+#define SPHMP_ODD_TAIL 0
+#endif
 
 __device__ __forceinline__ uint32_t next_bucket(uint32_t* ctr, unsigned lane) {
     uint32_t v = 0;
@@ -705,6 +708,24 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
                 uint32_t mine = 0;  // lane k keeps the mask word of chunk k
 #pragma unroll
                 for (int pr = 0; pr < kBucketChunks / 2; pr++) {
+#if SPHMP_ODD_TAIL
+                    if (2 * pr + 1 == nch) {  // a last chunk without a partner: scalar arithmetic
+                        float dx = __fadd_rn(px, NX[pr].x), dy = __fadd_rn(py, NY[pr].x), dz = __fadd_rn(pz, NZ[pr].x);
+                        if (!SS1) {
+                            dx = __fmul_rn(dx, ss);
+                            dy = __fmul_rn(dy, ss);
+                            dz = __fmul_rn(dz, ss);
+                        }
+                        float dsq = __fmul_rn(dx, dx);
+                        dsq = __fmaf_rn(dy, dy, dsq);
+                        dsq = __fmaf_rn(dz, dz, dsq);
+                        const float cc = fmaxf(__fmaf_rn(dsq, -1.f, r2), 0.f);
+                        const float c3 = __fmul_rn(__fmul_rn(cc, cc), cc);
+                        acc.x = __fmaf_rn(c3, __fmaf_rn(rho0, CV[pr].x, CW[pr].x), acc.x);
+                        const uint32_t b0 = __ballot_sync(0xffffffffu, dsq < r2list);
+                        mine = lane == (unsigned)(2 * pr) ? b0 : mine;
+                    } else
+#endif
                     if (2 * pr < nch) {
                         float2 dx = __fadd2_rn(PX, NX[pr]), dy = __fadd2_rn(PY, NY[pr]), dz = __fadd2_rn(PZ, NZ[pr]);
                         if (!SS1) {
@@ -1078,14 +1099,8 @@ __device__ __forceinline__ void alpha_change_slot(const DevParams& P, const DevB
                                                   const float4* __restrict__ pos4, const float4* __restrict__ vev4,
                                                   const float4* __restrict__ alpha4, int s, const float4 pi,
                                                   const float4 vei, const float4 ai, float (&out)[3]) {
-    float3 um[NP];
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        const float4 u = B.drift4[(size_t)k * P.cap + s];
-        um[k] = make_float3(u.x, u.y, u.z);
-    }
     AlphaChange<NP> acc;
-    acc.init(pi, vei, ai, um);
+    acc.init(pi, vei, ai, B.drift4 + s, (size_t)P.cap);
     for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
         // every load first, so that consecutive neighbours' gathers overlap
         const float4 pj = __ldg(&pos4[j]);
@@ -1174,18 +1189,12 @@ __global__ void __launch_bounds__(kThreads) k_advance(const __grid_constant__ De
 template <int NP>
 __device__ __forceinline__ void alpha_change_nrec(const DevParams& P, const DevBuffers& B, int s, const float4 pi,
                                                   const float4 vei, const float4 ai, float (&out)[3]) {
-    float3 um[NP];
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        const float4 u = B.drift4[(size_t)k * P.cap + s];
-        um[k] = make_float3(u.x, u.y, u.z);
-    }
     AlphaChange<NP> acc;
-    acc.init(pi, vei, ai, um);
+    acc.init(pi, vei, ai, B.drift4 + s, (size_t)P.cap);
     for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
-        const float4* __restrict__ r = B.nrec + (size_t)j * kNrecFloat4;
-        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
-        const float4 r4 = NP > 2 ? __ldg(r + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 q[5];
+        read_nrec<NP>(B, j, q);
+        const float4 r0 = q[0], r1 = q[1], r2 = q[2], r3 = q[3], r4 = q[4];
         float4 uj[NP];
         uj[0] = make_float4(r2.z, r2.w, r3.x, 0.f);
         if (NP > 1) uj[NP > 1 ? 1 : 0] = make_float4(r3.y, r3.z, r3.w, 0.f);
@@ -1201,18 +1210,12 @@ template <int NP>
 __device__ __forceinline__ void alpha_change_nrec_warp(const DevParams& P, const DevBuffers& B, const F4Set& S, int s,
                                                        float (&out)[3]) {
     const float4 pi = S.in[POS][s], vei = S.in[VEV][s], ai = S.in[ALPHA][s];
-    float3 um[NP];
-#pragma unroll
-    for (int k = 0; k < NP; k++) {
-        const float4 u = B.drift4[(size_t)k * P.cap + s];
-        um[k] = make_float3(u.x, u.y, u.z);
-    }
     AlphaChange<NP> acc;
-    acc.init(pi, vei, ai, um);
+    acc.init(pi, vei, ai, B.drift4 + s, (size_t)P.cap);
     warp_for_slot_list(P, B, s, pi.x, pi.y, pi.z, [&](uint32_t j) {
-        const float4* __restrict__ r = B.nrec + (size_t)j * kNrecFloat4;
-        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
-        const float4 r4 = NP > 2 ? __ldg(r + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 q[5];
+        read_nrec<NP>(B, j, q);
+        const float4 r0 = q[0], r1 = q[1], r2 = q[2], r3 = q[3], r4 = q[4];
         float4 uj[NP];
         uj[0] = make_float4(r2.z, r2.w, r3.x, 0.f);
         if (NP > 1) uj[NP > 1 ? 1 : 0] = make_float4(r3.y, r3.z, r3.w, 0.f);
