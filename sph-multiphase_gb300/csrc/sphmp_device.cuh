@@ -546,10 +546,6 @@ struct ProjectU {
 // Volume-fraction advance (MfComputeAlphaAdvanceCUDA)
 // ---------------------------------------------------------------------------
 
-#ifndef SPHMP_ALPHA_SUMS
-#define SPHMP_ALPHA_SUMS 0
-#endif
-
 // Alpha change of one in-grid fluid particle (contributeAlphaChange), Kahan-
 // compensated per phase. `pair` takes the neighbour's pos4, md = mass * (1/rho)
 // (zero for boundary neighbours, which exchange no volume fraction), veleval,
@@ -566,24 +562,13 @@ template <int NP>
 struct AlphaChange {
     float4 pi, vei;
     float ia[3];
-    float3 um[NP];
     Kahan acc[NP];
     const float4* udrift;  // the particle's own drift velocity of phase k at udrift[k * ustride]
     size_t ustride;
-#if SPHMP_ALPHA_SUMS
     float sdot = 0.f, sdx = 0.f, sdy = 0.f, sdz = 0.f;
-#endif
 
-    __device__ __forceinline__ void load_own_drift() {
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            const float4 u = udrift[(size_t)k * ustride];
-            um[k] = make_float3(u.x, u.y, u.z);
-        }
-    }
-
-    // u is the particle's drift velocity of phase 0 (phase k at u[k * stride]);
-    // with the factored sums it is read after the neighbour walk.
+    // u is the particle's drift velocity of phase 0 (phase k at u[k * stride]),
+    // read after the neighbour walk, in result().
     __device__ __forceinline__ void init(const float4 pi_, const float4 vei_, const float4 ai, const float4* u,
                                          size_t stride) {
         pi = pi_;
@@ -591,7 +576,6 @@ struct AlphaChange {
         ia[0] = ai.x; ia[1] = ai.y; ia[2] = ai.z;
         udrift = u;
         ustride = stride;
-        if (!SPHMP_ALPHA_SUMS) load_own_drift();
     }
 
     __device__ __forceinline__ void pair(const DevParams& P, const float4 pj, const float md, const float4 vej,
@@ -605,7 +589,6 @@ struct AlphaChange {
         const float cm = P.kspikydiff * c * c * rinv * md;
         const float dot1 = (vej.x - vei.x) * dx + (vej.y - vei.y) * dy + (vej.z - vei.z) * dz;
         const float ja[3] = {aj.x, aj.y, aj.z};
-#if SPHMP_ALPHA_SUMS
         sdot += cm * dot1;
         sdx += cm * dx;
         sdy += cm * dy;
@@ -616,16 +599,6 @@ struct AlphaChange {
             const float ud = uj[k].x * dx + uj[k].y * dy + uj[k].z * dz;
             acc[k].add(-(cm * (ja[k] * (hd + ud))));
         }
-#else
-#pragma unroll
-        for (int k = 0; k < NP; k++) {
-            acc[k].add(-(0.5f * cm * (ja[k] + ia[k]) * dot1));
-            const float vx = ja[k] * uj[k].x + ia[k] * um[k].x;
-            const float vy = ja[k] * uj[k].y + ia[k] * um[k].y;
-            const float vz = ja[k] * uj[k].z + ia[k] * um[k].z;
-            acc[k].add(-(cm * (vx * dx + vy * dy + vz * dz)));
-        }
-#endif
     }
 
     // Sum the lanes' compensated partial sums (warp-cooperative particles).
@@ -635,23 +608,19 @@ struct AlphaChange {
             acc[k].s = warp_sum_f(acc[k].s - acc[k].c);
             acc[k].c = 0.f;
         }
-#if SPHMP_ALPHA_SUMS
         sdot = warp_sum_f(sdot);
         sdx = warp_sum_f(sdx);
         sdy = warp_sum_f(sdy);
         sdz = warp_sum_f(sdz);
-#endif
     }
 
     // dalpha * dt clamped at -0.99, added to the start-of-step fraction.
     __device__ __forceinline__ void result(const DevParams& P, float (&out)[3]) {
-        if (SPHMP_ALPHA_SUMS) load_own_drift();
 #pragma unroll
         for (int k = 0; k < NP; k++) {
-#if SPHMP_ALPHA_SUMS
-            const float own = 0.5f * sdot + (um[k].x * sdx + um[k].y * sdy + um[k].z * sdz);
+            const float4 um = udrift[(size_t)k * ustride];
+            const float own = 0.5f * sdot + (um.x * sdx + um.y * sdy + um.z * sdz);
             acc[k].add(-(ia[k] * own));
-#endif
             float ch = acc[k].s * P.dt;
             // `ch < -0.99` in double is exactly `ch <= -0.99f` in float
             if (ch <= -0.99f) ch = -0.99f;

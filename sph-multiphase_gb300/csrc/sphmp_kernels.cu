@@ -17,6 +17,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "sphmp_device.cuh"
 #include "sphmp_features.cuh"
 #include "sphmp_emit.h"
@@ -596,9 +598,6 @@ __device__ __forceinline__ uint32_t seq_index(const uint32_t* rstart, const uint
 }
 
 constexpr int kBucketChunks = 8;
-#ifndef SPHMP_ODD_TAIL
-#define SPHMP_ODD_TAIL 0
-#endif
 
 __device__ __forceinline__ uint32_t next_bucket(uint32_t* ctr, unsigned lane) {
     uint32_t v = 0;
@@ -675,9 +674,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
         const float2 R2 = make_float2(r2, r2), NEG1 = make_float2(-1.f, -1.f);
         for (uint32_t base = 0; base < T; base += 32u * kBucketChunks) {
             // chunks 2p and 2p + 1 side by side in float2 pairs (packed FP32 arithmetic):
-            // negated coordinates, fluid mass (0 for boundary), boundary volume (0 for fluid)
-            float2 NX[kBucketChunks / 2], NY[kBucketChunks / 2], NZ[kBucketChunks / 2];
-            float2 CW[kBucketChunks / 2], CV[kBucketChunks / 2];
+            // negated coordinates and w (fluid mass > 0, minus the boundary volume < 0; 0 for padding)
+            float2 NX[kBucketChunks / 2], NY[kBucketChunks / 2], NZ[kBucketChunks / 2], CW[kBucketChunks / 2];
+            bool bnd = false;
 #pragma unroll
             for (int pr = 0; pr < kBucketChunks / 2; pr++) {
                 float4 c2[2];
@@ -686,76 +685,79 @@ __global__ void __launch_bounds__(kThreads, 4) k_density_bucket(const __grid_con
                     const uint32_t e = base + lane + 32u * (2 * pr + h);
                     c2[h] = make_float4(kFar, kFar, kFar, 0.f);
                     if (e < T) c2[h] = __ldg(&pos4[seq_index(rstart, roff, r, e)]);
+                    bnd |= c2[h].w < 0.f;
                 }
                 NX[pr] = make_float2(-c2[0].x, -c2[1].x);
                 NY[pr] = make_float2(-c2[0].y, -c2[1].y);
                 NZ[pr] = make_float2(-c2[0].z, -c2[1].z);
-                CW[pr] = make_float2(fmaxf(c2[0].w, 0.f), fmaxf(c2[1].w, 0.f));
-                CV[pr] = make_float2(fmaxf(-c2[0].w, 0.f), fmaxf(-c2[1].w, 0.f));
+                CW[pr] = make_float2(c2[0].w, c2[1].w);
             }
             const int nch = (int)min((T - base + 31u) >> 5, (uint32_t)kBucketChunks);
             const uint32_t word0 = base >> 5;
-            for (uint32_t fm = fluid; fm != 0u; fm &= fm - 1u) {
-                const int i = __ffs(fm) - 1;
-                const float px = __shfl_sync(0xffffffffu, pm.x, i);
-                const float py = __shfl_sync(0xffffffffu, pm.y, i);
-                const float pz = __shfl_sync(0xffffffffu, pm.z, i);
-                const float rho0 = __shfl_sync(0xffffffffu, rm, i);
-                const float2 PX = make_float2(px, px), PY = make_float2(py, py), PZ = make_float2(pz, pz);
-                const float2 RHO = make_float2(rho0, rho0);
-                const uint32_t t = w0 + (uint32_t)i;
-                float2 acc = make_float2(0.f, 0.f);
-                uint32_t mine = 0;  // lane k keeps the mask word of chunk k
+            // The member loop, with boundary candidates in the block or without (the usual case:
+            // no volume weights and no rest density to broadcast, so fewer live registers).
+            // The weight of a candidate is its mass, or rho0 V for a boundary particle; without
+            // boundary candidates rho0 * 0 + m is m exactly, so both forms give the same sums.
+            auto members = [&](auto with_boundary) {
+                constexpr bool BND = decltype(with_boundary)::value;
+                float2 CM[kBucketChunks / 2], CV[kBucketChunks / 2];
 #pragma unroll
                 for (int pr = 0; pr < kBucketChunks / 2; pr++) {
-#if SPHMP_ODD_TAIL
-                    if (2 * pr + 1 == nch) {  // a last chunk without a partner: scalar arithmetic
-                        float dx = __fadd_rn(px, NX[pr].x), dy = __fadd_rn(py, NY[pr].x), dz = __fadd_rn(pz, NZ[pr].x);
-                        if (!SS1) {
-                            dx = __fmul_rn(dx, ss);
-                            dy = __fmul_rn(dy, ss);
-                            dz = __fmul_rn(dz, ss);
-                        }
-                        float dsq = __fmul_rn(dx, dx);
-                        dsq = __fmaf_rn(dy, dy, dsq);
-                        dsq = __fmaf_rn(dz, dz, dsq);
-                        const float cc = fmaxf(__fmaf_rn(dsq, -1.f, r2), 0.f);
-                        const float c3 = __fmul_rn(__fmul_rn(cc, cc), cc);
-                        acc.x = __fmaf_rn(c3, __fmaf_rn(rho0, CV[pr].x, CW[pr].x), acc.x);
-                        const uint32_t b0 = __ballot_sync(0xffffffffu, dsq < r2list);
-                        mine = lane == (unsigned)(2 * pr) ? b0 : mine;
-                    } else
-#endif
-                    if (2 * pr < nch) {
-                        float2 dx = __fadd2_rn(PX, NX[pr]), dy = __fadd2_rn(PY, NY[pr]), dz = __fadd2_rn(PZ, NZ[pr]);
-                        if (!SS1) {
-                            const float2 SS = make_float2(ss, ss);
-                            dx = __fmul2_rn(dx, SS);
-                            dy = __fmul2_rn(dy, SS);
-                            dz = __fmul2_rn(dz, SS);
-                        }
-                        float2 dsq = __fmul2_rn(dx, dx);
-                        dsq = __ffma2_rn(dy, dy, dsq);
-                        dsq = __ffma2_rn(dz, dz, dsq);
-                        float2 cc = __ffma2_rn(dsq, NEG1, R2);  // r2 - dsq, rounded once
-                        cc.x = fmaxf(cc.x, 0.f);                // 0 outside h (and for the padding lanes)
-                        cc.y = fmaxf(cc.y, 0.f);
-                        const float2 c3 = __fmul2_rn(__fmul2_rn(cc, cc), cc);
-                        acc = __ffma2_rn(c3, __ffma2_rn(RHO, CV[pr], CW[pr]), acc);
-                        // coincident particles stay in the list (every consumer skips r == 0);
-                        // the member itself is cleared below
-                        const uint32_t b0 = __ballot_sync(0xffffffffu, dsq.x < r2list);
-                        const uint32_t b1 = __ballot_sync(0xffffffffu, dsq.y < r2list);
-                        mine = lane == (unsigned)(2 * pr) ? b0 : mine;
-                        mine = lane == (unsigned)(2 * pr + 1) ? b1 : mine;
+                    CM[pr] = CW[pr];
+                    CV[pr] = make_float2(0.f, 0.f);
+                    if (BND) {
+                        CM[pr] = make_float2(fmaxf(CW[pr].x, 0.f), fmaxf(CW[pr].y, 0.f));
+                        CV[pr] = make_float2(fmaxf(-CW[pr].x, 0.f), fmaxf(-CW[pr].y, 0.f));
                     }
                 }
-                const uint32_t es = t + self_base - base;  // the member's own bit, if in this block
-                if (es < 32u * kBucketChunks && lane == (es >> 5)) mine &= ~(1u << (es & 31u));
-                if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
-                const float part = warp_sum_f(acc.x + acc.y);
-                if (lane == (unsigned)i) msum.add(part);
-            }
+                for (uint32_t fm = fluid; fm != 0u; fm &= fm - 1u) {
+                    const int i = __ffs(fm) - 1;
+                    const float px = __shfl_sync(0xffffffffu, pm.x, i);
+                    const float py = __shfl_sync(0xffffffffu, pm.y, i);
+                    const float pz = __shfl_sync(0xffffffffu, pm.z, i);
+                    const float rho0 = BND ? __shfl_sync(0xffffffffu, rm, i) : 0.f;
+                    const float2 PX = make_float2(px, px), PY = make_float2(py, py), PZ = make_float2(pz, pz);
+                    const float2 RHO = make_float2(rho0, rho0);
+                    const uint32_t t = w0 + (uint32_t)i;
+                    float2 acc = make_float2(0.f, 0.f);
+                    uint32_t mine = 0;  // lane k keeps the mask word of chunk k
+#pragma unroll
+                    for (int pr = 0; pr < kBucketChunks / 2; pr++) {
+                        if (2 * pr < nch) {
+                            float2 dx = __fadd2_rn(PX, NX[pr]), dy = __fadd2_rn(PY, NY[pr]), dz = __fadd2_rn(PZ, NZ[pr]);
+                            if (!SS1) {
+                                const float2 SS = make_float2(ss, ss);
+                                dx = __fmul2_rn(dx, SS);
+                                dy = __fmul2_rn(dy, SS);
+                                dz = __fmul2_rn(dz, SS);
+                            }
+                            float2 dsq = __fmul2_rn(dx, dx);
+                            dsq = __ffma2_rn(dy, dy, dsq);
+                            dsq = __ffma2_rn(dz, dz, dsq);
+                            float2 cc = __ffma2_rn(dsq, NEG1, R2);  // r2 - dsq, rounded once
+                            cc.x = fmaxf(cc.x, 0.f);                // 0 outside h (and for the padding lanes)
+                            cc.y = fmaxf(cc.y, 0.f);
+                            const float2 c3 = __fmul2_rn(__fmul2_rn(cc, cc), cc);
+                            acc = __ffma2_rn(c3, BND ? __ffma2_rn(RHO, CV[pr], CM[pr]) : CM[pr], acc);
+                            // coincident particles stay in the list (every consumer skips r == 0);
+                            // the member itself is cleared below
+                            const uint32_t b0 = __ballot_sync(0xffffffffu, dsq.x < r2list);
+                            const uint32_t b1 = __ballot_sync(0xffffffffu, dsq.y < r2list);
+                            mine = lane == (unsigned)(2 * pr) ? b0 : mine;
+                            mine = lane == (unsigned)(2 * pr + 1) ? b1 : mine;
+                        }
+                    }
+                    const uint32_t es = t + self_base - base;  // the member's own bit, if in this block
+                    if (es < 32u * kBucketChunks && lane == (es >> 5)) mine &= ~(1u << (es & 31u));
+                    if (masked && (int)lane < nch) B.nmask[(size_t)(word0 + lane) * cap + t] = mine;
+                    const float part = warp_sum_f(acc.x + acc.y);
+                    if (lane == (unsigned)i) msum.add(part);
+                }
+            };
+            if (__any_sync(0xffffffffu, bnd))
+                members(std::true_type{});
+            else
+                members(std::false_type{});
         }
         if (tl < w1 && pm.w >= 0.f) {
             B.nbr_cnt[tl] = lst;

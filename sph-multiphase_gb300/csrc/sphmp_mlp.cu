@@ -410,8 +410,12 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
                     for (int i = 0; i < 16; i++)
                         sb_out.dzt[(size_t)(c0 + i) * sb_out.ldt + row] = __float2bfloat16_rn(h[i]);
                 } else {
+                    // four 16-byte stores per 16 columns (N is a multiple of 16, the partials 16-byte aligned)
+                    float4* d4 = reinterpret_cast<float4*>(drow + c0);
 #pragma unroll
-                    for (int i = 0; i < 16; i++) drow[c0 + i] = chunks ? v[i] : 0.f;
+                    for (int q = 0; q < 4; q++)
+                        d4[q] = chunks ? make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3])
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
                 }
             }
         }
