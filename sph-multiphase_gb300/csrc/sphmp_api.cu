@@ -721,7 +721,10 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     c->oct_valid = false;
     c->oct_built = false;
     c->pos_sorted = false;
-    drop_graph(c);
+    // a captured step serves any state of the same count (it starts with the
+    // sort and restores the buffer selectors), so it survives an upload of the
+    // same number of records; sphmp_step re-captures when the count differs
+    if (c->graph_n != (c->emit_on ? -2 : end)) drop_graph(c);
     CK(cudaStreamSynchronize(c->stream));
     return take_device_errors(c, nullptr);
 }
