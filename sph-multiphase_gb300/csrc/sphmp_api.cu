@@ -45,6 +45,7 @@ struct sphmp_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_n = -1;
     int graph_schedule = -1;
+    int graph_cur[kNumFloat4Fields] = {0, 0, 0, 0, 0};  // the buffer selectors the graph was captured with
     // asynchronous display downloads: two device staging buffers, copied to the
     // host on a separate stream while the context stream runs on
     cudaStream_t copy_stream = nullptr;
@@ -279,7 +280,7 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(cudaMemset(B.iis_dijpj, 0, sizeof(float4) * N));
     CK(cudaMemset(B.iis_pl, 0, sizeof(float) * N));
     CK(cudaMemset(B.iis_res, 0, sizeof(float) * N));
-    CK(dalloc(&B.nrec, (size_t)kNrecFloat4 * N));
+    CK(dalloc(&B.nrec, (size_t)kNrecFloat4 * N + 2));  // + 32 bytes: the alpha pass reads records 32 bytes at a time
     CK(dalloc(&B.opos, N));
     CK(dalloc(&B.oidx, N));
     CK(dalloc(&B.osrc, N));
@@ -721,9 +722,10 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
     c->oct_valid = false;
     c->oct_built = false;
     c->pos_sorted = false;
-    // a captured step serves any state of the same count (it starts with the
-    // sort and restores the buffer selectors), so it survives an upload of the
-    // same number of records; sphmp_step re-captures when the count differs
+    // a captured step serves any state of the same count and buffer selectors
+    // (it starts with the sort and restores the selectors), so it survives an
+    // upload of the same number of records; sphmp_step re-captures when the
+    // count or a selector differs
     if (c->graph_n != (c->emit_on ? -2 : end)) drop_graph(c);
     CK(cudaStreamSynchronize(c->stream));
     return take_device_errors(c, nullptr);
@@ -1275,7 +1277,12 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
     if (use_graph && nsteps >= per) {
         // with a device emitter the graph runs over the capacity and serves any count
         const int key = c->emit_on ? -2 : c->n;
-        if (!c->graph || c->graph_n != key || c->graph_schedule != schedule) {
+        // the graph reads and writes the buffers selected at capture: any host call
+        // that flipped a selector an odd number of times since (an eager step of
+        // the reference order, a per-pass call, the sort before the first step)
+        // needs a new capture
+        if (!c->graph || c->graph_n != key || c->graph_schedule != schedule ||
+            memcmp(c->graph_cur, c->cur, sizeof(c->graph_cur)) != 0) {
             drop_graph(c);
             cudaStream_t cap = c->stream;
             CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
@@ -1302,6 +1309,7 @@ sphmp_status sphmp_step(sphmp_ctx* c, int32_t nsteps, int32_t schedule, int32_t 
             }
             c->graph_n = key;
             c->graph_schedule = schedule;
+            memcpy(c->graph_cur, c->cur, sizeof(c->graph_cur));
         }
         for (int t = 0; t + per <= nsteps; t += per) CK(cudaGraphLaunch(c->graph, c->stream));
         if (c->emit_on) c->n_stale = true;

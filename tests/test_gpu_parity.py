@@ -292,6 +292,54 @@ def test_pass_after_graph_steps_uses_fresh_neighbours():
     assert bits_equal(res[0]["accel"], res[1]["accel"])
 
 
+def test_graph_after_buffer_flipping_calls_matches_eager():
+    """A captured step reads and writes the double buffers selected when it was
+    captured. Between replays, an eager step of the reference order flips every
+    selector an odd number of times; the next replay must use a graph captured
+    for the new selectors: same bits as the same sequence run eagerly."""
+    sc = _scene("tait3")
+    res = []
+    for use_graph in (False, True):
+        ctx = device_ctx(sc)
+        ctx.before_first_step()
+        ctx.step(1, abi.SCHEDULE_FUSED, use_graph=use_graph)  # with a graph: captured here
+        ctx.step(1, abi.SCHEDULE_REFERENCE, use_graph=False)  # odd number of selector flips
+        ctx.step(2, abi.SCHEDULE_FUSED, use_graph=use_graph)
+        ctx.sync()
+        res.append(download_state(ctx))
+        ctx.close()
+    for name in ("pos", "vel", "dens", "alpha", "accel"):
+        assert bits_equal(res[0][name], res[1][name]), name
+
+
+def test_graph_survives_a_reupload_and_first_sort():
+    """The end-to-end pattern: steps from a captured graph, then the same records
+    uploaded again and the first-step sort (which flips the selectors), then more
+    graph steps: same bits as a fresh context running the second part eagerly."""
+    sc = _scene("tait3")
+    calc = sc.calc.copy()
+    bnd = sc.disp["type"] == 1
+    calc["accel"][bnd] = 0
+    calc["pressure"][bnd] = 0
+    ctx = device_ctx(sc)
+    ctx.before_first_step()
+    ctx.step(3, abi.SCHEDULE_FUSED, use_graph=True)
+    ctx.upload_aos(sc.disp, calc)
+    ctx.before_first_step()
+    ctx.step(3, abi.SCHEDULE_FUSED, use_graph=True)
+    ctx.sync()
+    got = download_state(ctx)
+    ctx.close()
+    ref = device_ctx(sc)
+    ref.before_first_step()
+    ref.step(3, abi.SCHEDULE_FUSED, use_graph=False)
+    ref.sync()
+    want = download_state(ref)
+    ref.close()
+    for name in ("pos", "vel", "dens", "alpha", "accel"):
+        assert bits_equal(got[name], want[name]), name
+
+
 def test_passes_after_advance_without_resort_match_oracle():
     """MfComputePressure / MfComputeForce called after an advance with no new sort:
     the neighbour loops scan the 27 cells around each particle's cell from the
