@@ -280,7 +280,7 @@ sphmp_status alloc_buffers(sphmp_ctx* c) {
     CK(cudaMemset(B.iis_dijpj, 0, sizeof(float4) * N));
     CK(cudaMemset(B.iis_pl, 0, sizeof(float) * N));
     CK(cudaMemset(B.iis_res, 0, sizeof(float) * N));
-    CK(dalloc(&B.nrec, (size_t)kNrecFloat4 * N + 2));  // + 32 bytes: the alpha pass reads records 32 bytes at a time
+    CK(dalloc(&B.nrec, (size_t)kNrecFloat4 * N));
     CK(dalloc(&B.opos, N));
     CK(dalloc(&B.oidx, N));
     CK(dalloc(&B.osrc, N));

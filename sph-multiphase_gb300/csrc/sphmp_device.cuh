@@ -289,45 +289,18 @@ __device__ __forceinline__ void write_nrec(const DevBuffers& B, int s, const flo
     r[4] = make_float4(u[6], u[7], u[8], 0.f);
 }
 
-#ifndef SPHMP_NREC_V8
-#define SPHMP_NREC_V8 1
-#endif
-
-// A 32-byte load (sm_100 and later): one instruction and one sector per lane.
-// The address must be 32-byte aligned.
-__device__ __forceinline__ void ldg_v8(const float4* p, float4& a, float4& b) {
-    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-        : "l"(p));
-}
-
 // The five float4 of neighbour j's record (the fifth only with three phases).
-// Records are 80 bytes apart, so record j starts on a 32-byte boundary for even
-// j and 16 bytes past one for odd j: three 32-byte loads from the boundary at or
-// below the record cover it either way (three sector requests per lane instead of
-// five 16-byte loads), and the record is the six halves shifted by one for odd j.
-// The last record's third load reads 16 bytes past it: the array is allocated
-// with two float4 of padding.
+// (Reading the 80-byte records with three aligned 32-byte loads from the
+// 32-byte boundary at or below each record measured slower: 0.306 against
+// 0.291 ms per alpha pass at full size.)
 template <int NP>
 __device__ __forceinline__ void read_nrec(const DevBuffers& B, uint32_t j, float4 (&q)[5]) {
     const float4* __restrict__ r = B.nrec + (size_t)j * kNrecFloat4;
-#if SPHMP_NREC_V8
-    const bool odd = (j & 1u) != 0u;
-    const float4* a = r - (odd ? 1 : 0);
-    float4 h[6];
-    ldg_v8(a, h[0], h[1]);
-    ldg_v8(a + 2, h[2], h[3]);
-    ldg_v8(a + 4, h[4], h[5]);
-#pragma unroll
-    for (int k = 0; k < 5; k++) q[k] = odd ? h[k + 1] : h[k];
-    if (NP <= 2) q[4] = make_float4(0.f, 0.f, 0.f, 0.f);
-#else
     q[0] = __ldg(r);
     q[1] = __ldg(r + 1);
     q[2] = __ldg(r + 2);
     q[3] = __ldg(r + 3);
     q[4] = NP > 2 ? __ldg(r + 4) : make_float4(0.f, 0.f, 0.f, 0.f);
-#endif
 }
 
 // Accumulates the force (contributeForce_new) and / or the drift-velocity terms
