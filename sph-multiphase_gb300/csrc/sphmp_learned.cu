@@ -15,6 +15,10 @@
 #include "sphmp.h"
 #include "sphmp_device.cuh"
 #include "sphmp_internal.h"
+
+#ifndef SPHMP_FUSED_BACKWARD
+#define SPHMP_FUSED_BACKWARD 1
+#endif
 #include "sphmp_learned.h"
 #include "sphmp_mlp.h"
 
@@ -189,6 +193,7 @@ struct sphmp_corrector {
     // A operand (declared __restrict__) and writes the other
     bf16 *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
     float* part = nullptr;      // split-K partials
+    float* bpart = nullptr;     // the fused backward's per-CTA gradient partials [num_sms][kParams]
     float* rpart = nullptr;     // row-sum partials
     float* loss_part = nullptr;
     float* loss = nullptr;
@@ -257,6 +262,10 @@ sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t
     LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
     LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
     float* g = c->grads;
+#if SPHMP_FUSED_BACKWARD
+    LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, g, c->err, c->num_sms, s));
+    return SPHMP_OK;
+#endif
     const int kSplitK = split_k(batch);
     // layer 4: dW4 = dY^T H3, db4, dH3 = dY W4
     LCK(launch_gemm_tn(c->dyt, ld, c->h3t, ld, c->part, kOutPad, kHidden, batch, kSplitK, c->err, s));
@@ -333,6 +342,7 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
         A(&c->dz, B * kHidden); A(&c->dz2, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
         A(&c->part, (size_t)kMaxSplitK * kHidden * kHidden);
+        A(&c->bpart, (size_t)c->num_sms * kParams);
         A(&c->rpart, (size_t)kRowSumMaxRows * 16);
         A(&c->loss_part, B / 256 + 1);
         A(&c->loss, 1);

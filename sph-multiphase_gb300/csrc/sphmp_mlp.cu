@@ -430,6 +430,270 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// Fused backward: one persistent CTA per SM, 128-row tiles in turn
+// ---------------------------------------------------------------------------
+//
+// For each tile (rows r of the batch), with dY = the output gradient:
+//   dW4^T += H3^T dY          dH3 = dY W4
+//   dZ3 = dH3 * SiLU'(Z3)     dW3 += dZ3^T H2   db3 += sum_r dZ3   dH2 = dZ3 W3
+//   dZ2 = dH2 * SiLU'(Z2)     dW2 += dZ2^T H1   db2 += sum_r dZ2   dH1 = dZ2 W2
+//   dZ1 = dH1 * SiLU'(Z1)     dW1 += dZ1^T H0   db1 += sum_r dZ1
+// The weight and bias gradients accumulate in TMEM over all tiles of the CTA
+// (the bias sums as MMAs against a tile of ones), so nothing but the CTA's
+// final partial sums goes to memory; dH of the current layer lives in the
+// first 128 columns. Operands in shared memory, K-major without swizzling:
+// the weights W4^T, W3^T, W2^T (resident), dY [rows][16] and dY^T [16][rows],
+// dZ [rows][128] and dZ^T [128][rows] (written by the epilogues), and the saved
+// layer inputs H^T [width][rows], double-buffered and copied with cp.async one
+// step ahead of their MMA. The batch is a multiple of 128 rows (no tails).
+constexpr int kBwdThreads = 128;
+constexpr int kBOffW4t = 0;                                   // [128][16]   kc 16
+constexpr int kBOffW3t = kBOffW4t + kHidden * kOutPad * 2;    // [128][128]  kc 128
+constexpr int kBOffW2t = kBOffW3t + kHidden * kHidden * 2;    // [128][128]
+constexpr int kBOffOnes = kBOffW2t + kHidden * kHidden * 2;   // [16][128]   kc 128, all 1
+constexpr int kBOffDy = kBOffOnes + kOutPad * kTile * 2;      // [128][16]   kc 16
+constexpr int kBOffDyt = kBOffDy + kTile * kOutPad * 2;       // [16][128]   kc 128
+constexpr int kBOffDz = kBOffDyt + kOutPad * kTile * 2;       // [128][128]  kc 128
+constexpr int kBOffDzt = kBOffDz + kTile * kHidden * 2;       // [128][128]  kc 128
+constexpr int kBOffH = kBOffDzt + kHidden * kTile * 2;        // 2 x [128][128] kc 128
+constexpr int kBwdSmem = kBOffH + 2 * kHidden * kTile * 2;
+static_assert(kBwdSmem <= 227 * 1024, "shared memory of one CTA");
+static_assert(kBwdSmem > 116 * 1024, "one CTA per SM: the TMEM allocation takes every column");
+// TMEM columns
+constexpr uint32_t kTcDh = 0, kTcW3 = 128, kTcW2 = 256, kTcW1 = 384, kTcW4 = 448, kTcB3 = 464, kTcB2 = 480,
+                   kTcB1 = 496, kBwdTmemCols = 512;
+
+__device__ __forceinline__ void cp_async16(uint8_t* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Copy the tile's columns [row0, row0 + 128) of ht [width][ld] into buf as a
+// K-major operand (width rows, K = 128), 16 bytes per cp.async; one group.
+__device__ __forceinline__ void issue_h_tile(uint8_t* buf, const bf16* ht, int width, int ld, int row0, int tid) {
+    for (int q = tid; q < width * (kTile / 8); q += kBwdThreads) {
+        const int f = q >> 4, j = q & 15;
+        cp_async16(buf + tc::kmajor_offset(f, 8 * j, kTile), ht + (size_t)f * ld + row0 + 8 * j);
+    }
+    cp_async_commit();
+}
+
+// MMA chain D (+)= A B^T, K = 16 * ksteps, A and B K-major with K extent kc
+__device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, int kc, int ksteps, int n,
+                                          bool accumulate) {
+    const uint32_t idesc = tc::idesc_bf16_f32(kTile, n);
+    for (int ks = 0; ks < ksteps; ks++)
+        tc::mma_bf16(d, tc::kmajor_desc(a, kc, ks), tc::kmajor_desc(b, kc, ks), idesc,
+                     (accumulate || ks > 0) ? 1u : 0u);
+}
+
+// Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row, into the
+// dZ operand (unless null) and the dZ^T operand.
+__device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, const float* __restrict__ z,
+                                             int row0, uint8_t* dz, uint8_t* dzt) {
+    const int r = (warp & 3) * 32 + lane;
+    const float4* zr = reinterpret_cast<const float4*>(z + (size_t)(row0 + r) * kHidden);
+#pragma unroll 1
+    for (int c0 = 0; c0 < kHidden; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tc::tmem_lane_addr(tmem_dh, warp, c0), v);
+        float h[16];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const float4 zz = zr[c0 / 4 + q];
+            h[4 * q] = v[4 * q] * silu_grad(zz.x);
+            h[4 * q + 1] = v[4 * q + 1] * silu_grad(zz.y);
+            h[4 * q + 2] = v[4 * q + 2] * silu_grad(zz.z);
+            h[4 * q + 3] = v[4 * q + 3] * silu_grad(zz.w);
+        }
+        if (dz) {
+            uint4 lo, hi;
+            lo.x = pack2(h[0], h[1]); lo.y = pack2(h[2], h[3]); lo.z = pack2(h[4], h[5]); lo.w = pack2(h[6], h[7]);
+            hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
+            *reinterpret_cast<uint4*>(dz + tc::kmajor_offset(r, c0, kHidden)) = lo;
+            *reinterpret_cast<uint4*>(dz + tc::kmajor_offset(r, c0 + 8, kHidden)) = hi;
+        }
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            *reinterpret_cast<bf16*>(dzt + tc::kmajor_offset(c0 + i, r, kTile)) = __float2bfloat16_rn(h[i]);
+    }
+}
+
+// This CTA's partial gradients, in the flat parameter layout: row r of the
+// accumulators is TMEM lane r (thread r).
+__device__ __forceinline__ void bwd_store_partials(uint32_t tmem, int warp, int lane, bool have, const float* db4,
+                                                   float* __restrict__ out) {
+    const int r = (warp & 3) * 32 + lane;
+    auto row = [&](uint32_t col, int ncols, float* dst, int stride) {  // dst[c * stride] = D[r][col + c]
+        for (int c0 = 0; c0 < ncols; c0 += 16) {
+            float v[16];
+            if (have) tc::tmem_ld16(tc::tmem_lane_addr(tmem + col, warp, c0), v);
+#pragma unroll
+            for (int i = 0; i < 16; i++)
+                if (c0 + i < ncols) dst[(size_t)(c0 + i) * stride] = have ? v[i] : 0.f;
+        }
+    };
+    row(kTcW3, kHidden, out + kOffParamW3 + r * kHidden, 1);
+    row(kTcW2, kHidden, out + kOffParamW2 + r * kHidden, 1);
+    row(kTcW1, kFeatures, out + kOffParamW1 + r * kFeatures, 1);
+    row(kTcW4, kOutputs, out + kOffParamW4 + r, kHidden);  // D[h][o] = dW4[o][h]
+    row(kTcB3, 1, out + kOffParamB3 + r, 1);
+    row(kTcB2, 1, out + kOffParamB2 + r, 1);
+    row(kTcB1, 1, out + kOffParamB1 + r, 1);
+    if (r < kOutputs) out[kOffParamB4 + r] = db4[r];
+}
+
+__global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __restrict__ dy, const Saves S,
+                                                                 const bf16* __restrict__ w2t,
+                                                                 const bf16* __restrict__ w3t,
+                                                                 const bf16* __restrict__ w4t, int batch,
+                                                                 float* __restrict__ part, uint32_t* err) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ float db4s[kBwdThreads / 32][kOutputs];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint8_t* hb[2] = {smem + kBOffH, smem + kBOffH + kHidden * kTile * 2};
+    stage_weights(smem + kBOffW4t, w4t, kHidden, kOutPad, tid, kBwdThreads);
+    stage_weights(smem + kBOffW3t, w3t, kHidden, kHidden, tid, kBwdThreads);
+    stage_weights(smem + kBOffW2t, w2t, kHidden, kHidden, tid, kBwdThreads);
+    {
+        const bf16 one = __float2bfloat16_rn(1.f);
+        for (int q = tid; q < kOutPad * kTile; q += kBwdThreads)
+            *reinterpret_cast<bf16*>(smem + kBOffOnes + tc::kmajor_offset(q / kTile, q % kTile, kTile)) = one;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base, kBwdTmemCols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&bar, 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    const uint32_t a_w4t = tc::smem_addr(smem + kBOffW4t), a_w3t = tc::smem_addr(smem + kBOffW3t);
+    const uint32_t a_w2t = tc::smem_addr(smem + kBOffW2t), a_ones = tc::smem_addr(smem + kBOffOnes);
+    const uint32_t a_dy = tc::smem_addr(smem + kBOffDy), a_dyt = tc::smem_addr(smem + kBOffDyt);
+    const uint32_t a_dz = tc::smem_addr(smem + kBOffDz), a_dzt = tc::smem_addr(smem + kBOffDzt);
+    const uint32_t a_h[2] = {tc::smem_addr(hb[0]), tc::smem_addr(hb[1])};
+    const int ntiles = batch / kTile;
+    const int r = (warp & 3) * 32 + lane;
+    float db4[kOutputs] = {0.f, 0.f, 0.f, 0.f};
+    uint32_t parity = 0;
+    bool ok = true;
+    int done = 0;  // tiles of this CTA finished (the accumulators hold data once it is > 0)
+    int t = blockIdx.x;
+    if (t < ntiles) {  // the first tile's H3^T and H2^T
+        issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, t * kTile, tid);
+        issue_h_tile(hb[1], S.h2t, kHidden, S.ldh, t * kTile, tid);
+    }
+    for (; t < ntiles && ok; t += gridDim.x) {
+        const int row0 = t * kTile;
+        const int tn = t + gridDim.x;  // the next tile of this CTA
+        const bool acc = done > 0;
+        // dY [rows][16] and dY^T [16][rows] from the output gradient (bf16 [batch][16], zero padded)
+        {
+            const uint4* src = reinterpret_cast<const uint4*>(dy + (size_t)(row0 + r) * kOutPad);
+            const uint4 lo = src[0], hi = src[1];
+            *reinterpret_cast<uint4*>(smem + kBOffDy + tc::kmajor_offset(r, 0, kOutPad)) = lo;
+            *reinterpret_cast<uint4*>(smem + kBOffDy + tc::kmajor_offset(r, 8, kOutPad)) = hi;
+            const bf16* e = reinterpret_cast<const bf16*>(&lo);
+            const bf16* e2 = reinterpret_cast<const bf16*>(&hi);
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                *reinterpret_cast<bf16*>(smem + kBOffDyt + tc::kmajor_offset(o, r, kTile)) = e[o];
+                *reinterpret_cast<bf16*>(smem + kBOffDyt + tc::kmajor_offset(o + 8, r, kTile)) = e2[o];
+            }
+#pragma unroll
+            for (int o = 0; o < kOutputs; o++) db4[o] += __bfloat162float(e[o]);
+        }
+        cp_async_wait<1>();  // H3^T
+        handoff_to_mma();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            mma_chain(tmem + kTcW4, a_h[0], a_dyt, kTile, kTile / 16, kOutPad, acc);  // dW4^T += H3^T dY
+            mma_chain(tmem + kTcDh, a_dy, a_w4t, kOutPad, 1, kHidden, false);          // dH3 = dY W4
+            tc::mma_commit(&bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        issue_h_tile(hb[0], S.h1t, kHidden, S.ldh, row0, tid);
+        bwd_epilogue(tmem + kTcDh, warp, lane, S.z3, row0, smem + kBOffDz, smem + kBOffDzt);
+        cp_async_wait<1>();  // H2^T
+        handoff_to_mma();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            mma_chain(tmem + kTcW3, a_dzt, a_h[1], kTile, kTile / 16, kHidden, acc);  // dW3 += dZ3^T H2
+            mma_chain(tmem + kTcB3, a_dzt, a_ones, kTile, kTile / 16, kOutPad, acc);  // db3 (every column)
+            mma_chain(tmem + kTcDh, a_dz, a_w3t, kHidden, kHidden / 16, kHidden, false);  // dH2 = dZ3 W3
+            tc::mma_commit(&bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        issue_h_tile(hb[1], S.h0t, kInPad, S.ldh, row0, tid);
+        bwd_epilogue(tmem + kTcDh, warp, lane, S.z2, row0, smem + kBOffDz, smem + kBOffDzt);
+        cp_async_wait<1>();  // H1^T
+        handoff_to_mma();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            mma_chain(tmem + kTcW2, a_dzt, a_h[0], kTile, kTile / 16, kHidden, acc);  // dW2 += dZ2^T H1
+            mma_chain(tmem + kTcB2, a_dzt, a_ones, kTile, kTile / 16, kOutPad, acc);
+            mma_chain(tmem + kTcDh, a_dz, a_w2t, kHidden, kHidden / 16, kHidden, false);  // dH1 = dZ2 W2
+            tc::mma_commit(&bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        if (tn < ntiles) issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, tn * kTile, tid);
+        bwd_epilogue(tmem + kTcDh, warp, lane, S.z1, row0, nullptr, smem + kBOffDzt);
+        if (tn < ntiles) cp_async_wait<1>();  // H0^T (the next tile's H3^T may still be in flight)
+        else cp_async_wait<0>();
+        handoff_to_mma();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            mma_chain(tmem + kTcW1, a_dzt, a_h[1], kTile, kTile / 16, kInPad, acc);  // dW1 += dZ1^T H0
+            mma_chain(tmem + kTcB1, a_dzt, a_ones, kTile, kTile / 16, kOutPad, acc);
+            tc::mma_commit(&bar);
+        }
+        if (!(ok = wait_all(&bar, parity))) break;
+        if (tn < ntiles) issue_h_tile(hb[1], S.h2t, kHidden, S.ldh, tn * kTile, tid);
+        done++;
+    }
+    cp_async_wait<0>();
+    if (!ok) {
+        if (tid == 0) atomicOr(err, kErrMmaTimeout);
+        tc::mbar_wait(&bar, parity ^ 1u, tc::kWaitLimitNs);  // the chain still in flight, bounded
+    }
+    // db4: the sum over this CTA's rows, in a fixed order
+#pragma unroll
+    for (int o = 0; o < kOutputs; o++) {
+        float v = db4[o];
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+        if (lane == 0) db4s[warp][o] = v;
+    }
+    __syncthreads();
+    float db4t[kOutputs];
+#pragma unroll
+    for (int o = 0; o < kOutputs; o++) db4t[o] = db4s[0][o] + db4s[1][o] + db4s[2][o] + db4s[3][o];
+    bwd_store_partials(tmem, warp, lane, ok && done > 0, db4t, part + (size_t)blockIdx.x * kParams);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem_base, kBwdTmemCols);
+}
+
+// grads[p] = sum over the CTAs' partials, in CTA order (one thread per parameter)
+__global__ void k_sum_partials(const float* __restrict__ part, int nparts, float* __restrict__ grads) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= kParams) return;
+    float s = 0.f;
+    for (int k = 0; k < nparts; k++) s += part[(size_t)k * kParams + p];
+    grads[p] = s;
+}
+
+// ---------------------------------------------------------------------------
 // Backward and optimiser helpers
 // ---------------------------------------------------------------------------
 
@@ -661,6 +925,21 @@ cudaError_t launch_row_sum(const bf16* xt, int ld, int rows, int count, float* p
     if ((ld % 8) != 0 || rows > kRowSumMaxRows) return cudaErrorInvalidValue;
     k_row_sum_part<<<dim3(rows, kRowSplits), 256, 0, s>>>(xt, ld, count, part);
     k_row_sum_final<<<1, kRowSumMaxRows, 0, s>>>(part, rows, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_backward(const bf16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
+                            float* grads, uint32_t* err, int num_sms, cudaStream_t s) {
+    // the saved inputs are copied 16 bytes at a time: their row stride must keep that alignment
+    if (batch <= 0 || batch % kTile != 0 || !S.z1 || !S.h0t || S.ldh % 8 != 0 || S.ldh < batch)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdSmem);
+    if (e != cudaSuccess) return e;
+    const int tiles = batch / kTile;
+    const int grid = tiles < num_sms ? tiles : num_sms;
+    k_mlp_backward<<<grid, kBwdThreads, kBwdSmem, s>>>(dy, S, W.w2t, W.w3t, W.w4t, batch, part, err);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_sum_partials<<<(kParams + 255) / 256, 256, 0, s>>>(part, grid, grads);
     return cudaGetLastError();
 }
 

@@ -66,6 +66,11 @@ cudaError_t launch_gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16*
 cudaError_t launch_gemm_silu_back(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int K,
                                   const float* z, __nv_bfloat16* dz, __nv_bfloat16* dzt, int ldt, uint32_t* err,
                                   cudaStream_t s);
+// The whole backward pass after launch_out_grad (fused, one persistent CTA per
+// SM): gradients of every parameter into grads (flat layout). batch a multiple
+// of 128; part: scratch of num_sms * kParams floats.
+cudaError_t launch_backward(const __nv_bfloat16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
+                            float* grads, uint32_t* err, int num_sms, cudaStream_t s);
 cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, __nv_bfloat16* dy,
                             __nv_bfloat16* dyt, float* loss_part, float* loss, cudaStream_t s);
 cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
