@@ -492,23 +492,34 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, in
 }
 
 // Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row, into the
-// dZ operand (unless null) and the dZ^T operand.
+// dZ operand (unless null) and the dZ^T operand. The next chunk's Z loads are
+// issued before this chunk's arithmetic; in dZ^T two lanes (rows 2k, 2k + 1)
+// write one 32-bit word per feature.
 __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, const float* __restrict__ z,
                                              int row0, uint8_t* dz, uint8_t* dzt) {
     const int r = (warp & 3) * 32 + lane;
     const float4* zr = reinterpret_cast<const float4*>(z + (size_t)(row0 + r) * kHidden);
+    float4 zn[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) zn[q] = zr[q];
 #pragma unroll 1
     for (int c0 = 0; c0 < kHidden; c0 += 16) {
+        float4 zc[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) zc[q] = zn[q];
+        if (c0 + 16 < kHidden) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) zn[q] = zr[(c0 + 16) / 4 + q];
+        }
         float v[16];
         tc::tmem_ld16(tc::tmem_lane_addr(tmem_dh, warp, c0), v);
         float h[16];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            const float4 zz = zr[c0 / 4 + q];
-            h[4 * q] = v[4 * q] * silu_grad(zz.x);
-            h[4 * q + 1] = v[4 * q + 1] * silu_grad(zz.y);
-            h[4 * q + 2] = v[4 * q + 2] * silu_grad(zz.z);
-            h[4 * q + 3] = v[4 * q + 3] * silu_grad(zz.w);
+            h[4 * q] = v[4 * q] * silu_grad(zc[q].x);
+            h[4 * q + 1] = v[4 * q + 1] * silu_grad(zc[q].y);
+            h[4 * q + 2] = v[4 * q + 2] * silu_grad(zc[q].z);
+            h[4 * q + 3] = v[4 * q + 3] * silu_grad(zc[q].w);
         }
         if (dz) {
             uint4 lo, hi;
@@ -517,9 +528,14 @@ __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lan
             *reinterpret_cast<uint4*>(dz + tc::kmajor_offset(r, c0, kHidden)) = lo;
             *reinterpret_cast<uint4*>(dz + tc::kmajor_offset(r, c0 + 8, kHidden)) = hi;
         }
+        // dZ^T: element (feature, row) at kmajor_offset(feature, row): rows 2k and 2k + 1 are
+        // adjacent bf16, so the even lane stores both (its odd neighbour's value by shuffle)
 #pragma unroll
-        for (int i = 0; i < 16; i++)
-            *reinterpret_cast<bf16*>(dzt + tc::kmajor_offset(c0 + i, r, kTile)) = __float2bfloat16_rn(h[i]);
+        for (int i = 0; i < 16; i++) {
+            const float other = __shfl_down_sync(0xffffffffu, h[i], 1);
+            if ((lane & 1) == 0)
+                *reinterpret_cast<uint32_t*>(dzt + tc::kmajor_offset(c0 + i, r, kTile)) = pack2(h[i], other);
+        }
     }
 }
 
