@@ -445,8 +445,10 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
 // the weights W4^T, W3^T, W2^T (resident), dY [rows][16] and dY^T [16][rows],
 // dZ [rows][128] and dZ^T [128][rows] (written by the epilogues), and the saved
 // layer inputs H^T [width][rows], double-buffered and copied with cp.async one
-// step ahead of their MMA. The batch is a multiple of 128 rows (no tails).
-constexpr int kBwdThreads = 128;
+// step ahead of their MMA. The batch is a multiple of 128 rows (no tails). Warp
+// w handles rows 32 (w % 4) .. + 31 (its TMEM lane quadrant) and columns
+// 64 (w / 4) .. + 63 of every epilogue.
+constexpr int kBwdThreads = 256;  // 8 warps: two per TMEM lane quadrant, one per column half
 constexpr int kBOffW4t = 0;                                   // [128][16]   kc 16
 constexpr int kBOffW3t = kBOffW4t + kHidden * kOutPad * 2;    // [128][128]  kc 128
 constexpr int kBOffW2t = kBOffW3t + kHidden * kHidden * 2;    // [128][128]
@@ -491,35 +493,35 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, in
                      (accumulate || ks > 0) ? 1u : 0u);
 }
 
-// Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row, into the
-// dZ operand (unless null) and the dZ^T operand. The next chunk's Z loads are
-// issued before this chunk's arithmetic; in dZ^T two lanes (rows 2k, 2k + 1)
-// write one 32-bit word per feature.
-__device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, const float* __restrict__ z,
-                                             int row0, uint8_t* dz, uint8_t* dzt) {
+// Half (64 columns) of this thread's row of Z, into registers.
+__device__ __forceinline__ void load_z_half(const float* __restrict__ z, int row0, int r, int half,
+                                            float4 (&zb)[16]) {
+    const float4* zr = reinterpret_cast<const float4*>(z + (size_t)(row0 + r) * kHidden) + half * 16;
+#pragma unroll
+    for (int q = 0; q < 16; q++) zb[q] = zr[q];
+}
+
+// Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row and column
+// half, into the dZ operand (unless null) and the dZ^T operand. zb holds that
+// half of the row of Z (loaded by the caller before the MMAs it waited for). In
+// dZ^T two lanes (rows 2k, 2k + 1) write one 32-bit word per feature.
+__device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, uint8_t* dz, uint8_t* dzt,
+                                             const float4 (&zb)[16]) {
     const int r = (warp & 3) * 32 + lane;
-    const float4* zr = reinterpret_cast<const float4*>(z + (size_t)(row0 + r) * kHidden);
-    float4 zn[4];
+    const int half = warp >> 2;
 #pragma unroll
-    for (int q = 0; q < 4; q++) zn[q] = zr[q];
-#pragma unroll 1
-    for (int c0 = 0; c0 < kHidden; c0 += 16) {
-        float4 zc[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) zc[q] = zn[q];
-        if (c0 + 16 < kHidden) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) zn[q] = zr[(c0 + 16) / 4 + q];
-        }
+    for (int ch = 0; ch < 4; ch++) {
+        const int c0 = half * 64 + ch * 16;
         float v[16];
         tc::tmem_ld16(tc::tmem_lane_addr(tmem_dh, warp, c0), v);
         float h[16];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            h[4 * q] = v[4 * q] * silu_grad(zc[q].x);
-            h[4 * q + 1] = v[4 * q + 1] * silu_grad(zc[q].y);
-            h[4 * q + 2] = v[4 * q + 2] * silu_grad(zc[q].z);
-            h[4 * q + 3] = v[4 * q + 3] * silu_grad(zc[q].w);
+            const float4 zz = zb[ch * 4 + q];
+            h[4 * q] = v[4 * q] * silu_grad(zz.x);
+            h[4 * q + 1] = v[4 * q + 1] * silu_grad(zz.y);
+            h[4 * q + 2] = v[4 * q + 2] * silu_grad(zz.z);
+            h[4 * q + 3] = v[4 * q + 3] * silu_grad(zz.w);
         }
         if (dz) {
             uint4 lo, hi;
@@ -540,7 +542,7 @@ __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lan
 }
 
 // This CTA's partial gradients, in the flat parameter layout: row r of the
-// accumulators is TMEM lane r (thread r).
+// accumulators is TMEM lane r; the two warps of a lane quadrant share the work.
 __device__ __forceinline__ void bwd_store_partials(uint32_t tmem, int warp, int lane, bool have, const float* db4,
                                                    float* __restrict__ out) {
     const int r = (warp & 3) * 32 + lane;
@@ -553,14 +555,17 @@ __device__ __forceinline__ void bwd_store_partials(uint32_t tmem, int warp, int 
                 if (c0 + i < ncols) dst[(size_t)(c0 + i) * stride] = have ? v[i] : 0.f;
         }
     };
-    row(kTcW3, kHidden, out + kOffParamW3 + r * kHidden, 1);
-    row(kTcW2, kHidden, out + kOffParamW2 + r * kHidden, 1);
-    row(kTcW1, kFeatures, out + kOffParamW1 + r * kFeatures, 1);
-    row(kTcW4, kOutputs, out + kOffParamW4 + r, kHidden);  // D[h][o] = dW4[o][h]
-    row(kTcB3, 1, out + kOffParamB3 + r, 1);
-    row(kTcB2, 1, out + kOffParamB2 + r, 1);
-    row(kTcB1, 1, out + kOffParamB1 + r, 1);
-    if (r < kOutputs) out[kOffParamB4 + r] = db4[r];
+    if (warp < 4) {
+        row(kTcW3, kHidden, out + kOffParamW3 + r * kHidden, 1);
+        row(kTcW1, kFeatures, out + kOffParamW1 + r * kFeatures, 1);
+        row(kTcB3, 1, out + kOffParamB3 + r, 1);
+        if (r < kOutputs) out[kOffParamB4 + r] = db4[r];
+    } else {
+        row(kTcW2, kHidden, out + kOffParamW2 + r * kHidden, 1);
+        row(kTcW4, kOutputs, out + kOffParamW4 + r, kHidden);  // D[h][o] = dW4[o][h]
+        row(kTcB2, 1, out + kOffParamB2 + r, 1);
+        row(kTcB1, 1, out + kOffParamB1 + r, 1);
+    }
 }
 
 __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __restrict__ dy, const Saves S,
@@ -571,7 +576,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tmem_base;
-    __shared__ float db4s[kBwdThreads / 32][kOutputs];
+    __shared__ float db4s[4][kOutputs];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t* hb[2] = {smem + kBOffH, smem + kBOffH + kHidden * kTile * 2};
     stage_weights(smem + kBOffW4t, w4t, kHidden, kOutPad, tid, kBwdThreads);
@@ -613,7 +618,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         const int tn = t + gridDim.x;  // the next tile of this CTA
         const bool acc = done > 0;
         // dY [rows][16] and dY^T [16][rows] from the output gradient (bf16 [batch][16], zero padded)
-        {
+        if (warp < 4) {
             const uint4* src = reinterpret_cast<const uint4*>(dy + (size_t)(row0 + r) * kOutPad);
             const uint4 lo = src[0], hi = src[1];
             *reinterpret_cast<uint4*>(smem + kBOffDy + tc::kmajor_offset(r, 0, kOutPad)) = lo;
@@ -628,6 +633,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
 #pragma unroll
             for (int o = 0; o < kOutputs; o++) db4[o] += __bfloat162float(e[o]);
         }
+        float4 zb[16];
+        load_z_half(S.z3, row0, r, warp >> 2, zb);  // in flight while the MMAs run
         cp_async_wait<1>();  // H3^T
         handoff_to_mma();
         if (tid == 0) {
@@ -638,7 +645,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[0], S.h1t, kHidden, S.ldh, row0, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, S.z3, row0, smem + kBOffDz, smem + kBOffDzt);
+        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
+        load_z_half(S.z2, row0, r, warp >> 2, zb);
         cp_async_wait<1>();  // H2^T
         handoff_to_mma();
         if (tid == 0) {
@@ -650,7 +658,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[1], S.h0t, kInPad, S.ldh, row0, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, S.z2, row0, smem + kBOffDz, smem + kBOffDzt);
+        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
+        load_z_half(S.z1, row0, r, warp >> 2, zb);
         cp_async_wait<1>();  // H1^T
         handoff_to_mma();
         if (tid == 0) {
@@ -662,7 +671,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         if (tn < ntiles) issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, tn * kTile, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, S.z1, row0, nullptr, smem + kBOffDzt);
+        bwd_epilogue(tmem + kTcDh, warp, lane, nullptr, smem + kBOffDzt, zb);
         if (tn < ntiles) cp_async_wait<1>();  // H0^T (the next tile's H3^T may still be in flight)
         else cp_async_wait<0>();
         handoff_to_mma();
@@ -681,13 +690,13 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         if (tid == 0) atomicOr(err, kErrMmaTimeout);
         tc::mbar_wait(&bar, parity ^ 1u, tc::kWaitLimitNs);  // the chain still in flight, bounded
     }
-    // db4: the sum over this CTA's rows, in a fixed order
+    // db4: the sum over this CTA's rows (warps 0-3), in a fixed order
 #pragma unroll
     for (int o = 0; o < kOutputs; o++) {
         float v = db4[o];
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-        if (lane == 0) db4s[warp][o] = v;
+        if (lane == 0 && warp < 4) db4s[warp][o] = v;
     }
     __syncthreads();
     float db4t[kOutputs];
