@@ -4,6 +4,7 @@
 // (include/sphmp_learned.h). The network kernels are in sphmp_mlp.cu; the
 // features are filled by the force pass of a corrected step (sphmp_features.cuh).
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -16,9 +17,6 @@
 #include "sphmp_device.cuh"
 #include "sphmp_internal.h"
 
-#ifndef SPHMP_FUSED_BACKWARD
-#define SPHMP_FUSED_BACKWARD 1
-#endif
 #include "sphmp_learned.h"
 #include "sphmp_mlp.h"
 
@@ -186,15 +184,13 @@ struct sphmp_corrector {
     float* bias = nullptr;      // [3 * 128 + 16]
     float* norm = nullptr;      // fshift [48], fscale [48], out_scale [4]
     uint32_t* err = nullptr;
-    // training buffers (max_batch rows)
-    float *z1 = nullptr, *z2 = nullptr, *z3 = nullptr, *y = nullptr;
+    // training buffers (max_batch rows): SiLU'(z) of the hidden layers, outputs,
+    // the layer inputs transposed, the output gradient
+    __half *s1 = nullptr, *s2 = nullptr, *s3 = nullptr;
+    float* y = nullptr;
     bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
-    // dz and dz2 alternate between layers: the SiLU-backward GEMM reads one as its
-    // A operand (declared __restrict__) and writes the other
-    bf16 *dz = nullptr, *dz2 = nullptr, *dzt = nullptr, *dy = nullptr, *dyt = nullptr;
-    float* part = nullptr;      // split-K partials
+    bf16 *dy = nullptr, *dyt = nullptr;
     float* bpart = nullptr;     // the fused backward's per-CTA gradient partials [num_sms][kParams]
-    float* rpart = nullptr;     // row-sum partials
     float* loss_part = nullptr;
     float* loss = nullptr;
     std::vector<void*> allocs;
@@ -217,14 +213,6 @@ sphmp_status lfail(sphmp_status st, const char* fmt, ...) {
         cudaError_t e_ = (call);                                                       \
         if (e_ != cudaSuccess) return lfail(SPHMP_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
-
-// K splits of the weight-gradient GEMMs (K = the batch): 256 rows of the batch
-// per CTA, at most 256 CTAs, partials summed in a fixed order
-constexpr int kMaxSplitK = 256;
-int split_k(int batch) {
-    const int s = batch / 256;
-    return s < 1 ? 1 : (s > kMaxSplitK ? kMaxSplitK : s);
-}
 
 template <class T>
 sphmp_status lalloc(sphmp_corrector* c, T** p, size_t count) {
@@ -258,34 +246,10 @@ sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t
     using namespace mlp;
     const cudaStream_t s = c->stream;
     const int ld = c->max_batch;
-    const Saves S{c->z1, c->z2, c->z3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
+    const Saves S{c->s1, c->s2, c->s3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
     LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
     LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
-    float* g = c->grads;
-#if SPHMP_FUSED_BACKWARD
-    LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, g, c->err, c->num_sms, s));
-    return SPHMP_OK;
-#endif
-    const int kSplitK = split_k(batch);
-    // layer 4: dW4 = dY^T H3, db4, dH3 = dY W4
-    LCK(launch_gemm_tn(c->dyt, ld, c->h3t, ld, c->part, kOutPad, kHidden, batch, kSplitK, c->err, s));
-    LCK(launch_reduce_splits(c->part, kSplitK, kOutPad, kHidden, kOutputs, kHidden, g + kOffParamW4, s));
-    LCK(launch_row_sum(c->dyt, ld, kOutputs, batch, c->rpart, g + kOffParamB4, s));
-    LCK(launch_gemm_silu_back(c->dy, kOutPad, c->w4t, kOutPad, batch, kOutPad, c->z3, c->dz, c->dzt, ld, c->err, s));
-    // layer 3
-    LCK(launch_gemm_tn(c->dzt, ld, c->h2t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
-    LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW3, s));
-    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB3, s));
-    LCK(launch_gemm_silu_back(c->dz, kHidden, c->w3t, kHidden, batch, kHidden, c->z2, c->dz2, c->dzt, ld, c->err, s));
-    // layer 2
-    LCK(launch_gemm_tn(c->dzt, ld, c->h1t, ld, c->part, kHidden, kHidden, batch, kSplitK, c->err, s));
-    LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kHidden, kHidden, kHidden, g + kOffParamW2, s));
-    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB2, s));
-    LCK(launch_gemm_silu_back(c->dz2, kHidden, c->w2t, kHidden, batch, kHidden, c->z1, c->dz, c->dzt, ld, c->err, s));
-    // layer 1: dW1 = dZ1^T H0 (the first 48 of the 64 padded inputs)
-    LCK(launch_gemm_tn(c->dzt, ld, c->h0t, ld, c->part, kHidden, kInPad, batch, kSplitK, c->err, s));
-    LCK(launch_reduce_splits(c->part, kSplitK, kHidden, kInPad, kHidden, kFeatures, g + kOffParamW1, s));
-    LCK(launch_row_sum(c->dzt, ld, kHidden, batch, c->rpart, g + kOffParamB1, s));
+    LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, c->grads, c->err, c->num_sms, s));
     return SPHMP_OK;
 }
 
@@ -337,13 +301,11 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
     A(&c->err, 1);
     const size_t B = (size_t)max_batch;
     if (B > 0) {
-        A(&c->z1, B * kHidden); A(&c->z2, B * kHidden); A(&c->z3, B * kHidden);
+        A(&c->s1, B * kHidden); A(&c->s2, B * kHidden); A(&c->s3, B * kHidden);
         A(&c->y, B * 4);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
-        A(&c->dz, B * kHidden); A(&c->dz2, B * kHidden); A(&c->dzt, kHidden * B); A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
-        A(&c->part, (size_t)kMaxSplitK * kHidden * kHidden);
+        A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
         A(&c->bpart, (size_t)c->num_sms * kParams);
-        A(&c->rpart, (size_t)kRowSumMaxRows * 16);
         A(&c->loss_part, B / 256 + 1);
         A(&c->loss, 1);
     }

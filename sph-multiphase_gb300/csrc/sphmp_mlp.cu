@@ -8,15 +8,19 @@
 //   each layer is one chain of MMAs
 //   into TMEM, and its epilogue (bias, SiLU, bf16) writes the next layer's
 //   operand tile back into shared memory. With the training saves it also
-//   stores the pre-activations (FP32) and the bf16 activations transposed
-//   (feature-major), the operands of the weight-gradient GEMMs.
+//   stores SiLU'(z) of each hidden layer (FP16) and the bf16 layer inputs
+//   transposed (feature-major), the operands of the backward pass.
+// * k_mlp_backward: the whole backward pass in one persistent kernel, one CTA
+//   per SM over 128-row tiles: dH GEMMs, the SiLU backward in their epilogues,
+//   and the weight and bias gradients accumulated in TMEM over the CTA's tiles;
+//   k_sum_partials adds the CTAs' partial gradients in a fixed order.
 // * k_gemm_tn: D = A B^T for K-major bf16 A [M][K] and B [N][K] (N <= 128),
-//   M in tiles of 128, K split over gridDim.y into FP32 partials (summed in a
-//   fixed order by k_reduce_splits), for the backward pass.
-// * elementwise kernels: the output gradient, bias gradients, Adam, and the
-//   packing of the FP32 master parameters into the padded bf16 operand layouts
-//   (the SiLU backward runs in the epilogue of the dH GEMM).
+//   M in tiles of 128, K split over gridDim.y into FP32 partials (the library's
+//   GEMM entry point).
+// * elementwise kernels: the output gradient, Adam, and the packing of the FP32
+//   master parameters into the padded bf16 operand layouts.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -147,7 +151,7 @@ __device__ __forceinline__ void group_handoff(int g) {
 // Epilogue of a hidden layer for this thread's row (all 128 columns): bias +
 // SiLU, the bf16 activations into the operand tile (K = 128), the training saves.
 __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lane, const float* bias, uint8_t* act,
-                                                int row0, int n, float* z_save, bf16* ht_save, int ldh) {
+                                                int row0, int n, __half* s_save, bf16* ht_save, int ldh) {
     const int r = (warp & 3) * 32 + lane;
     const int grow = row0 + r;
     const bool live = grow < n;
@@ -167,10 +171,13 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lan
         hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
         *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0, kHidden)) = lo;
         *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0 + 8, kHidden)) = hi;
-        if (z_save && live) {
-            float4* zs = reinterpret_cast<float4*>(z_save + (size_t)grow * kHidden + c0);
+        if (s_save && live) {  // SiLU'(z) for the backward pass, FP16 (relative error 2^-11)
+            __half2 g[8];
 #pragma unroll
-            for (int i = 0; i < 4; i++) zs[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+            for (int i = 0; i < 8; i++) g[i] = __floats2half2_rn(silu_grad(v[2 * i]), silu_grad(v[2 * i + 1]));
+            uint4* ss = reinterpret_cast<uint4*>(s_save + (size_t)grow * kHidden + c0);
+            ss[0] = *reinterpret_cast<const uint4*>(&g[0]);
+            ss[1] = *reinterpret_cast<const uint4*>(&g[4]);
         }
         if (ht_save && live) {
 #pragma unroll
@@ -255,7 +262,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
             issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW1), kInPad, kHidden, bar);
         }
         if (!(ok = group_wait(bar, parity, g))) break;
-        hidden_epilogue(tmem, warp, lane, bias, act, row0, n, S.z1, S.h1t, S.ldh);
+        hidden_epilogue(tmem, warp, lane, bias, act, row0, n, S.s1, S.h1t, S.ldh);
         group_handoff(g);
         // layer 2
         if (gt == 0) {
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
             issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW2), kHidden, kHidden, bar);
         }
         if (!(ok = group_wait(bar, parity, g))) break;
-        hidden_epilogue(tmem, warp, lane, bias + kHidden, act, row0, n, S.z2, S.h2t, S.ldh);
+        hidden_epilogue(tmem, warp, lane, bias + kHidden, act, row0, n, S.s2, S.h2t, S.ldh);
         group_handoff(g);
         // layer 3
         if (gt == 0) {
@@ -271,7 +278,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
             issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW3), kHidden, kHidden, bar);
         }
         if (!(ok = group_wait(bar, parity, g))) break;
-        hidden_epilogue(tmem, warp, lane, bias + 2 * kHidden, act, row0, n, S.z3, S.h3t, S.ldh);
+        hidden_epilogue(tmem, warp, lane, bias + 2 * kHidden, act, row0, n, S.s3, S.h3t, S.ldh);
         group_handoff(g);
         // layer 4 (N = 16: outputs 0..3 and zero padding)
         if (gt == 0) {
@@ -313,21 +320,9 @@ constexpr int kKc = 64;
 constexpr int kStageBytes = kTile * kKc * 2 + 128 * kKc * 2;
 constexpr int kGemmSmem = 2 * kStageBytes;
 
-// Epilogue of the SiLU-backward form (one K split, N = 128): dZ = D * SiLU'(Z)
-// straight from the accumulators, bf16, row-major [M][128] and transposed
-// [128][ldt] (D itself is not stored).
-struct SiluBack {
-    const float* z;
-    bf16* dz;
-    bf16* dzt;
-    int ldt;
-};
-
-template <bool SILU>
 __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict__ A, int lda,
                                                           const bf16* __restrict__ B, int ldb, float* __restrict__ D,
-                                                          int M, int N, int K, int kper, uint32_t* err,
-                                                          const SiluBack sb_out) {
+                                                          int M, int N, int K, int kper, uint32_t* err) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t bar;
     __shared__ uint32_t tmem_base;
@@ -383,40 +378,18 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
         chunks++;
     }
     const int r = warp * 32 + lane;
-    float* drow = SILU ? nullptr : D + ((size_t)blockIdx.y * M + (m0 + r)) * N;
+    float* drow = D + ((size_t)blockIdx.y * M + (m0 + r)) * N;
     if (ok) {
         for (int c0 = 0; c0 < N; c0 += 16) {
             float v[16];
             tc::tmem_ld16(tc::tmem_lane_addr(tmem, warp, c0), v);
             if (m0 + r < M) {
-                if (SILU) {
-                    const size_t row = (size_t)(m0 + r);
-                    const float4* zr = reinterpret_cast<const float4*>(sb_out.z + row * kHidden + c0);
-                    float h[16];
+                // four 16-byte stores per 16 columns (N is a multiple of 16, the partials 16-byte aligned)
+                float4* d4 = reinterpret_cast<float4*>(drow + c0);
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        const float4 zz = zr[q];
-                        const float zv[4] = {zz.x, zz.y, zz.z, zz.w};
-#pragma unroll
-                        for (int j = 0; j < 4; j++) h[4 * q + j] = (chunks ? v[4 * q + j] : 0.f) * silu_grad(zv[j]);
-                    }
-                    uint4 lo, hi;
-                    lo.x = pack2(h[0], h[1]); lo.y = pack2(h[2], h[3]); lo.z = pack2(h[4], h[5]); lo.w = pack2(h[6], h[7]);
-                    hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
-                    uint4* dst = reinterpret_cast<uint4*>(sb_out.dz + row * kHidden + c0);
-                    dst[0] = lo;
-                    dst[1] = hi;
-#pragma unroll
-                    for (int i = 0; i < 16; i++)
-                        sb_out.dzt[(size_t)(c0 + i) * sb_out.ldt + row] = __float2bfloat16_rn(h[i]);
-                } else {
-                    // four 16-byte stores per 16 columns (N is a multiple of 16, the partials 16-byte aligned)
-                    float4* d4 = reinterpret_cast<float4*>(drow + c0);
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        d4[q] = chunks ? make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3])
-                                       : make_float4(0.f, 0.f, 0.f, 0.f);
-                }
+                for (int q = 0; q < 4; q++)
+                    d4[q] = chunks ? make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3])
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
     } else {
@@ -435,7 +408,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
 //
 // For each tile (rows r of the batch), with dY = the output gradient:
 //   dW4^T += H3^T dY          dH3 = dY W4
-//   dZ3 = dH3 * SiLU'(Z3)     dW3 += dZ3^T H2   db3 += sum_r dZ3   dH2 = dZ3 W3
+//   dZ3 = dH3 * SiLU'(Z3)     dW3 += dZ3^T H2   db3 += sum_r dZ3   dH2 = dZ3 W3   (SiLU'(Z) saved, FP16)
 //   dZ2 = dH2 * SiLU'(Z2)     dW2 += dZ2^T H1   db2 += sum_r dZ2   dH1 = dZ2 W2
 //   dZ1 = dH1 * SiLU'(Z1)     dW1 += dZ1^T H0   db1 += sum_r dZ1
 // The weight and bias gradients accumulate in TMEM over all tiles of the CTA
@@ -493,20 +466,20 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, in
                      (accumulate || ks > 0) ? 1u : 0u);
 }
 
-// Half (64 columns) of this thread's row of Z, into registers.
-__device__ __forceinline__ void load_z_half(const float* __restrict__ z, int row0, int r, int half,
-                                            float4 (&zb)[16]) {
-    const float4* zr = reinterpret_cast<const float4*>(z + (size_t)(row0 + r) * kHidden) + half * 16;
+// Half (64 columns) of this thread's row of SiLU'(z), FP16, into registers.
+__device__ __forceinline__ void load_s_half(const __half* __restrict__ sv, int row0, int r, int half,
+                                            uint4 (&sb)[8]) {
+    const uint4* sr = reinterpret_cast<const uint4*>(sv + (size_t)(row0 + r) * kHidden) + half * 8;
 #pragma unroll
-    for (int q = 0; q < 16; q++) zb[q] = zr[q];
+    for (int q = 0; q < 8; q++) sb[q] = sr[q];
 }
 
 // Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row and column
-// half, into the dZ operand (unless null) and the dZ^T operand. zb holds that
-// half of the row of Z (loaded by the caller before the MMAs it waited for). In
-// dZ^T two lanes (rows 2k, 2k + 1) write one 32-bit word per feature.
+// half, into the dZ operand (unless null) and the dZ^T operand. sb holds that
+// half of the row of SiLU'(z) (loaded by the caller before the MMAs it waited
+// for). In dZ^T two lanes (rows 2k, 2k + 1) write one 32-bit word per feature.
 __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, uint8_t* dz, uint8_t* dzt,
-                                             const float4 (&zb)[16]) {
+                                             const uint4 (&sb)[8]) {
     const int r = (warp & 3) * 32 + lane;
     const int half = warp >> 2;
 #pragma unroll
@@ -516,12 +489,14 @@ __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lan
         tc::tmem_ld16(tc::tmem_lane_addr(tmem_dh, warp, c0), v);
         float h[16];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const float4 zz = zb[ch * 4 + q];
-            h[4 * q] = v[4 * q] * silu_grad(zz.x);
-            h[4 * q + 1] = v[4 * q + 1] * silu_grad(zz.y);
-            h[4 * q + 2] = v[4 * q + 2] * silu_grad(zz.z);
-            h[4 * q + 3] = v[4 * q + 3] * silu_grad(zz.w);
+        for (int q = 0; q < 2; q++) {
+            const __half2* g = reinterpret_cast<const __half2*>(&sb[ch * 2 + q]);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 d = __half22float2(g[j]);
+                h[8 * q + 2 * j] = v[8 * q + 2 * j] * d.x;
+                h[8 * q + 2 * j + 1] = v[8 * q + 2 * j + 1] * d.y;
+            }
         }
         if (dz) {
             uint4 lo, hi;
@@ -633,8 +608,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
 #pragma unroll
             for (int o = 0; o < kOutputs; o++) db4[o] += __bfloat162float(e[o]);
         }
-        float4 zb[16];
-        load_z_half(S.z3, row0, r, warp >> 2, zb);  // in flight while the MMAs run
+        uint4 sb[8];
+        load_s_half(S.s3, row0, r, warp >> 2, sb);  // in flight while the MMAs run
         cp_async_wait<1>();  // H3^T
         handoff_to_mma();
         if (tid == 0) {
@@ -645,8 +620,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[0], S.h1t, kHidden, S.ldh, row0, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
-        load_z_half(S.z2, row0, r, warp >> 2, zb);
+        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, sb);
+        load_s_half(S.s2, row0, r, warp >> 2, sb);
         cp_async_wait<1>();  // H2^T
         handoff_to_mma();
         if (tid == 0) {
@@ -658,8 +633,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[1], S.h0t, kInPad, S.ldh, row0, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
-        load_z_half(S.z1, row0, r, warp >> 2, zb);
+        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, sb);
+        load_s_half(S.s1, row0, r, warp >> 2, sb);
         cp_async_wait<1>();  // H1^T
         handoff_to_mma();
         if (tid == 0) {
@@ -671,7 +646,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         if (tn < ntiles) issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, tn * kTile, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, nullptr, smem + kBOffDzt, zb);
+        bwd_epilogue(tmem + kTcDh, warp, lane, nullptr, smem + kBOffDzt, sb);
         if (tn < ntiles) cp_async_wait<1>();  // H0^T (the next tile's H3^T may still be in flight)
         else cp_async_wait<0>();
         handoff_to_mma();
@@ -772,70 +747,6 @@ __global__ void k_loss_sum(const float* __restrict__ part, int nparts, int batch
     if (threadIdx.x == 0) *loss = red[0] / (float)batch;
 }
 
-// out[r * cols + c] = sum over the splits of part[s][r][c] (r < rows, c < cols):
-// 8 warps per block of 32 outputs, warp w sums every 8th split from w, then
-// warp 0 adds the eight partial sums in order (a fixed order for any launch).
-__global__ void __launch_bounds__(256) k_reduce_splits(const float* __restrict__ part, int splits, int M, int N,
-                                                       int rows, int cols, float* __restrict__ out) {
-    __shared__ float sh[8][32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int i = blockIdx.x * 32 + lane;
-    float s = 0.f;
-    if (i < rows * cols) {
-        const int r = i / cols, c = i % cols;
-        for (int k = w; k < splits; k += 8) s += part[((size_t)k * M + r) * N + c];
-    }
-    sh[w][lane] = s;
-    __syncthreads();
-    if (w == 0 && i < rows * cols) {
-        float t = 0.f;
-#pragma unroll
-        for (int k = 0; k < 8; k++) t += sh[k][lane];
-        out[i] = t;
-    }
-}
-
-// out[r] = sum over the first `count` entries of row r of xt, in two fixed-order
-// passes: block (r, k) sums chunk k of row r (8 bf16 per 16-byte load), then
-// one thread per row sums the chunks.
-constexpr int kRowSplits = 16;
-__global__ void k_row_sum_part(const bf16* __restrict__ xt, int ld, int count, float* __restrict__ part) {
-    __shared__ float red[256];
-    const int r = blockIdx.x, k = blockIdx.y;
-    const int chunk = ((count + kRowSplits - 1) / kRowSplits + 7) / 8 * 8;
-    const int b = k * chunk, e = min(count, b + chunk);
-    const bf16* row = xt + (size_t)r * ld;
-    float s = 0.f;
-    for (int i = b + 8 * (int)threadIdx.x; i < e; i += 8 * blockDim.x) {
-        if (i + 8 <= e) {
-            const uint4 q = *reinterpret_cast<const uint4*>(row + i);
-            const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float2 f = __bfloat1622float2(h[j]);
-                s += f.x + f.y;
-            }
-        } else {
-            for (int j = i; j < e; j++) s += __bfloat162float(row[j]);
-        }
-    }
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[r * kRowSplits + k] = red[0];
-}
-
-__global__ void k_row_sum_final(const float* __restrict__ part, int rows, float* __restrict__ out) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rows) return;
-    float s = 0.f;
-    for (int k = 0; k < kRowSplits; k++) s += part[r * kRowSplits + k];
-    out[r] = s;
-}
-
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, int count, float lr, float b1, float b2, float eps, float c1,
                        float c2) {
@@ -910,24 +821,10 @@ cudaError_t launch_gemm_tn(const bf16* A, int lda, const bf16* B, int ldb, float
     int kper = (K + splits - 1) / splits;
     kper = (kper + kKc - 1) / kKc * kKc;
     if (kper == 0) kper = kKc;
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
     if (e != cudaSuccess) return e;
     dim3 grid((M + kTile - 1) / kTile, splits);
-    k_gemm_tn<false><<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err, SiluBack{});
-    return cudaGetLastError();
-}
-
-cudaError_t launch_gemm_silu_back(const bf16* A, int lda, const bf16* B, int ldb, int M, int K, const float* z,
-                                  bf16* dz, bf16* dzt, int ldt, uint32_t* err, cudaStream_t s) {
-    if (M <= 0 || K < 0 || (K % 8) != 0 || (lda % 8) != 0 || (ldb % 8) != 0 || ldt < M)
-        return cudaErrorInvalidValue;
-    int kper = (K + kKc - 1) / kKc * kKc;
-    if (kper == 0) kper = kKc;
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGemmSmem);
-    if (e != cudaSuccess) return e;
-    dim3 grid((M + kTile - 1) / kTile, 1);
-    k_gemm_tn<true><<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, nullptr, M, kHidden, K, kper, err,
-                                                          SiluBack{z, dz, dzt, ldt});
+    k_gemm_tn<<<grid, kGemmThreads, kGemmSmem, s>>>(A, lda, B, ldb, D, M, N, K, kper, err);
     return cudaGetLastError();
 }
 
@@ -940,23 +837,10 @@ cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, b
     return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
-                                 cudaStream_t s) {
-    k_reduce_splits<<<(rows * cols + 31) / 32, 256, 0, s>>>(part, splits, M, N, rows, cols, out);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_row_sum(const bf16* xt, int ld, int rows, int count, float* part, float* out, cudaStream_t s) {
-    if ((ld % 8) != 0 || rows > kRowSumMaxRows) return cudaErrorInvalidValue;
-    k_row_sum_part<<<dim3(rows, kRowSplits), 256, 0, s>>>(xt, ld, count, part);
-    k_row_sum_final<<<1, kRowSumMaxRows, 0, s>>>(part, rows, out);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_backward(const bf16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
                             float* grads, uint32_t* err, int num_sms, cudaStream_t s) {
     // the saved inputs are copied 16 bytes at a time: their row stride must keep that alignment
-    if (batch <= 0 || batch % kTile != 0 || !S.z1 || !S.h0t || S.ldh % 8 != 0 || S.ldh < batch)
+    if (batch <= 0 || batch % kTile != 0 || !S.s1 || !S.h0t || S.ldh % 8 != 0 || S.ldh < batch)
         return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdSmem);
     if (e != cudaSuccess) return e;

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -48,10 +49,10 @@ struct PackedMut {
     float* bias;
 };
 
-// Training saves of the forward pass (all null for inference): pre-activations
-// [n][128] FP32 and the bf16 layer inputs transposed, [width][ldh].
+// Training saves of the forward pass (all null for inference): SiLU'(z) of the
+// hidden layers [n][128] FP16 and the bf16 layer inputs transposed, [width][ldh].
 struct Saves {
-    float *z1, *z2, *z3;
+    __half *s1, *s2, *s3;
     __nv_bfloat16 *h0t, *h1t, *h2t, *h3t;  // h0t [64][ldh] (rows 48..63 zero), the others [128][ldh]
     int ldh;
 };
@@ -61,11 +62,6 @@ cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& 
 // D[split][M][N] = A[M][K] B[N][K]^T over the split's K range; N a multiple of 16, <= 128
 cudaError_t launch_gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* D, int M, int N,
                            int K, int splits, uint32_t* err, cudaStream_t s);
-// dZ = (A B^T) * SiLU'(Z) for N = 128 (the dH GEMM of a hidden layer with its SiLU backward in the
-// epilogue): bf16 dz [M][128] and dzt [128][ldt]
-cudaError_t launch_gemm_silu_back(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, int M, int K,
-                                  const float* z, __nv_bfloat16* dz, __nv_bfloat16* dzt, int ldt, uint32_t* err,
-                                  cudaStream_t s);
 // The whole backward pass after launch_out_grad (fused, one persistent CTA per
 // SM): gradients of every parameter into grads (flat layout). batch a multiple
 // of 128; part: scratch of num_sms * kParams floats.
@@ -73,13 +69,6 @@ cudaError_t launch_backward(const __nv_bfloat16* dy, const Saves& S, const Packe
                             float* grads, uint32_t* err, int num_sms, cudaStream_t s);
 cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, __nv_bfloat16* dy,
                             __nv_bfloat16* dyt, float* loss_part, float* loss, cudaStream_t s);
-cudaError_t launch_reduce_splits(const float* part, int splits, int M, int N, int rows, int cols, float* out,
-                                 cudaStream_t s);
-// out[r] = sum of the first count entries of row r (rows <= kRowSumMaxRows); part: scratch of
-// kRowSumMaxRows * 16 floats
-constexpr int kRowSumMaxRows = 128;
-cudaError_t launch_row_sum(const __nv_bfloat16* xt, int ld, int rows, int count, float* part, float* out,
-                           cudaStream_t s);
 cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int count, float lr, float b1, float b2,
                         float eps, int step, cudaStream_t s);
 cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s);
