@@ -15,8 +15,8 @@ pass against finite differences, its features against a hand-computed pair
   TMEM on the GPU), and SiLU is exact here (the GPU's forward pass computes it
   as z/2 (1 + tanh(z/2)) with the hardware tanh), so the two agree to the
   accumulation rounding and an occasional bf16 rounding step of an activation.
-  The forward pass saves SiLU'(z) of each hidden layer in FP16 for the backward
-  pass, which multiplies dH by that saved value (rounded to FP16 here too).
+  The forward pass saves z of each hidden layer in FP16 for the backward pass,
+  which multiplies dH by SiLU'(z) of that saved value (rounded to FP16 here too).
   Loss = sum over the batch and the 4 outputs of (y - t)^2, divided by the batch.
 * adam: one Adam step with bias correction (beta1 0.9, beta2 0.999, eps 1e-8).
 * features: the 48 per-particle features of include/sphmp_learned.h's large
@@ -121,10 +121,10 @@ def mlp_backward(params, shift, scale, X, T, rnd=None):
     dz = dy
     for i in (3, 2, 1):  # layer i + 1 back to layer 1
         dh = dz @ W[i]  # W[i] is layer (i + 1)'s weight
-        sg = silu_grad(zs[i - 1])
-        if rnd is None:  # the FP16 save of the forward pass
-            sg = sg.astype(np.float32).astype(np.float16).astype(np.float32)
-        dz = bf16((dh.astype(f32) * sg).astype(f32)).astype(np.float64)
+        z = zs[i - 1]
+        if rnd is None:  # the forward pass saves z in FP16
+            z = np.asarray(z, np.float32).astype(np.float16).astype(np.float32)
+        dz = bf16((dh.astype(f32) * silu_grad(z)).astype(f32)).astype(np.float64)
         g[f"W{i}"] = dz.T @ hs[i - 1]
         g[f"b{i}"] = dz.sum(0)
     g["W1"] = g["W1"][:, :FEATURES]

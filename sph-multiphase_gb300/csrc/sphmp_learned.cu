@@ -184,9 +184,9 @@ struct sphmp_corrector {
     float* bias = nullptr;      // [3 * 128 + 16]
     float* norm = nullptr;      // fshift [48], fscale [48], out_scale [4]
     uint32_t* err = nullptr;
-    // training buffers (max_batch rows): SiLU'(z) of the hidden layers, outputs,
+    // training buffers (max_batch rows): the hidden layers' z (FP16), outputs,
     // the layer inputs transposed, the output gradient
-    __half *s1 = nullptr, *s2 = nullptr, *s3 = nullptr;
+    __half *z1 = nullptr, *z2 = nullptr, *z3 = nullptr;
     float* y = nullptr;
     bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
     bf16 *dy = nullptr, *dyt = nullptr;
@@ -246,7 +246,7 @@ sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t
     using namespace mlp;
     const cudaStream_t s = c->stream;
     const int ld = c->max_batch;
-    const Saves S{c->s1, c->s2, c->s3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
+    const Saves S{c->z1, c->z2, c->z3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
     LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
     LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
     LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, c->grads, c->err, c->num_sms, s));
@@ -301,7 +301,7 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
     A(&c->err, 1);
     const size_t B = (size_t)max_batch;
     if (B > 0) {
-        A(&c->s1, B * kHidden); A(&c->s2, B * kHidden); A(&c->s3, B * kHidden);
+        A(&c->z1, B * kHidden); A(&c->z2, B * kHidden); A(&c->z3, B * kHidden);
         A(&c->y, B * 4);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
         A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);

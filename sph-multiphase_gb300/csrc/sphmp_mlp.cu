@@ -8,8 +8,8 @@
 //   each layer is one chain of MMAs
 //   into TMEM, and its epilogue (bias, SiLU, bf16) writes the next layer's
 //   operand tile back into shared memory. With the training saves it also
-//   stores SiLU'(z) of each hidden layer (FP16) and the bf16 layer inputs
-//   transposed (feature-major), the operands of the backward pass.
+//   stores z of each hidden layer (FP16) and the bf16 layer inputs transposed
+//   (feature-major), the operands of the backward pass.
 // * k_mlp_backward: the whole backward pass in one persistent kernel, one CTA
 //   per SM over 128-row tiles: dH GEMMs, the SiLU backward in their epilogues,
 //   and the weight and bias gradients accumulated in TMEM over the CTA's tiles;
@@ -151,7 +151,7 @@ __device__ __forceinline__ void group_handoff(int g) {
 // Epilogue of a hidden layer for this thread's row (all 128 columns): bias +
 // SiLU, the bf16 activations into the operand tile (K = 128), the training saves.
 __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lane, const float* bias, uint8_t* act,
-                                                int row0, int n, __half* s_save, bf16* ht_save, int ldh) {
+                                                int row0, int n, __half* z_save, bf16* ht_save, int ldh) {
     const int r = (warp & 3) * 32 + lane;
     const int grow = row0 + r;
     const bool live = grow < n;
@@ -171,17 +171,24 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lan
         hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
         *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0, kHidden)) = lo;
         *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0 + 8, kHidden)) = hi;
-        if (s_save && live) {  // SiLU'(z) for the backward pass, FP16 (relative error 2^-11)
+        if (z_save && live) {  // z for the backward pass, FP16 (relative error 2^-11)
             __half2 g[8];
 #pragma unroll
-            for (int i = 0; i < 8; i++) g[i] = __floats2half2_rn(silu_grad(v[2 * i]), silu_grad(v[2 * i + 1]));
-            uint4* ss = reinterpret_cast<uint4*>(s_save + (size_t)grow * kHidden + c0);
-            ss[0] = *reinterpret_cast<const uint4*>(&g[0]);
-            ss[1] = *reinterpret_cast<const uint4*>(&g[4]);
+            for (int i = 0; i < 8; i++) g[i] = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+            uint4* zs = reinterpret_cast<uint4*>(z_save + (size_t)grow * kHidden + c0);
+            zs[0] = *reinterpret_cast<const uint4*>(&g[0]);
+            zs[1] = *reinterpret_cast<const uint4*>(&g[4]);
         }
-        if (ht_save && live) {
+        if (ht_save) {  // transposed: rows 2k and 2k + 1 adjacent, one 32-bit store by the even lane
 #pragma unroll
-            for (int i = 0; i < 16; i++) ht_save[(size_t)(c0 + i) * ldh + grow] = __float2bfloat16_rn(h[i]);
+            for (int i = 0; i < 16; i++) {
+                const float other = __shfl_down_sync(0xffffffffu, h[i], 1);
+                bf16* dst = ht_save + (size_t)(c0 + i) * ldh + grow;
+                if ((lane & 1) == 0 && grow + 1 < n)
+                    *reinterpret_cast<uint32_t*>(dst) = pack2(h[i], other);
+                else if ((lane & 1) == 0 && live)
+                    *dst = __float2bfloat16_rn(h[i]);
+            }
         }
     }
 }
@@ -262,7 +269,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
             issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW1), kInPad, kHidden, bar);
         }
         if (!(ok = group_wait(bar, parity, g))) break;
-        hidden_epilogue(tmem, warp, lane, bias, act, row0, n, S.s1, S.h1t, S.ldh);
+        hidden_epilogue(tmem, warp, lane, bias, act, row0, n, S.z1, S.h1t, S.ldh);
         group_handoff(g);
         // layer 2
         if (gt == 0) {
@@ -270,7 +277,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
             issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW2), kHidden, kHidden, bar);
         }
         if (!(ok = group_wait(bar, parity, g))) break;
-        hidden_epilogue(tmem, warp, lane, bias + kHidden, act, row0, n, S.s2, S.h2t, S.ldh);
+        hidden_epilogue(tmem, warp, lane, bias + kHidden, act, row0, n, S.z2, S.h2t, S.ldh);
         group_handoff(g);
         // layer 3
         if (gt == 0) {
@@ -278,7 +285,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
             issue_layer(tmem, a_act, tc::smem_addr(smem + kOffW3), kHidden, kHidden, bar);
         }
         if (!(ok = group_wait(bar, parity, g))) break;
-        hidden_epilogue(tmem, warp, lane, bias + 2 * kHidden, act, row0, n, S.s3, S.h3t, S.ldh);
+        hidden_epilogue(tmem, warp, lane, bias + 2 * kHidden, act, row0, n, S.z3, S.h3t, S.ldh);
         group_handoff(g);
         // layer 4 (N = 16: outputs 0..3 and zero padding)
         if (gt == 0) {
@@ -408,7 +415,7 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm_tn(const bf16* __restrict
 //
 // For each tile (rows r of the batch), with dY = the output gradient:
 //   dW4^T += H3^T dY          dH3 = dY W4
-//   dZ3 = dH3 * SiLU'(Z3)     dW3 += dZ3^T H2   db3 += sum_r dZ3   dH2 = dZ3 W3   (SiLU'(Z) saved, FP16)
+//   dZ3 = dH3 * SiLU'(Z3)     dW3 += dZ3^T H2   db3 += sum_r dZ3   dH2 = dZ3 W3   (Z saved in FP16)
 //   dZ2 = dH2 * SiLU'(Z2)     dW2 += dZ2^T H1   db2 += sum_r dZ2   dH1 = dZ2 W2
 //   dZ1 = dH1 * SiLU'(Z1)     dW1 += dZ1^T H0   db1 += sum_r dZ1
 // The weight and bias gradients accumulate in TMEM over all tiles of the CTA
@@ -466,20 +473,20 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, in
                      (accumulate || ks > 0) ? 1u : 0u);
 }
 
-// Half (64 columns) of this thread's row of SiLU'(z), FP16, into registers.
-__device__ __forceinline__ void load_s_half(const __half* __restrict__ sv, int row0, int r, int half,
-                                            uint4 (&sb)[8]) {
-    const uint4* sr = reinterpret_cast<const uint4*>(sv + (size_t)(row0 + r) * kHidden) + half * 8;
+// Half (64 columns) of this thread's row of z (FP16), into registers.
+__device__ __forceinline__ void load_z_half(const __half* __restrict__ zv, int row0, int r, int half,
+                                            uint4 (&zb)[8]) {
+    const uint4* zr = reinterpret_cast<const uint4*>(zv + (size_t)(row0 + r) * kHidden) + half * 8;
 #pragma unroll
-    for (int q = 0; q < 8; q++) sb[q] = sr[q];
+    for (int q = 0; q < 8; q++) zb[q] = zr[q];
 }
 
 // Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row and column
-// half, into the dZ operand (unless null) and the dZ^T operand. sb holds that
-// half of the row of SiLU'(z) (loaded by the caller before the MMAs it waited
+// half, into the dZ operand (unless null) and the dZ^T operand. zb holds that
+// half of the row of z (FP16, loaded by the caller before the MMAs it waited
 // for). In dZ^T two lanes (rows 2k, 2k + 1) write one 32-bit word per feature.
 __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, uint8_t* dz, uint8_t* dzt,
-                                             const uint4 (&sb)[8]) {
+                                             const uint4 (&zb)[8]) {
     const int r = (warp & 3) * 32 + lane;
     const int half = warp >> 2;
 #pragma unroll
@@ -490,12 +497,12 @@ __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lan
         float h[16];
 #pragma unroll
         for (int q = 0; q < 2; q++) {
-            const __half2* g = reinterpret_cast<const __half2*>(&sb[ch * 2 + q]);
+            const __half2* g = reinterpret_cast<const __half2*>(&zb[ch * 2 + q]);
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const float2 d = __half22float2(g[j]);
-                h[8 * q + 2 * j] = v[8 * q + 2 * j] * d.x;
-                h[8 * q + 2 * j + 1] = v[8 * q + 2 * j + 1] * d.y;
+                const float2 zz = __half22float2(g[j]);
+                h[8 * q + 2 * j] = v[8 * q + 2 * j] * silu_grad(zz.x);
+                h[8 * q + 2 * j + 1] = v[8 * q + 2 * j + 1] * silu_grad(zz.y);
             }
         }
         if (dz) {
@@ -608,8 +615,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
 #pragma unroll
             for (int o = 0; o < kOutputs; o++) db4[o] += __bfloat162float(e[o]);
         }
-        uint4 sb[8];
-        load_s_half(S.s3, row0, r, warp >> 2, sb);  // in flight while the MMAs run
+        uint4 zb[8];
+        load_z_half(S.z3, row0, r, warp >> 2, zb);  // in flight while the MMAs run
         cp_async_wait<1>();  // H3^T
         handoff_to_mma();
         if (tid == 0) {
@@ -620,8 +627,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[0], S.h1t, kHidden, S.ldh, row0, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, sb);
-        load_s_half(S.s2, row0, r, warp >> 2, sb);
+        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
+        load_z_half(S.z2, row0, r, warp >> 2, zb);
         cp_async_wait<1>();  // H2^T
         handoff_to_mma();
         if (tid == 0) {
@@ -633,8 +640,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[1], S.h0t, kInPad, S.ldh, row0, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, sb);
-        load_s_half(S.s1, row0, r, warp >> 2, sb);
+        bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
+        load_z_half(S.z1, row0, r, warp >> 2, zb);
         cp_async_wait<1>();  // H1^T
         handoff_to_mma();
         if (tid == 0) {
@@ -646,7 +653,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         }
         if (!(ok = wait_all(&bar, parity))) break;
         if (tn < ntiles) issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, tn * kTile, tid);
-        bwd_epilogue(tmem + kTcDh, warp, lane, nullptr, smem + kBOffDzt, sb);
+        bwd_epilogue(tmem + kTcDh, warp, lane, nullptr, smem + kBOffDzt, zb);
         if (tn < ntiles) cp_async_wait<1>();  // H0^T (the next tile's H3^T may still be in flight)
         else cp_async_wait<0>();
         handoff_to_mma();
@@ -840,7 +847,7 @@ cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, b
 cudaError_t launch_backward(const bf16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
                             float* grads, uint32_t* err, int num_sms, cudaStream_t s) {
     // the saved inputs are copied 16 bytes at a time: their row stride must keep that alignment
-    if (batch <= 0 || batch % kTile != 0 || !S.s1 || !S.h0t || S.ldh % 8 != 0 || S.ldh < batch)
+    if (batch <= 0 || batch % kTile != 0 || !S.z1 || !S.h0t || S.ldh % 8 != 0 || S.ldh < batch)
         return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdSmem);
     if (e != cudaSuccess) return e;

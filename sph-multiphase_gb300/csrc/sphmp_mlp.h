@@ -49,10 +49,11 @@ struct PackedMut {
     float* bias;
 };
 
-// Training saves of the forward pass (all null for inference): SiLU'(z) of the
-// hidden layers [n][128] FP16 and the bf16 layer inputs transposed, [width][ldh].
+// Training saves of the forward pass (all null for inference): the hidden
+// layers' pre-activations z [n][128] in FP16 and the bf16 layer inputs
+// transposed, [width][ldh].
 struct Saves {
-    __half *s1, *s2, *s3;
+    __half *z1, *z2, *z3;
     __nv_bfloat16 *h0t, *h1t, *h2t, *h3t;  // h0t [64][ldh] (rows 48..63 zero), the others [128][ldh]
     int ldh;
 };
