@@ -301,7 +301,7 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
     A(&c->err, 1);
     const size_t B = (size_t)max_batch;
     if (B > 0) {
-        A(&c->z1, B * kHidden); A(&c->z2, B * kHidden); A(&c->z3, B * kHidden);
+        A(&c->z1, kHidden * B); A(&c->z2, kHidden * B); A(&c->z3, kHidden * B);  // [128][max_batch]
         A(&c->y, B * 4);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
         A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);

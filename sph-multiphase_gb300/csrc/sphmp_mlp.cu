@@ -171,23 +171,23 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int warp, int lan
         hi.x = pack2(h[8], h[9]); hi.y = pack2(h[10], h[11]); hi.z = pack2(h[12], h[13]); hi.w = pack2(h[14], h[15]);
         *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0, kHidden)) = lo;
         *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, c0 + 8, kHidden)) = hi;
-        if (z_save && live) {  // z for the backward pass, FP16 (relative error 2^-11)
-            __half2 g[8];
-#pragma unroll
-            for (int i = 0; i < 8; i++) g[i] = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
-            uint4* zs = reinterpret_cast<uint4*>(z_save + (size_t)grow * kHidden + c0);
-            zs[0] = *reinterpret_cast<const uint4*>(&g[0]);
-            zs[1] = *reinterpret_cast<const uint4*>(&g[4]);
-        }
-        if (ht_save) {  // transposed: rows 2k and 2k + 1 adjacent, one 32-bit store by the even lane
+        // the training saves, transposed ([feature][row]): rows 2k and 2k + 1 are adjacent,
+        // so the even lane stores both with one 32-bit store (a warp writes 64 contiguous
+        // bytes per feature): z in FP16 (relative error 2^-11) and the bf16 activations
+        if (ht_save) {
 #pragma unroll
             for (int i = 0; i < 16; i++) {
-                const float other = __shfl_down_sync(0xffffffffu, h[i], 1);
-                bf16* dst = ht_save + (size_t)(c0 + i) * ldh + grow;
-                if ((lane & 1) == 0 && grow + 1 < n)
-                    *reinterpret_cast<uint32_t*>(dst) = pack2(h[i], other);
-                else if ((lane & 1) == 0 && live)
-                    *dst = __float2bfloat16_rn(h[i]);
+                const float oh = __shfl_down_sync(0xffffffffu, h[i], 1);
+                const float oz = __shfl_down_sync(0xffffffffu, v[i], 1);
+                const size_t at = (size_t)(c0 + i) * ldh + grow;
+                if ((lane & 1) == 0 && grow + 1 < n) {
+                    *reinterpret_cast<uint32_t*>(ht_save + at) = pack2(h[i], oh);
+                    const __half2 zz = __floats2half2_rn(v[i], oz);
+                    *reinterpret_cast<__half2*>(z_save + at) = zz;
+                } else if ((lane & 1) == 0 && live) {
+                    ht_save[at] = __float2bfloat16_rn(h[i]);
+                    z_save[at] = __float2half_rn(v[i]);
+                }
             }
         }
     }
@@ -253,9 +253,14 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_forward(const float* __r
                 uint4 q;
                 q.x = pack2(f[0], f[1]); q.y = pack2(f[2], f[3]); q.z = pack2(f[4], f[5]); q.w = pack2(f[6], f[7]);
                 *reinterpret_cast<uint4*>(act + tc::kmajor_offset(r, 8 * c, kInPad)) = q;
-                if (S.h0t && live) {
+                if (S.h0t) {  // transposed, a 32-bit store per row pair (as in the hidden layers)
 #pragma unroll
-                    for (int i = 0; i < 8; i++) S.h0t[(size_t)(8 * c + i) * S.ldh + grow] = __float2bfloat16_rn(f[i]);
+                    for (int i = 0; i < 8; i++) {
+                        const float o = __shfl_down_sync(0xffffffffu, f[i], 1);
+                        bf16* dst = S.h0t + (size_t)(8 * c + i) * S.ldh + grow;
+                        if ((gt & 1) == 0 && grow + 1 < n) *reinterpret_cast<uint32_t*>(dst) = pack2(f[i], o);
+                        else if ((gt & 1) == 0 && live) *dst = __float2bfloat16_rn(f[i]);
+                    }
                 }
             }
             const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
@@ -441,6 +446,7 @@ constexpr int kBOffH = kBOffDzt + kHidden * kTile * 2;        // 2 x [128][128] 
 constexpr int kBwdSmem = kBOffH + 2 * kHidden * kTile * 2;
 static_assert(kBwdSmem <= 227 * 1024, "shared memory of one CTA");
 static_assert(kBwdSmem > 116 * 1024, "one CTA per SM: the TMEM allocation takes every column");
+static_assert(kBwdSmem - kBOffDz >= kHidden * (kHidden + 4) * 4, "the partials' staging tile fits the operand buffers");
 // TMEM columns
 constexpr uint32_t kTcDh = 0, kTcW3 = 128, kTcW2 = 256, kTcW1 = 384, kTcW4 = 448, kTcB3 = 464, kTcB2 = 480,
                    kTcB1 = 496, kBwdTmemCols = 512;
@@ -473,12 +479,14 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a, uint32_t b, in
                      (accumulate || ks > 0) ? 1u : 0u);
 }
 
-// Half (64 columns) of this thread's row of z (FP16), into registers.
-__device__ __forceinline__ void load_z_half(const __half* __restrict__ zv, int row0, int r, int half,
-                                            uint4 (&zb)[8]) {
-    const uint4* zr = reinterpret_cast<const uint4*>(zv + (size_t)(row0 + r) * kHidden) + half * 8;
+// This thread's row of z (FP16, saved transposed [feature][ldh]) for the 64
+// features of its column half: one 2-byte load per feature, a warp reading 64
+// contiguous bytes per feature.
+__device__ __forceinline__ void load_z_half(const __half* __restrict__ zt, int ldh, int row0, int r, int half,
+                                            __half (&zb)[64]) {
+    const __half* src = zt + (size_t)(half * 64) * ldh + row0 + r;
 #pragma unroll
-    for (int q = 0; q < 8; q++) zb[q] = zr[q];
+    for (int f = 0; f < 64; f++) zb[f] = src[(size_t)f * ldh];
 }
 
 // Epilogue of a hidden layer: dZ = dH * SiLU'(Z) for this thread's row and column
@@ -486,7 +494,7 @@ __device__ __forceinline__ void load_z_half(const __half* __restrict__ zv, int r
 // half of the row of z (FP16, loaded by the caller before the MMAs it waited
 // for). In dZ^T two lanes (rows 2k, 2k + 1) write one 32-bit word per feature.
 __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lane, uint8_t* dz, uint8_t* dzt,
-                                             const uint4 (&zb)[8]) {
+                                             const __half (&zb)[64]) {
     const int r = (warp & 3) * 32 + lane;
     const int half = warp >> 2;
 #pragma unroll
@@ -496,15 +504,7 @@ __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lan
         tc::tmem_ld16(tc::tmem_lane_addr(tmem_dh, warp, c0), v);
         float h[16];
 #pragma unroll
-        for (int q = 0; q < 2; q++) {
-            const __half2* g = reinterpret_cast<const __half2*>(&zb[ch * 2 + q]);
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float2 zz = __half22float2(g[j]);
-                h[8 * q + 2 * j] = v[8 * q + 2 * j] * silu_grad(zz.x);
-                h[8 * q + 2 * j + 1] = v[8 * q + 2 * j + 1] * silu_grad(zz.y);
-            }
-        }
+        for (int i = 0; i < 16; i++) h[i] = v[i] * silu_grad(__half2float(zb[ch * 16 + i]));
         if (dz) {
             uint4 lo, hi;
             lo.x = pack2(h[0], h[1]); lo.y = pack2(h[2], h[3]); lo.z = pack2(h[4], h[5]); lo.w = pack2(h[6], h[7]);
@@ -524,29 +524,50 @@ __device__ __forceinline__ void bwd_epilogue(uint32_t tmem_dh, int warp, int lan
 }
 
 // This CTA's partial gradients, in the flat parameter layout: row r of the
-// accumulators is TMEM lane r; the two warps of a lane quadrant share the work.
-__device__ __forceinline__ void bwd_store_partials(uint32_t tmem, int warp, int lane, bool have, const float* db4,
-                                                   float* __restrict__ out) {
+// accumulators is TMEM lane r; the two warps of a lane quadrant share the
+// columns. The weight blocks go through a shared-memory tile (rows padded by 4
+// floats) so that the global stores are contiguous; called by every thread
+// once the operand buffers are free (tile: at least 128 x 132 floats).
+__device__ __forceinline__ void bwd_store_partials(uint32_t tmem, int warp, int lane, int tid, bool have,
+                                                   const float* db4, float* tile, float* __restrict__ out) {
     const int r = (warp & 3) * 32 + lane;
-    auto row = [&](uint32_t col, int ncols, float* dst, int stride) {  // dst[c * stride] = D[r][col + c]
-        for (int c0 = 0; c0 < ncols; c0 += 16) {
+    const int half = warp >> 2;
+    auto block = [&](uint32_t col, int ncols, float* dst) {  // dst [128][ncols] = D[.][col .. col + ncols)
+        const int ts = ncols + 4;
+        for (int c0 = 16 * half; c0 < ncols; c0 += 32) {
             float v[16];
             if (have) tc::tmem_ld16(tc::tmem_lane_addr(tmem + col, warp, c0), v);
 #pragma unroll
-            for (int i = 0; i < 16; i++)
-                if (c0 + i < ncols) dst[(size_t)(c0 + i) * stride] = have ? v[i] : 0.f;
+            for (int q = 0; q < 4; q++)
+                *reinterpret_cast<float4*>(tile + r * ts + c0 + 4 * q) =
+                    have ? make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3])
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        __syncthreads();
+        const int q4 = ncols / 4;
+        for (int q = tid; q < kHidden * q4; q += kBwdThreads) {
+            const int rr = q / q4, cc = (q % q4) * 4;
+            *reinterpret_cast<float4*>(dst + (size_t)rr * ncols + cc) = *reinterpret_cast<const float4*>(tile + rr * ts + cc);
+        }
+        __syncthreads();
     };
-    if (warp < 4) {
-        row(kTcW3, kHidden, out + kOffParamW3 + r * kHidden, 1);
-        row(kTcW1, kFeatures, out + kOffParamW1 + r * kFeatures, 1);
-        row(kTcB3, 1, out + kOffParamB3 + r, 1);
+    block(kTcW3, kHidden, out + kOffParamW3);
+    block(kTcW2, kHidden, out + kOffParamW2);
+    block(kTcW1, kFeatures, out + kOffParamW1);
+    // W4 (D[h][o] = dW4[o][h]) and the biases: one value per row and column, contiguous across lanes
+    float v[16];
+    if (half == 0) {
+        if (have) tc::tmem_ld16(tc::tmem_lane_addr(tmem + kTcW4, warp, 0), v);
+#pragma unroll
+        for (int o = 0; o < kOutputs; o++) out[kOffParamW4 + o * kHidden + r] = have ? v[o] : 0.f;
+        if (have) tc::tmem_ld16(tc::tmem_lane_addr(tmem + kTcB3, warp, 0), v);
+        out[kOffParamB3 + r] = have ? v[0] : 0.f;
         if (r < kOutputs) out[kOffParamB4 + r] = db4[r];
     } else {
-        row(kTcW2, kHidden, out + kOffParamW2 + r * kHidden, 1);
-        row(kTcW4, kOutputs, out + kOffParamW4 + r, kHidden);  // D[h][o] = dW4[o][h]
-        row(kTcB2, 1, out + kOffParamB2 + r, 1);
-        row(kTcB1, 1, out + kOffParamB1 + r, 1);
+        if (have) tc::tmem_ld16(tc::tmem_lane_addr(tmem + kTcB2, warp, 0), v);
+        out[kOffParamB2 + r] = have ? v[0] : 0.f;
+        if (have) tc::tmem_ld16(tc::tmem_lane_addr(tmem + kTcB1, warp, 0), v);
+        out[kOffParamB1 + r] = have ? v[0] : 0.f;
     }
 }
 
@@ -561,6 +582,12 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
     __shared__ float db4s[4][kOutputs];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t* hb[2] = {smem + kBOffH, smem + kBOffH + kHidden * kTile * 2};
+    const int ntiles = batch / kTile;
+    int t = blockIdx.x;
+    if (t < ntiles) {  // the first tile's H3^T and H2^T, in flight while the weights are staged
+        issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, t * kTile, tid);
+        issue_h_tile(hb[1], S.h2t, kHidden, S.ldh, t * kTile, tid);
+    }
     stage_weights(smem + kBOffW4t, w4t, kHidden, kOutPad, tid, kBwdThreads);
     stage_weights(smem + kBOffW3t, w3t, kHidden, kHidden, tid, kBwdThreads);
     stage_weights(smem + kBOffW2t, w2t, kHidden, kHidden, tid, kBwdThreads);
@@ -584,17 +611,11 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
     const uint32_t a_dy = tc::smem_addr(smem + kBOffDy), a_dyt = tc::smem_addr(smem + kBOffDyt);
     const uint32_t a_dz = tc::smem_addr(smem + kBOffDz), a_dzt = tc::smem_addr(smem + kBOffDzt);
     const uint32_t a_h[2] = {tc::smem_addr(hb[0]), tc::smem_addr(hb[1])};
-    const int ntiles = batch / kTile;
     const int r = (warp & 3) * 32 + lane;
     float db4[kOutputs] = {0.f, 0.f, 0.f, 0.f};
     uint32_t parity = 0;
     bool ok = true;
     int done = 0;  // tiles of this CTA finished (the accumulators hold data once it is > 0)
-    int t = blockIdx.x;
-    if (t < ntiles) {  // the first tile's H3^T and H2^T
-        issue_h_tile(hb[0], S.h3t, kHidden, S.ldh, t * kTile, tid);
-        issue_h_tile(hb[1], S.h2t, kHidden, S.ldh, t * kTile, tid);
-    }
     for (; t < ntiles && ok; t += gridDim.x) {
         const int row0 = t * kTile;
         const int tn = t + gridDim.x;  // the next tile of this CTA
@@ -615,8 +636,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
 #pragma unroll
             for (int o = 0; o < kOutputs; o++) db4[o] += __bfloat162float(e[o]);
         }
-        uint4 zb[8];
-        load_z_half(S.z3, row0, r, warp >> 2, zb);  // in flight while the MMAs run
+        __half zb[64];
+        load_z_half(S.z3, S.ldh, row0, r, warp >> 2, zb);  // in flight while the MMAs run
         cp_async_wait<1>();  // H3^T
         handoff_to_mma();
         if (tid == 0) {
@@ -628,7 +649,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[0], S.h1t, kHidden, S.ldh, row0, tid);
         bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
-        load_z_half(S.z2, row0, r, warp >> 2, zb);
+        load_z_half(S.z2, S.ldh, row0, r, warp >> 2, zb);
         cp_async_wait<1>();  // H2^T
         handoff_to_mma();
         if (tid == 0) {
@@ -641,7 +662,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
         if (!(ok = wait_all(&bar, parity))) break;
         issue_h_tile(hb[1], S.h0t, kInPad, S.ldh, row0, tid);
         bwd_epilogue(tmem + kTcDh, warp, lane, smem + kBOffDz, smem + kBOffDzt, zb);
-        load_z_half(S.z1, row0, r, warp >> 2, zb);
+        load_z_half(S.z1, S.ldh, row0, r, warp >> 2, zb);
         cp_async_wait<1>();  // H1^T
         handoff_to_mma();
         if (tid == 0) {
@@ -684,7 +705,8 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
     float db4t[kOutputs];
 #pragma unroll
     for (int o = 0; o < kOutputs; o++) db4t[o] = db4s[0][o] + db4s[1][o] + db4s[2][o] + db4s[3][o];
-    bwd_store_partials(tmem, warp, lane, ok && done > 0, db4t, part + (size_t)blockIdx.x * kParams);
+    bwd_store_partials(tmem, warp, lane, tid, ok && done > 0, db4t, reinterpret_cast<float*>(smem + kBOffDz),
+                       part + (size_t)blockIdx.x * kParams);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();

@@ -50,8 +50,8 @@ struct PackedMut {
 };
 
 // Training saves of the forward pass (all null for inference): the hidden
-// layers' pre-activations z [n][128] in FP16 and the bf16 layer inputs
-// transposed, [width][ldh].
+// layers' pre-activations z in FP16 and the bf16 layer inputs, all transposed
+// ([width][ldh], feature-major).
 struct Saves {
     __half *z1, *z2, *z3;
     __nv_bfloat16 *h0t, *h1t, *h2t, *h3t;  // h0t [64][ldh] (rows 48..63 zero), the others [128][ldh]
