@@ -242,14 +242,15 @@ sphmp_status take_errors(sphmp_corrector* c) {
 }
 
 // forward with saves, output gradient, backward into c->grads
-sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t, int batch) {
+sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t, int batch,
+                              const mlp::AdamStep& adam) {
     using namespace mlp;
     const cudaStream_t s = c->stream;
     const int ld = c->max_batch;
     const Saves S{c->z1, c->z2, c->z3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
     LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
     LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
-    LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, c->grads, c->err, c->num_sms, s));
+    LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, c->grads, adam, c->err, c->num_sms, s));
     return SPHMP_OK;
 }
 
@@ -380,7 +381,7 @@ sphmp_status sphmp_corrector_gradients(sphmp_corrector* c, const float* x, const
                                        float* grads, float* loss) {
     if (!c || !grads) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
     if (sphmp_status st = check_batch(c, x, t, batch)) return st;
-    if (sphmp_status st = enqueue_backward(c, x, t, batch)) return st;
+    if (sphmp_status st = enqueue_backward(c, x, t, batch, mlp::AdamStep{})) return st;  // no update
     LCK(cudaMemcpyAsync(grads, c->grads, sizeof(float) * mlp::kParams, cudaMemcpyDeviceToHost, c->stream));
     if (loss) LCK(cudaMemcpyAsync(loss, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     return take_errors(c);
@@ -391,10 +392,12 @@ sphmp_status sphmp_corrector_train_step(sphmp_corrector* c, const float* x, cons
     if (!c) return lfail(SPHMP_ERR_INVALID_ARG, "corrector is NULL");
     if (sphmp_status st = check_batch(c, x, t, batch)) return st;
     if (!(lr > 0.f) || !isfinite(lr)) return lfail(SPHMP_ERR_INVALID_ARG, "lr must be > 0");
-    if (sphmp_status st = enqueue_backward(c, x, t, batch)) return st;
     c->adam_step++;
-    LCK(mlp::launch_adam(c->params, c->grads, c->adam_m, c->adam_v, mlp::kParams, lr, 0.9f, 0.999f, 1e-8f,
-                         c->adam_step, c->stream));
+    const mlp::AdamStep adam = mlp::adam_step(c->params, c->adam_m, c->adam_v, lr, 0.9f, 0.999f, 1e-8f, c->adam_step);
+    if (sphmp_status st = enqueue_backward(c, x, t, batch, adam)) {
+        c->adam_step--;
+        return st;
+    }
     LCK(mlp::launch_pack(c->params, packed_mut(c), c->stream));
     if (loss) {
         LCK(cudaMemcpyAsync(loss, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));

@@ -17,8 +17,9 @@
 // * k_gemm_tn: D = A B^T for K-major bf16 A [M][K] and B [N][K] (N <= 128),
 //   M in tiles of 128, K split over gridDim.y into FP32 partials (the library's
 //   GEMM entry point).
-// * elementwise kernels: the output gradient, Adam, and the packing of the FP32
-//   master parameters into the padded bf16 operand layouts.
+// * elementwise kernels: the output gradient, the sum of the partial gradients
+//   with the Adam step, and the packing of the FP32 master parameters into the
+//   padded bf16 operand layouts.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -713,13 +714,31 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
     if (warp == 0) tc::tmem_dealloc(tmem_base, kBwdTmemCols);
 }
 
-// grads[p] = sum over the CTAs' partials, in CTA order (one thread per parameter)
-__global__ void k_sum_partials(const float* __restrict__ part, int nparts, float* __restrict__ grads) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= kParams) return;
+// grads[p] = the sum over the CTAs' partials: 64 parameters per block, four
+// threads per parameter summing every fourth CTA's partial (a warp reads 32
+// consecutive parameters of one partial), the four sums added in a fixed order;
+// with an Adam step (adam.lr > 0) the parameter is updated in the same pass.
+constexpr int kSumParams = 64;
+__global__ void __launch_bounds__(4 * kSumParams) k_sum_partials(const float* __restrict__ part, int nparts,
+                                                                 float* __restrict__ grads, const AdamStep adam) {
+    __shared__ float sh[4][kSumParams];
+    const int j = threadIdx.x / kSumParams, q = threadIdx.x % kSumParams;
+    const int p = blockIdx.x * kSumParams + q;
     float s = 0.f;
-    for (int k = 0; k < nparts; k++) s += part[(size_t)k * kParams + p];
-    grads[p] = s;
+    if (p < kParams)
+        for (int k = j; k < nparts; k += 4) s += part[(size_t)k * kParams + p];
+    sh[j][q] = s;
+    __syncthreads();
+    if (j != 0 || p >= kParams) return;
+    const float g = (sh[0][q] + sh[1][q]) + (sh[2][q] + sh[3][q]);
+    grads[p] = g;
+    if (adam.lr > 0.f) {
+        const float mi = adam.b1 * adam.m[p] + (1.f - adam.b1) * g;
+        const float vi = adam.b2 * adam.v[p] + (1.f - adam.b2) * g * g;
+        adam.m[p] = mi;
+        adam.v[p] = vi;
+        adam.p[p] -= adam.lr * (mi / adam.c1) / (sqrtf(vi / adam.c2) + adam.eps);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -776,18 +795,6 @@ __global__ void k_loss_sum(const float* __restrict__ part, int nparts, int batch
     if (threadIdx.x == 0) *loss = red[0] / (float)batch;
 }
 
-__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
-                       float* __restrict__ v, int count, float lr, float b1, float b2, float eps, float c1,
-                       float c2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= count) return;
-    const float gi = g[i];
-    const float mi = b1 * m[i] + (1.f - b1) * gi;
-    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
-}
 
 // FP32 master parameters -> padded bf16 operands (and their transposes) + biases
 __global__ void k_pack(const float* __restrict__ p, PackedMut W) {
@@ -867,7 +874,7 @@ cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, b
 }
 
 cudaError_t launch_backward(const bf16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
-                            float* grads, uint32_t* err, int num_sms, cudaStream_t s) {
+                            float* grads, const AdamStep& adam, uint32_t* err, int num_sms, cudaStream_t s) {
     // the saved inputs are copied 16 bytes at a time: their row stride must keep that alignment
     if (batch <= 0 || batch % kTile != 0 || !S.z1 || !S.h0t || S.ldh % 8 != 0 || S.ldh < batch)
         return cudaErrorInvalidValue;
@@ -877,15 +884,12 @@ cudaError_t launch_backward(const bf16* dy, const Saves& S, const PackedMut& W, 
     const int grid = tiles < num_sms ? tiles : num_sms;
     k_mlp_backward<<<grid, kBwdThreads, kBwdSmem, s>>>(dy, S, W.w2t, W.w3t, W.w4t, batch, part, err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_sum_partials<<<(kParams + 255) / 256, 256, 0, s>>>(part, grid, grads);
+    k_sum_partials<<<(kParams + kSumParams - 1) / kSumParams, 4 * kSumParams, 0, s>>>(part, grid, grads, adam);
     return cudaGetLastError();
 }
 
-cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int count, float lr, float b1, float b2,
-                        float eps, int step, cudaStream_t s) {
-    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
-    k_adam<<<(count + 255) / 256, 256, 0, s>>>(p, g, m, v, count, lr, b1, b2, eps, c1, c2);
-    return cudaGetLastError();
+AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, float eps, int step) {
+    return AdamStep{p, m, v, lr, b1, b2, eps, 1.f - powf(b1, (float)step), 1.f - powf(b2, (float)step)};
 }
 
 cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s) {

@@ -63,15 +63,21 @@ cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& 
 // D[split][M][N] = A[M][K] B[N][K]^T over the split's K range; N a multiple of 16, <= 128
 cudaError_t launch_gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* D, int M, int N,
                            int K, int splits, uint32_t* err, cudaStream_t s);
+// One Adam step (bias-corrected; lr <= 0: none) applied where the gradients are formed.
+struct AdamStep {
+    float *p, *m, *v;
+    float lr, b1, b2, eps, c1, c2;  // c1, c2: 1 - beta^step
+};
+AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, float eps, int step);
+
 // The whole backward pass after launch_out_grad (fused, one persistent CTA per
-// SM): gradients of every parameter into grads (flat layout). batch a multiple
-// of 128; part: scratch of num_sms * kParams floats.
+// SM): gradients of every parameter into grads (flat layout), then the Adam
+// step if adam.lr > 0. batch a multiple of 128; part: scratch of num_sms *
+// kParams floats.
 cudaError_t launch_backward(const __nv_bfloat16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
-                            float* grads, uint32_t* err, int num_sms, cudaStream_t s);
+                            float* grads, const AdamStep& adam, uint32_t* err, int num_sms, cudaStream_t s);
 cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, __nv_bfloat16* dy,
                             __nv_bfloat16* dyt, float* loss_part, float* loss, cudaStream_t s);
-cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int count, float lr, float b1, float b2,
-                        float eps, int step, cudaStream_t s);
 cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s);
 
 }  // namespace mlp
