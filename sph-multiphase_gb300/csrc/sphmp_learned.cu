@@ -189,7 +189,7 @@ struct sphmp_corrector {
     __half *z1 = nullptr, *z2 = nullptr, *z3 = nullptr;
     float* y = nullptr;
     bf16 *h0t = nullptr, *h1t = nullptr, *h2t = nullptr, *h3t = nullptr;
-    bf16 *dy = nullptr, *dyt = nullptr;
+    bf16* dy = nullptr;
     float* bpart = nullptr;     // the fused backward's per-CTA gradient partials [num_sms][kParams]
     float* loss_part = nullptr;
     float* loss = nullptr;
@@ -243,13 +243,13 @@ sphmp_status take_errors(sphmp_corrector* c) {
 
 // forward with saves, output gradient, backward into c->grads
 sphmp_status enqueue_backward(sphmp_corrector* c, const float* x, const float* t, int batch,
-                              const mlp::AdamStep& adam) {
+                              const mlp::AdamStep& adam, bool want_loss) {
     using namespace mlp;
     const cudaStream_t s = c->stream;
     const int ld = c->max_batch;
     const Saves S{c->z1, c->z2, c->z3, c->h0t, c->h1t, c->h2t, c->h3t, ld};
     LCK(launch_forward(x, batch, packed(c), S, c->y, c->err, c->num_sms, s));
-    LCK(launch_out_grad(c->y, t, batch, ld, c->dy, c->dyt, c->loss_part, c->loss, s));
+    LCK(launch_out_grad(c->y, t, batch, ld, c->dy, nullptr, c->loss_part, want_loss ? c->loss : nullptr, s));
     LCK(launch_backward(c->dy, S, packed_mut(c), batch, c->bpart, c->grads, adam, c->err, c->num_sms, s));
     return SPHMP_OK;
 }
@@ -305,7 +305,7 @@ sphmp_status sphmp_corrector_create(int32_t max_batch, void* stream, sphmp_corre
         A(&c->z1, kHidden * B); A(&c->z2, kHidden * B); A(&c->z3, kHidden * B);  // [128][max_batch]
         A(&c->y, B * 4);
         A(&c->h0t, (size_t)kInPad * B); A(&c->h1t, kHidden * B); A(&c->h2t, kHidden * B); A(&c->h3t, kHidden * B);
-        A(&c->dy, B * kOutPad); A(&c->dyt, (size_t)kOutPad * B);
+        A(&c->dy, B * kOutPad);
         A(&c->bpart, (size_t)c->num_sms * kParams);
         A(&c->loss_part, B / 256 + 1);
         A(&c->loss, 1);
@@ -381,7 +381,7 @@ sphmp_status sphmp_corrector_gradients(sphmp_corrector* c, const float* x, const
                                        float* grads, float* loss) {
     if (!c || !grads) return lfail(SPHMP_ERR_INVALID_ARG, "bad arguments");
     if (sphmp_status st = check_batch(c, x, t, batch)) return st;
-    if (sphmp_status st = enqueue_backward(c, x, t, batch, mlp::AdamStep{})) return st;  // no update
+    if (sphmp_status st = enqueue_backward(c, x, t, batch, mlp::AdamStep{}, loss != nullptr)) return st;
     LCK(cudaMemcpyAsync(grads, c->grads, sizeof(float) * mlp::kParams, cudaMemcpyDeviceToHost, c->stream));
     if (loss) LCK(cudaMemcpyAsync(loss, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     return take_errors(c);
@@ -393,12 +393,12 @@ sphmp_status sphmp_corrector_train_step(sphmp_corrector* c, const float* x, cons
     if (sphmp_status st = check_batch(c, x, t, batch)) return st;
     if (!(lr > 0.f) || !isfinite(lr)) return lfail(SPHMP_ERR_INVALID_ARG, "lr must be > 0");
     c->adam_step++;
-    const mlp::AdamStep adam = mlp::adam_step(c->params, c->adam_m, c->adam_v, lr, 0.9f, 0.999f, 1e-8f, c->adam_step);
-    if (sphmp_status st = enqueue_backward(c, x, t, batch, adam)) {
+    const mlp::AdamStep adam =
+        mlp::adam_step(c->params, c->adam_m, c->adam_v, lr, 0.9f, 0.999f, 1e-8f, c->adam_step, packed_mut(c));
+    if (sphmp_status st = enqueue_backward(c, x, t, batch, adam, loss != nullptr)) {  // also repacks the operands
         c->adam_step--;
         return st;
     }
-    LCK(mlp::launch_pack(c->params, packed_mut(c), c->stream));
     if (loss) {
         LCK(cudaMemcpyAsync(loss, c->loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
         return take_errors(c);

@@ -718,6 +718,34 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_mlp_backward(const bf16* __r
 // threads per parameter summing every fourth CTA's partial (a warp reads 32
 // consecutive parameters of one partial), the four sums added in a fixed order;
 // with an Adam step (adam.lr > 0) the parameter is updated in the same pass.
+// Parameter p (flat layout) into its bf16 operand positions, as k_pack writes them.
+__device__ __forceinline__ void pack_param(const PackedMut& W, int p, float val) {
+    const bf16 b = __float2bfloat16_rn(val);
+    if (p < kOffParamB1) {  // W1 [128][48] -> w1 [128][64]
+        W.w1[(p / kFeatures) * kInPad + p % kFeatures] = b;
+    } else if (p < kOffParamW2) {
+        W.bias[p - kOffParamB1] = val;
+    } else if (p < kOffParamB2) {  // W2 [128][128], and transposed
+        const int i = p - kOffParamW2;
+        W.w2[i] = b;
+        W.w2t[(i % kHidden) * kHidden + i / kHidden] = b;
+    } else if (p < kOffParamW3) {
+        W.bias[kHidden + p - kOffParamB2] = val;
+    } else if (p < kOffParamB3) {
+        const int i = p - kOffParamW3;
+        W.w3[i] = b;
+        W.w3t[(i % kHidden) * kHidden + i / kHidden] = b;
+    } else if (p < kOffParamW4) {
+        W.bias[2 * kHidden + p - kOffParamB3] = val;
+    } else if (p < kOffParamB4) {  // W4 [4][128] -> w4 [16][128], w4t [128][16]
+        const int i = p - kOffParamW4;
+        W.w4[i] = b;
+        W.w4t[(i % kHidden) * kOutPad + i / kHidden] = b;
+    } else {
+        W.bias[3 * kHidden + p - kOffParamB4] = val;
+    }
+}
+
 constexpr int kSumParams = 64;
 __global__ void __launch_bounds__(4 * kSumParams) k_sum_partials(const float* __restrict__ part, int nparts,
                                                                  float* __restrict__ grads, const AdamStep adam) {
@@ -737,7 +765,9 @@ __global__ void __launch_bounds__(4 * kSumParams) k_sum_partials(const float* __
         const float vi = adam.b2 * adam.v[p] + (1.f - adam.b2) * g * g;
         adam.m[p] = mi;
         adam.v[p] = vi;
-        adam.p[p] -= adam.lr * (mi / adam.c1) / (sqrtf(vi / adam.c2) + adam.eps);
+        const float np = adam.p[p] - adam.lr * (mi / adam.c1) / (sqrtf(vi / adam.c2) + adam.eps);
+        adam.p[p] = np;
+        pack_param(adam.w, p, np);
     }
 }
 
@@ -766,7 +796,7 @@ __global__ void k_out_grad(const float4* __restrict__ y, const float4* __restric
         reinterpret_cast<uint4*>(dy + (size_t)i * kOutPad)[1] = hi;
 #pragma unroll
         for (int o = 0; o < 4; o++) {
-            dyt[(size_t)o * ld + i] = __float2bfloat16_rn(s * d[o]);
+            if (dyt) dyt[(size_t)o * ld + i] = __float2bfloat16_rn(s * d[o]);
             se += d[o] * d[o];
         }
     }
@@ -869,7 +899,7 @@ cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, b
     const int blocks = (batch + 255) / 256;
     k_out_grad<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4*>(y), reinterpret_cast<const float4*>(t), batch,
                                       ld, dy, dyt, loss_part);
-    k_loss_sum<<<1, 256, 0, s>>>(loss_part, blocks, batch, loss);
+    if (loss) k_loss_sum<<<1, 256, 0, s>>>(loss_part, blocks, batch, loss);
     return cudaGetLastError();
 }
 
@@ -888,8 +918,9 @@ cudaError_t launch_backward(const bf16* dy, const Saves& S, const PackedMut& W, 
     return cudaGetLastError();
 }
 
-AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, float eps, int step) {
-    return AdamStep{p, m, v, lr, b1, b2, eps, 1.f - powf(b1, (float)step), 1.f - powf(b2, (float)step)};
+AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, float eps, int step,
+                   const PackedMut& w) {
+    return AdamStep{p, m, v, lr, b1, b2, eps, 1.f - powf(b1, (float)step), 1.f - powf(b2, (float)step), w};
 }
 
 cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s) {

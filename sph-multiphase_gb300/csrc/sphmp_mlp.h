@@ -63,12 +63,16 @@ cudaError_t launch_forward(const float* x, int n, const Packed& W, const Saves& 
 // D[split][M][N] = A[M][K] B[N][K]^T over the split's K range; N a multiple of 16, <= 128
 cudaError_t launch_gemm_tn(const __nv_bfloat16* A, int lda, const __nv_bfloat16* B, int ldb, float* D, int M, int N,
                            int K, int splits, uint32_t* err, cudaStream_t s);
-// One Adam step (bias-corrected; lr <= 0: none) applied where the gradients are formed.
+// One Adam step (bias-corrected; lr <= 0: none) applied where the gradients are
+// formed, each updated parameter also written into its bf16 operand positions
+// (the padding of the packed layouts is written once by launch_pack).
 struct AdamStep {
     float *p, *m, *v;
     float lr, b1, b2, eps, c1, c2;  // c1, c2: 1 - beta^step
+    PackedMut w;
 };
-AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, float eps, int step);
+AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, float eps, int step,
+                   const PackedMut& w);
 
 // The whole backward pass after launch_out_grad (fused, one persistent CTA per
 // SM): gradients of every parameter into grads (flat layout), then the Adam
@@ -76,6 +80,8 @@ AdamStep adam_step(float* p, float* m, float* v, float lr, float b1, float b2, f
 // kParams floats.
 cudaError_t launch_backward(const __nv_bfloat16* dy, const Saves& S, const PackedMut& W, int batch, float* part,
                             float* grads, const AdamStep& adam, uint32_t* err, int num_sms, cudaStream_t s);
+// dY (bf16 [batch][16], zero padded; transposed into dyt [4][ld] unless null) and
+// the loss into *loss (unless null)
 cudaError_t launch_out_grad(const float* y, const float* t, int batch, int ld, __nv_bfloat16* dy,
                             __nv_bfloat16* dyt, float* loss_part, float* loss, cudaStream_t s);
 cudaError_t launch_pack(const float* p, const PackedMut& W, cudaStream_t s);
