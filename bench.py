@@ -657,25 +657,23 @@ def run_learned(args):
     cases, training = {}, {}
     for case in ("bubbles", "liquid"):
         liquid = case == "liquid"
-        # training pairs: three scenes of the rollout's physics and depth (64 x 128 x 64 sites,
-        # 32 bubbles: the rollout lattice's bubble density), 16 starts spread over the rollout's
-        # time span, a quarter of each start's particles
+        # training pairs from the batched plain solver: three scenes of the rollout's physics and
+        # depth (64 x 128 x 64 sites, 32 bubbles: the rollout lattice's bubble density) tiled into
+        # one domain, so that every pass of their plain steps covers all three in one launch; 16
+        # starts spread over the rollout's time span, a quarter of each start's particles
         t0 = time.perf_counter()
-        Xs, Ts = [], []
         gen = torch.Generator(device=dev)
         gen.manual_seed(3)
-        for seed in (21, 22, 23):
-            sc = scenes.rollout_bubbles(seed=seed, lattice=(64, 128, 64), n_bubbles=32, liquid_only=liquid)
-            c = fresh(sc, 50)
-            large, plain = sphmp.Context(sc.params), sphmp.Context(sc.params)
-            X, T = SL.generate_pairs(c, large, plain, factor, starts=16, gap=max(1, sim_steps // 16))
-            keep = torch.randperm(X.shape[0], device=dev, generator=gen)[: X.shape[0] // 4]
-            Xs.append(X[keep])
-            Ts.append(np.nan_to_num(T[keep.cpu().numpy()], nan=0.0, posinf=0.0, neginf=0.0))
-            for x in (c, large, plain):
-                x.close()
-        X, T = torch.cat(Xs), np.concatenate(Ts)
-        X = torch.nan_to_num(X, nan=0.0, posinf=0.0, neginf=0.0)
+        tiled, _ = scenes.tile([scenes.rollout_bubbles(seed=seed, lattice=(64, 128, 64), n_bubbles=32,
+                                                       liquid_only=liquid) for seed in (21, 22, 23)])
+        c = fresh(tiled, 50)
+        large, plain = sphmp.Context(tiled.params), sphmp.Context(tiled.params)
+        X, T = SL.generate_pairs(c, large, plain, factor, starts=16, gap=max(1, sim_steps // 16))
+        keep = torch.randperm(X.shape[0], device=dev, generator=gen)[: X.shape[0] // 4]
+        X = torch.nan_to_num(X[keep], nan=0.0, posinf=0.0, neginf=0.0)
+        T = np.nan_to_num(T[keep.cpu().numpy()], nan=0.0, posinf=0.0, neginf=0.0)
+        for x in (c, large, plain):
+            x.close()
         t_pairs = time.perf_counter() - t0
         shift, scale, osc = SL.normalisation(X, T)
         cor = sphmp.Corrector(65536)
@@ -776,9 +774,10 @@ def run_learned(args):
             "config": {"workload": "rollout_256x128x128_2phase_256bubbles", "d": 0.005, "h": 0.01, "dt": 1e-4,
                        "large_step": f"{factor} dt", "audit_every_large_steps": audit_every, "tolerance": tol,
                        "simulated_s": sim_steps * 1e-4, "eos": "linear k=3",
-                       "training": "3 scenes of 64x128x64 sites with the rollout's physics and depth (32 bubbles "
-                                   "each, or all liquid), 16 starts over the rollout's time span, a quarter of "
-                                   "each start's particles, 1500 Adam steps at 65,536 per batch, lr 1e-3",
+                       "training": "pairs from the batched plain solver: 3 scenes of 64x128x64 sites with the "
+                                   "rollout's physics and depth (32 bubbles each, or all liquid) tiled into one "
+                                   "domain, 16 starts over the rollout's time span, a quarter of each start's "
+                                   "particles; 1500 Adam steps at 65,536 per batch, lr 1e-3",
                        "timing": "host clock around each arm (the rollout synchronises at its audits)"},
             "cases": cases, "training": training}
     print(json.dumps(line))
