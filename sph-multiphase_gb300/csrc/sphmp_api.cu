@@ -708,6 +708,12 @@ static sphmp_status upload_records(sphmp_ctx* c, const sphmp_display_pack* disp,
         CK(cudaMemcpyAsync(d_disp, disp, sizeof(sphmp_display_pack) * (size_t)m, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemcpyAsync(d_calc, calc, sizeof(sphmp_calc_pack) * (size_t)m, cudaMemcpyHostToDevice, c->stream));
     }
+    // a full upload rewrites every double-buffered field, so it can start from the
+    // first buffer of each: the selectors are then those of a fresh context, and a
+    // step captured after a fresh upload and the first sort serves again after this
+    // upload and that sort (an append keeps the selectors of the particles before it)
+    if (start == 0)
+        for (int f = 0; f < kNumFloat4Fields; f++) c->cur[f] = 0;
     c->n = end;
     c->prm.num = end;
     c->n_stale = false;
