@@ -359,7 +359,10 @@ __device__ __forceinline__ void warp_sort_cell(const DevParams& P, const DevBuff
 }
 
 // One warp per cell (cells of up to kWarpSortMax members).
-__global__ void __launch_bounds__(kThreads) k_cell_sort(const __grid_constant__ DevParams P,
+// Six blocks per SM (at most 40 registers): the warps' dependent load chains
+// overlap; the large-cell paths spill a little (cell order 0.071 -> 0.066 ms per
+// step on the 2^20-particle scene; 77 registers without the bound).
+__global__ void __launch_bounds__(kThreads, 6) k_cell_sort(const __grid_constant__ DevParams P,
                                                         const __grid_constant__ DevBuffers B,
                                                         const float4* __restrict__ pos_in) {
     __shared__ uint32_t sm[kThreads / 32][kWarpSortMax];
