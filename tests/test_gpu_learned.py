@@ -132,6 +132,30 @@ def test_train_steps_are_adam(built):
     cor.close()
 
 
+def test_train_step_repacks_the_operands(built):
+    """The Adam pass writes each updated parameter into the bf16 operands the
+    forward pass reads: after training steps, the network's outputs equal those
+    of a corrector given the same parameters afresh (packed whole), bit for bit."""
+    cor, p, shift, scale, rng = _net(7, 256)
+    for _ in range(3):
+        X = torch.from_numpy(rng.standard_normal((256, 48)).astype(np.float32)).to(DEV)
+        T = torch.from_numpy(rng.standard_normal((256, 4)).astype(np.float32)).to(DEV)
+        cor.train_step(X, T, 1e-3)
+    fresh = sphmp.Corrector(0)
+    fresh.set_params(cor.get_params())
+    fresh.set_normalisation(shift, scale, np.ones(4, np.float32))
+    X = torch.from_numpy(rng.standard_normal((1000, 48)).astype(np.float32)).to(DEV)
+    y1 = torch.empty((1000, 4), dtype=torch.float32, device=DEV)
+    y2 = torch.empty((1000, 4), dtype=torch.float32, device=DEV)
+    cor.forward(X, y1)
+    fresh.forward(X, y2)
+    cor.sync()
+    fresh.sync()
+    assert torch.equal(y1, y2)
+    cor.close()
+    fresh.close()
+
+
 def test_training_fits_a_teacher_network(built):
     """Targets from another network of the same shape: 400 Adam steps bring the
     loss below a fifth of its start."""
