@@ -84,6 +84,25 @@ def test_backward_matches_finite_differences():
         assert abs(fd - g[i]) <= 2e-3 * max(1e-2, abs(fd)), (i, fd, g[i])
 
 
+def test_gpu_rounding_mode_stays_close_to_exact_gradients():
+    """The oracle's GPU-rounding mode (bf16 operands, z saved in FP16, as the
+    library's training kernels compute) against the exact float64 gradients of
+    the same network: every parameter tensor within 2 % in norm, so the FP16
+    save and the bf16 operands change the descent direction only slightly."""
+    rng = np.random.default_rng(9)
+    p = OL.init_params(6)
+    X = rng.standard_normal((512, 48)).astype(np.float32)
+    T = rng.standard_normal((512, 4)).astype(np.float32)
+    shift, scale = np.zeros(48, np.float32), np.ones(48, np.float32)
+    ident = lambda a: np.asarray(a, np.float64)
+    g_gpu, l_gpu = OL.mlp_backward(p, shift, scale, X, T)
+    g_ex, l_ex = OL.mlp_backward(p.astype(np.float64), shift, scale, X, T, rnd=ident)
+    assert abs(l_gpu - l_ex) <= 1e-4 * l_ex
+    G, R = OL.unpack(g_gpu), OL.unpack(g_ex.astype(np.float32))
+    for k in R:
+        assert np.linalg.norm(G[k] - R[k]) <= 1e-2 * np.linalg.norm(R[k]), k
+
+
 def test_adam_first_step_moves_each_parameter_by_lr():
     p = np.zeros(5, np.float32)
     g = np.array([1.0, -2.0, 0.5, 1e-3, -1e-6], np.float32)
