@@ -550,17 +550,17 @@ struct ProjectU {
 // ---------------------------------------------------------------------------
 
 // Alpha change of one in-grid fluid particle (contributeAlphaChange), Kahan-
-// compensated per phase. `pair` takes the neighbour's pos4, md = mass * (1/rho)
-// (zero for boundary neighbours, which exchange no volume fraction), veleval,
-// alpha4 and drift velocities.
+// compensated per phase. `pair` takes the neighbour's pos4, md = mass * (1/rho),
+// veleval, alpha4 and drift velocities.
 //
 // Per pair and phase k the reference adds
 //   -(0.5 cm (a_jk + a_ik) dot1) - cm (a_jk u_jk + a_ik u_ik) . d
 // with cm the kernel-gradient factor times md and dot1 = (v_j - v_i) . d. The
 // terms in a_ik are the particle's own fraction times the sums S_dot = sum cm
-// dot1 and S_d = sum cm d, which are taken once for all phases; the neighbour
-// terms -cm a_jk (0.5 dot1 + u_jk . d) are summed per phase (Kahan), and
-// result() adds -a_ik (0.5 S_dot + u_ik . S_d) to each phase's compensated sum.
+// dot1 and S_d = sum cm d, which are taken once for all phases (plain FP32
+// sums); the neighbour terms -cm a_jk (0.5 dot1 + u_jk . d) are summed per phase
+// (Kahan), and result() adds -a_ik (0.5 S_dot + u_ik . S_d) to each phase's
+// compensated sum. Boundary neighbours (pos4.w <= 0) exchange no fraction.
 template <int NP>
 struct AlphaChange {
     float4 pi, vei;
