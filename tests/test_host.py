@@ -225,3 +225,31 @@ def test_oracle_generators_build_the_library_scenes(lib, build):
     assert a.n == b.n and a.n_fluid == b.n_fluid
     assert a.disp.tobytes() == b.disp.tobytes()
     assert a.calc.tobytes() == b.calc.tobytes()
+
+
+def test_tiled_scenes_stay_apart_with_unique_ids(lib):
+    """sphmp.scenes.tile (the batched solver's layout, also the source of the
+    corrector's training pairs): every scene keeps its records in order, moved by
+    a whole number of grid cells, born ids renumbered to stay unique, and no two
+    scenes' particles within two cells of each other."""
+    solo = [scenes.bubble_scene(seed=s, n_particles=1500) for s in (1, 2, 3)]
+    big, layout = scenes.tile(solo)
+    p = big.params
+    cell = float(p.cellsize) / float(p.simscale)
+    assert big.n == sum(s.n for s in solo) and big.n_fluid == sum(s.n_fluid for s in solo)
+    ids = big.calc["bornid"][:big.n]
+    assert len(np.unique(ids)) == big.n
+    boxes = []
+    for s, (first, count, off) in zip(solo, layout):
+        assert count == s.n
+        frac = np.asarray(off, np.float64) / cell
+        assert np.allclose(frac, np.round(frac), atol=1e-4)
+        pos = big.disp["pos"][first:first + count]
+        assert np.allclose(pos, s.disp["pos"][:s.n] + off, atol=1e-6)
+        assert np.array_equal(big.calc["restdens"][first:first + count], s.calc["restdens"][:s.n])
+        boxes.append((pos.min(axis=0), pos.max(axis=0)))
+    for i in range(len(boxes)):
+        for j in range(i + 1, len(boxes)):
+            (alo, ahi), (blo, bhi) = boxes[i], boxes[j]
+            gap = np.maximum(blo - ahi, alo - bhi)  # per axis; positive where the boxes are apart
+            assert gap.max() >= 2 * cell - 1e-6
